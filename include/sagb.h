@@ -1,0 +1,216 @@
+/* sagb.h -- C ABI of the GB300 solve phase of int-AMG-FGMRES(m)
+ *
+ * The reference (suzuki-hpc/SC23-AD, a header-only C++ library) has no FFI of
+ * its own; its solve phase is reached through C++ objects.  Every entry point
+ * below replaces one of those reference interfaces, cited as Library/<file>:line.
+ * The C++ drop-in headers under include/senk/ are written on top of this ABI.
+ *
+ * Conventions
+ *  - Every function returns SA_OK (0) or an SA_ERR_* code; none calls exit()
+ *    or traps.  sa_last_error() returns a message for the calling thread.
+ *  - Vector arguments may be host or device pointers (device = cudaMalloc'd or
+ *    managed memory); host buffers are staged through device memory.
+ *  - Integer vectors are int32 fixed point with `bits` fractional bits; the
+ *    arithmetic is the reference's, bit for bit (int64 products and sums,
+ *    arithmetic right shifts, int32 wrap-around), and any int32 overflow is
+ *    reported through the status flags instead of being silent.
+ *  - One context = one GPU and one CUDA stream; calls on a context are
+ *    serialised by the caller.
+ */
+#ifndef SAGB_H
+#define SAGB_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- codes */
+#define SA_OK 0
+#define SA_ERR_ARG 1      /* invalid argument                                  */
+#define SA_ERR_CUDA 2     /* CUDA runtime error (no GPU, out of memory, ...)   */
+#define SA_ERR_SETUP 3    /* the host setup rejected the matrix                */
+#define SA_ERR_NUMERIC 4  /* a device status flag stopped the solve            */
+
+/* device status flags (sa_ctx_flags) */
+#define SA_FLAG_OVERFLOW 1u       /* an int32 result wrapped (the reference would silently wrap) */
+#define SA_FLAG_TIMEOUT 2u        /* a bounded device-side wait ran out                          */
+#define SA_FLAG_DIVZERO 4u        /* zero Hessenberg / Givens denominator                        */
+#define SA_FLAG_NORM_OVERFLOW 8u  /* int64 sum of squares wrapped                                */
+
+/* precisions */
+#define SA_INT 0 /* int32 fixed point, int64 accumulation (FGMRESflex/intAMGflex) */
+#define SA_F64 1 /* FP64 (FGMRES<double>/dfAMG<...,double>)                      */
+#define SA_F32 2 /* FP32 (FGMRES<float>/dfAMG<...,float>)                        */
+
+/* matrix kinds for sa_mat_create */
+#define SA_MAT_FIXED 0 /* CSR<Fixed<bit>>: (int)(a * 2^bit)       Library/matrix/spmat.hpp:55-70  */
+#define SA_MAT_FLEX 1  /* CSRflex: own bit from max|a|            Library/matrix/spmat.hpp:89-121 */
+#define SA_MAT_F64 2   /* CSR<double>                             Library/matrix/spmat.hpp:21-36  */
+#define SA_MAT_F32 3   /* CSR<float>                              Library/matrix/spmat.hpp:21-36  */
+
+/* operators of a hierarchy (sa_amg_level_spmv, sa_setup_view, ...) */
+#define SA_OP_A0 0  /* fine operator                                  */
+#define SA_OP_CA 1  /* coarse operator C_A[level]                      */
+#define SA_OP_P 2   /* interpolation Intrpl[level]                     */
+#define SA_OP_R 3   /* restriction Intrpl_t[level]                     */
+#define SA_OP_LD 4  /* smoother lower factor (D^-1 last in each row)   */
+#define SA_OP_U 5   /* smoother upper part                             */
+#define SA_OP_LUL 6 /* coarsest LU, unit lower factor (ltri)           */
+#define SA_OP_LUU 7 /* coarsest LU, D^-1 U (dutri)                     */
+#define SA_OP_BJ 8  /* block boundaries of a BlockSOR smoother (rptr)  */
+
+/* synthetic systems for sa_gen */
+#define SA_GEN_POISSON2D 0  /* 5-point, 4/-1                             */
+#define SA_GEN_POISSON3D 1  /* 7-point, 6/-1                             */
+#define SA_GEN_ANISO2D 2    /* 5-point, -u_xx - p*u_yy                   */
+#define SA_GEN_STENCIL27 3  /* 27-point, diag 26+U[0.1,1], off -1        */
+#define SA_GEN_CONVDIFF3D 4 /* 7-point upwinded convection-diffusion, Pe=p */
+#define SA_GEN_VARCOEF3D 5  /* 7-point lognormal(0,p) harmonic-mean faces */
+
+typedef struct sa_context *sa_ctx;
+typedef struct sa_matrix *sa_mat;
+typedef struct sa_multigrid *sa_amg;
+typedef struct sa_krylov *sa_solver;
+typedef struct sa_hierarchy *sa_setup;
+typedef struct sa_host_csr *sa_hcsr;
+typedef struct sa_timer *sa_event;
+
+typedef struct {
+    int n, m;
+    int64_t nnz;
+    const int32_t *rptr, *cind;
+    const void *val; /* double for FP64 views, int32 for integer views, float for FP32 */
+    int bit, dbit;
+} sa_csr_view;
+
+typedef struct {
+    int max_levels;      /* AMGParam::level (20)                      Library/parameters.hpp:253-264 */
+    double theta;        /* AMGParam::theta (0.8 in Work/main.cpp:32)                                */
+    int smoother_blocks; /* 0: SOR, >0: BlockSOR with this many blocks  Library/parameters.hpp:223-241 */
+    double omega;        /* SORParam::omega (1.0)                                                     */
+    int smooth_iter;     /* SORParam::iter (1)                                                        */
+} sa_amg_params;
+
+typedef struct {
+    int m;                 /* restart length (FGMRES m)                Library/solver/gmres.hpp:276-297 */
+    double eps;            /* relative tolerance (1e-10)                                                */
+    int max_outer;         /* Restarted max cycles (1000/m)            Library/solver/irsolver.hpp:50-57 */
+    int frac_bits;         /* F_G of the integer solver (FGMRESflex bit)                                */
+    int verbose;           /* print the reference's "# [j] res" / "[Res]" lines                         */
+    int overflow_fallback; /* int only: on an overflow flag, redo the cycle with F-1 (0: reference behaviour) */
+} sa_solver_params;
+
+/* ------------------------------------------------------------- library */
+const char *sa_version(void);
+const char *sa_last_error(void);
+
+/* ------------------------------------------------------------- context */
+int sa_ctx_create(int device, sa_ctx *out);
+int sa_ctx_destroy(sa_ctx ctx);
+#define SA_OPT_FP_EXACT 0 /* FP kernels in the reference's sequential order, no FMA (bit-exact) */
+#define SA_OPT_GRAPHS 1   /* capture Arnoldi steps into CUDA graphs (default on)              */
+int sa_ctx_set_option(sa_ctx ctx, int option, int value);
+int sa_ctx_flags(sa_ctx ctx, unsigned *flags, int clear);
+int sa_ctx_launches(sa_ctx ctx, long long *count);
+int sa_ctx_sync(sa_ctx ctx);
+int sa_ctx_stream(sa_ctx ctx, void **stream); /* the cudaStream_t all work is queued on */
+
+/* device memory and timing helpers (no library state) */
+int sa_device_alloc(sa_ctx ctx, uint64_t bytes, void **ptr);
+int sa_device_free(sa_ctx ctx, void *ptr);
+int sa_memcpy(sa_ctx ctx, void *dst, const void *src, uint64_t bytes); /* any direction, synchronous */
+int sa_event_create(sa_event *out);
+int sa_event_record(sa_ctx ctx, sa_event ev);
+int sa_event_elapsed_ms(sa_event start, sa_event stop, float *ms);
+int sa_event_destroy(sa_event ev);
+
+/* ------------------------------------------------- host CSR and generators */
+/* io::ReadMM(path, true, false)                      Library/io/mm.hpp:24-98 */
+int sa_hcsr_read_mm(const char *path, sa_hcsr *out);
+int sa_hcsr_create(int n, int m, const int32_t *rptr, const int32_t *cind, const double *val, sa_hcsr *out);
+int sa_hcsr_view(sa_hcsr A, sa_csr_view *out);
+/* CSRMat::LMax1Scaling(b)                            Library/matrix/csrmat.hpp:70-80 */
+int sa_hcsr_lmax1_scaling(sa_hcsr A, double *b);
+/* x* ~ U[-1,1] (splitmix64 seed), b = A x* (row order) -- synthetic right-hand side */
+int sa_hcsr_rhs(sa_hcsr A, uint64_t seed, double *xstar, double *b);
+int sa_hcsr_destroy(sa_hcsr A);
+int sa_gen(int kind, int nx, double param, uint64_t seed, sa_hcsr *out);
+
+/* ------------------------------------------------------------ matrices */
+/* CSR<Fixed<bit>>(CSRMat*) / CSRflex(CSRMat*) / CSR<double> / CSR<float>
+ *                                   Library/matrix/spmat.hpp:28-36, 62-70, 96-121 */
+int sa_mat_create(sa_ctx ctx, int kind, int bit, int n, int m, const int32_t *rptr, const int32_t *cind,
+                  const double *val, sa_mat *out);
+/* an already quantised int32 CSR with `bit` fractional bits */
+int sa_mat_create_i32(sa_ctx ctx, int n, int m, const int32_t *rptr, const int32_t *cind, const int32_t *val,
+                      int bit, sa_mat *out);
+int sa_mat_destroy(sa_mat A);
+int sa_mat_info(sa_mat A, int *n, int *m, int64_t *nnz, int *bit, int *precision);
+/* SpMat<T>::SpMV(in, out)          Library/matrix/spmat.hpp:43-52, 77-86, 128-137 */
+int sa_spmv(sa_ctx ctx, sa_mat A, const void *x, void *y);
+
+/* --------------------------------------------------------- host AMG setup */
+void sa_amg_params_default(sa_amg_params *p);
+/* the hierarchy a dfAMG / intAMGflex constructor builds (host only, no GPU):
+ *                                   Library/preconditioner/INTAMG.hpp:25-84, 149-245 */
+int sa_setup_create(int precision, const sa_amg_params *p, int n, const int32_t *rptr, const int32_t *cind,
+                    const double *val, sa_setup *out);
+int sa_setup_destroy(sa_setup s);
+int sa_setup_depth(sa_setup s);
+int sa_setup_view(sa_setup s, int op, int level, sa_csr_view *out);
+
+/* ------------------------------------------------------------------ AMG */
+/* dfAMG<...>(CSRMat*, SpMat<T>*, AMGParam*) / intAMGflex<...>(CSRMat*, SpMat<int>*, AMGParam*):
+ * host setup + upload.             Library/preconditioner/INTAMG.hpp:25-84, 149-245 */
+int sa_amg_create(sa_ctx ctx, int precision, const sa_amg_params *p, int n, const int32_t *rptr,
+                  const int32_t *cind, const double *val, sa_amg *out);
+int sa_amg_create_from_setup(sa_ctx ctx, sa_setup s, sa_amg *out);
+int sa_amg_destroy(sa_amg M);
+int sa_amg_depth(sa_amg M);
+int sa_amg_precision(sa_amg M);
+/* Preconditioner<T>::Precondition(in, out): one V-cycle
+ *                                   Library/preconditioner/INTAMG.hpp:108-133, 269-293 */
+int sa_amg_precondition(sa_ctx ctx, sa_amg M, const void *in, void *out);
+/* Smoother<T>::Smooth(in, out, isInited) of level l
+ *                                   Library/smoother/stationary.hpp:238-255, 415-430, 997-1012 */
+int sa_amg_smooth(sa_ctx ctx, sa_amg M, int level, const void *in, void *out, int inited);
+/* ldtri::SpMat<T>::SpTRSV of level l's smoother (one Gauss-Seidel sweep)
+ *                                   Library/matrix/trimat/ldtri.hpp:49-58, 172-183, 398-412, 511-525 */
+int sa_amg_sweep(sa_ctx ctx, sa_amg M, int level, const void *in, void *out);
+/* direct::LUflex::Solve / LU<T>::Solve   Library/solver/lu.hpp:30-33, 91-94 */
+int sa_amg_coarse_solve(sa_ctx ctx, sa_amg M, const void *in, void *out);
+/* SpMV with one operator of the hierarchy (SA_OP_A0, _CA, _P, _R, _U) */
+int sa_amg_level_spmv(sa_ctx ctx, sa_amg M, int op, int level, const void *in, void *out);
+/* sizes of an operator; nlev = number of dependency levels of a triangular sweep */
+int sa_amg_level_info(sa_amg M, int op, int level, int *n, int *m, int64_t *nnz, int *bit, int *nlev);
+
+/* --------------------------------------------------------------- solvers */
+void sa_solver_params_default(sa_solver_params *p);
+/* FGMRESflex(A, m, eps, M, bit) / FGMRES<T>(A, m, eps, M) inside Restarted(dA, inner, max, eps)
+ *                                   Library/solver/gmres.hpp:110-129, 192-211, 276-297;
+ *                                   Library/solver/irsolver.hpp:50-57 */
+int sa_solver_create(sa_ctx ctx, int precision, sa_mat dA, sa_mat A, sa_amg M, const sa_solver_params *p,
+                     sa_solver *out);
+int sa_solver_destroy(sa_solver S);
+/* Restarted::Solve(b, nrm_b, x): returns iterations (0 if not converged, as
+ * Converge.iter)                    Library/solver/irsolver.hpp:61-77 */
+int sa_solver_solve(sa_solver S, const double *b, double nrm_b, double *x, int *iters, int *converged);
+/* one inner FGMRES*::Solve(r, nrm_b, x) call.  e0: optional injected norm of r;
+ * dumps: optional host buffers {V, Z, H, c, s, e, y} (integer solver)
+ *                                   Library/solver/gmres.hpp:130-170, 212-252, 307-353 */
+int sa_solver_cycle(sa_solver S, const double *r, double nrm_b, double *x, const double *e0, int *iters,
+                    int *converged, void *const *dumps);
+int sa_solver_set_bits(sa_solver S, int frac_bits);
+int sa_solver_bits(sa_solver S, int *frac_bits);
+/* per-iteration residual estimates and status flags of the last solve */
+int sa_solver_history(sa_solver S, double *hist, int cap, int *n, unsigned *flags);
+
+/* Work/main.cpp:153-161: one FP64 V-cycle on b, F = rule(max|c| / ||b||) */
+int sa_rule_bits(sa_ctx ctx, sa_amg M_f64, const double *b, double nrm_b, int *frac_bits);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

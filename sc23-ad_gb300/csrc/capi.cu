@@ -1,0 +1,862 @@
+// C ABI (include/sagb.h) over the host setup and the CUDA kernels.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+
+#include "../../include/sagb.h"
+#include "cuda/common.cuh"
+#include "host/generators.hpp"
+#include "sagb_internal.hpp"
+
+using namespace sagb;
+
+static thread_local std::string g_err;
+
+static int fail(int code, const std::string &msg) {
+    g_err = msg;
+    return code;
+}
+
+#define SA_GUARD_BEGIN try {
+#define SA_GUARD_END                                                      \
+    }                                                                     \
+    catch (const CudaError &e) {                                          \
+        return fail(SA_ERR_CUDA, e.msg);                                  \
+    }                                                                     \
+    catch (const SetupError &e) {                                         \
+        return fail(SA_ERR_SETUP, e.msg);                                 \
+    }                                                                     \
+    catch (const std::bad_alloc &) {                                      \
+        return fail(SA_ERR_SETUP, "host allocation failed");              \
+    }                                                                     \
+    catch (const std::exception &e) {                                     \
+        return fail(SA_ERR_ARG, e.what());                                \
+    }
+
+struct sa_context {
+    Ctx c;
+};
+struct sa_matrix {
+    sa_context *ctx;
+    DevCsr d;
+    int precision;
+};
+struct sa_hierarchy {
+    int precision = SA_INT;
+    sa_amg_params p{};
+    std::shared_ptr<IntHierarchy> hi;
+    std::shared_ptr<FpHierarchy<double>> hd;
+    std::shared_ptr<FpHierarchy<float>> hf;
+};
+struct sa_multigrid {
+    sa_context *ctx;
+    std::unique_ptr<DevAmg> M;
+    int precision;
+};
+struct sa_krylov {
+    sa_context *ctx;
+    int precision;
+    sa_solver_params p;
+    std::unique_ptr<Solver> S;
+    DevCsr *dA;
+    int N;
+    double *db = nullptr, *dx = nullptr;  // staging for host b / x
+    SolveStats last;
+};
+struct sa_host_csr {
+    CsrD A;
+};
+struct sa_timer {
+    cudaEvent_t e;
+};
+
+// ------------------------------------------------------------------ helpers
+
+static bool is_device_ptr(const void *p) {
+    if (!p) return false;
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+}
+
+// A device view of a caller buffer: device pointers pass through, host
+// buffers are copied in (and, for outputs, back out at the end).
+class Staged {
+  public:
+    Staged(Ctx &c, const void *p, size_t bytes, bool in, bool out) : c_(c), user_(const_cast<void *>(p)),
+                                                                       bytes_(bytes), out_(out) {
+        if (is_device_ptr(p)) {
+            dev_ = user_;
+        } else {
+            own_ = dmalloc(bytes);
+            dev_ = own_;
+            if (in) SAGB_CUDA(cudaMemcpyAsync(dev_, p, bytes, cudaMemcpyHostToDevice, c.stream));
+        }
+    }
+    ~Staged() {
+        if (own_) {
+            cudaStreamSynchronize(c_.stream);
+            dfree(own_);
+        }
+    }
+    void finish() {
+        if (own_ && out_) SAGB_CUDA(cudaMemcpyAsync(user_, dev_, bytes_, cudaMemcpyDeviceToHost, c_.stream));
+        SAGB_CUDA(cudaStreamSynchronize(c_.stream));
+    }
+    void *get() const { return dev_; }
+
+  private:
+    Ctx &c_;
+    void *user_, *dev_ = nullptr, *own_ = nullptr;
+    size_t bytes_;
+    bool out_;
+};
+
+// ---------------------------------------------------------------- library
+
+extern "C" const char *sa_version(void) { return "sagb 0.1 (sm_103a)"; }
+extern "C" const char *sa_last_error(void) { return g_err.c_str(); }
+
+extern "C" int sa_ctx_create(int device, sa_ctx *out) {
+    if (!out) return fail(SA_ERR_ARG, "null output");
+    SA_GUARD_BEGIN
+    int ndev = 0;
+    SAGB_CUDA(cudaGetDeviceCount(&ndev));
+    if (device < 0 || device >= ndev) return fail(SA_ERR_ARG, "no such device");
+    SAGB_CUDA(cudaSetDevice(device));
+    auto *h = new sa_context();
+    h->c.device = device;
+    SAGB_CUDA(cudaDeviceGetAttribute(&h->c.num_sms, cudaDevAttrMultiProcessorCount, device));
+    SAGB_CUDA(cudaStreamCreateWithFlags(&h->c.stream, cudaStreamNonBlocking));
+    h->c.d_flags = (unsigned *)dmalloc(sizeof(unsigned) * 4);
+    SAGB_CUDA(cudaMemset(h->c.d_flags, 0, sizeof(unsigned) * 4));
+    SAGB_CUDA(cudaMallocHost(&h->c.h_flags, sizeof(unsigned) * 4));
+    init_kernel_attributes();
+    *out = h;
+    return SA_OK;
+    SA_GUARD_END
+}
+
+extern "C" int sa_ctx_destroy(sa_ctx ctx) {
+    if (!ctx) return SA_OK;
+    cudaStreamSynchronize(ctx->c.stream);
+    dfree(ctx->c.d_flags);
+    cudaFreeHost(ctx->c.h_flags);
+    cudaStreamDestroy(ctx->c.stream);
+    delete ctx;
+    return SA_OK;
+}
+
+extern "C" int sa_ctx_set_option(sa_ctx ctx, int option, int value) {
+    if (!ctx) return fail(SA_ERR_ARG, "null context");
+    if (option == SA_OPT_FP_EXACT) ctx->c.fp_exact = value != 0;
+    else if (option == SA_OPT_GRAPHS) ctx->c.use_graphs = value != 0;
+    else return fail(SA_ERR_ARG, "unknown option");
+    return SA_OK;
+}
+
+extern "C" int sa_ctx_flags(sa_ctx ctx, unsigned *flags, int clear) {
+    if (!ctx) return fail(SA_ERR_ARG, "null context");
+    SA_GUARD_BEGIN
+    SAGB_CUDA(cudaMemcpyAsync(ctx->c.h_flags, ctx->c.d_flags, sizeof(unsigned), cudaMemcpyDeviceToHost,
+                              ctx->c.stream));
+    SAGB_CUDA(cudaStreamSynchronize(ctx->c.stream));
+    if (flags) *flags = ctx->c.h_flags[0];
+    if (clear) {
+        SAGB_CUDA(cudaMemsetAsync(ctx->c.d_flags, 0, sizeof(unsigned), ctx->c.stream));
+        SAGB_CUDA(cudaStreamSynchronize(ctx->c.stream));
+    }
+    return SA_OK;
+    SA_GUARD_END
+}
+
+extern "C" int sa_ctx_launches(sa_ctx ctx, long long *count) {
+    if (!ctx || !count) return fail(SA_ERR_ARG, "null argument");
+    *count = ctx->c.launches;
+    return SA_OK;
+}
+
+extern "C" int sa_ctx_sync(sa_ctx ctx) {
+    if (!ctx) return fail(SA_ERR_ARG, "null context");
+    SA_GUARD_BEGIN
+    SAGB_CUDA(cudaStreamSynchronize(ctx->c.stream));
+    SAGB_CUDA(cudaGetLastError());
+    return SA_OK;
+    SA_GUARD_END
+}
+
+extern "C" int sa_ctx_stream(sa_ctx ctx, void **stream) {
+    if (!ctx || !stream) return fail(SA_ERR_ARG, "null argument");
+    *stream = (void *)ctx->c.stream;
+    return SA_OK;
+}
+
+extern "C" int sa_device_alloc(sa_ctx ctx, uint64_t bytes, void **ptr) {
+    if (!ctx || !ptr) return fail(SA_ERR_ARG, "null argument");
+    SA_GUARD_BEGIN
+    *ptr = dmalloc(bytes);
+    return SA_OK;
+    SA_GUARD_END
+}
+extern "C" int sa_device_free(sa_ctx ctx, void *ptr) {
+    (void)ctx;
+    dfree(ptr);
+    return SA_OK;
+}
+extern "C" int sa_memcpy(sa_ctx ctx, void *dst, const void *src, uint64_t bytes) {
+    if (!ctx) return fail(SA_ERR_ARG, "null context");
+    SA_GUARD_BEGIN
+    SAGB_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDefault, ctx->c.stream));
+    SAGB_CUDA(cudaStreamSynchronize(ctx->c.stream));
+    return SA_OK;
+    SA_GUARD_END
+}
+extern "C" int sa_event_create(sa_event *out) {
+    if (!out) return fail(SA_ERR_ARG, "null output");
+    SA_GUARD_BEGIN
+    auto *t = new sa_timer();
+    SAGB_CUDA(cudaEventCreate(&t->e));
+    *out = t;
+    return SA_OK;
+    SA_GUARD_END
+}
+extern "C" int sa_event_record(sa_ctx ctx, sa_event ev) {
+    if (!ctx || !ev) return fail(SA_ERR_ARG, "null argument");
+    SA_GUARD_BEGIN
+    SAGB_CUDA(cudaEventRecord(ev->e, ctx->c.stream));
+    return SA_OK;
+    SA_GUARD_END
+}
+extern "C" int sa_event_elapsed_ms(sa_event a, sa_event b, float *ms) {
+    if (!a || !b || !ms) return fail(SA_ERR_ARG, "null argument");
+    SA_GUARD_BEGIN
+    SAGB_CUDA(cudaEventSynchronize(b->e));
+    SAGB_CUDA(cudaEventElapsedTime(ms, a->e, b->e));
+    return SA_OK;
+    SA_GUARD_END
+}
+extern "C" int sa_event_destroy(sa_event ev) {
+    if (ev) {
+        cudaEventDestroy(ev->e);
+        delete ev;
+    }
+    return SA_OK;
+}
+
+// ------------------------------------------------------------ host CSR
+
+extern "C" int sa_hcsr_read_mm(const char *path, sa_hcsr *out) {
+    if (!path || !out) return fail(SA_ERR_ARG, "null argument");
+    SA_GUARD_BEGIN
+    auto *h = new sa_host_csr();
+    h->A = read_matrix_market(path);
+    *out = h;
+    return SA_OK;
+    SA_GUARD_END
+}
+
+static int check_csr(int n, int m, const int32_t *rptr, const int32_t *cind) {
+    if (n < 0 || m < 0 || !rptr || (!cind && n > 0 && rptr[n] > 0)) return fail(SA_ERR_ARG, "invalid CSR");
+    if (rptr[0] != 0) return fail(SA_ERR_ARG, "rptr[0] must be 0");
+    for (int i = 0; i < n; i++) {
+        if (rptr[i + 1] < rptr[i]) return fail(SA_ERR_ARG, "rptr not monotone");
+        for (int j = rptr[i]; j < rptr[i + 1]; j++)
+            if (cind[j] < 0 || cind[j] >= m) return fail(SA_ERR_ARG, "column index out of range");
+    }
+    return SA_OK;
+}
+
+extern "C" int sa_hcsr_create(int n, int m, const int32_t *rptr, const int32_t *cind, const double *val,
+                              sa_hcsr *out) {
+    if (!out) return fail(SA_ERR_ARG, "null output");
+    if (int e = check_csr(n, m, rptr, cind)) return e;
+    SA_GUARD_BEGIN
+    auto *h = new sa_host_csr();
+    h->A.n = n;
+    h->A.m = m;
+    h->A.rptr.assign(rptr, rptr + n + 1);
+    h->A.cind.assign(cind, cind + rptr[n]);
+    h->A.val.assign(val, val + rptr[n]);
+    *out = h;
+    return SA_OK;
+    SA_GUARD_END
+}
+
+extern "C" int sa_hcsr_view(sa_hcsr A, sa_csr_view *out) {
+    if (!A || !out) return fail(SA_ERR_ARG, "null argument");
+    out->n = A->A.n;
+    out->m = A->A.m;
+    out->nnz = A->A.nnz();
+    out->rptr = A->A.rptr.data();
+    out->cind = A->A.cind.data();
+    out->val = A->A.val.data();
+    out->bit = out->dbit = 0;
+    return SA_OK;
+}
+
+extern "C" int sa_hcsr_lmax1_scaling(sa_hcsr A, double *b) {
+    if (!A) return fail(SA_ERR_ARG, "null matrix");
+    lmax1_scaling(A->A, b);
+    return SA_OK;
+}
+
+extern "C" int sa_hcsr_rhs(sa_hcsr A, uint64_t seed, double *xstar, double *b) {
+    if (!A || !xstar || !b) return fail(SA_ERR_ARG, "null argument");
+    gen_rhs(A->A, seed, xstar, b);
+    return SA_OK;
+}
+
+extern "C" int sa_hcsr_destroy(sa_hcsr A) {
+    delete A;
+    return SA_OK;
+}
+
+extern "C" int sa_gen(int kind, int nx, double param, uint64_t seed, sa_hcsr *out) {
+    if (!out || nx <= 0) return fail(SA_ERR_ARG, "invalid argument");
+    SA_GUARD_BEGIN
+    auto *h = new sa_host_csr();
+    switch (kind) {
+        case SA_GEN_POISSON2D: h->A = gen_poisson2d(nx); break;
+        case SA_GEN_POISSON3D: h->A = gen_poisson3d(nx); break;
+        case SA_GEN_ANISO2D: h->A = gen_aniso2d(nx, param); break;
+        case SA_GEN_STENCIL27: h->A = gen_stencil27(nx, seed); break;
+        case SA_GEN_CONVDIFF3D: h->A = gen_convdiff3d(nx, param); break;
+        case SA_GEN_VARCOEF3D: h->A = gen_varcoef3d(nx, param, seed); break;
+        default: delete h; return fail(SA_ERR_ARG, "unknown generator");
+    }
+    *out = h;
+    return SA_OK;
+    SA_GUARD_END
+}
+
+// -------------------------------------------------------------- matrices
+
+extern "C" int sa_mat_create(sa_ctx ctx, int kind, int bit, int n, int m, const int32_t *rptr,
+                             const int32_t *cind, const double *val, sa_mat *out) {
+    if (!ctx || !out) return fail(SA_ERR_ARG, "null argument");
+    if (int e = check_csr(n, m, rptr, cind)) return e;
+    if (kind == SA_MAT_FIXED && (bit < 0 || bit > 30)) return fail(SA_ERR_ARG, "bit must be in [0, 30]");
+    SA_GUARD_BEGIN
+    CsrD A;
+    A.n = n;
+    A.m = m;
+    A.rptr.assign(rptr, rptr + n + 1);
+    A.cind.assign(cind, cind + rptr[n]);
+    A.val.assign(val, val + rptr[n]);
+    auto *h = new sa_matrix();
+    h->ctx = ctx;
+    if (kind == SA_MAT_FIXED || kind == SA_MAT_FLEX) {
+        h->d = upload_csr_i32(kind == SA_MAT_FIXED ? to_fixed(A, bit) : to_flex(A));
+        h->precision = SA_INT;
+    } else if (kind == SA_MAT_F64) {
+        h->d = upload_csr_f64(A);
+        h->precision = SA_F64;
+    } else if (kind == SA_MAT_F32) {
+        CsrT<float> F;
+        F.n = n;
+        F.m = m;
+        F.rptr = A.rptr;
+        F.cind = A.cind;
+        F.val.resize(A.val.size());
+        for (size_t j = 0; j < A.val.size(); j++) F.val[j] = (float)A.val[j];
+        h->d = upload_csr_fp<float>(F);
+        h->precision = SA_F32;
+    } else {
+        delete h;
+        return fail(SA_ERR_ARG, "unknown matrix kind");
+    }
+    *out = h;
+    return SA_OK;
+    SA_GUARD_END
+}
+
+extern "C" int sa_mat_create_i32(sa_ctx ctx, int n, int m, const int32_t *rptr, const int32_t *cind,
+                                 const int32_t *val, int bit, sa_mat *out) {
+    if (!ctx || !out) return fail(SA_ERR_ARG, "null argument");
+    if (int e = check_csr(n, m, rptr, cind)) return e;
+    if (bit < 0 || bit > 62) return fail(SA_ERR_ARG, "bit out of range");
+    SA_GUARD_BEGIN
+    CsrI A;
+    A.n = n;
+    A.m = m;
+    A.bit = bit;
+    A.rptr.assign(rptr, rptr + n + 1);
+    A.cind.assign(cind, cind + rptr[n]);
+    A.val.assign(val, val + rptr[n]);
+    auto *h = new sa_matrix();
+    h->ctx = ctx;
+    h->d = upload_csr_i32(A);
+    h->precision = SA_INT;
+    *out = h;
+    return SA_OK;
+    SA_GUARD_END
+}
+
+extern "C" int sa_mat_destroy(sa_mat A) {
+    if (!A) return SA_OK;
+    A->d.release();
+    delete A;
+    return SA_OK;
+}
+
+extern "C" int sa_mat_info(sa_mat A, int *n, int *m, int64_t *nnz, int *bit, int *precision) {
+    if (!A) return fail(SA_ERR_ARG, "null matrix");
+    if (n) *n = A->d.n;
+    if (m) *m = A->d.m;
+    if (nnz) *nnz = A->d.nnz;
+    if (bit) *bit = A->d.bit;
+    if (precision) *precision = A->precision;
+    return SA_OK;
+}
+
+static size_t esize(int precision) { return precision == SA_F64 ? 8 : 4; }
+
+extern "C" int sa_spmv(sa_ctx ctx, sa_mat A, const void *x, void *y) {
+    if (!ctx || !A || !x || !y) return fail(SA_ERR_ARG, "null argument");
+    SA_GUARD_BEGIN
+    Ctx &c = ctx->c;
+    const size_t es = esize(A->precision);
+    Staged sx(c, x, es * A->d.m, true, false);
+    Staged sy(c, y, es * A->d.n, false, true);
+    spmv(c, A->d, sx.get(), sy.get());
+    sy.finish();
+    SAGB_CUDA(cudaGetLastError());
+    return SA_OK;
+    SA_GUARD_END
+}
+
+// ------------------------------------------------------------ host setup
+
+extern "C" void sa_amg_params_default(sa_amg_params *p) {
+    if (!p) return;
+    p->max_levels = 20;
+    p->theta = 0.8;
+    p->smoother_blocks = 0;
+    p->omega = 1.0;
+    p->smooth_iter = 1;
+}
+
+static void build_setup(sa_hierarchy &s, const CsrD &A) {
+    if (s.p.theta <= 0 || s.p.theta > 1) throw SetupError{"Theta must be in 0 < theta <= 1"};
+    RsChain chain = rs_chain(A, s.p.theta, s.p.max_levels);
+    SmootherSpec sm;
+    sm.block = s.p.smoother_blocks;
+    sm.omega = s.p.omega;
+    sm.iter = s.p.smooth_iter;
+    if (s.precision == SA_INT) s.hi = std::make_shared<IntHierarchy>(build_int_hierarchy(A, chain, sm));
+    else if (s.precision == SA_F64) s.hd = std::make_shared<FpHierarchy<double>>(build_f64_hierarchy(A, chain, sm));
+    else s.hf = std::make_shared<FpHierarchy<float>>(build_f32_hierarchy(A, chain, sm));
+}
+
+extern "C" int sa_setup_create(int precision, const sa_amg_params *p, int n, const int32_t *rptr,
+                               const int32_t *cind, const double *val, sa_setup *out) {
+    if (!out || precision < SA_INT || precision > SA_F32) return fail(SA_ERR_ARG, "invalid argument");
+    if (int e = check_csr(n, n, rptr, cind)) return e;
+    SA_GUARD_BEGIN
+    auto *s = new sa_hierarchy();
+    s->precision = precision;
+    if (p) s->p = *p;
+    else sa_amg_params_default(&s->p);
+    if (s->p.smooth_iter < 1 || s->p.max_levels < 1 || s->p.smoother_blocks < 0) {
+        delete s;
+        return fail(SA_ERR_ARG, "invalid AMG parameters");
+    }
+    CsrD A;
+    A.n = A.m = n;
+    A.rptr.assign(rptr, rptr + n + 1);
+    A.cind.assign(cind, cind + rptr[n]);
+    A.val.assign(val, val + rptr[n]);
+    try {
+        build_setup(*s, A);
+    } catch (...) {
+        delete s;
+        throw;
+    }
+    *out = s;
+    return SA_OK;
+    SA_GUARD_END
+}
+
+extern "C" int sa_setup_destroy(sa_setup s) {
+    delete s;
+    return SA_OK;
+}
+
+extern "C" int sa_setup_depth(sa_setup s) {
+    if (!s) return -1;
+    if (s->hi) return s->hi->depth;
+    if (s->hd) return s->hd->depth;
+    if (s->hf) return s->hf->depth;
+    return -1;
+}
+
+template <typename M>
+static void view_of(const M &a, sa_csr_view *o, int bit, int dbit) {
+    o->n = a.n;
+    o->m = a.m;
+    o->nnz = a.nnz();
+    o->rptr = a.rptr.data();
+    o->cind = a.cind.data();
+    o->val = a.val.data();
+    o->bit = bit;
+    o->dbit = dbit;
+}
+
+template <typename H, typename B>
+static int view_hier(const H &h, int op, int level, sa_csr_view *o, B bits) {
+    const int D = h.depth;
+    auto bad = [&] { return fail(SA_ERR_ARG, "no such operator/level"); };
+    switch (op) {
+        case SA_OP_A0: view_of(h.A0, o, bits(h.A0).first, 0); return SA_OK;
+        case SA_OP_CA: if (level < 0 || level >= D - 1) return bad(); view_of(h.CA[level], o, bits(h.CA[level]).first, 0); return SA_OK;
+        case SA_OP_P: if (level < 0 || level >= D) return bad(); view_of(h.P[level], o, bits(h.P[level]).first, 0); return SA_OK;
+        case SA_OP_R: if (level < 0 || level >= D) return bad(); view_of(h.R[level], o, bits(h.R[level]).first, 0); return SA_OK;
+        case SA_OP_LD: if (level < 0 || level >= D) return bad(); view_of(h.LD[level], o, bits(h.LD[level]).first, bits(h.LD[level]).second); return SA_OK;
+        case SA_OP_U: if (level < 0 || level >= D) return bad(); view_of(h.U[level], o, bits(h.U[level]).first, 0); return SA_OK;
+        case SA_OP_LUL: view_of(h.LUL, o, bits(h.LUL).first, 0); return SA_OK;
+        case SA_OP_LUU: view_of(h.LUU, o, bits(h.LUU).first, bits(h.LUU).second); return SA_OK;
+        case SA_OP_BJ:
+            if (level < 0 || level >= D || h.bj[level].empty()) return bad();
+            o->n = (int)h.bj[level].size() - 1;
+            o->m = 0;
+            o->nnz = 0;
+            o->rptr = h.bj[level].data();
+            o->cind = nullptr;
+            o->val = nullptr;
+            o->bit = o->dbit = 0;
+            return SA_OK;
+    }
+    return bad();
+}
+
+extern "C" int sa_setup_view(sa_setup s, int op, int level, sa_csr_view *out) {
+    if (!s || !out) return fail(SA_ERR_ARG, "null argument");
+    if (s->hi) return view_hier(*s->hi, op, level, out, [](const CsrI &m) { return std::make_pair(m.bit, m.dbit); });
+    auto nob = [](const auto &) { return std::make_pair(0, 0); };
+    if (s->hd) return view_hier(*s->hd, op, level, out, nob);
+    if (s->hf) return view_hier(*s->hf, op, level, out, nob);
+    return fail(SA_ERR_ARG, "empty setup");
+}
+
+// ------------------------------------------------------------------- AMG
+
+extern "C" int sa_amg_create_from_setup(sa_ctx ctx, sa_setup s, sa_amg *out) {
+    if (!ctx || !s || !out) return fail(SA_ERR_ARG, "null argument");
+    SA_GUARD_BEGIN
+    auto *h = new sa_multigrid();
+    h->ctx = ctx;
+    h->precision = s->precision;
+    if (s->hi) h->M = upload_amg_int(ctx->c, s->hi);
+    else if (s->hd) h->M = upload_amg_f64(ctx->c, s->hd);
+    else h->M = upload_amg_f32(ctx->c, s->hf);
+    SAGB_CUDA(cudaDeviceSynchronize());
+    *out = h;
+    return SA_OK;
+    SA_GUARD_END
+}
+
+extern "C" int sa_amg_create(sa_ctx ctx, int precision, const sa_amg_params *p, int n, const int32_t *rptr,
+                             const int32_t *cind, const double *val, sa_amg *out) {
+    if (!ctx) return fail(SA_ERR_ARG, "null context");
+    sa_setup s = nullptr;
+    int e = sa_setup_create(precision, p, n, rptr, cind, val, &s);
+    if (e) return e;
+    e = sa_amg_create_from_setup(ctx, s, out);
+    sa_setup_destroy(s);
+    return e;
+}
+
+extern "C" int sa_amg_destroy(sa_amg M) {
+    if (!M) return SA_OK;
+    cudaStreamSynchronize(M->ctx->c.stream);
+    M->M->release();
+    delete M;
+    return SA_OK;
+}
+
+extern "C" int sa_amg_depth(sa_amg M) { return M ? M->M->depth : -1; }
+extern "C" int sa_amg_precision(sa_amg M) { return M ? M->precision : -1; }
+
+extern "C" int sa_amg_precondition(sa_ctx ctx, sa_amg M, const void *in, void *out) {
+    if (!ctx || !M || !in || !out) return fail(SA_ERR_ARG, "null argument");
+    SA_GUARD_BEGIN
+    Ctx &c = ctx->c;
+    const size_t bytes = esize(M->precision) * M->M->A0.n;
+    Staged si(c, in, bytes, true, false);
+    Staged so(c, out, bytes, false, true);
+    vcycle(c, *M->M, si.get(), so.get());
+    so.finish();
+    SAGB_CUDA(cudaGetLastError());
+    return SA_OK;
+    SA_GUARD_END
+}
+
+static int level_n(sa_amg M, int level) { return M->M->LD[level].n; }
+
+extern "C" int sa_amg_smooth(sa_ctx ctx, sa_amg M, int level, const void *in, void *out, int inited) {
+    if (!ctx || !M || !in || !out) return fail(SA_ERR_ARG, "null argument");
+    if (level < 0 || level >= M->M->depth) return fail(SA_ERR_ARG, "no such level");
+    SA_GUARD_BEGIN
+    Ctx &c = ctx->c;
+    const size_t bytes = esize(M->precision) * level_n(M, level);
+    Staged si(c, in, bytes, true, false);
+    Staged so(c, out, bytes, inited != 0, true);
+    smooth(c, *M->M, level, si.get(), so.get(), inited != 0);
+    so.finish();
+    SAGB_CUDA(cudaGetLastError());
+    return SA_OK;
+    SA_GUARD_END
+}
+
+extern "C" int sa_amg_sweep(sa_ctx ctx, sa_amg M, int level, const void *in, void *out) {
+    if (!ctx || !M || !in || !out) return fail(SA_ERR_ARG, "null argument");
+    if (level < 0 || level >= M->M->depth) return fail(SA_ERR_ARG, "no such level");
+    SA_GUARD_BEGIN
+    Ctx &c = ctx->c;
+    const size_t bytes = esize(M->precision) * level_n(M, level);
+    Staged si(c, in, bytes, true, false);
+    Staged so(c, out, bytes, false, true);
+    trsv(c, M->M->LD[level], si.get(), so.get());
+    so.finish();
+    SAGB_CUDA(cudaGetLastError());
+    return SA_OK;
+    SA_GUARD_END
+}
+
+extern "C" int sa_amg_coarse_solve(sa_ctx ctx, sa_amg M, const void *in, void *out) {
+    if (!ctx || !M || !in || !out) return fail(SA_ERR_ARG, "null argument");
+    SA_GUARD_BEGIN
+    Ctx &c = ctx->c;
+    const size_t bytes = esize(M->precision) * M->M->LU.n;
+    Staged si(c, in, bytes, true, false);
+    Staged so(c, out, bytes, false, true);
+    lu_solve(c, M->M->LU, si.get(), so.get());
+    so.finish();
+    SAGB_CUDA(cudaGetLastError());
+    return SA_OK;
+    SA_GUARD_END
+}
+
+static const DevCsr *level_op(sa_amg M, int op, int level) {
+    DevAmg &A = *M->M;
+    const int D = A.depth;
+    switch (op) {
+        case SA_OP_A0: return &A.A0;
+        case SA_OP_CA: return level >= 0 && level < D - 1 ? &A.CA[level] : nullptr;
+        case SA_OP_P: return level >= 0 && level < D ? &A.P[level] : nullptr;
+        case SA_OP_R: return level >= 0 && level < D ? &A.R[level] : nullptr;
+        case SA_OP_U: return level >= 0 && level < D ? &A.U[level] : nullptr;
+    }
+    return nullptr;
+}
+
+extern "C" int sa_amg_level_spmv(sa_ctx ctx, sa_amg M, int op, int level, const void *in, void *out) {
+    if (!ctx || !M || !in || !out) return fail(SA_ERR_ARG, "null argument");
+    const DevCsr *A = level_op(M, op, level);
+    if (!A) return fail(SA_ERR_ARG, "no such operator/level");
+    SA_GUARD_BEGIN
+    Ctx &c = ctx->c;
+    const size_t es = esize(M->precision);
+    Staged si(c, in, es * A->m, true, false);
+    Staged so(c, out, es * A->n, false, true);
+    spmv(c, *A, si.get(), so.get());
+    so.finish();
+    SAGB_CUDA(cudaGetLastError());
+    return SA_OK;
+    SA_GUARD_END
+}
+
+extern "C" int sa_amg_level_info(sa_amg M, int op, int level, int *n, int *m, int64_t *nnz, int *bit, int *nlev) {
+    if (!M) return fail(SA_ERR_ARG, "null multigrid");
+    DevAmg &A = *M->M;
+    if (op == SA_OP_LD) {
+        if (level < 0 || level >= A.depth) return fail(SA_ERR_ARG, "no such level");
+        const DevTri &T = A.LD[level];
+        if (n) *n = T.n;
+        if (m) *m = T.n;
+        if (nnz) *nnz = T.nnz_off + T.n;
+        if (bit) *bit = T.bit;
+        if (nlev) *nlev = T.nlev;
+        return SA_OK;
+    }
+    if (op == SA_OP_LUL || op == SA_OP_LUU) {
+        if (n) *n = A.LU.n;
+        if (m) *m = A.LU.n;
+        if (nnz) *nnz = (int64_t)A.LU.n * A.LU.n;
+        if (bit) *bit = op == SA_OP_LUL ? A.LU.bitL : A.LU.bitU;
+        if (nlev) *nlev = A.LU.n;
+        return SA_OK;
+    }
+    const DevCsr *D = level_op(M, op, level);
+    if (!D) return fail(SA_ERR_ARG, "no such operator/level");
+    if (n) *n = D->n;
+    if (m) *m = D->m;
+    if (nnz) *nnz = D->nnz;
+    if (bit) *bit = D->bit;
+    if (nlev) *nlev = 0;
+    return SA_OK;
+}
+
+// ----------------------------------------------------------------- solvers
+
+extern "C" void sa_solver_params_default(sa_solver_params *p) {
+    if (!p) return;
+    p->m = 30;
+    p->eps = 1.0e-10;
+    p->max_outer = 1000 / 30;
+    p->frac_bits = 29;
+    p->verbose = 0;
+    p->overflow_fallback = 1;
+}
+
+extern "C" int sa_solver_create(sa_ctx ctx, int precision, sa_mat dA, sa_mat A, sa_amg M, const sa_solver_params *p,
+                                sa_solver *out) {
+    if (!ctx || !dA || !A || !M || !out) return fail(SA_ERR_ARG, "null argument");
+    if (dA->precision != SA_F64) return fail(SA_ERR_ARG, "the refinement operator must be FP64");
+    if (A->precision != precision || M->precision != precision)
+        return fail(SA_ERR_ARG, "operator / preconditioner precision mismatch");
+    if (dA->d.n != A->d.n || A->d.n != M->M->A0.n) return fail(SA_ERR_ARG, "size mismatch");
+    sa_solver_params q;
+    if (p) q = *p;
+    else sa_solver_params_default(&q);
+    if (q.m < 1 || q.m > 64 || q.max_outer < 1 || q.eps <= 0) return fail(SA_ERR_ARG, "invalid solver parameters");
+    if (precision == SA_INT && (q.frac_bits < 1 || q.frac_bits > 30)) return fail(SA_ERR_ARG, "frac_bits must be in [1, 30]");
+    SA_GUARD_BEGIN
+    auto *h = new sa_krylov();
+    h->ctx = ctx;
+    h->precision = precision;
+    h->p = q;
+    h->dA = &dA->d;
+    h->N = dA->d.n;
+    KrylovParams kp;
+    kp.m = q.m;
+    kp.eps = q.eps;
+    kp.max_outer = q.max_outer;
+    kp.bit = q.frac_bits;
+    kp.verbose = q.verbose;
+    kp.fallback = precision == SA_INT ? q.overflow_fallback : 0;
+    h->S = make_solver(ctx->c, precision == SA_INT ? VT_I32 : (precision == SA_F64 ? VT_F64 : VT_F32), &dA->d, &A->d,
+                       M->M.get(), kp);
+    *out = h;
+    return SA_OK;
+    SA_GUARD_END
+}
+
+extern "C" int sa_solver_destroy(sa_solver S) {
+    if (!S) return SA_OK;
+    cudaStreamSynchronize(S->ctx->c.stream);
+    S->S.reset();
+    dfree(S->db);
+    dfree(S->dx);
+    delete S;
+    return SA_OK;
+}
+
+extern "C" int sa_solver_solve(sa_solver S, const double *b, double nrm_b, double *x, int *iters, int *converged) {
+    if (!S || !b || !x) return fail(SA_ERR_ARG, "null argument");
+    SA_GUARD_BEGIN
+    Ctx &c = S->ctx->c;
+    const size_t bytes = sizeof(double) * (size_t)S->N;
+    const double *db = b;
+    double *dx = x;
+    const bool hb = !is_device_ptr(b), hx = !is_device_ptr(x);
+    if (hb) {
+        if (!S->db) S->db = (double *)dmalloc(bytes);
+        SAGB_CUDA(cudaMemcpyAsync(S->db, b, bytes, cudaMemcpyHostToDevice, c.stream));
+        db = S->db;
+    }
+    if (hx) {
+        if (!S->dx) S->dx = (double *)dmalloc(bytes);
+        SAGB_CUDA(cudaMemcpyAsync(S->dx, x, bytes, cudaMemcpyHostToDevice, c.stream));
+        dx = S->dx;
+    }
+    SAGB_CUDA(cudaMemsetAsync(c.d_flags, 0, sizeof(unsigned), c.stream));
+    int it = S->S->solve(db, nrm_b, dx, S->last);
+    if (hx) SAGB_CUDA(cudaMemcpyAsync(x, dx, bytes, cudaMemcpyDeviceToHost, c.stream));
+    SAGB_CUDA(cudaStreamSynchronize(c.stream));
+    SAGB_CUDA(cudaGetLastError());
+    if (iters) *iters = it;
+    if (converged) *converged = S->last.converged;
+    if (S->precision == SA_INT && S->last.final_bit > 0) S->p.frac_bits = S->last.final_bit;
+    if (S->last.flags & ST_TIMEOUT) return fail(SA_ERR_NUMERIC, "device wait timed out");
+    return SA_OK;
+    SA_GUARD_END
+}
+
+extern "C" int sa_solver_cycle(sa_solver S, const double *r, double nrm_b, double *x, const double *e0, int *iters,
+                               int *converged, void *const *dumps) {
+    if (!S || !r || !x) return fail(SA_ERR_ARG, "null argument");
+    SA_GUARD_BEGIN
+    Ctx &c = S->ctx->c;
+    const size_t bytes = sizeof(double) * (size_t)S->N;
+    Staged sr(c, r, bytes, true, false);
+    Staged sx(c, x, bytes, true, true);
+    int conv = 0;
+    SAGB_CUDA(cudaMemsetAsync(c.d_flags, 0, sizeof(unsigned), c.stream));
+    int it = S->S->cycle((const double *)sr.get(), nrm_b, (double *)sx.get(), e0, &conv, dumps);
+    if (it < 0) {
+        sx.finish();
+        if (iters) *iters = 0;
+        if (converged) *converged = 0;
+        return fail(SA_ERR_NUMERIC, "integer overflow in the cycle (lower frac_bits)");
+    }
+    sx.finish();
+    SAGB_CUDA(cudaGetLastError());
+    if (iters) *iters = it;
+    if (converged) *converged = conv;
+    return SA_OK;
+    SA_GUARD_END
+}
+
+extern "C" int sa_solver_set_bits(sa_solver S, int bits) {
+    if (!S) return fail(SA_ERR_ARG, "null solver");
+    if (S->precision != SA_INT) return fail(SA_ERR_ARG, "only the integer solver has fractional bits");
+    if (bits < 1 || bits > 30) return fail(SA_ERR_ARG, "frac_bits must be in [1, 30]");
+    S->p.frac_bits = bits;
+    S->S->set_bit(bits);
+    return SA_OK;
+}
+
+extern "C" int sa_solver_bits(sa_solver S, int *bits) {
+    if (!S || !bits) return fail(SA_ERR_ARG, "null argument");
+    *bits = S->p.frac_bits;
+    return SA_OK;
+}
+
+extern "C" int sa_solver_history(sa_solver S, double *hist, int cap, int *n, unsigned *flags) {
+    if (!S) return fail(SA_ERR_ARG, "null solver");
+    const int k = (int)S->last.history.size();
+    if (n) *n = k;
+    if (flags) *flags = S->last.flags;
+    if (hist)
+        for (int i = 0; i < k && i < cap; i++) hist[i] = S->last.history[i];
+    return SA_OK;
+}
+
+extern "C" int sa_rule_bits(sa_ctx ctx, sa_amg M, const double *b, double nrm_b, int *bits) {
+    if (!ctx || !M || !b || !bits) return fail(SA_ERR_ARG, "null argument");
+    if (M->precision != SA_F64) return fail(SA_ERR_ARG, "the bit rule uses the FP64 preconditioner");
+    SA_GUARD_BEGIN
+    Ctx &c = ctx->c;
+    const int N = M->M->A0.n;
+    std::vector<double> ch(N);
+    Staged sb(c, b, sizeof(double) * N, true, false);
+    double *dc = (double *)dmalloc(sizeof(double) * N);
+    vcycle(c, *M->M, sb.get(), dc);
+    SAGB_CUDA(cudaMemcpyAsync(ch.data(), dc, sizeof(double) * N, cudaMemcpyDeviceToHost, c.stream));
+    SAGB_CUDA(cudaStreamSynchronize(c.stream));
+    dfree(dc);
+    double cmax = 0;
+    for (int i = 0; i < N; i++)
+        if (std::fabs(ch[i]) > cmax) cmax = std::fabs(ch[i]);
+    *bits = rule_frac_bits(cmax, nrm_b);
+    return SA_OK;
+    SA_GUARD_END
+}

@@ -1,0 +1,768 @@
+// Host AMG setup (see amg_setup.hpp).  Reference paths are relative to the
+// suzuki-hpc/SC23-AD tree.  The algorithms are restated step for step where the
+// result depends on the order of operations (tie breaking in the coarsening,
+// FP summation order); the data structures are our own (dense accumulators in
+// place of the reference's realloc-per-column sparse vectors).
+#include "amg_setup.hpp"
+#include "sort.hpp"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <numeric>
+#include <utility>
+
+namespace sagb {
+
+// ============================================================ conversion rules
+
+int ceil_log2_int(int64_t k) {
+    if (k <= 1) return 0;
+    int b = 0;
+    uint64_t v = (uint64_t)(k - 1);
+    while (v) { b++; v >>= 1; }
+    return b;
+}
+
+static int32_t cvtt_i32(double v) {  // x86 cvttsd2si: truncate, INT_MIN if out of range / NaN
+    if (!(v > -2147483649.0 && v < 2147483648.0)) return INT32_MIN;
+    return (int32_t)v;
+}
+
+int flex_bit(double max) {
+    if (max < 1) return 30;
+    return 32 - (ceil_log2_int((int64_t)cvtt_i32(max) + 1) + 1);
+}
+
+int while_bit(double max) {
+    int bit = 0;
+    while (bit < 30 && max * (double)(1 << bit) < (double)(1 << 30)) bit++;
+    return bit;
+}
+
+int32_t quantize(double v, int bit) { return cvtt_i32(v * (double)(1 << bit)); }
+
+int rule_frac_bits(double c_max, double nrm_b) {
+    double q = c_max / nrm_b;
+    if (q < 1) return 29;
+    return 31 - (ceil_log2_int((int64_t)cvtt_i32(q) + 1) + 1);
+}
+
+// =============================================================== preprocessing
+
+void lmax1_scaling(CsrD &A, double *b) {
+    for (int i = 0; i < A.n; i++) {
+        double mx = 0;
+        for (int j = A.rptr[i]; j < A.rptr[i + 1]; j++)
+            if (std::fabs(A.val[j]) > mx) mx = std::fabs(A.val[j]);
+        for (int j = A.rptr[i]; j < A.rptr[i + 1]; j++) A.val[j] /= mx;
+        if (b) b[i] /= mx;
+    }
+}
+
+// ======================================================= Ruge-Stueben coarsening
+
+struct Pattern {  // CSR without values
+    int n = 0;
+    std::vector<int> rptr, cind;
+};
+
+// get_strong_weak_set (helper_multigrid.hpp:67-108): off-diagonal a_ij is strong
+// when |a_ij| >= theta * max_k!=i |a_ik|; everything else (diagonal included)
+// goes to the weak set.
+static void strong_weak(const CsrD &A, double theta, CsrD &S, CsrD &W) {
+    const int N = A.n;
+    S.n = W.n = S.m = W.m = N;
+    S.rptr.assign(N + 1, 0);
+    W.rptr.assign(N + 1, 0);
+    S.cind.clear(); S.val.clear(); W.cind.clear(); W.val.clear();
+    S.cind.reserve(A.nnz()); S.val.reserve(A.nnz());
+    W.cind.reserve(A.nnz()); W.val.reserve(A.nnz());
+    for (int i = 0; i < N; i++) {
+        double mx = 0;
+        for (int j = A.rptr[i]; j < A.rptr[i + 1]; j++)
+            if (A.cind[j] != i && std::fabs(A.val[j]) > mx) mx = std::fabs(A.val[j]);
+        const double thr = theta * mx;
+        for (int j = A.rptr[i]; j < A.rptr[i + 1]; j++) {
+            if (A.cind[j] != i && std::fabs(A.val[j]) >= thr) {
+                S.cind.push_back(A.cind[j]); S.val.push_back(A.val[j]);
+            } else {
+                W.cind.push_back(A.cind[j]); W.val.push_back(A.val[j]);
+            }
+        }
+        S.rptr[i + 1] = (int)S.cind.size();
+        W.rptr[i + 1] = (int)W.cind.size();
+    }
+}
+
+// get_influence_set (helper_multigrid.hpp:110-136): transpose of the pattern.
+static Pattern transpose_pattern(const CsrD &S) {
+    Pattern T;
+    const int N = S.n;
+    T.n = N;
+    T.rptr.assign(N + 1, 0);
+    for (int c : S.cind) T.rptr[c + 1]++;
+    for (int i = 0; i < N; i++) T.rptr[i + 1] += T.rptr[i];
+    T.cind.resize(S.cind.size());
+    std::vector<int> fill(T.rptr.begin(), T.rptr.end() - 1);
+    for (int i = 0; i < N; i++)
+        for (int j = S.rptr[i]; j < S.rptr[i + 1]; j++) T.cind[fill[S.cind[j]]++] = i;
+    return T;
+}
+
+// first_pass (helper_multigrid.hpp:138-266): greedy C/F selection by the number
+// of points a candidate strongly influences, kept in buckets that are updated
+// in place as points are classified.
+static void first_pass(const CsrD &S, const Pattern &St, std::vector<int> &is_coarse) {
+    const int N = S.n;
+    is_coarse.assign(N, 0);
+    std::vector<int> visited(N, 0), card(N), scard(N), infl(N, 0), index(N), where(N, 0);
+    for (int i = 0; i < N; i++) {
+        card[i] = St.rptr[i + 1] - St.rptr[i];
+        scard[i] = S.rptr[i + 1] - S.rptr[i];
+        index[i] = i;
+        if (card[i] == 0 && scard[i] == 0) {
+            is_coarse[i] = 0;
+            visited[i] = 1;
+        } else {
+            is_coarse[i] = -38;  // unclassified marker checked by second_pass
+        }
+        for (int j = St.rptr[i]; j < St.rptr[i + 1]; j++) {
+            int k = St.cind[j];
+            infl[i] += S.rptr[k + 1] - S.rptr[k];
+        }
+    }
+    if (N > 0) hoare_sort(0, N - 1, false, card.data(), scard.data(), infl.data(), index.data());
+
+    int maxc = N > 0 ? card[0] : 0;
+    // bptr[c] = number of entries whose count is >= c (entries are sorted by
+    // decreasing count, so bucket c occupies [bptr[c+1], bptr[c])).
+    std::vector<int> bptr(maxc + 2);
+    bptr[maxc + 1] = 0;
+    int start = 0;
+    for (int c = maxc; c >= 0; c--) {
+        int num = 0;
+        bool cut = false;
+        for (int j = start; j < N; j++) {
+            if (card[j] == c) {
+                num++;
+            } else {
+                bptr[c] = bptr[c + 1] + num;
+                start = j;
+                cut = true;
+                break;
+            }
+        }
+        if (cut) continue;
+        bptr[c] = bptr[c + 1] + num;
+    }
+    for (int c = maxc; c >= 0; c--)
+        if (bptr[c] - bptr[c + 1] > 1) hoare_sort(bptr[c + 1], bptr[c] - 1, true, infl.data(), index.data());
+
+    for (int i = 0; i < N; i++) where[index[i]] = i;
+    auto exchange = [&](int a, int b) {
+        std::swap(card[a], card[b]);
+        std::swap(index[a], index[b]);
+        std::swap(where[index[a]], where[index[b]]);
+    };
+    int pos = 0;
+    while (pos < N) {
+        while (pos < N && visited[index[pos]]) pos++;
+        if (pos >= N) break;
+        const int cpt = index[pos];
+        visited[cpt] = 1;
+        is_coarse[cpt] = 1;
+        for (int t = St.rptr[cpt]; t < St.rptr[cpt + 1]; t++) {
+            const int f = St.cind[t];
+            if (visited[f]) continue;
+            visited[f] = 1;
+            is_coarse[f] = 0;
+            for (int u = S.rptr[f]; u < S.rptr[f + 1]; u++) {
+                const int k = S.cind[u];
+                if (visited[k]) continue;
+                const int idx = where[k];
+                if (idx <= pos) printf("Warning 1: %d %d\n", idx, pos);
+                card[idx]++;
+                const int v = card[idx];
+                int obj;
+                if (v > maxc) {
+                    maxc = v;
+                    if (bptr[v] > pos + 1) printf("Warning 2: %d %d\n", bptr[v], pos + 1);
+                    obj = pos + 1;
+                    bptr.push_back(pos + 1);
+                    bptr[maxc] = pos + 2;
+                } else if (bptr[v] > pos + 1) {
+                    obj = bptr[v];
+                    bptr[v] += 1;
+                } else {
+                    obj = pos + 1;
+                    bptr[v] = pos + 2;
+                }
+                exchange(idx, obj);
+            }
+        }
+        for (int u = S.rptr[cpt]; u < S.rptr[cpt + 1]; u++) {
+            const int k = S.cind[u];
+            if (visited[k]) continue;
+            const int idx = where[k];
+            if (card[idx] == 0) continue;
+            card[idx]--;
+            const int obj = bptr[card[idx] + 1] - 1;
+            bptr[card[idx] + 1] -= 1;
+            exchange(idx, obj);
+        }
+        pos++;
+    }
+}
+
+// second_pass (helper_multigrid.hpp:378-417): a fine point with a strong fine
+// neighbour that shares no strong coarse point with it becomes coarse.
+static void second_pass(const CsrD &S, std::vector<int> &is_coarse) {
+    const int N = S.n;
+    for (int i = 0; i < N; i++) {
+        if (is_coarse[i] == -38) {
+            fprintf(stderr, "sagb: unclassified point in the coarsening\n");
+            exit(1);  // the reference exits here as well (helper_multigrid.hpp:384)
+        }
+        if (is_coarse[i]) continue;
+        for (int j = S.rptr[i]; j < S.rptr[i + 1]; j++) {
+            const int f = S.cind[j];
+            if (is_coarse[f]) continue;
+            bool shared = false;
+            int a = S.rptr[i], b = S.rptr[f];
+            while (a < S.rptr[i + 1] && b < S.rptr[f + 1]) {
+                if (S.cind[b] < S.cind[a]) {
+                    b++;
+                } else if (S.cind[b] == S.cind[a]) {
+                    if (is_coarse[S.cind[a]]) { shared = true; break; }
+                    a++; b++;
+                } else {
+                    a++;
+                }
+            }
+            if (shared) continue;
+            is_coarse[i] = 1;
+            break;
+        }
+    }
+}
+
+// sepalate_strong_to_coarse_fine + get_interpolation_matrix
+// (helper_multigrid.hpp:419-532): direct interpolation
+//   w_ij = -(a_ij + sum_m a_im a_mj / sum_{k in C_i} a_mk) / sum(weak row i)
+// with the sum over strong fine neighbours m in row order.
+static CsrD interpolation(const CsrD &A, const CsrD &S, const CsrD &W, const std::vector<int> &is_coarse) {
+    const int N = A.n;
+    std::vector<int> col(N, -1);
+    int nc = 0;
+    for (int i = 0; i < N; i++)
+        if (is_coarse[i]) col[i] = nc++;
+    CsrD P;
+    P.n = N;
+    P.m = nc;
+    P.rptr.assign(N + 1, 0);
+    // strong connections split by the class of the column
+    std::vector<int> cs, cf;        // column lists of C_Stg row i / DS_Stg row i
+    std::vector<double> vs, vf;
+    std::vector<double> amk_m, amj;
+    for (int i = 0; i < N; i++) {
+        if (is_coarse[i]) {
+            P.cind.push_back(col[i]);
+            P.val.push_back(1);
+            P.rptr[i + 1] = (int)P.cind.size();
+            continue;
+        }
+        cs.clear(); vs.clear(); cf.clear(); vf.clear();
+        for (int j = S.rptr[i]; j < S.rptr[i + 1]; j++) {
+            if (is_coarse[S.cind[j]]) { cs.push_back(S.cind[j]); vs.push_back(S.val[j]); }
+            else { cf.push_back(S.cind[j]); vf.push_back(S.val[j]); }
+        }
+        double deno = 0;
+        for (int j = W.rptr[i]; j < W.rptr[i + 1]; j++) deno += W.val[j];
+        const int ncs = (int)cs.size(), ncf = (int)cf.size();
+        // sum_{k in C_i} a_mk for each strong fine m (merge in column order),
+        // and a_mj for each (m, j) pair
+        amk_m.assign(ncf, 0.0);
+        amj.assign((size_t)ncf * ncs, 0.0);
+        for (int q = 0; q < ncf && ncs > 0; q++) {
+            const int mrow = cf[q];
+            double amk = 0;
+            bool hit = false;
+            int a = A.rptr[mrow], k = 0;
+            while (a < A.rptr[mrow + 1] && k < ncs) {
+                if (A.cind[a] < cs[k]) {
+                    a++;
+                } else if (A.cind[a] == cs[k]) {
+                    amk += A.val[a];
+                    amj[(size_t)q * ncs + k] = A.val[a];
+                    hit = true;
+                    a++; k++;
+                } else {
+                    k++;
+                }
+            }
+            if (amk == 0) {
+                if (hit) {
+                    for (int k = 0; k < ncs; k++) printf("1 amk = 0\n");  // once per (j, m) pair
+                    amk = 0.00001;
+                } else {
+                    printf("2 amk = 0\n");
+                    exit(1);  // as the reference (helper_multigrid.hpp:518)
+                }
+            }
+            amk_m[q] = amk;
+        }
+        for (int k = 0; k < ncs; k++) {
+            double aij = vs[k];
+            for (int q = 0; q < ncf; q++) aij += vf[q] * amj[(size_t)q * ncs + k] / amk_m[q];
+            P.cind.push_back(col[cs[k]]);
+            P.val.push_back(-aij / deno);
+        }
+        P.rptr[i + 1] = (int)P.cind.size();
+    }
+    return P;
+}
+
+// transpose_interpolation_matrix (helper_multigrid.hpp:534-562)
+static CsrD transpose(const CsrD &P) {
+    CsrD R;
+    R.n = P.m;
+    R.m = P.n;
+    R.rptr.assign(R.n + 1, 0);
+    for (int c : P.cind) R.rptr[c + 1]++;
+    for (int i = 0; i < R.n; i++) R.rptr[i + 1] += R.rptr[i];
+    R.cind.resize(P.cind.size());
+    R.val.resize(P.val.size());
+    std::vector<int> fill(R.rptr.begin(), R.rptr.end() - 1);
+    for (int i = 0; i < P.n; i++)
+        for (int j = P.rptr[i]; j < P.rptr[i + 1]; j++) {
+            int p = fill[P.cind[j]]++;
+            R.cind[p] = i;
+            R.val[p] = P.val[j];
+        }
+    return R;
+}
+
+// helper::sparse::cscSpMM (helper_sparse.hpp:257-285) with the left and right
+// operands given as compressed columns: column i of the result accumulates
+// alpha_k * left[:, r_k] over the entries (r_k, alpha_k) of right[:, i] in
+// order; each entry is updated as y + alpha*x, and an entry that becomes exactly
+// zero is removed (and restarts from alpha*x if hit again, which is the same as
+// adding to 0.0).  A dense accumulator gives the same values; the touched rows
+// are emitted in increasing order, as the merge-based original does.
+static void csc_product(const std::vector<int> &lp, const std::vector<int> &li, const std::vector<double> &lv,
+                        int L, const std::vector<int> &rp, const std::vector<int> &ri, const std::vector<double> &rv,
+                        int R, std::vector<int> &op, std::vector<int> &oi, std::vector<double> &ov) {
+    std::vector<double> acc(L, 0.0);
+    std::vector<int> stamp(L, -1);
+    std::vector<int> touched;
+    op.assign(R + 1, 0);
+    oi.clear();
+    ov.clear();
+    for (int c = 0; c < R; c++) {
+        touched.clear();
+        for (int k = rp[c]; k < rp[c + 1]; k++) {
+            const int src = ri[k];
+            const double alpha = rv[k];
+            for (int t = lp[src]; t < lp[src + 1]; t++) {
+                const int row = li[t];
+                if (stamp[row] != c) {
+                    stamp[row] = c;
+                    acc[row] = 0.0;
+                    touched.push_back(row);
+                }
+                acc[row] = acc[row] + alpha * lv[t];
+            }
+        }
+        std::sort(touched.begin(), touched.end());
+        for (int row : touched) {
+            if (std::fabs(acc[row]) == 0.0) continue;
+            oi.push_back(row);
+            ov.push_back(acc[row]);
+        }
+        op[c + 1] = (int)oi.size();
+    }
+}
+
+// get_coarse_matrix (helper_multigrid.hpp:564-586): the reference passes CSR
+// arrays where compressed columns are expected, so the first product forms
+// T = A^T P and the second P^T T; read back as CSR this is C = P^T A P.
+static CsrD galerkin(const CsrD &A, const CsrD &P, const CsrD &R) {
+    std::vector<int> tp, ti, cp, ci;
+    std::vector<double> tv, cv;
+    csc_product(A.rptr, A.cind, A.val, A.n, R.rptr, R.cind, R.val, P.m, tp, ti, tv);
+    csc_product(P.rptr, P.cind, P.val, P.m, tp, ti, tv, P.m, cp, ci, cv);
+    CsrD C;
+    C.n = C.m = P.m;
+    C.rptr = std::move(cp);
+    C.cind = std::move(ci);
+    C.val = std::move(cv);
+    return C;
+}
+
+void rs_level(const CsrD &A, double theta, CsrD &CA, CsrD &P, CsrD &R) {
+    if (theta <= 0 || 1 < theta) {
+        printf("Error: Theta must be in 0 < theta <= 1\n");
+        exit(EXIT_FAILURE);
+    }
+    CsrD S, W;
+    strong_weak(A, theta, S, W);
+    Pattern St = transpose_pattern(S);
+    std::vector<int> is_coarse;
+    first_pass(S, St, is_coarse);
+    second_pass(S, is_coarse);
+    P = interpolation(A, S, W, is_coarse);
+    R = transpose(P);
+    CA = galerkin(A, P, R);
+}
+
+RsChain rs_chain(const CsrD &A, double theta, int max_levels) {
+    RsChain ch;
+    ch.CA.emplace_back();
+    ch.P.emplace_back();
+    ch.R.emplace_back();
+    rs_level(A, theta, ch.CA[0], ch.P[0], ch.R[0]);
+    int depth = 1;
+    while (max_levels > depth && ch.CA[depth - 1].n > 2000) {
+        depth++;
+        CsrD ca, p, r;
+        rs_level(ch.CA[depth - 2], theta, ca, p, r);
+        ch.CA.push_back(std::move(ca));
+        ch.P.push_back(std::move(p));
+        ch.R.push_back(std::move(r));
+    }
+    return ch;
+}
+
+// ============================================================= smoother splits
+
+void sor_split(const CsrD &A, double omega, CsrD &LD, CsrD &U) {
+    const int N = A.n;
+    LD.n = LD.m = U.n = U.m = N;
+    LD.rptr.assign(N + 1, 0);
+    U.rptr.assign(N + 1, 0);
+    LD.cind.clear(); LD.val.clear(); U.cind.clear(); U.val.clear();
+    for (int i = 0; i < N; i++) {
+        // split "LD-U" (helper_matrix.hpp:530-604): cind <= i to LD in row order
+        int last_ld = -1;
+        for (int j = A.rptr[i]; j < A.rptr[i + 1]; j++)
+            if (A.cind[j] <= i) {
+                LD.cind.push_back(A.cind[j]);
+                LD.val.push_back(A.val[j]);
+                last_ld = (int)LD.val.size() - 1;
+            }
+        // the last LD entry of the row is taken as the diagonal
+        // (stationary.hpp:209-217): U gets (1 - 1/omega) d first, LD keeps d / omega
+        const double d = last_ld >= 0 ? LD.val[last_ld] : 0.0;
+        const int dcol = last_ld >= 0 ? LD.cind[last_ld] : 0;
+        U.cind.push_back(dcol);
+        U.val.push_back((1 - 1.0 / omega) * d);
+        if (last_ld >= 0) LD.val[last_ld] = 1.0 / omega * d;
+        for (int j = A.rptr[i]; j < A.rptr[i + 1]; j++)
+            if (A.cind[j] > i) {
+                U.cind.push_back(A.cind[j]);
+                U.val.push_back(A.val[j]);
+            }
+        LD.rptr[i + 1] = (int)LD.cind.size();
+        U.rptr[i + 1] = (int)U.cind.size();
+    }
+}
+
+void block_sor_split(const CsrD &A, double omega, int nb, CsrD &LD, CsrD &U, std::vector<int> &bj) {
+    const int N = A.n;
+    const int size = (N + nb - 1) / nb;
+    bj.assign(nb + 1, 0);
+    for (int b = 0; b < nb; b++) bj[b + 1] = bj[b] + size;
+    bj[nb] = N;
+    LD.n = LD.m = U.n = U.m = N;
+    LD.rptr.assign(N + 1, 0);
+    U.rptr.assign(N + 1, 0);
+    LD.cind.clear(); LD.val.clear(); U.cind.clear(); U.val.clear();
+    for (int i = 0; i < N; i++) {
+        const int left = bj[i / size];
+        for (int j = A.rptr[i]; j < A.rptr[i + 1]; j++) {
+            const int c = A.cind[j];
+            if (c == i) {
+                LD.cind.push_back(c); LD.val.push_back((1.0 / omega) * A.val[j]);
+                U.cind.push_back(c); U.val.push_back((1 - 1.0 / omega) * A.val[j]);
+            } else if (left <= c && c < i) {
+                LD.cind.push_back(c); LD.val.push_back(A.val[j]);
+            } else {
+                U.cind.push_back(c); U.val.push_back(A.val[j]);
+            }
+        }
+        LD.rptr[i + 1] = (int)LD.cind.size();
+        U.rptr[i + 1] = (int)U.cind.size();
+    }
+}
+
+static CsrD filter_rows(const CsrD &A, int mode) {  // 0: LDinv, 1: L, 2: DinvU
+    CsrD B;
+    B.n = A.n;
+    B.m = A.m;
+    B.rptr.assign(A.n + 1, 0);
+    for (int i = 0; i < A.n; i++) {
+        for (int j = A.rptr[i]; j < A.rptr[i + 1]; j++) {
+            const int c = A.cind[j];
+            if (c == i && mode != 1) {
+                B.cind.push_back(c); B.val.push_back(1 / A.val[j]);
+            } else if ((mode == 0 || mode == 1) && c < i) {
+                B.cind.push_back(c); B.val.push_back(A.val[j]);
+            } else if (mode == 2 && c > i) {
+                B.cind.push_back(c); B.val.push_back(A.val[j]);
+            }
+        }
+        B.rptr[i + 1] = (int)B.cind.size();
+    }
+    return B;
+}
+CsrD extract_ldinv(const CsrD &A) { return filter_rows(A, 0); }
+CsrD extract_l(const CsrD &A) { return filter_rows(A, 1); }
+CsrD extract_dinvu(const CsrD &A) { return filter_rows(A, 2); }
+
+// helper::matrix::ilu (helper_matrix.hpp:978-1061), row by row with a dense
+// work row: columns are eliminated in increasing order; an existing entry
+// becomes a - pivot*u, a fill-in entry (-pivot)*u; no entry is dropped.  A row
+// without a stored diagonal keeps the previous pivot, as the original does.
+CsrD ilu_full(const CsrD &A) {
+    const int N = A.n;
+    CsrD F;
+    F.n = F.m = N;
+    F.rptr.assign(N + 1, 0);
+    if (N == 0) return F;
+    std::vector<double> w(N, 0.0);
+    std::vector<char> nz(N, 0);
+    std::vector<int> diagpos(N, -1);
+    for (int j = A.rptr[0]; j < A.rptr[1]; j++) {
+        F.cind.push_back(A.cind[j]);
+        F.val.push_back(A.val[j]);
+        if (A.cind[j] == 0) diagpos[0] = j - A.rptr[0];
+    }
+    F.rptr[1] = (int)F.cind.size();
+    double pivot = 0;
+    for (int i = 1; i < N; i++) {
+        int lo = N;
+        for (int j = A.rptr[i]; j < A.rptr[i + 1]; j++) {
+            const int c = A.cind[j];
+            w[c] = A.val[j];
+            nz[c] = 1;
+            lo = std::min(lo, c);
+        }
+        for (int k = lo; k < i; k++) {
+            if (!nz[k]) continue;
+            const int rs = F.rptr[k], re = F.rptr[k + 1];
+            int dj = diagpos[k] >= 0 ? rs + diagpos[k] : -1;
+            if (dj >= 0) pivot = w[k] / F.val[dj];
+            w[k] = pivot;
+            if (dj < 0) continue;
+            for (int t = dj + 1; t < re; t++) {
+                const int c = F.cind[t];
+                if (nz[c]) {
+                    w[c] = w[c] - pivot * F.val[t];
+                } else {
+                    nz[c] = 1;
+                    w[c] = -pivot * F.val[t];
+                }
+            }
+        }
+        const int base = (int)F.cind.size();
+        for (int c = lo; c < N; c++) {
+            if (!nz[c]) continue;
+            if (c == i) diagpos[i] = (int)F.cind.size() - base;
+            F.cind.push_back(c);
+            F.val.push_back(w[c]);
+            nz[c] = 0;
+            w[c] = 0.0;
+        }
+        F.rptr[i + 1] = (int)F.cind.size();
+    }
+    return F;
+}
+
+// ================================================================ quantisation
+
+static CsrI shell_of(const CsrD &A) {
+    CsrI B;
+    B.n = A.n;
+    B.m = A.m;
+    B.rptr = A.rptr;
+    B.cind = A.cind;
+    B.val.resize(A.val.size());
+    return B;
+}
+
+CsrI to_fixed(const CsrD &A, int bit) {
+    CsrI B = shell_of(A);
+    const double fact = (double)(1 << bit);
+    for (size_t j = 0; j < A.val.size(); j++) B.val[j] = cvtt_i32(A.val[j] * fact);
+    B.bit = bit;
+    return B;
+}
+
+CsrI to_flex(const CsrD &A) {
+    double mx = 0;
+    for (double v : A.val)
+        if (std::fabs(v) > mx) mx = std::fabs(v);
+    CsrI B = shell_of(A);
+    B.bit = flex_bit(mx);
+    for (size_t j = 0; j < A.val.size(); j++) B.val[j] = quantize(A.val[j], B.bit);
+    return B;
+}
+
+static void diag_offdiag_max(const CsrD &A, double &mx, double &dmx) {
+    mx = 0;
+    dmx = 0;
+    for (int i = 0; i < A.n; i++)
+        for (int j = A.rptr[i]; j < A.rptr[i + 1]; j++) {
+            const double a = std::fabs(A.val[j]);
+            if (A.cind[j] == i) {
+                if (a > dmx) dmx = a;
+            } else if (a > mx) {
+                mx = a;
+            }
+        }
+}
+
+static CsrI quantize_split(const CsrD &A, int bit, int dbit) {
+    CsrI B = shell_of(A);
+    B.bit = bit;
+    B.dbit = dbit;
+    for (int i = 0; i < A.n; i++)
+        for (int j = A.rptr[i]; j < A.rptr[i + 1]; j++)
+            B.val[j] = quantize(A.val[j], A.cind[j] == i ? dbit : bit);
+    return B;
+}
+
+CsrI to_ldtri_flex(const CsrD &LDinv) {
+    double mx, dmx;
+    diag_offdiag_max(LDinv, mx, dmx);
+    return quantize_split(LDinv, flex_bit(mx), flex_bit(dmx));
+}
+
+CsrI to_ltri_flex(const CsrD &L) {
+    double mx = 0;
+    for (double v : L.val)
+        if (std::fabs(v) > mx) mx = std::fabs(v);
+    CsrI B = shell_of(L);
+    B.bit = while_bit(mx);
+    for (size_t j = 0; j < L.val.size(); j++) B.val[j] = quantize(L.val[j], B.bit);
+    return B;
+}
+
+CsrI to_dutri_flex(const CsrD &DinvU) {
+    double mx, dmx;
+    diag_offdiag_max(DinvU, mx, dmx);
+    return quantize_split(DinvU, while_bit(mx), while_bit(dmx));
+}
+
+// ================================================================= hierarchies
+
+static void smoother_split(const CsrD &A, const SmootherSpec &sm, CsrD &LD, CsrD &U, std::vector<int> &bj) {
+    if (sm.block > 0) {
+        block_sor_split(A, sm.omega, sm.block, LD, U, bj);
+    } else {
+        sor_split(A, sm.omega, LD, U);
+        bj.clear();
+    }
+}
+
+IntHierarchy build_int_hierarchy(const CsrD &A, const RsChain &chain, const SmootherSpec &sm) {
+    IntHierarchy h;
+    const int D = chain.depth();
+    h.depth = D;
+    h.smooth_iter = sm.iter;
+    h.A0 = to_fixed(A, 30);
+    // row scaling of the coarse operators and restrictions (INTAMG.hpp:165-211)
+    std::vector<CsrD> CA = chain.CA, It = chain.R;
+    std::vector<double> prev(A.n, 0.0), mx;
+    auto scale_level = [&](int t, bool use_prev) {
+        CsrD &C = CA[t];
+        CsrD &R = It[t];
+        mx.assign(C.n, 0.0);
+        for (int i = 0; i < C.n; i++) {
+            for (int j = C.rptr[i]; j < C.rptr[i + 1]; j++)
+                if (std::abs(C.val[j]) > mx[i]) mx[i] = std::abs(C.val[j]);
+            for (int j = C.rptr[i]; j < C.rptr[i + 1]; j++) C.val[j] /= mx[i];
+            for (int j = R.rptr[i]; j < R.rptr[i + 1]; j++) R.val[j] /= mx[i];
+            if (!use_prev) continue;
+            for (int j = R.rptr[i]; j < R.rptr[i + 1]; j++) R.val[j] *= prev[R.cind[j]];
+        }
+    };
+    for (int d = 2; d <= D; d++) {
+        scale_level(d - 2, d != 2);
+        std::copy(mx.begin(), mx.end(), prev.begin());
+    }
+    // the coarsest level always multiplies by prev; with a single coarse level
+    // prev is still all zero, so the restriction becomes zero (INTAMG.hpp:197-211)
+    scale_level(D - 1, true);
+
+    h.LD.resize(D);
+    h.U.resize(D);
+    h.bj.resize(D);
+    for (int l = 0; l < D; l++) {
+        const CsrD &Al = l == 0 ? A : CA[l - 1];
+        CsrD LD, U;
+        smoother_split(Al, sm, LD, U, h.bj[l]);
+        h.LD[l] = to_ldtri_flex(extract_ldinv(LD));
+        h.U[l] = to_flex(U);
+    }
+    for (int i = 0; i < D; i++) {
+        if (i < D - 1) h.CA.push_back(to_flex(CA[i]));
+        h.P.push_back(to_flex(chain.P[i]));
+        h.R.push_back(to_flex(It[i]));
+    }
+    CsrD F = ilu_full(CA[D - 1]);
+    h.LUL = to_ltri_flex(extract_l(F));
+    h.LUU = to_dutri_flex(extract_dinvu(F));
+    return h;
+}
+
+template <typename T>
+static CsrT<T> convert(const CsrD &A) {
+    CsrT<T> B;
+    B.n = A.n;
+    B.m = A.m;
+    B.rptr = A.rptr;
+    B.cind = A.cind;
+    B.val.resize(A.val.size());
+    for (size_t j = 0; j < A.val.size(); j++) B.val[j] = (T)A.val[j];
+    return B;
+}
+
+template <typename T>
+static FpHierarchy<T> build_fp(const CsrD &A, const RsChain &chain, const SmootherSpec &sm) {
+    FpHierarchy<T> h;
+    const int D = chain.depth();
+    h.depth = D;
+    h.smooth_iter = sm.iter;
+    h.A0 = convert<T>(A);
+    h.LD.resize(D);
+    h.U.resize(D);
+    h.bj.resize(D);
+    for (int l = 0; l < D; l++) {
+        const CsrD &Al = l == 0 ? A : chain.CA[l - 1];
+        CsrD LD, U;
+        smoother_split(Al, sm, LD, U, h.bj[l]);
+        h.LD[l] = convert<T>(extract_ldinv(LD));
+        h.U[l] = convert<T>(U);
+    }
+    for (int i = 0; i < D; i++) {
+        if (i < D - 1) h.CA.push_back(convert<T>(chain.CA[i]));
+        h.P.push_back(convert<T>(chain.P[i]));
+        h.R.push_back(convert<T>(chain.R[i]));
+    }
+    CsrD F = ilu_full(chain.CA[D - 1]);
+    h.LUL = convert<T>(extract_l(F));
+    h.LUU = convert<T>(extract_dinvu(F));
+    return h;
+}
+
+FpHierarchy<double> build_f64_hierarchy(const CsrD &A, const RsChain &chain, const SmootherSpec &sm) {
+    return build_fp<double>(A, chain, sm);
+}
+FpHierarchy<float> build_f32_hierarchy(const CsrD &A, const RsChain &chain, const SmootherSpec &sm) {
+    return build_fp<float>(A, chain, sm);
+}
+
+}  // namespace sagb

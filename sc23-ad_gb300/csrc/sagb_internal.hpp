@@ -1,0 +1,187 @@
+// Internal declarations shared by the CUDA translation units and the C ABI.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "host/amg_setup.hpp"
+#include "host/csr.hpp"
+#include "host/schedule.hpp"
+
+namespace sagb {
+
+enum VType : int { VT_I32 = 0, VT_F64 = 1, VT_F32 = 2 };
+
+inline size_t vt_size(int vt) { return vt == VT_F64 ? 8 : 4; }
+
+struct CudaError {
+    std::string msg;
+};
+void cuda_check(cudaError_t e, const char *what);
+#define SAGB_CUDA(call) ::sagb::cuda_check((call), #call)
+
+// One GPU, one stream.  All kernels of a context run on `stream`.
+struct Ctx {
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr;
+    unsigned *d_flags = nullptr;     // device status bits (ST_* in common.cuh)
+    unsigned *h_flags = nullptr;     // pinned mirror
+    bool fp_exact = false;           // FP kernels in sequential order without FMA
+    bool use_graphs = true;
+    long long launches = 0;          // kernels launched by this context (for reporting)
+    std::string err;
+};
+
+void *dmalloc(size_t bytes);
+void dfree(void *p);
+template <typename T>
+T *dupload(const std::vector<T> &v) {
+    if (v.empty()) return nullptr;
+    T *p = (T *)dmalloc(v.size() * sizeof(T));
+    SAGB_CUDA(cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+    return p;
+}
+
+// ------------------------------------------------------------------ matrices
+struct DevCsr {
+    int n = 0, m = 0;
+    int64_t nnz = 0;
+    int bit = 0;
+    int vt = VT_I32;
+    int group = 1;  // lanes per row in the SpMV kernel
+    int *rptr = nullptr, *cind = nullptr;
+    void *val = nullptr;
+    void release();
+};
+
+DevCsr upload_csr_i32(const CsrI &A);
+template <typename T>
+DevCsr upload_csr_fp(const CsrT<T> &A);
+DevCsr upload_csr_f64(const CsrD &A);
+int pick_group(double avg_nnz_per_row);
+
+// SpMV modes
+enum SpmvMode : int {
+    SPMV_SET = 0,    // y = A x
+    SPMV_RESID = 1,  // y = z - A x
+    SPMV_ADD = 2,    // y = A x + y
+};
+void spmv(Ctx &c, const DevCsr &A, const void *x, void *y, int mode = SPMV_SET, const void *z = nullptr);
+// FP64 residual in the reference's row order without contraction (bit-exact with
+// the CPU): r = b - A x  (irsolver.hpp:66-67)
+void spmv_resid_f64_exact(Ctx &c, const DevCsr &A, const double *x, const double *b, double *r);
+
+// ------------------------------------------------------ triangular sweeps
+struct TriSync {
+    unsigned ticket, done, epoch, pad;
+};
+
+struct DevTri {
+    int n = 0, kind = 0, vt = VT_I32;
+    int bit = 0, dbit = 0;
+    int nchunks = 0, group = 1, grid = 0;
+    int nlev = 0, max_level_rows = 0;
+    int64_t nnz_off = 0;
+    int *perm = nullptr, *prp = nullptr, *pci = nullptr;
+    void *pval = nullptr, *dinv = nullptr;
+    int *chunk_lv = nullptr, *sub_bound = nullptr;
+    unsigned long long *pk = nullptr;  // packed {epoch, value} per row (int32 / f32)
+    unsigned *flag = nullptr;          // ready epoch per row (f64)
+    TriSync *sync = nullptr;
+    void release();
+};
+
+// Builds the schedule from a triangular CSR (kind: TRI_LD / TRI_L / TRI_DU) and
+// uploads it.  vals points at int32 / double / float values of the source CSR.
+DevTri upload_tri(const Ctx &c, int n, const int *rptr, const int *cind, const void *vals, int vt, int kind,
+                  int bit, int dbit);
+void trsv(Ctx &c, const DevTri &T, const void *in, void *out);
+
+// Dense coarsest-level LU: strict lower L (unit), strict upper U and D^-1,
+// row-major n x n, solved by one block.
+struct DevDenseLU {
+    int n = 0, vt = VT_I32;
+    int bitL = 0, bitU = 0, dbitU = 0;
+    void *L = nullptr, *U = nullptr, *dinv = nullptr;
+    void *tmp = nullptr;
+    void release();
+};
+DevDenseLU upload_dense_lu(const int *Lrptr, const int *Lcind, const void *Lval, const int *Urptr,
+                           const int *Ucind, const void *Uval, int n, int vt, int bitL, int bitU, int dbitU);
+void lu_solve(Ctx &c, const DevDenseLU &LU, const void *in, void *out);
+void init_kernel_attributes();
+
+// ------------------------------------------------------------------- AMG
+struct DevAmg {
+    int vt = VT_I32;
+    int depth = 0;
+    int smooth_iter = 1;
+    int nbj = 0;
+    DevCsr A0;
+    std::vector<DevCsr> CA, P, R, U;
+    std::vector<DevTri> LD;
+    DevDenseLU LU;
+    void *r = nullptr;                   // fine-level residual / prolongation buffer
+    std::vector<void *> rr, ee, xx, tmp; // per coarse level (tmp: per smoother level)
+    // host copies kept for export and inspection
+    std::shared_ptr<IntHierarchy> hi;
+    std::shared_ptr<FpHierarchy<double>> hd;
+    std::shared_ptr<FpHierarchy<float>> hf;
+    void release();
+};
+
+std::unique_ptr<DevAmg> upload_amg_int(Ctx &c, std::shared_ptr<IntHierarchy> h);
+std::unique_ptr<DevAmg> upload_amg_f64(Ctx &c, std::shared_ptr<FpHierarchy<double>> h);
+std::unique_ptr<DevAmg> upload_amg_f32(Ctx &c, std::shared_ptr<FpHierarchy<float>> h);
+void smooth(Ctx &c, DevAmg &M, int level, const void *in, void *out, bool inited);
+void vcycle(Ctx &c, DevAmg &M, const void *in, void *out);
+
+// --------------------------------------------------------------- elementwise
+void vec_sub(Ctx &c, int vt, int n, const void *x, void *y);  // y = x - y
+void vec_add(Ctx &c, int vt, int n, const void *x, void *y);  // y = x + y
+
+// ----------------------------------------------------------------- Krylov
+struct SolveStats {
+    int iters = 0;
+    int converged = 0;
+    int restarts = 0;
+    int fallbacks = 0;
+    int final_bit = 0;
+    unsigned flags = 0;
+    double seconds = 0;
+    std::vector<double> history;  // per inner iteration relative residual estimate
+};
+
+struct KrylovParams {
+    int m = 30;
+    double eps = 1e-10;
+    int max_outer = 33;
+    int bit = 29;
+    int verbose = 0;
+    int fallback = 1;  // int: on overflow, discard the cycle and redo it with bit - 1
+};
+
+class Solver;
+std::unique_ptr<Solver> make_solver(Ctx &c, int vt, const DevCsr *dA, const DevCsr *A, DevAmg *M,
+                                    const KrylovParams &p);
+class Solver {
+  public:
+    virtual ~Solver() {}
+    // Restarted::Solve (irsolver.hpp:61-77); b, x device pointers
+    virtual int solve(const double *b, double nrm_b, double *x, SolveStats &st) = 0;
+    // one inner cycle (FGMRES*::Solve) on a device residual r; e0: optional
+    // injected norm; dumps: optional host buffers for V,Z,H,c,s,e,y
+    virtual int cycle(const double *r, double nrm_b, double *x, const double *e0, int *converged,
+                      void *const *dumps) = 0;
+    virtual void set_bit(int bit) = 0;
+};
+
+// FP64 norm of a device vector (deterministic reduction order)
+double nrm2_f64(Ctx &c, const double *x, int n);
+void nrm2_f64_dev(Ctx &c, const double *x, int n, double *d_out);
+
+}  // namespace sagb

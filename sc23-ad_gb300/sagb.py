@@ -1,0 +1,461 @@
+"""ctypes bindings of the sagb C ABI (include/sagb.h).
+
+This is the Python face of the same library a C or C++ caller links: every
+call goes through the C ABI of _build/libsagb.so.  It raises if the library
+is missing; nothing here computes on the CPU in place of the GPU.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libsagb.so")
+
+SA_OK, SA_ERR_ARG, SA_ERR_CUDA, SA_ERR_SETUP, SA_ERR_NUMERIC = 0, 1, 2, 3, 4
+FLAG_OVERFLOW, FLAG_TIMEOUT, FLAG_DIVZERO, FLAG_NORM_OVERFLOW = 1, 2, 4, 8
+INT, F64, F32 = 0, 1, 2
+MAT_FIXED, MAT_FLEX, MAT_F64, MAT_F32 = 0, 1, 2, 3
+OP_A0, OP_CA, OP_P, OP_R, OP_LD, OP_U, OP_LUL, OP_LUU, OP_BJ = range(9)
+GEN_POISSON2D, GEN_POISSON3D, GEN_ANISO2D, GEN_STENCIL27, GEN_CONVDIFF3D, GEN_VARCOEF3D = range(6)
+OPT_FP_EXACT, OPT_GRAPHS = 0, 1
+
+VP = C.c_void_p
+I32P = C.POINTER(C.c_int32)
+F64P = C.POINTER(C.c_double)
+
+
+class CsrView(C.Structure):
+    _fields_ = [("n", C.c_int), ("m", C.c_int), ("nnz", C.c_int64), ("rptr", I32P), ("cind", I32P),
+                ("val", VP), ("bit", C.c_int), ("dbit", C.c_int)]
+
+
+class AmgParams(C.Structure):
+    _fields_ = [("max_levels", C.c_int), ("theta", C.c_double), ("smoother_blocks", C.c_int),
+                ("omega", C.c_double), ("smooth_iter", C.c_int)]
+
+
+class SolverParams(C.Structure):
+    _fields_ = [("m", C.c_int), ("eps", C.c_double), ("max_outer", C.c_int), ("frac_bits", C.c_int),
+                ("verbose", C.c_int), ("overflow_fallback", C.c_int)]
+
+
+# name -> (restype, argtypes); the list is the ABI, checked by the CPU tests
+SIGNATURES = {
+    "sa_version": (C.c_char_p, []),
+    "sa_last_error": (C.c_char_p, []),
+    "sa_ctx_create": (C.c_int, [C.c_int, C.POINTER(VP)]),
+    "sa_ctx_destroy": (C.c_int, [VP]),
+    "sa_ctx_set_option": (C.c_int, [VP, C.c_int, C.c_int]),
+    "sa_ctx_flags": (C.c_int, [VP, C.POINTER(C.c_uint), C.c_int]),
+    "sa_ctx_launches": (C.c_int, [VP, C.POINTER(C.c_longlong)]),
+    "sa_ctx_sync": (C.c_int, [VP]),
+    "sa_ctx_stream": (C.c_int, [VP, C.POINTER(VP)]),
+    "sa_device_alloc": (C.c_int, [VP, C.c_uint64, C.POINTER(VP)]),
+    "sa_device_free": (C.c_int, [VP, VP]),
+    "sa_memcpy": (C.c_int, [VP, VP, VP, C.c_uint64]),
+    "sa_event_create": (C.c_int, [C.POINTER(VP)]),
+    "sa_event_record": (C.c_int, [VP, VP]),
+    "sa_event_elapsed_ms": (C.c_int, [VP, VP, C.POINTER(C.c_float)]),
+    "sa_event_destroy": (C.c_int, [VP]),
+    "sa_hcsr_read_mm": (C.c_int, [C.c_char_p, C.POINTER(VP)]),
+    "sa_hcsr_create": (C.c_int, [C.c_int, C.c_int, I32P, I32P, F64P, C.POINTER(VP)]),
+    "sa_hcsr_view": (C.c_int, [VP, C.POINTER(CsrView)]),
+    "sa_hcsr_lmax1_scaling": (C.c_int, [VP, F64P]),
+    "sa_hcsr_rhs": (C.c_int, [VP, C.c_uint64, F64P, F64P]),
+    "sa_hcsr_destroy": (C.c_int, [VP]),
+    "sa_gen": (C.c_int, [C.c_int, C.c_int, C.c_double, C.c_uint64, C.POINTER(VP)]),
+    "sa_mat_create": (C.c_int, [VP, C.c_int, C.c_int, C.c_int, C.c_int, I32P, I32P, F64P, C.POINTER(VP)]),
+    "sa_mat_create_i32": (C.c_int, [VP, C.c_int, C.c_int, I32P, I32P, I32P, C.c_int, C.POINTER(VP)]),
+    "sa_mat_destroy": (C.c_int, [VP]),
+    "sa_mat_info": (C.c_int, [VP, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int64),
+                              C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "sa_spmv": (C.c_int, [VP, VP, VP, VP]),
+    "sa_amg_params_default": (None, [C.POINTER(AmgParams)]),
+    "sa_setup_create": (C.c_int, [C.c_int, C.POINTER(AmgParams), C.c_int, I32P, I32P, F64P, C.POINTER(VP)]),
+    "sa_setup_destroy": (C.c_int, [VP]),
+    "sa_setup_depth": (C.c_int, [VP]),
+    "sa_setup_view": (C.c_int, [VP, C.c_int, C.c_int, C.POINTER(CsrView)]),
+    "sa_amg_create": (C.c_int, [VP, C.c_int, C.POINTER(AmgParams), C.c_int, I32P, I32P, F64P, C.POINTER(VP)]),
+    "sa_amg_create_from_setup": (C.c_int, [VP, VP, C.POINTER(VP)]),
+    "sa_amg_destroy": (C.c_int, [VP]),
+    "sa_amg_depth": (C.c_int, [VP]),
+    "sa_amg_precision": (C.c_int, [VP]),
+    "sa_amg_precondition": (C.c_int, [VP, VP, VP, VP]),
+    "sa_amg_smooth": (C.c_int, [VP, VP, C.c_int, VP, VP, C.c_int]),
+    "sa_amg_sweep": (C.c_int, [VP, VP, C.c_int, VP, VP]),
+    "sa_amg_coarse_solve": (C.c_int, [VP, VP, VP, VP]),
+    "sa_amg_level_spmv": (C.c_int, [VP, VP, C.c_int, C.c_int, VP, VP]),
+    "sa_amg_level_info": (C.c_int, [VP, C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                    C.POINTER(C.c_int64), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "sa_solver_params_default": (None, [C.POINTER(SolverParams)]),
+    "sa_solver_create": (C.c_int, [VP, C.c_int, VP, VP, VP, C.POINTER(SolverParams), C.POINTER(VP)]),
+    "sa_solver_destroy": (C.c_int, [VP]),
+    "sa_solver_solve": (C.c_int, [VP, VP, C.c_double, VP, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "sa_solver_cycle": (C.c_int, [VP, VP, C.c_double, VP, F64P, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                  C.POINTER(VP)]),
+    "sa_solver_set_bits": (C.c_int, [VP, C.c_int]),
+    "sa_solver_bits": (C.c_int, [VP, C.POINTER(C.c_int)]),
+    "sa_solver_history": (C.c_int, [VP, F64P, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_uint)]),
+    "sa_rule_bits": (C.c_int, [VP, VP, VP, C.c_double, C.POINTER(C.c_int)]),
+}
+
+_lib = None
+
+
+class SagbError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"sagb error {code}: {msg}")
+        self.code = code
+
+
+def lib():
+    """Load libsagb.so (built by sc23-ad_gb300/build.py); raises if missing."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise FileNotFoundError(f"{LIB_PATH} not built; run sc23-ad_gb300/build.py")
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def check(code):
+    if code != SA_OK:
+        raise SagbError(code, lib().sa_last_error().decode())
+
+
+def _ptr(a, t=VP):
+    return a.ctypes.data_as(t) if isinstance(a, np.ndarray) else a
+
+
+def ctype_of(precision):
+    return {INT: np.int32, F64: np.float64, F32: np.float32}[precision]
+
+
+def view_arrays(v, kind="f64"):
+    """Copy a CsrView into numpy arrays (rptr, cind, val)."""
+    n = v.n
+    rptr = np.ctypeslib.as_array(v.rptr, shape=(n + 1,)).copy() if n >= 0 else None
+    nnz = int(v.nnz)
+    cind = np.ctypeslib.as_array(v.cind, shape=(nnz,)).copy() if nnz else np.zeros(0, np.int32)
+    dt = {"f64": C.c_double, "i32": C.c_int32, "f32": C.c_float}[kind]
+    if nnz:
+        val = np.ctypeslib.as_array(C.cast(v.val, C.POINTER(dt)), shape=(nnz,)).copy()
+    else:
+        val = np.zeros(0, {"f64": np.float64, "i32": np.int32, "f32": np.float32}[kind])
+    return rptr, cind, val
+
+
+# ------------------------------------------------------------------ objects
+
+class HostCsr:
+    def __init__(self, handle):
+        self.h = handle
+
+    @staticmethod
+    def generate(kind, nx, param=0.0, seed=0):
+        h = VP()
+        check(lib().sa_gen(kind, nx, param, seed, C.byref(h)))
+        return HostCsr(h)
+
+    @staticmethod
+    def from_arrays(rptr, cind, val, m=None):
+        rptr = np.ascontiguousarray(rptr, np.int32)
+        cind = np.ascontiguousarray(cind, np.int32)
+        val = np.ascontiguousarray(val, np.float64)
+        n = len(rptr) - 1
+        h = VP()
+        check(lib().sa_hcsr_create(n, n if m is None else m, _ptr(rptr, I32P), _ptr(cind, I32P),
+                                   _ptr(val, F64P), C.byref(h)))
+        return HostCsr(h)
+
+    @staticmethod
+    def read_mm(path):
+        h = VP()
+        check(lib().sa_hcsr_read_mm(path.encode(), C.byref(h)))
+        return HostCsr(h)
+
+    def arrays(self):
+        v = CsrView()
+        check(lib().sa_hcsr_view(self.h, C.byref(v)))
+        return view_arrays(v, "f64")
+
+    @property
+    def n(self):
+        v = CsrView()
+        check(lib().sa_hcsr_view(self.h, C.byref(v)))
+        return v.n
+
+    def rhs(self, seed):
+        n = self.n
+        xs, b = np.zeros(n), np.zeros(n)
+        check(lib().sa_hcsr_rhs(self.h, seed, _ptr(xs, F64P), _ptr(b, F64P)))
+        return xs, b
+
+    def lmax1_scaling(self, b):
+        check(lib().sa_hcsr_lmax1_scaling(self.h, _ptr(b, F64P)))
+
+    def close(self):
+        if self.h:
+            lib().sa_hcsr_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+
+def amg_params(max_levels=20, theta=0.8, smoother_blocks=0, omega=1.0, smooth_iter=1):
+    return AmgParams(max_levels, theta, smoother_blocks, omega, smooth_iter)
+
+
+class Setup:
+    """Host hierarchy (no GPU)."""
+
+    def __init__(self, precision, rptr, cind, val, params=None):
+        rptr = np.ascontiguousarray(rptr, np.int32)
+        cind = np.ascontiguousarray(cind, np.int32)
+        val = np.ascontiguousarray(val, np.float64)
+        p = params or amg_params()
+        self.precision = precision
+        self.h = VP()
+        check(lib().sa_setup_create(precision, C.byref(p), len(rptr) - 1, _ptr(rptr, I32P), _ptr(cind, I32P),
+                                    _ptr(val, F64P), C.byref(self.h)))
+
+    @property
+    def depth(self):
+        return lib().sa_setup_depth(self.h)
+
+    def view(self, op, level=0):
+        v = CsrView()
+        check(lib().sa_setup_view(self.h, op, level, C.byref(v)))
+        if op == OP_BJ:
+            return np.ctypeslib.as_array(v.rptr, shape=(v.n + 1,)).copy()
+        kind = {INT: "i32", F64: "f64", F32: "f32"}[self.precision]
+        r, c, val = view_arrays(v, kind)
+        return r, c, val, v.bit, v.dbit, v.m
+
+    def close(self):
+        if self.h:
+            lib().sa_setup_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+
+class Context:
+    def __init__(self, device=0):
+        self.h = VP()
+        check(lib().sa_ctx_create(device, C.byref(self.h)))
+
+    def set_option(self, opt, value):
+        check(lib().sa_ctx_set_option(self.h, opt, int(value)))
+
+    def flags(self, clear=False):
+        f = C.c_uint()
+        check(lib().sa_ctx_flags(self.h, C.byref(f), int(clear)))
+        return f.value
+
+    def launches(self):
+        n = C.c_longlong()
+        check(lib().sa_ctx_launches(self.h, C.byref(n)))
+        return n.value
+
+    def sync(self):
+        check(lib().sa_ctx_sync(self.h))
+
+    def stream(self):
+        s = VP()
+        check(lib().sa_ctx_stream(self.h, C.byref(s)))
+        return s.value
+
+    def close(self):
+        if self.h:
+            lib().sa_ctx_destroy(self.h)
+            self.h = None
+
+
+class DeviceArray:
+    """Device buffer owned through the C ABI (no torch needed)."""
+
+    def __init__(self, ctx, shape, dtype):
+        self.ctx = ctx
+        self.dtype = np.dtype(dtype)
+        self.shape = (shape,) if np.isscalar(shape) else tuple(shape)
+        self.nbytes = int(np.prod(self.shape)) * self.dtype.itemsize
+        self.ptr = VP()
+        check(lib().sa_device_alloc(ctx.h, max(self.nbytes, 16), C.byref(self.ptr)))
+
+    @staticmethod
+    def from_host(ctx, a):
+        a = np.ascontiguousarray(a)
+        d = DeviceArray(ctx, a.shape, a.dtype)
+        d.upload(a)
+        return d
+
+    def upload(self, a):
+        a = np.ascontiguousarray(a, self.dtype)
+        check(lib().sa_memcpy(self.ctx.h, self.ptr, a.ctypes.data_as(VP), a.nbytes))
+
+    def download(self, out=None):
+        out = np.empty(self.shape, self.dtype) if out is None else out
+        check(lib().sa_memcpy(self.ctx.h, out.ctypes.data_as(VP), self.ptr, self.nbytes))
+        return out
+
+    def close(self):
+        if self.ptr:
+            lib().sa_device_free(self.ctx.h, self.ptr)
+            self.ptr = None
+
+    __del__ = close
+
+
+def _arg(x):
+    if isinstance(x, DeviceArray):
+        return x.ptr
+    if isinstance(x, np.ndarray):
+        return x.ctypes.data_as(VP)
+    return x
+
+
+class Matrix:
+    def __init__(self, ctx, kind, rptr, cind, val, bit=30, m=None):
+        rptr = np.ascontiguousarray(rptr, np.int32)
+        cind = np.ascontiguousarray(cind, np.int32)
+        n = len(rptr) - 1
+        self.ctx = ctx
+        self.h = VP()
+        if kind == "i32":
+            val = np.ascontiguousarray(val, np.int32)
+            check(lib().sa_mat_create_i32(ctx.h, n, n if m is None else m, _ptr(rptr, I32P), _ptr(cind, I32P),
+                                          _ptr(val, I32P), bit, C.byref(self.h)))
+        else:
+            val = np.ascontiguousarray(val, np.float64)
+            check(lib().sa_mat_create(ctx.h, kind, bit, n, n if m is None else m, _ptr(rptr, I32P),
+                                      _ptr(cind, I32P), _ptr(val, F64P), C.byref(self.h)))
+        self.info()
+
+    def info(self):
+        n, m, nnz, bit, prec = C.c_int(), C.c_int(), C.c_int64(), C.c_int(), C.c_int()
+        check(lib().sa_mat_info(self.h, C.byref(n), C.byref(m), C.byref(nnz), C.byref(bit), C.byref(prec)))
+        self.n, self.m, self.nnz, self.bit, self.precision = n.value, m.value, nnz.value, bit.value, prec.value
+        return self
+
+    def spmv(self, x, y=None):
+        if y is None:
+            y = np.zeros(self.n, ctype_of(self.precision))
+        check(lib().sa_spmv(self.ctx.h, self.h, _arg(x), _arg(y)))
+        return y
+
+    def close(self):
+        if self.h:
+            lib().sa_mat_destroy(self.h)
+            self.h = None
+
+
+class Amg:
+    def __init__(self, ctx, precision, rptr=None, cind=None, val=None, params=None, setup=None):
+        self.ctx = ctx
+        self.precision = precision
+        self.h = VP()
+        if setup is not None:
+            check(lib().sa_amg_create_from_setup(ctx.h, setup.h, C.byref(self.h)))
+        else:
+            rptr = np.ascontiguousarray(rptr, np.int32)
+            cind = np.ascontiguousarray(cind, np.int32)
+            val = np.ascontiguousarray(val, np.float64)
+            p = params or amg_params()
+            check(lib().sa_amg_create(ctx.h, precision, C.byref(p), len(rptr) - 1, _ptr(rptr, I32P),
+                                      _ptr(cind, I32P), _ptr(val, F64P), C.byref(self.h)))
+        self.depth = lib().sa_amg_depth(self.h)
+        self.n = self.level_info(OP_A0)[0]
+
+    def level_info(self, op, level=0):
+        n, m, nnz, bit, nlev = C.c_int(), C.c_int(), C.c_int64(), C.c_int(), C.c_int()
+        check(lib().sa_amg_level_info(self.h, op, level, C.byref(n), C.byref(m), C.byref(nnz), C.byref(bit),
+                                      C.byref(nlev)))
+        return n.value, m.value, nnz.value, bit.value, nlev.value
+
+    def _out(self, n, out):
+        return np.zeros(n, ctype_of(self.precision)) if out is None else out
+
+    def precondition(self, x, out=None):
+        out = self._out(self.n, out)
+        check(lib().sa_amg_precondition(self.ctx.h, self.h, _arg(x), _arg(out)))
+        return out
+
+    def smooth(self, level, x, out=None, inited=False):
+        out = self._out(self.level_info(OP_LD, level)[0], out)
+        check(lib().sa_amg_smooth(self.ctx.h, self.h, level, _arg(x), _arg(out), int(inited)))
+        return out
+
+    def sweep(self, level, x, out=None):
+        out = self._out(self.level_info(OP_LD, level)[0], out)
+        check(lib().sa_amg_sweep(self.ctx.h, self.h, level, _arg(x), _arg(out)))
+        return out
+
+    def coarse_solve(self, x, out=None):
+        out = self._out(self.level_info(OP_LUL)[0], out)
+        check(lib().sa_amg_coarse_solve(self.ctx.h, self.h, _arg(x), _arg(out)))
+        return out
+
+    def level_spmv(self, op, level, x, out=None):
+        out = self._out(self.level_info(op, level)[0], out)
+        check(lib().sa_amg_level_spmv(self.ctx.h, self.h, op, level, _arg(x), _arg(out)))
+        return out
+
+    def close(self):
+        if self.h:
+            lib().sa_amg_destroy(self.h)
+            self.h = None
+
+
+def solver_params(m=30, eps=1e-10, max_outer=None, frac_bits=29, verbose=0, overflow_fallback=1):
+    return SolverParams(m, eps, 1000 // m if max_outer is None else max_outer, frac_bits, verbose, overflow_fallback)
+
+
+class Solver:
+    def __init__(self, ctx, precision, dA, A, M, params=None):
+        self.ctx = ctx
+        self.h = VP()
+        p = params or solver_params()
+        self.m = p.m
+        check(lib().sa_solver_create(ctx.h, precision, dA.h, A.h, M.h, C.byref(p), C.byref(self.h)))
+
+    def solve(self, b, nrm_b, x):
+        it, conv = C.c_int(), C.c_int()
+        check(lib().sa_solver_solve(self.h, _arg(b), nrm_b, _arg(x), C.byref(it), C.byref(conv)))
+        return it.value, conv.value
+
+    def cycle(self, r, nrm_b, x, e0=None, dumps=None):
+        it, conv = C.c_int(), C.c_int()
+        e0p = C.byref(C.c_double(e0)) if e0 is not None else None
+        dp = None
+        if dumps is not None:
+            dp = (VP * 7)(*[d.ctypes.data_as(VP) if d is not None else None for d in dumps])
+        check(lib().sa_solver_cycle(self.h, _arg(r), nrm_b, _arg(x), e0p, C.byref(it), C.byref(conv), dp))
+        return it.value, conv.value
+
+    def set_bits(self, bits):
+        check(lib().sa_solver_set_bits(self.h, bits))
+
+    def history(self):
+        n, f = C.c_int(), C.c_uint()
+        check(lib().sa_solver_history(self.h, None, 0, C.byref(n), C.byref(f)))
+        h = np.zeros(n.value)
+        check(lib().sa_solver_history(self.h, _ptr(h, F64P), n.value, C.byref(n), C.byref(f)))
+        return h, f.value
+
+    def close(self):
+        if self.h:
+            lib().sa_solver_destroy(self.h)
+            self.h = None
+
+
+def rule_bits(ctx, M64, b, nrm_b):
+    bits = C.c_int()
+    check(lib().sa_rule_bits(ctx.h, M64.h, _arg(b), nrm_b, C.byref(bits)))
+    return bits.value
