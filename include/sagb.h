@@ -121,6 +121,8 @@ int sa_ctx_stream(sa_ctx ctx, void **stream); /* the cudaStream_t all work is qu
 int sa_device_alloc(sa_ctx ctx, uint64_t bytes, void **ptr);
 int sa_device_free(sa_ctx ctx, void *ptr);
 int sa_memcpy(sa_ctx ctx, void *dst, const void *src, uint64_t bytes); /* any direction, synchronous */
+int sa_host_alloc(uint64_t bytes, void **ptr); /* page-locked host memory (fast host<->device copies) */
+int sa_host_free(void *ptr);
 int sa_event_create(sa_event *out);
 int sa_event_record(sa_ctx ctx, sa_event ev);
 int sa_event_elapsed_ms(sa_event start, sa_event stop, float *ms);
@@ -157,6 +159,10 @@ void sa_amg_params_default(sa_amg_params *p);
  *                                   Library/preconditioner/INTAMG.hpp:25-84, 149-245 */
 int sa_setup_create(int precision, const sa_amg_params *p, int n, const int32_t *rptr, const int32_t *cind,
                     const double *val, sa_setup *out);
+/* the hierarchy of another precision over the same coarsening (the Ruge-Stueben
+ * chain does not depend on the precision; dfAMG and intAMGflex both build it from
+ * the unscaled operators, Library/preconditioner/INTAMG.hpp:38-51, 162-173) */
+int sa_setup_derive(sa_setup s, int precision, sa_setup *out);
 int sa_setup_destroy(sa_setup s);
 int sa_setup_depth(sa_setup s);
 int sa_setup_view(sa_setup s, int op, int level, sa_csr_view *out);

@@ -48,6 +48,8 @@ struct sa_matrix {
 struct sa_hierarchy {
     int precision = SA_INT;
     sa_amg_params p{};
+    std::shared_ptr<CsrD> A;         // the scaled fine matrix
+    std::shared_ptr<RsChain> chain;  // coarsening shared by all precisions
     std::shared_ptr<IntHierarchy> hi;
     std::shared_ptr<FpHierarchy<double>> hd;
     std::shared_ptr<FpHierarchy<float>> hf;
@@ -106,8 +108,11 @@ class Staged {
             dfree(own_);
         }
     }
+    // Host outputs are copied back and the stream is synchronised; with device
+    // buffers only, the call stays asynchronous on the context's stream.
     void finish() {
-        if (own_ && out_) SAGB_CUDA(cudaMemcpyAsync(user_, dev_, bytes_, cudaMemcpyDeviceToHost, c_.stream));
+        if (!own_) return;
+        if (out_) SAGB_CUDA(cudaMemcpyAsync(user_, dev_, bytes_, cudaMemcpyDeviceToHost, c_.stream));
         SAGB_CUDA(cudaStreamSynchronize(c_.stream));
     }
     void *get() const { return dev_; }
@@ -217,6 +222,17 @@ extern "C" int sa_memcpy(sa_ctx ctx, void *dst, const void *src, uint64_t bytes)
     SAGB_CUDA(cudaStreamSynchronize(ctx->c.stream));
     return SA_OK;
     SA_GUARD_END
+}
+extern "C" int sa_host_alloc(uint64_t bytes, void **ptr) {
+    if (!ptr) return fail(SA_ERR_ARG, "null argument");
+    SA_GUARD_BEGIN
+    SAGB_CUDA(cudaMallocHost(ptr, bytes ? bytes : 16));
+    return SA_OK;
+    SA_GUARD_END
+}
+extern "C" int sa_host_free(void *ptr) {
+    if (ptr) cudaFreeHost(ptr);
+    return SA_OK;
 }
 extern "C" int sa_event_create(sa_event *out) {
     if (!out) return fail(SA_ERR_ARG, "null output");
@@ -445,7 +461,8 @@ extern "C" void sa_amg_params_default(sa_amg_params *p) {
 
 static void build_setup(sa_hierarchy &s, const CsrD &A) {
     if (s.p.theta <= 0 || s.p.theta > 1) throw SetupError{"Theta must be in 0 < theta <= 1"};
-    RsChain chain = rs_chain(A, s.p.theta, s.p.max_levels);
+    if (!s.chain) s.chain = std::make_shared<RsChain>(rs_chain(A, s.p.theta, s.p.max_levels));
+    const RsChain &chain = *s.chain;
     SmootherSpec sm;
     sm.block = s.p.smoother_blocks;
     sm.omega = s.p.omega;
@@ -468,18 +485,38 @@ extern "C" int sa_setup_create(int precision, const sa_amg_params *p, int n, con
         delete s;
         return fail(SA_ERR_ARG, "invalid AMG parameters");
     }
-    CsrD A;
-    A.n = A.m = n;
-    A.rptr.assign(rptr, rptr + n + 1);
-    A.cind.assign(cind, cind + rptr[n]);
-    A.val.assign(val, val + rptr[n]);
+    auto A = std::make_shared<CsrD>();
+    A->n = A->m = n;
+    A->rptr.assign(rptr, rptr + n + 1);
+    A->cind.assign(cind, cind + rptr[n]);
+    A->val.assign(val, val + rptr[n]);
+    s->A = A;
     try {
-        build_setup(*s, A);
+        build_setup(*s, *A);
     } catch (...) {
         delete s;
         throw;
     }
     *out = s;
+    return SA_OK;
+    SA_GUARD_END
+}
+
+extern "C" int sa_setup_derive(sa_setup s, int precision, sa_setup *out) {
+    if (!s || !out || precision < SA_INT || precision > SA_F32) return fail(SA_ERR_ARG, "invalid argument");
+    SA_GUARD_BEGIN
+    auto *d = new sa_hierarchy();
+    d->precision = precision;
+    d->p = s->p;
+    d->A = s->A;
+    d->chain = s->chain;
+    try {
+        build_setup(*d, *d->A);
+    } catch (...) {
+        delete d;
+        throw;
+    }
+    *out = d;
     return SA_OK;
     SA_GUARD_END
 }

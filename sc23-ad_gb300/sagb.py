@@ -54,6 +54,8 @@ SIGNATURES = {
     "sa_device_alloc": (C.c_int, [VP, C.c_uint64, C.POINTER(VP)]),
     "sa_device_free": (C.c_int, [VP, VP]),
     "sa_memcpy": (C.c_int, [VP, VP, VP, C.c_uint64]),
+    "sa_host_alloc": (C.c_int, [C.c_uint64, C.POINTER(VP)]),
+    "sa_host_free": (C.c_int, [VP]),
     "sa_event_create": (C.c_int, [C.POINTER(VP)]),
     "sa_event_record": (C.c_int, [VP, VP]),
     "sa_event_elapsed_ms": (C.c_int, [VP, VP, C.POINTER(C.c_float)]),
@@ -73,6 +75,7 @@ SIGNATURES = {
     "sa_spmv": (C.c_int, [VP, VP, VP, VP]),
     "sa_amg_params_default": (None, [C.POINTER(AmgParams)]),
     "sa_setup_create": (C.c_int, [C.c_int, C.POINTER(AmgParams), C.c_int, I32P, I32P, F64P, C.POINTER(VP)]),
+    "sa_setup_derive": (C.c_int, [VP, C.c_int, C.POINTER(VP)]),
     "sa_setup_destroy": (C.c_int, [VP]),
     "sa_setup_depth": (C.c_int, [VP]),
     "sa_setup_view": (C.c_int, [VP, C.c_int, C.c_int, C.POINTER(CsrView)]),
@@ -215,7 +218,10 @@ def amg_params(max_levels=20, theta=0.8, smoother_blocks=0, omega=1.0, smooth_it
 class Setup:
     """Host hierarchy (no GPU)."""
 
-    def __init__(self, precision, rptr, cind, val, params=None):
+    def __init__(self, precision, rptr=None, cind=None, val=None, params=None, _handle=None):
+        if _handle is not None:
+            self.precision, self.h = precision, _handle
+            return
         rptr = np.ascontiguousarray(rptr, np.int32)
         cind = np.ascontiguousarray(cind, np.int32)
         val = np.ascontiguousarray(val, np.float64)
@@ -224,6 +230,12 @@ class Setup:
         self.h = VP()
         check(lib().sa_setup_create(precision, C.byref(p), len(rptr) - 1, _ptr(rptr, I32P), _ptr(cind, I32P),
                                     _ptr(val, F64P), C.byref(self.h)))
+
+    def derive(self, precision):
+        """The same coarsening in another precision."""
+        h = VP()
+        check(lib().sa_setup_derive(self.h, precision, C.byref(h)))
+        return Setup(precision, _handle=h)
 
     @property
     def depth(self):
@@ -313,7 +325,50 @@ class DeviceArray:
     __del__ = close
 
 
+class PinnedArray:
+    """Page-locked host buffer exposed as a numpy array (.a)."""
+
+    def __init__(self, shape, dtype):
+        dtype = np.dtype(dtype)
+        n = int(np.prod((shape,) if np.isscalar(shape) else shape))
+        self.ptr = VP()
+        check(lib().sa_host_alloc(max(n * dtype.itemsize, 16), C.byref(self.ptr)))
+        buf = (C.c_char * (n * dtype.itemsize)).from_address(self.ptr.value)
+        self.a = np.frombuffer(buf, dtype=dtype, count=n)
+
+    def close(self):
+        if self.ptr:
+            self.a = None
+            lib().sa_host_free(self.ptr)
+            self.ptr = None
+
+    __del__ = close
+
+
+class Event:
+    def __init__(self):
+        self.h = VP()
+        check(lib().sa_event_create(C.byref(self.h)))
+
+    def record(self, ctx):
+        check(lib().sa_event_record(ctx.h, self.h))
+
+    def elapsed_ms(self, later):
+        ms = C.c_float()
+        check(lib().sa_event_elapsed_ms(self.h, later.h, C.byref(ms)))
+        return ms.value
+
+    def close(self):
+        if self.h:
+            lib().sa_event_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+
 def _arg(x):
+    if isinstance(x, PinnedArray):
+        return x.ptr
     if isinstance(x, DeviceArray):
         return x.ptr
     if isinstance(x, np.ndarray):
