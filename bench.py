@@ -173,7 +173,9 @@ def run_ours(a, dist):
     dA = sagb.Matrix(ctx, sagb.MAT_F64, r, c, v)
     A0 = sagb.Matrix(ctx, sagb.MAT_FIXED, r, c, v, bit=30)
     bits = sagb.rule_bits(ctx, M64, b, nrm_b)
-    S = sagb.Solver(ctx, sagb.INT, dA, A0, M, sagb.solver_params(m=a.m, frac_bits=bits))
+    # explicit_stop: the metric is the explicit residual; the reference's inner
+    # estimate alone stops above 1e-10 on this system
+    S = sagb.Solver(ctx, sagb.INT, dA, A0, M, sagb.solver_params(m=a.m, frac_bits=bits, explicit_stop=1))
     db = sagb.DeviceArray.from_host(ctx, b)
     dx = sagb.DeviceArray(ctx, N, np.float64)
     zeros = sagb.DeviceArray.from_host(ctx, np.zeros(N))
@@ -228,7 +230,7 @@ def run_ours(a, dist):
     # ---- kernel roofline: level-0 sweep family and the fine SpMV, timed alone
     out["kernels"] = kernel_rooflines(ctx, M, A0, N, a)
     # ---- FP64-AMG-FGMRES on the same GPU (comparison row)
-    S64 = sagb.Solver(ctx, sagb.F64, dA, dA, M64, sagb.solver_params(m=a.m))
+    S64 = sagb.Solver(ctx, sagb.F64, dA, dA, M64, sagb.solver_params(m=a.m, explicit_stop=1))
     dx.upload(np.zeros(N))
     S64.solve(db, nrm_b, dx)
     e0.record(ctx)

@@ -100,6 +100,8 @@ typedef struct {
     int frac_bits;         /* F_G of the integer solver (FGMRESflex bit)                                */
     int verbose;           /* print the reference's "# [j] res" / "[Res]" lines                         */
     int overflow_fallback; /* int only: on an overflow flag, redo the cycle with F-1 (0: reference behaviour) */
+    int explicit_stop;     /* 1: stop only when ||b - A x|| / ||b|| <= eps in FP64 (the reference stops on
+                              the inner solver's implicit estimate, which can leave it above eps)      */
 } sa_solver_params;
 
 /* ------------------------------------------------------------- library */

@@ -751,6 +751,7 @@ extern "C" void sa_solver_params_default(sa_solver_params *p) {
     p->frac_bits = 29;
     p->verbose = 0;
     p->overflow_fallback = 1;
+    p->explicit_stop = 0;
 }
 
 extern "C" int sa_solver_create(sa_ctx ctx, int precision, sa_mat dA, sa_mat A, sa_amg M, const sa_solver_params *p,
@@ -779,6 +780,7 @@ extern "C" int sa_solver_create(sa_ctx ctx, int precision, sa_mat dA, sa_mat A, 
     kp.bit = q.frac_bits;
     kp.verbose = q.verbose;
     kp.fallback = precision == SA_INT ? q.overflow_fallback : 0;
+    kp.explicit_check = q.explicit_stop;
     h->S = make_solver(ctx->c, precision == SA_INT ? VT_I32 : (precision == SA_F64 ? VT_F64 : VT_F32), &dA->d, &A->d,
                        M->M.get(), kp);
     *out = h;

@@ -517,6 +517,14 @@ class SolverBase : public Solver {
             SAGB_CUDA(cudaStreamSynchronize(c_.stream));
             const double nrm_r = *nrm_h_;
             st.restarts++;
+            st.explicit_res = nrm_r / nrm_b;
+            if (p_.explicit_check && i > 0 && nrm_r <= p_.eps * nrm_b) {
+                // explicit relative residual reached: stop here rather than on
+                // the inner solver's implicit estimate
+                st.converged = 1;
+                st.iters = iter;
+                return iter;
+            }
             if (std::fabs(nrm_r - prev) / nrm_r < 1.0e-8) {
                 st.converged = 0;
                 st.iters = 0;
@@ -541,7 +549,20 @@ class SolverBase : public Solver {
             st.final_bit = p_.bit;
             if (st.flags & ST_TIMEOUT) return 0;
             iter += it;
-            if (conv) {
+            if (conv && !p_.explicit_check) {
+                st.converged = 1;
+                st.iters = iter;
+                return iter;
+            }
+        }
+        if (p_.explicit_check) {
+            // the last cycle's update has not been checked yet
+            spmv_resid_f64_exact(c_, *dA_, x, b, r_);
+            nrm2_f64_dev(c_, r_, N_, nrm_);
+            SAGB_CUDA(cudaMemcpyAsync(nrm_h_, nrm_, sizeof(double), cudaMemcpyDeviceToHost, c_.stream));
+            SAGB_CUDA(cudaStreamSynchronize(c_.stream));
+            st.explicit_res = *nrm_h_ / nrm_b;
+            if (*nrm_h_ <= p_.eps * nrm_b) {
                 st.converged = 1;
                 st.iters = iter;
                 return iter;

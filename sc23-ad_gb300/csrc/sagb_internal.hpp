@@ -151,6 +151,7 @@ struct SolveStats {
     int restarts = 0;
     int fallbacks = 0;
     int final_bit = 0;
+    double explicit_res = 0;
     unsigned flags = 0;
     double seconds = 0;
     std::vector<double> history;  // per inner iteration relative residual estimate
@@ -163,6 +164,7 @@ struct KrylovParams {
     int bit = 29;
     int verbose = 0;
     int fallback = 1;  // int: on overflow, discard the cycle and redo it with bit - 1
+    int explicit_check = 0;  // stop on the explicit FP64 residual instead of the inner estimate
 };
 
 class Solver;
