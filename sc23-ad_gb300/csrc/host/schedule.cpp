@@ -44,6 +44,7 @@ TriSchedule build_tri_schedule(const int *rptr, const int *cind, int n, int kind
     for (int i = 0; i < n; i++) cnt[level[i] + 1]++;
     for (int l = 0; l < nlev; l++) cnt[l + 1] += cnt[l];
     std::vector<int> lptr(cnt);
+    s.lvl_ptr = lptr;
     s.perm.resize(n);
     if (kind == TRI_DU) {
         for (int i = n - 1; i >= 0; i--) s.perm[cnt[level[i]]++] = i;

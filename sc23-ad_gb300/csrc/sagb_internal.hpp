@@ -89,6 +89,8 @@ struct DevTri {
     int *perm = nullptr, *prp = nullptr, *pci = nullptr;
     void *pval = nullptr, *dinv = nullptr;
     int *chunk_lv = nullptr, *sub_bound = nullptr;
+    int *lvl_ptr = nullptr;            // level boundaries (single-CTA mode)
+    bool one_cta = false;              // whole sweep in one CTA with the result in shared memory
     unsigned long long *pk = nullptr;  // packed {epoch, value} per row (int32 / f32)
     unsigned *flag = nullptr;          // ready epoch per row (f64)
     TriSync *sync = nullptr;
