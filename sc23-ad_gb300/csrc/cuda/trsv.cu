@@ -5,22 +5,27 @@
 // and its block-Jacobi form BJCSRflex (ldtri.hpp:511-525):
 //   t = in_i << bit;  t -= sum_j a_ij * out_j;  out_i = (int)((t >> bit) * dinv_i >> dbit)
 // FP sweeps follow ldtri::CSR<T> / BJCSR<T> (ldtri.hpp:49-58, 398-412).
-// Rows are stored in level order (host/schedule.hpp); a row only waits for the
-// rows it reads, so the integer results are those of the sequential loop.
+// Rows are grouped into dependency levels (host/schedule.hpp); every row of a
+// level only reads rows of earlier levels, so computing level after level gives
+// the integer results of the sequential loop.
 //
 // Two kernels:
-//  * k_tri_cta: the whole sweep in one CTA, the result vector in shared memory.
-//    Levels are separated by block barriers; while one level is computed, the
-//    row data of the next level is already being loaded (it does not depend on
-//    the solve).  Used when the vector fits in shared memory (coarse levels).
-//  * k_tri: many CTAs claim chunks of level-ordered rows by ticket and wait
-//    only for the rows they read.  Integer and FP32 results are published as
-//    one 64-bit word {epoch, value}; FP64 results use an epoch flag with
-//    release/acquire.  All reads of one row's dependencies are issued together.
-//    Every wait is bounded in time (ST_TIMEOUT); once a wait has timed out, all
-//    CTAs stop waiting.  Ticket and epoch are advanced by the last CTA, so the
-//    kernel replays from a CUDA graph.
+//  * k_tri_cta (coarse levels, the vector fits in shared memory): one CTA.  The
+//    result vector lives in shared memory, seeded with `in` (a row reads its own
+//    input once and then overwrites it).  Each level's row data is one 16-byte
+//    aligned block that a bulk copy (cp.async.bulk + mbarrier) brings into a
+//    ring of shared-memory stages several levels ahead, so a level costs shared
+//    memory traffic and one block barrier.
+//  * k_tri (fine levels): CTAs claim chunks of level-ordered rows by ticket.
+//    Before a chunk of level L runs, one thread waits until level L-1 is
+//    complete (a per-level counter, cumulative over sweeps).  Level L-1
+//    complete implies every earlier level is complete, because each of its
+//    rows waited the same way.  Chunks are claimed in level order, so the wait
+//    cannot deadlock.  One poller per CTA keeps L2 free of spin traffic.
+// All waits are bounded in time (ST_TIMEOUT); ticket and epoch are advanced by
+// the last CTA, so both kernels replay from a CUDA graph.
 #include <algorithm>
+#include <cstring>
 #include <type_traits>
 
 #include "../sagb_internal.hpp"
@@ -31,49 +36,79 @@ namespace sagb {
 constexpr int kTriThreads = 256;   // multi-CTA kernel
 constexpr int kCtaThreads = 1024;  // single-CTA kernel
 constexpr int kBatch = 4;          // dependencies read together per lane (multi-CTA)
-constexpr int kCtaBatch = 8;       // entries held in registers per lane (single CTA)
-constexpr size_t kCtaSmem = 200 * 1024;
+constexpr int kStages = 4;         // bulk-copy ring depth (single CTA)
+constexpr size_t kSmemMax = 227 * 1024;
+constexpr size_t kCtaVecMax = 150 * 1024;  // largest shared result vector
 
 template <int VT>
 using vt_t = typename std::conditional<VT == VT_I32, int, typename std::conditional<VT == VT_F64, double, float>::type>::type;
-
-struct TriArgs {
-    int n, nchunks, bit, dbit;
-    const int *perm, *prp, *pci;
-    const void *pval, *dinv;
-    const int *chunk_lv, *sub_bound;
-    unsigned long long *pk;
-    unsigned *flag;
-    TriSync *sync;
-};
+template <int VT>
+using acc_t = typename std::conditional<VT == VT_I32, long long, vt_t<VT>>::type;
 
 __device__ __forceinline__ bool aborted(const unsigned *flags) {
     return (*(volatile const unsigned *)flags & ST_TIMEOUT) != 0;
 }
 
-__device__ __forceinline__ unsigned long long wait_packed(unsigned long long *pk, int c, unsigned ep,
-                                                          unsigned *flags) {
-    const unsigned long long t0 = globaltimer_ns();
-    unsigned it = 0;
-    for (;;) {
-        const unsigned long long w = ld_relaxed_u64(pk + c);
-        if ((unsigned)(w >> 32) == ep) return w;
-        if ((++it & 63u) == 0) {
-            if (aborted(flags)) return w;
-            if (globaltimer_ns() - t0 > kSpinLimitNs) {
-                atomicOr(flags, ST_TIMEOUT);
-                return w;
-            }
-        }
+// t - v*o in the accumulator type of each precision
+template <int VT, bool EXACT>
+__device__ __forceinline__ acc_t<VT> acc_sub(acc_t<VT> t, vt_t<VT> v, vt_t<VT> o) {
+    if constexpr (VT == VT_I32) return wsub(t, (long long)v * (long long)o);
+    else if constexpr (EXACT && VT == VT_F64) return __dsub_rn(t, __dmul_rn(v, o));
+    else if constexpr (EXACT) return __fsub_rn(t, __fmul_rn(v, o));
+    else return t - v * o;
+}
+template <int VT>
+__device__ __forceinline__ acc_t<VT> acc_init(vt_t<VT> in, int bit) {
+    if constexpr (VT == VT_I32) return wshl((long long)in, bit);
+    else return in;
+}
+template <int VT>
+__device__ __forceinline__ acc_t<VT> acc_reduce(acc_t<VT> t, int G) {
+    for (int o = G / 2; o > 0; o >>= 1) {
+        if constexpr (VT == VT_I32) t = wadd(t, shfl_xor(t, o));
+        else t += shfl_xor(t, o);
+    }
+    return t;
+}
+// out_i from the accumulated row: (t >> bit) * dinv >> dbit, or t * dinv
+template <int VT>
+__device__ __forceinline__ vt_t<VT> acc_finish(acc_t<VT> t, vt_t<VT> d, int bit, int dbit, bool &ovf) {
+    if constexpr (VT == VT_I32) {
+        const long long s = wmul(t >> bit, (long long)d) >> dbit;
+        ovf |= !fits32(s);
+        return lo32(s);
+    } else if constexpr (VT == VT_F64) {
+        return __dmul_rn(t, d);
+    } else {
+        return __fmul_rn(t, d);
     }
 }
 
-__device__ __forceinline__ void wait_flag(const unsigned *flag, int c, unsigned ep, unsigned *flags) {
+// ============================================================== multi-CTA
+
+struct TriArgs {
+    int n, nchunks, bit, dbit;
+    const int *perm, *prp, *pci;
+    const void *pval, *dinv;
+    const int *chunk_lv, *sub_bound, *sub_level, *lvl_ptr;
+    unsigned long long *lvl_done;
+    TriSync *sync;
+};
+
+__device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long *p) {
+    unsigned long long v;
+    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// thread 0: wait until the counter reaches target (bounded)
+__device__ __forceinline__ void wait_count(const unsigned long long *cnt, unsigned long long target,
+                                           unsigned *flags) {
+    if (ld_acquire_u64(cnt) >= target) return;
     const unsigned long long t0 = globaltimer_ns();
-    unsigned it = 0;
-    for (;;) {
-        if (ld_acquire_u32(flag + c) == ep) return;
-        if ((++it & 63u) == 0) {
+    for (unsigned it = 1;; it++) {
+        if (ld_acquire_u64(cnt) >= target) return;
+        if ((it & 31u) == 0) {
             if (aborted(flags)) return;
             if (globaltimer_ns() - t0 > kSpinLimitNs) {
                 atomicOr(flags, ST_TIMEOUT);
@@ -83,129 +118,128 @@ __device__ __forceinline__ void wait_flag(const unsigned *flag, int c, unsigned 
     }
 }
 
-__device__ __forceinline__ double ld_relaxed_f64(const double *p) {
-    double v;
-    asm volatile("ld.relaxed.gpu.global.f64 %0, [%1];" : "=d"(v) : "l"(p) : "memory");
-    return v;
-}
+template <int VT, int G>
+struct RowRegs {
+    int row, jb, je;
+    vt_t<VT> in, dinv;
+    int c[kBatch];
+    vt_t<VT> v[kBatch];
+};
 
-// t - v*o in the accumulator type of each precision
-template <int VT, bool EXACT>
-__device__ __forceinline__ auto acc_sub(typename std::conditional<VT == VT_I32, long long, vt_t<VT>>::type t,
-                                        vt_t<VT> v, vt_t<VT> o) {
-    if constexpr (VT == VT_I32) return wsub(t, (long long)v * (long long)o);
-    else if constexpr (EXACT && VT == VT_F64) return __dsub_rn(t, __dmul_rn(v, o));
-    else if constexpr (EXACT) return __fsub_rn(t, __fmul_rn(v, o));
-    else return t - v * o;
+template <int VT, int G>
+__device__ __forceinline__ void load_row(RowRegs<VT, G> &r, const TriArgs &a, int p, bool valid, int g,
+                                         const vt_t<VT> *in) {
+    using V = vt_t<VT>;
+    r.row = 0;
+    r.jb = r.je = 0;
+    r.in = V(0);
+    r.dinv = V(0);
+#pragma unroll
+    for (int k = 0; k < kBatch; k++) {
+        r.c[k] = 0;
+        r.v[k] = V(0);
+    }
+    if (!valid) return;
+    r.row = __ldg(a.perm + p);
+    r.jb = __ldg(a.prp + p);
+    r.je = __ldg(a.prp + p + 1);
+    r.in = __ldg(in + r.row);
+    r.dinv = __ldg((const V *)a.dinv + p);
+#pragma unroll
+    for (int k = 0; k < kBatch; k++) {
+        const int j = r.jb + g + k * G;
+        if (j < r.je) {
+            r.c[k] = __ldg(a.pci + j);
+            r.v[k] = __ldg((const V *)a.pval + j);
+        }
+    }
 }
-
-// ============================================================== multi-CTA
 
 template <int VT, int G, bool EXACT>
-__device__ __forceinline__ void tri_row(const TriArgs &a, int p, bool valid, int g, unsigned ep, const void *in_,
-                                        void *out_, unsigned *flags, bool &ovf) {
+__device__ __forceinline__ void compute_row(const RowRegs<VT, G> &r, const TriArgs &a, bool valid, int g,
+                                            vt_t<VT> *out, bool &ovf) {
     using V = vt_t<VT>;
-    using A = typename std::conditional<VT == VT_I32, long long, V>::type;
-    const V *in = (const V *)in_;
-    V *out = (V *)out_;
-    const V *pv = (const V *)a.pval;
-    A t = 0;
-    int row = 0;
+    acc_t<VT> t = 0;
     if (valid) {
-        row = __ldg(a.perm + p);
-        if (g == 0) {
-            if constexpr (VT == VT_I32) t = wshl((long long)__ldg(in + row), a.bit);
-            else t = __ldg(in + row);
-        }
-        const int jb = __ldg(a.prp + p), je = __ldg(a.prp + p + 1);
-        for (int j0 = jb + g; j0 < je; j0 += G * kBatch) {
+        if (g == 0) t = acc_init<VT>(r.in, a.bit);
+        // the first batch is in registers: read all its dependencies at once
+        V o[kBatch];
+#pragma unroll
+        for (int k = 0; k < kBatch; k++) o[k] = r.jb + g + k * G < r.je ? __ldcg(out + r.c[k]) : V(0);
+#pragma unroll
+        for (int k = 0; k < kBatch; k++) t = acc_sub<VT, EXACT>(t, r.v[k], o[k]);
+        for (int j0 = r.jb + g + kBatch * G; j0 < r.je; j0 += kBatch * G) {
             int c[kBatch];
             V v[kBatch];
 #pragma unroll
             for (int k = 0; k < kBatch; k++) {
                 const int j = j0 + k * G;
-                c[k] = j < je ? __ldg(a.pci + j) : -1;
-                v[k] = j < je ? __ldg(pv + j) : V(0);
+                c[k] = j < r.je ? __ldg(a.pci + j) : -1;
+                v[k] = j < r.je ? __ldg((const V *)a.pval + j) : V(0);
             }
-            if constexpr (VT == VT_F64) {
-                // relaxed reads of all ready flags, then one acquire fence
-                unsigned f[kBatch];
 #pragma unroll
-                for (int k = 0; k < kBatch; k++) f[k] = c[k] >= 0 ? ld_relaxed_u32(a.flag + c[k]) : ep;
+            for (int k = 0; k < kBatch; k++) o[k] = c[k] >= 0 ? __ldcg(out + c[k]) : V(0);
 #pragma unroll
-                for (int k = 0; k < kBatch; k++)
-                    if (f[k] != ep) wait_flag(a.flag, c[k], ep, flags);
-                fence_acq_rel_gpu();
-#pragma unroll
-                for (int k = 0; k < kBatch; k++)
-                    if (c[k] >= 0) t = acc_sub<VT, EXACT>(t, v[k], ld_relaxed_f64((const double *)out + c[k]));
-            } else {
-                unsigned long long w[kBatch];
-#pragma unroll
-                for (int k = 0; k < kBatch; k++) w[k] = c[k] >= 0 ? ld_relaxed_u64(a.pk + c[k]) : 0ull;
-#pragma unroll
-                for (int k = 0; k < kBatch; k++) {
-                    if (c[k] < 0) continue;
-                    if ((unsigned)(w[k] >> 32) != ep) w[k] = wait_packed(a.pk, c[k], ep, flags);
-                    V o;
-                    if constexpr (VT == VT_I32) o = (int)(unsigned)w[k];
-                    else o = __uint_as_float((unsigned)w[k]);
-                    t = acc_sub<VT, EXACT>(t, v[k], o);
-                }
-            }
+            for (int k = 0; k < kBatch; k++) t = acc_sub<VT, EXACT>(t, v[k], o[k]);
         }
     }
-#pragma unroll
-    for (int o = G / 2; o > 0; o >>= 1) {
-        if constexpr (VT == VT_I32) t = wadd(t, shfl_xor(t, o));
-        else t += shfl_xor(t, o);
-    }
-    if (valid && g == 0) {
-        if constexpr (VT == VT_I32) {
-            const long long s = wmul(t >> a.bit, (long long)__ldg((const int *)a.dinv + p)) >> a.dbit;
-            const int o = lo32(s);
-            ovf |= !fits32(s);
-            out[row] = o;
-            st_relaxed_u64(a.pk + row, ((unsigned long long)ep << 32) | (unsigned)o);
-        } else {
-            const V d = __ldg((const V *)a.dinv + p);
-            V r;
-            if constexpr (VT == VT_F64) r = __dmul_rn(t, d);
-            else r = __fmul_rn(t, d);
-            out[row] = r;
-            if constexpr (VT == VT_F64) st_release_u32(a.flag + row, ep);
-            else st_relaxed_u64(a.pk + row, ((unsigned long long)ep << 32) | __float_as_uint(r));
-        }
-    }
+    t = acc_reduce<VT>(t, G);
+    if (valid && g == 0) out[r.row] = acc_finish<VT>(t, r.dinv, a.bit, a.dbit, ovf);
 }
 
 template <int VT, int G, bool EXACT>
-__global__ void __launch_bounds__(kTriThreads) k_tri(TriArgs a, const void *in, void *out, unsigned *flags) {
+__global__ void __launch_bounds__(kTriThreads) k_tri(TriArgs a, const void *in_, void *out_, unsigned *flags) {
+    using V = vt_t<VT>;
+    const V *in = (const V *)in_;
+    V *out = (V *)out_;
     __shared__ int s_chunk;
     __shared__ unsigned s_epoch;
     if (threadIdx.x == 0) s_epoch = ld_acquire_u32(&a.sync->epoch) + 1;
     __syncthreads();
-    const unsigned ep = s_epoch;
+    const unsigned long long ep = s_epoch;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     constexpr int RPW = 32 / G;  // rows per warp per pass
     constexpr int NW = kTriThreads / 32;
     const int g = lane % G, sub = lane / G;
     bool ovf = false;
+    RowRegs<VT, G> r;
     for (;;) {
         if (threadIdx.x == 0) s_chunk = aborted(flags) ? a.nchunks : (int)atomicAdd(&a.sync->ticket, 1u);
         __syncthreads();
         const int ch = s_chunk;
         if (ch >= a.nchunks) break;
         const int s0 = __ldg(a.chunk_lv + ch), s1 = __ldg(a.chunk_lv + ch + 1);
-        for (int s = s0; s < s1; s++) {
-            const int p0 = __ldg(a.sub_bound + s), p1 = __ldg(a.sub_bound + s + 1);
-            for (int base = p0 + warp * RPW; base < p1; base += NW * RPW) {
-                const int p = base + sub;
-                tri_row<VT, G, EXACT>(a, p, p < p1, g, ep, in, out, flags, ovf);
-            }
-            if (s + 1 < s1) __syncthreads();
+        const int L0 = __ldg(a.sub_level + s0);
+        // row data of the first pass does not depend on the sweep: load it
+        // while the previous level completes
+        int p0 = __ldg(a.sub_bound + s0), p1 = __ldg(a.sub_bound + s0 + 1);
+        load_row<VT, G>(r, a, p0 + warp * RPW + sub, p0 + warp * RPW + sub < p1, g, in);
+        if (threadIdx.x == 0 && L0 > 0) {
+            const unsigned long long size = (unsigned long long)(__ldg(a.lvl_ptr + L0) - __ldg(a.lvl_ptr + L0 - 1));
+            wait_count(a.lvl_done + L0 - 1, ep * size, flags);
         }
         __syncthreads();
+        for (int s = s0; s < s1; s++) {
+            if (s > s0) {
+                p0 = p1;
+                p1 = __ldg(a.sub_bound + s + 1);
+                __syncthreads();  // earlier sub-level of this chunk written
+            }
+            bool first = true;
+            for (int base = p0 + warp * RPW; base < p1; base += NW * RPW) {
+                const int p = base + sub;
+                if (!first || s > s0) load_row<VT, G>(r, a, p, p < p1, g, in);
+                first = false;
+                compute_row<VT, G, EXACT>(r, a, p < p1, g, out, ovf);
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            __threadfence();
+            for (int s = s0; s < s1; s++)
+                atomicAdd(a.lvl_done + __ldg(a.sub_level + s),
+                          (unsigned long long)(__ldg(a.sub_bound + s + 1) - __ldg(a.sub_bound + s)));
+        }
     }
     if (ovf) atomicOr(flags, ST_OVERFLOW);
     if (threadIdx.x == 0) {
@@ -215,111 +249,128 @@ __global__ void __launch_bounds__(kTriThreads) k_tri(TriArgs a, const void *in, 
             a.sync->ticket = 0;
             a.sync->done = 0;
             __threadfence();
-            st_release_u32(&a.sync->epoch, ep);
+            st_release_u32(&a.sync->epoch, (unsigned)ep);
         }
     }
 }
 
 // ============================================================= single CTA
-
-template <int VT>
-struct RowPre {
-    int row, jb, je;
-    vt_t<VT> in, dinv;
-    int c[kCtaBatch];
-    vt_t<VT> v[kCtaBatch];
-};
-
-template <int VT, int G>
-__device__ __forceinline__ void cta_load(RowPre<VT> &r, const TriArgs &a, int p, bool valid, int g,
-                                         const vt_t<VT> *in) {
-    using V = vt_t<VT>;
-    r.row = 0;
-    r.jb = r.je = 0;
-    if (!valid) return;
-    r.row = __ldg(a.perm + p);
-    r.jb = __ldg(a.prp + p);
-    r.je = __ldg(a.prp + p + 1);
-    r.in = __ldg(in + r.row);
-    r.dinv = __ldg((const V *)a.dinv + p);
-#pragma unroll
-    for (int k = 0; k < kCtaBatch; k++) {
-        const int j = r.jb + g + k * G;
-        r.c[k] = j < r.je ? __ldg(a.pci + j) : 0;
-        r.v[k] = j < r.je ? __ldg((const V *)a.pval + j) : V(0);
-    }
-}
+//
+// Level block (host layout, 16-byte aligned, size a multiple of 16):
+//   int32 header[8] = {R, E, off_val, off_dinv, off_perm, off_rp, 0, 0}
+//   val[E] (V), dinv[R] (V), perm[R], rp[R+1] (0-based inside the block), pci[E]
 
 template <int VT, int G, bool EXACT>
-__device__ __forceinline__ void cta_row(const RowPre<VT> &r, const TriArgs &a, bool valid, int g,
-                                        vt_t<VT> *s_out, bool &ovf) {
+__device__ __forceinline__ void cta_level(const unsigned char *blk, vt_t<VT> *s_out, int bit, int dbit, int warp,
+                                          int sub, int g, bool &ovf) {
     using V = vt_t<VT>;
-    using A = typename std::conditional<VT == VT_I32, long long, V>::type;
-    A t = 0;
-    if (valid) {
-        if (g == 0) {
-            if constexpr (VT == VT_I32) t = wshl((long long)r.in, a.bit);
-            else t = r.in;
+    constexpr int RPW = 32 / G;
+    constexpr int NW = kCtaThreads / 32;
+    const int *hdr = (const int *)blk;
+    const int R = hdr[0];
+    const V *val = (const V *)(blk + hdr[2]);
+    const V *dv = (const V *)(blk + hdr[3]);
+    const int *perm = (const int *)(blk + hdr[4]);
+    const int *rp = (const int *)(blk + hdr[5]);
+    const int *pci = rp + R + 1;
+    for (int base = warp * RPW; base < R; base += NW * RPW) {
+        const int r = base + sub;
+        const bool valid = r < R;
+        acc_t<VT> t = 0;
+        int row = 0;
+        if (valid) {
+            row = perm[r];
+            const int jb = rp[r], je = rp[r + 1];
+            if (g == 0) t = acc_init<VT>(s_out[row], bit);
+            for (int j = jb + g; j < je; j += G) t = acc_sub<VT, EXACT>(t, val[j], s_out[pci[j]]);
         }
-#pragma unroll
-        for (int k = 0; k < kCtaBatch; k++)
-            if (r.jb + g + k * G < r.je) t = acc_sub<VT, EXACT>(t, r.v[k], s_out[r.c[k]]);
-        for (int j = r.jb + g + kCtaBatch * G; j < r.je; j += G)
-            t = acc_sub<VT, EXACT>(t, __ldg((const V *)a.pval + j), s_out[__ldg(a.pci + j)]);
-    }
-#pragma unroll
-    for (int o = G / 2; o > 0; o >>= 1) {
-        if constexpr (VT == VT_I32) t = wadd(t, shfl_xor(t, o));
-        else t += shfl_xor(t, o);
-    }
-    if (valid && g == 0) {
-        if constexpr (VT == VT_I32) {
-            const long long s = wmul(t >> a.bit, (long long)r.dinv) >> a.dbit;
-            ovf |= !fits32(s);
-            s_out[r.row] = lo32(s);
-        } else if constexpr (VT == VT_F64) {
-            s_out[r.row] = __dmul_rn(t, r.dinv);
-        } else {
-            s_out[r.row] = __fmul_rn(t, r.dinv);
-        }
+        t = acc_reduce<VT>(t, G);
+        if (valid && g == 0) s_out[row] = acc_finish<VT>(t, dv[r], bit, dbit, ovf);
     }
 }
 
 template <int VT, int G, bool EXACT>
 __global__ void __launch_bounds__(kCtaThreads, 1)
-k_tri_cta(TriArgs a, const int *__restrict__ lvl_ptr, int nlev, const void *in_, void *out_, unsigned *flags) {
+k_tri_cta(const unsigned char *__restrict__ blocks, const long long *__restrict__ blk_off, int nlev, int n,
+          int bit, int dbit, int stage_bytes, const void *in_, void *out_, unsigned *flags) {
     using V = vt_t<VT>;
-    extern __shared__ unsigned char smem_raw[];
+    extern __shared__ __align__(16) unsigned char smem_raw[];
     V *s_out = (V *)smem_raw;
+    const size_t vec_bytes = ((size_t)n * sizeof(V) + 15) & ~(size_t)15;
+    unsigned char *stage = smem_raw + vec_bytes;
+    unsigned long long *bar = (unsigned long long *)(stage + (size_t)kStages * stage_bytes);
     const V *in = (const V *)in_;
     V *out = (V *)out_;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    constexpr int RPW = 32 / G;
-    constexpr int NW = kCtaThreads / 32;
     const int g = lane % G, sub = lane / G;
-    const int gid = warp * RPW + sub;
     bool ovf = false;
-    RowPre<VT> pre, cur;
-    int p0 = nlev > 0 ? __ldg(lvl_ptr) : 0;
-    int p1 = nlev > 0 ? __ldg(lvl_ptr + 1) : 0;
-    cta_load<VT, G>(pre, a, p0 + gid, p0 + gid < p1, g, in);
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < kStages; s++) mbar_init(bar + s, 1);
+        fence_mbar_init();
+    }
+    for (int i = threadIdx.x; i < n; i += kCtaThreads) s_out[i] = in[i];
+    __syncthreads();
+    auto issue = [&](int d) {  // thread 0: bring level d's block into its stage
+        const long long o0 = __ldg(blk_off + d), o1 = __ldg(blk_off + d + 1);
+        const unsigned bytes = (unsigned)(o1 - o0);
+        if ((int)bytes > stage_bytes) return;
+        const int s = d % kStages;
+        fence_proxy_async_smem();
+        mbar_expect_tx(bar + s, bytes);
+        bulk_g2s(stage + (size_t)s * stage_bytes, blocks + o0, bytes, bar + s);
+    };
+    if (threadIdx.x == 0)
+        for (int d = 0; d < nlev && d < kStages; d++) issue(d);
+    unsigned phase = 0;  // bit s: parity of stage s's next completion
+    int stuck = -1;      // level whose copy did not arrive in time
     for (int d = 0; d < nlev; d++) {
-        cur = pre;
-        const int q0 = p1, q1 = d + 2 <= nlev ? __ldg(lvl_ptr + d + 2) : p1;
-        // the next level's first row of this group, loaded while this level runs
-        cta_load<VT, G>(pre, a, q0 + gid, q0 + gid < q1, g, in);
-        bool first = true;
-        for (int base = p0 + warp * RPW; base < p1; base += NW * RPW) {
-            const int p = base + sub;
-            if (!first) cta_load<VT, G>(cur, a, p, p < p1, g, in);
-            first = false;
-            cta_row<VT, G, EXACT>(cur, a, p < p1, g, s_out, ovf);
+        const long long o0 = __ldg(blk_off + d), o1 = __ldg(blk_off + d + 1);
+        const bool staged = (int)(o1 - o0) <= stage_bytes;
+        const int s = d % kStages;
+        const unsigned char *blk = blocks + o0;
+        bool timed_out = false;
+        if (staged) {
+            // bounded wait for the bulk copy of this level
+            const unsigned par = (phase >> s) & 1u;
+            if (!mbar_try_wait(bar + s, par)) {
+                const unsigned long long t0 = globaltimer_ns();
+                while (!mbar_try_wait(bar + s, par)) {
+                    if (globaltimer_ns() - t0 > kSpinLimitNs) {
+                        timed_out = true;
+                        break;
+                    }
+                }
+            }
+            blk = stage + (size_t)s * stage_bytes;
+        }
+        if (__syncthreads_or(timed_out)) {
+            stuck = d;
+            break;
+        }
+        if (staged) phase ^= 1u << s;
+        cta_level<VT, G, EXACT>(blk, s_out, bit, dbit, warp, sub, g, ovf);
+        __syncthreads();
+        if (threadIdx.x == 0 && d + kStages < nlev) issue(d + kStages);
+    }
+    if (stuck >= 0) {
+        // report, then wait (bounded) for the copies this CTA still has in
+        // flight before its shared memory goes away
+        if (threadIdx.x == 0) {
+            atomicOr(flags, ST_TIMEOUT);
+            const unsigned long long t0 = globaltimer_ns();
+            for (int dd = stuck; dd < nlev && dd < stuck + kStages; dd++) {
+                if ((int)(__ldg(blk_off + dd + 1) - __ldg(blk_off + dd)) > stage_bytes) continue;
+                const int s = dd % kStages;
+                while (!mbar_try_wait(bar + s, (phase >> s) & 1u) && globaltimer_ns() - t0 < kSpinLimitNs) {
+                }
+                phase ^= 1u << s;
+            }
         }
         __syncthreads();
-        p0 = q0;
-        p1 = q1;
+        return;
     }
-    for (int i = threadIdx.x; i < a.n; i += kCtaThreads) out[i] = s_out[i];
+    for (int i = threadIdx.x; i < n; i += kCtaThreads) out[i] = s_out[i];
     if (ovf) atomicOr(flags, ST_OVERFLOW);
 }
 
@@ -333,15 +384,18 @@ void DevTri::release() {
     dfree(dinv);
     dfree(chunk_lv);
     dfree(sub_bound);
+    dfree(chunk_level);
     dfree(lvl_ptr);
-    dfree(pk);
-    dfree(flag);
+    dfree(lvl_done);
     dfree(sync);
-    perm = prp = pci = chunk_lv = sub_bound = lvl_ptr = nullptr;
+    dfree(blocks);
+    dfree(blk_off);
+    perm = prp = pci = chunk_lv = sub_bound = chunk_level = lvl_ptr = nullptr;
     pval = dinv = nullptr;
-    pk = nullptr;
-    flag = nullptr;
+    lvl_done = nullptr;
     sync = nullptr;
+    blocks = nullptr;
+    blk_off = nullptr;
 }
 
 template <typename T>
@@ -351,6 +405,40 @@ static void gather_vals(const TriSchedule &s, const T *vals, std::vector<T> &pv,
     dv.assign(s.n, T(0));
     for (int p = 0; p < s.n; p++)
         if (s.diag_src[p] >= 0) dv[p] = vals[s.diag_src[p]];
+}
+
+static size_t up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+// one block per level (see the layout above k_tri_cta)
+template <typename T>
+static void build_blocks(const TriSchedule &s, const std::vector<T> &pv, const std::vector<T> &dv,
+                         std::vector<unsigned char> &blob, std::vector<long long> &off) {
+    off.assign(s.nlev + 1, 0);
+    blob.clear();
+    for (int l = 0; l < s.nlev; l++) {
+        const int p0 = s.lvl_ptr[l], p1 = s.lvl_ptr[l + 1];
+        const int R = p1 - p0;
+        const int e0 = s.prp[p0], e1 = s.prp[p1];
+        const int E = e1 - e0;
+        const size_t o_val = 32;
+        const size_t o_dinv = up(o_val + sizeof(T) * E, 8);
+        const size_t o_perm = up(o_dinv + sizeof(T) * R, 4);
+        const size_t o_rp = o_perm + 4 * (size_t)R;
+        const size_t o_pci = o_rp + 4 * (size_t)(R + 1);
+        const size_t size = up(o_pci + 4 * (size_t)E, 16);
+        const size_t base = blob.size();
+        blob.resize(base + size, 0);
+        unsigned char *b = blob.data() + base;
+        int hdr[8] = {R, E, (int)o_val, (int)o_dinv, (int)o_perm, (int)o_rp, 0, 0};
+        memcpy(b, hdr, sizeof hdr);
+        memcpy(b + o_val, pv.data() + e0, sizeof(T) * E);
+        memcpy(b + o_dinv, dv.data() + p0, sizeof(T) * R);
+        memcpy(b + o_perm, s.perm.data() + p0, 4 * (size_t)R);
+        int *rp = (int *)(b + o_rp);
+        for (int r = 0; r <= R; r++) rp[r] = s.prp[p0 + r] - e0;
+        memcpy(b + o_pci, s.pci.data() + e0, 4 * (size_t)E);
+        off[l + 1] = (long long)blob.size();
+    }
 }
 
 static int pow2_at_least(double x) {
@@ -370,11 +458,11 @@ DevTri upload_tri(const Ctx &c, int n, const int *rptr, const int *cind, const v
     d.dbit = dbit;
     const int64_t nnz = n ? rptr[n] : 0;
     const double avg = n ? (double)(nnz - n) / n : 0.0;
-    d.one_cta = (size_t)n * vt_size(vt) <= kCtaSmem;
-    int G;
-    if (d.one_cta) G = pow2_at_least(avg / kCtaBatch);        // registers hold G * kCtaBatch entries
-    else G = pow2_at_least(avg / kBatch);                    // one batch covers a typical row
-    if (vt != VT_I32 && c.fp_exact) G = 1;                   // sequential order inside a row
+    const size_t es = vt_size(vt);
+    const size_t vec_bytes = up((size_t)n * es, 16);
+    d.one_cta = vec_bytes <= kCtaVecMax;
+    int G = pow2_at_least(avg / (d.one_cta ? 4 : kBatch));
+    if (vt != VT_I32 && c.fp_exact) G = 1;  // sequential order inside a row
     d.group = G;
     const int rows_per_chunk = 2 * kTriThreads / G;
     TriSchedule s = build_tri_schedule(rptr, cind, n, kind, rows_per_chunk, 1 << 20);
@@ -382,51 +470,53 @@ DevTri upload_tri(const Ctx &c, int n, const int *rptr, const int *cind, const v
     d.max_level_rows = s.max_level_rows;
     d.nnz_off = (int64_t)s.pci.size();
     d.nchunks = s.nchunks();
-    d.perm = dupload(s.perm);
-    d.prp = dupload(s.prp);
-    d.pci = s.pci.empty() ? (int *)dmalloc(16) : dupload(s.pci);
-    if (vt == VT_I32) {
-        std::vector<int32_t> pv, dv;
-        gather_vals(s, (const int32_t *)vals, pv, dv);
-        d.pval = pv.empty() ? dmalloc(16) : (void *)dupload(pv);
-        d.dinv = dupload(dv);
-    } else if (vt == VT_F64) {
-        std::vector<double> pv, dv;
-        gather_vals(s, (const double *)vals, pv, dv);
-        d.pval = pv.empty() ? dmalloc(16) : (void *)dupload(pv);
-        d.dinv = dupload(dv);
-    } else {
-        std::vector<float> pv, dv;
-        gather_vals(s, (const float *)vals, pv, dv);
-        d.pval = pv.empty() ? dmalloc(16) : (void *)dupload(pv);
-        d.dinv = dupload(dv);
-    }
-    d.chunk_lv = dupload(s.chunk_lv);
-    d.sub_bound = dupload(s.sub_bound);
-    d.lvl_ptr = dupload(s.lvl_ptr);
-    if (!d.one_cta) {
-        if (vt == VT_F64) {
-            d.flag = (unsigned *)dmalloc(sizeof(unsigned) * std::max(n, 1));
-            SAGB_CUDA(cudaMemset(d.flag, 0, sizeof(unsigned) * std::max(n, 1)));
+    std::vector<unsigned char> blob;
+    std::vector<long long> off;
+    auto put_vals = [&](auto tag) {
+        using T = decltype(tag);
+        std::vector<T> pv, dv;
+        gather_vals(s, (const T *)vals, pv, dv);
+        if (d.one_cta) {
+            build_blocks(s, pv, dv, blob, off);
         } else {
-            d.pk = (unsigned long long *)dmalloc(sizeof(unsigned long long) * std::max(n, 1));
-            SAGB_CUDA(cudaMemset(d.pk, 0, sizeof(unsigned long long) * std::max(n, 1)));
+            d.pval = pv.empty() ? dmalloc(16) : (void *)dupload(pv);
+            d.dinv = dupload(dv);
         }
+    };
+    if (vt == VT_I32) put_vals(int32_t());
+    else if (vt == VT_F64) put_vals(double());
+    else put_vals(float());
+    if (d.one_cta) {
+        d.blocks = blob.empty() ? (unsigned char *)dmalloc(16) : dupload(blob);
+        d.blk_off = dupload(off);
+        const size_t avail = kSmemMax - vec_bytes - 64;
+        d.stage_bytes = (int)std::min<size_t>(avail / kStages / 16 * 16, 64 * 1024);
+        d.cta_smem = vec_bytes + (size_t)kStages * d.stage_bytes + 8 * kStages;
+    } else {
+        d.perm = dupload(s.perm);
+        d.prp = dupload(s.prp);
+        d.pci = s.pci.empty() ? (int *)dmalloc(16) : dupload(s.pci);
+        d.chunk_lv = dupload(s.chunk_lv);
+        d.sub_bound = dupload(s.sub_bound);
+        d.chunk_level = dupload(s.sub_level);
+        d.lvl_ptr = dupload(s.lvl_ptr);
+        d.lvl_done = (unsigned long long *)dmalloc(sizeof(unsigned long long) * std::max(s.nlev, 1));
+        SAGB_CUDA(cudaMemset(d.lvl_done, 0, sizeof(unsigned long long) * std::max(s.nlev, 1)));
         d.sync = (TriSync *)dmalloc(sizeof(TriSync));
         SAGB_CUDA(cudaMemset(d.sync, 0, sizeof(TriSync)));
+        d.grid = std::max(1, std::min(d.nchunks, c.num_sms * 2));
     }
-    d.grid = std::max(1, std::min(d.nchunks, c.num_sms * 4));
     return d;
 }
 
 template <int VT, int G, bool EXACT>
 static void launch_tri(Ctx &c, const DevTri &T, const void *in, void *out) {
-    TriArgs a{T.n, T.nchunks, T.bit, T.dbit, T.perm, T.prp, T.pci, T.pval, T.dinv,
-              T.chunk_lv, T.sub_bound, T.pk, T.flag, T.sync};
     if (T.one_cta) {
-        const size_t smem = (size_t)T.n * sizeof(vt_t<VT>);
-        k_tri_cta<VT, G, EXACT><<<1, kCtaThreads, smem, c.stream>>>(a, T.lvl_ptr, T.nlev, in, out, c.d_flags);
+        k_tri_cta<VT, G, EXACT><<<1, kCtaThreads, T.cta_smem, c.stream>>>(
+            T.blocks, T.blk_off, T.nlev, T.n, T.bit, T.dbit, T.stage_bytes, in, out, c.d_flags);
     } else {
+        TriArgs a{T.n, T.nchunks, T.bit, T.dbit, T.perm, T.prp, T.pci, T.pval, T.dinv,
+                  T.chunk_lv, T.sub_bound, T.chunk_level, T.lvl_ptr, T.lvl_done, T.sync};
         k_tri<VT, G, EXACT><<<T.grid, kTriThreads, 0, c.stream>>>(a, in, out, c.d_flags);
     }
     c.launches++;
@@ -474,8 +564,8 @@ __global__ void __launch_bounds__(kLuThreads, 1)
 k_dense_lu(int n, const void *__restrict__ L_, const void *__restrict__ U_, const void *__restrict__ dinv_,
            int bitL, int bitU, int dbitU, const void *__restrict__ in_, void *__restrict__ out_, unsigned *flags) {
     using V = vt_t<VT>;
-    using T = typename std::conditional<VT == VT_I32, long long, V>::type;
-    extern __shared__ unsigned char smem_raw[];
+    using T = acc_t<VT>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
     T *t = (T *)smem_raw;                           // n accumulators
     V *x = (V *)(smem_raw + sizeof(T) * (size_t)n); // n solved values
     const V *L = (const V *)L_;
@@ -487,10 +577,7 @@ k_dense_lu(int n, const void *__restrict__ L_, const void *__restrict__ U_, cons
     bool ovf = false;
 
     // ---------------- forward: unit lower, t = in << bit
-    for (int i = tid; i < n; i += kLuThreads) {
-        if constexpr (VT == VT_I32) t[i] = wshl((long long)in[i], bitL);
-        else t[i] = in[i];
-    }
+    for (int i = tid; i < n; i += kLuThreads) t[i] = acc_init<VT>(in[i], bitL);
     __syncthreads();
     for (int k0 = 0; k0 < n; k0 += 32) {
         const int kb = min(32, n - k0);
@@ -507,11 +594,7 @@ k_dense_lu(int n, const void *__restrict__ L_, const void *__restrict__ U_, cons
                 const V *row = L + (size_t)(k0 + warp) * n;
                 T acc = 0;
                 for (int c = lane; c < k0; c += 32) acc = acc_sub<VT, false>(acc, __ldg(row + c), x[c]);
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1) {
-                    if constexpr (VT == VT_I32) acc = wadd(acc, shfl_xor(acc, o));
-                    else acc += shfl_xor(acc, o);
-                }
+                acc = acc_reduce<VT>(acc, 32);
                 if (lane == 0) {
                     if constexpr (VT == VT_I32) t[k0 + warp] = wadd(t[k0 + warp], acc);
                     else t[k0 + warp] += acc;
@@ -544,10 +627,7 @@ k_dense_lu(int n, const void *__restrict__ L_, const void *__restrict__ U_, cons
         __syncthreads();
     }
     // ---------------- backward: D^-1 U, last panel first
-    for (int i = tid; i < n; i += kLuThreads) {
-        if constexpr (VT == VT_I32) t[i] = wshl((long long)x[i], bitU);
-        else t[i] = x[i];
-    }
+    for (int i = tid; i < n; i += kLuThreads) t[i] = acc_init<VT>(x[i], bitU);
     __syncthreads();
     for (int k1 = n; k1 > 0; k1 -= 32) {
         const int kb = min(32, k1);
@@ -564,11 +644,7 @@ k_dense_lu(int n, const void *__restrict__ L_, const void *__restrict__ U_, cons
                 const V *row = U + (size_t)(k0 + warp) * n;
                 T acc = 0;
                 for (int c = k1 + lane; c < n; c += 32) acc = acc_sub<VT, false>(acc, __ldg(row + c), x[c]);
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1) {
-                    if constexpr (VT == VT_I32) acc = wadd(acc, shfl_xor(acc, o));
-                    else acc += shfl_xor(acc, o);
-                }
+                acc = acc_reduce<VT>(acc, 32);
                 if (lane == 0) {
                     if constexpr (VT == VT_I32) t[k0 + warp] = wadd(t[k0 + warp], acc);
                     else t[k0 + warp] += acc;
@@ -587,17 +663,7 @@ k_dense_lu(int n, const void *__restrict__ L_, const void *__restrict__ U_, cons
             for (int c = 31; c >= 0; c--) {
                 if (c < kb) {
                     V xc = V(0);
-                    if (lane == c) {
-                        if constexpr (VT == VT_I32) {
-                            const long long s = wmul(tr >> bitU, (long long)dv) >> dbitU;
-                            ovf |= !fits32(s);
-                            xc = lo32(s);
-                        } else if constexpr (VT == VT_F64) {
-                            xc = __dmul_rn(tr, dv);
-                        } else {
-                            xc = __fmul_rn(tr, dv);
-                        }
-                    }
+                    if (lane == c) xc = acc_finish<VT>(tr, dv, bitU, dbitU, ovf);
                     xc = __shfl_sync(0xffffffffu, xc, c);
                     if (lane < c) tr = acc_sub<VT, EXACT>(tr, dblk[c], xc);
                     if (lane == c) x[k0 + c] = xc;
@@ -658,9 +724,7 @@ DevDenseLU upload_dense_lu(const int *Lrptr, const int *Lcind, const void *Lval,
 
 template <int VT, bool EXACT>
 static void launch_lu(Ctx &c, const DevDenseLU &LU, const void *in, void *out) {
-    const size_t acc = VT == VT_F32 ? 4 : 8;
-    const size_t val = VT == VT_F64 ? 8 : 4;
-    const size_t smem = (acc + val) * (size_t)LU.n;
+    const size_t smem = (sizeof(acc_t<VT>) + sizeof(vt_t<VT>)) * (size_t)LU.n;
     k_dense_lu<VT, EXACT><<<1, kLuThreads, smem, c.stream>>>(LU.n, LU.L, LU.U, LU.dinv, LU.bitL, LU.bitU,
                                                                 LU.dbitU, in, out, c.d_flags);
     c.launches++;
@@ -668,7 +732,7 @@ static void launch_lu(Ctx &c, const DevDenseLU &LU, const void *in, void *out) {
 
 template <int VT, bool EXACT>
 static void cta_attrs() {
-    const int mx = 227 * 1024;
+    const int mx = (int)kSmemMax;
     SAGB_CUDA(cudaFuncSetAttribute(k_tri_cta<VT, 1, EXACT>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
     SAGB_CUDA(cudaFuncSetAttribute(k_tri_cta<VT, 2, EXACT>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
     SAGB_CUDA(cudaFuncSetAttribute(k_tri_cta<VT, 4, EXACT>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
@@ -688,7 +752,7 @@ void init_kernel_attributes() {
 
 void lu_solve(Ctx &c, const DevDenseLU &LU, const void *in, void *out) {
     if (LU.n == 0) return;
-    if ((size_t)LU.n * 16 > 227 * 1024) throw CudaError{"coarsest level too large for the dense LU kernel"};
+    if ((size_t)LU.n * 16 > kSmemMax) throw CudaError{"coarsest level too large for the dense LU kernel"};
     if (LU.vt == VT_I32) return launch_lu<VT_I32, false>(c, LU, in, out);
     if (LU.vt == VT_F64) return c.fp_exact ? launch_lu<VT_F64, true>(c, LU, in, out)
                                            : launch_lu<VT_F64, false>(c, LU, in, out);

@@ -85,6 +85,7 @@ TriSchedule build_tri_schedule(const int *rptr, const int *cind, int n, int kind
             for (int q = 0; q < pieces; q++) {
                 const int a = lptr[l] + (int)((int64_t)sz * q / pieces);
                 s.sub_bound.push_back(a);
+                s.sub_level.push_back(l);
                 s.chunk_lv.push_back((int)s.sub_bound.size());
             }
             l++;
@@ -95,6 +96,7 @@ TriSchedule build_tri_schedule(const int *rptr, const int *cind, int n, int kind
                 const int z = lptr[l + 1] - lptr[l];
                 if (runl > 0 && (z > rows_per_chunk / 2 || rows + z > rows_per_chunk)) break;
                 s.sub_bound.push_back(lptr[l]);
+                s.sub_level.push_back(l);
                 rows += z;
                 runl++;
                 l++;

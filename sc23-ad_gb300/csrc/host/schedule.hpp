@@ -35,6 +35,7 @@ struct TriSchedule {
     std::vector<int> chunk_lv;            // chunk c covers sub-levels [chunk_lv[c], chunk_lv[c+1])
     std::vector<int> sub_bound;           // sub-level s covers positions [sub_bound[s], sub_bound[s+1])
     std::vector<int> lvl_ptr;             // level l covers positions [lvl_ptr[l], lvl_ptr[l+1])
+    std::vector<int> sub_level;           // level of each sub-level
     int max_level_rows = 0;
     int nchunks() const { return (int)chunk_lv.size() - 1; }
 };
