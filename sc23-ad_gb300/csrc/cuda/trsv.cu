@@ -16,12 +16,13 @@
 //    aligned block that a bulk copy (cp.async.bulk + mbarrier) brings into a
 //    ring of shared-memory stages several levels ahead, so a level costs shared
 //    memory traffic and one block barrier.
-//  * k_tri (fine levels): CTAs claim chunks of level-ordered rows by ticket.
-//    Before a chunk of level L runs, one thread waits until level L-1 is
-//    complete (a per-level counter, cumulative over sweeps).  Level L-1
-//    complete implies every earlier level is complete, because each of its
-//    rows waited the same way.  Chunks are claimed in level order, so the wait
-//    cannot deadlock.  One poller per CTA keeps L2 free of spin traffic.
+//  * k_tri (fine levels): one CTA per SM claims chunks of level-ordered rows
+//    by ticket; a row waits only for the rows it reads.  Integer and FP32
+//    results are published as one 64-bit word {epoch, value}, so a dependency
+//    costs one L2 load; FP64 results use an epoch flag with release/acquire.
+//    Each lane reads a batch of dependencies at once and spins only on those
+//    not yet published.  Chunks are claimed in level order and depend only on
+//    earlier chunks, so the waits cannot deadlock.
 // All waits are bounded in time (ST_TIMEOUT); ticket and epoch are advanced by
 // the last CTA, so both kernels replay from a CUDA graph.
 #include <algorithm>
@@ -90,156 +91,142 @@ struct TriArgs {
     int n, nchunks, bit, dbit;
     const int *perm, *prp, *pci;
     const void *pval, *dinv;
-    const int *chunk_lv, *sub_bound, *sub_level, *lvl_ptr;
-    unsigned long long *lvl_done;
+    const int *chunk_lv, *sub_bound;
+    unsigned long long *pk;
+    unsigned *flag;
     TriSync *sync;
 };
 
-__device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long *p) {
-    unsigned long long v;
-    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
-    return v;
-}
-
-// thread 0: wait until the counter reaches target (bounded)
-__device__ __forceinline__ void wait_count(const unsigned long long *cnt, unsigned long long target,
-                                           unsigned *flags) {
-    if (ld_acquire_u64(cnt) >= target) return;
+// spin on one packed {epoch, value} word until it carries epoch ep (bounded;
+// the shared status word is read only on the slow path)
+__device__ __forceinline__ unsigned long long wait_packed(unsigned long long *pk, int c, unsigned ep,
+                                                          unsigned *flags) {
     const unsigned long long t0 = globaltimer_ns();
     for (unsigned it = 1;; it++) {
-        if (ld_acquire_u64(cnt) >= target) return;
-        if ((it & 31u) == 0) {
-            if (aborted(flags)) return;
+        const unsigned long long w = ld_relaxed_u64(pk + c);
+        if ((unsigned)(w >> 32) == ep) return w;
+        if ((it & 255u) == 0) {
+            if (globaltimer_ns() - t0 > kSpinLimitNs) {
+                atomicOr(flags, ST_TIMEOUT);
+                return w;
+            }
+            if (aborted(flags)) return w;
+        }
+    }
+}
+
+__device__ __forceinline__ void wait_flag(const unsigned *flag, int c, unsigned ep, unsigned *flags) {
+    const unsigned long long t0 = globaltimer_ns();
+    for (unsigned it = 1;; it++) {
+        if (ld_relaxed_u32(flag + c) == ep) return;
+        if ((it & 255u) == 0) {
             if (globaltimer_ns() - t0 > kSpinLimitNs) {
                 atomicOr(flags, ST_TIMEOUT);
                 return;
             }
+            if (aborted(flags)) return;
         }
     }
 }
 
-template <int VT, int G>
-struct RowRegs {
-    int row, jb, je;
-    vt_t<VT> in, dinv;
-    int c[kBatch];
-    vt_t<VT> v[kBatch];
-};
-
-template <int VT, int G>
-__device__ __forceinline__ void load_row(RowRegs<VT, G> &r, const TriArgs &a, int p, bool valid, int g,
-                                         const vt_t<VT> *in) {
-    using V = vt_t<VT>;
-    r.row = 0;
-    r.jb = r.je = 0;
-    r.in = V(0);
-    r.dinv = V(0);
-#pragma unroll
-    for (int k = 0; k < kBatch; k++) {
-        r.c[k] = 0;
-        r.v[k] = V(0);
-    }
-    if (!valid) return;
-    r.row = __ldg(a.perm + p);
-    r.jb = __ldg(a.prp + p);
-    r.je = __ldg(a.prp + p + 1);
-    r.in = __ldg(in + r.row);
-    r.dinv = __ldg((const V *)a.dinv + p);
-#pragma unroll
-    for (int k = 0; k < kBatch; k++) {
-        const int j = r.jb + g + k * G;
-        if (j < r.je) {
-            r.c[k] = __ldg(a.pci + j);
-            r.v[k] = __ldg((const V *)a.pval + j);
-        }
-    }
+__device__ __forceinline__ double ld_relaxed_f64(const double *p) {
+    double v;
+    asm volatile("ld.relaxed.gpu.global.f64 %0, [%1];" : "=d"(v) : "l"(p) : "memory");
+    return v;
 }
 
+// one row, G lanes; each lane reads kBatch dependencies at a time, all
+// together, and spins only on those not yet published
 template <int VT, int G, bool EXACT>
-__device__ __forceinline__ void compute_row(const RowRegs<VT, G> &r, const TriArgs &a, bool valid, int g,
-                                            vt_t<VT> *out, bool &ovf) {
+__device__ __forceinline__ void tri_row(const TriArgs &a, int p, bool valid, int g, unsigned ep, const void *in_,
+                                        void *out_, unsigned *flags, bool &ovf) {
     using V = vt_t<VT>;
+    const V *in = (const V *)in_;
+    V *out = (V *)out_;
+    const V *pv = (const V *)a.pval;
     acc_t<VT> t = 0;
+    int row = 0;
     if (valid) {
-        if (g == 0) t = acc_init<VT>(r.in, a.bit);
-        // the first batch is in registers: read all its dependencies at once
-        V o[kBatch];
-#pragma unroll
-        for (int k = 0; k < kBatch; k++) o[k] = r.jb + g + k * G < r.je ? __ldcg(out + r.c[k]) : V(0);
-#pragma unroll
-        for (int k = 0; k < kBatch; k++) t = acc_sub<VT, EXACT>(t, r.v[k], o[k]);
-        for (int j0 = r.jb + g + kBatch * G; j0 < r.je; j0 += kBatch * G) {
+        row = __ldg(a.perm + p);
+        if (g == 0) t = acc_init<VT>(__ldg(in + row), a.bit);
+        const int jb = __ldg(a.prp + p), je = __ldg(a.prp + p + 1);
+        for (int j0 = jb + g; j0 < je; j0 += G * kBatch) {
             int c[kBatch];
             V v[kBatch];
 #pragma unroll
             for (int k = 0; k < kBatch; k++) {
                 const int j = j0 + k * G;
-                c[k] = j < r.je ? __ldg(a.pci + j) : -1;
-                v[k] = j < r.je ? __ldg((const V *)a.pval + j) : V(0);
+                c[k] = j < je ? __ldg(a.pci + j) : -1;
+                v[k] = j < je ? __ldg(pv + j) : V(0);
             }
+            if constexpr (VT == VT_F64) {
+                unsigned f[kBatch];
 #pragma unroll
-            for (int k = 0; k < kBatch; k++) o[k] = c[k] >= 0 ? __ldcg(out + c[k]) : V(0);
+                for (int k = 0; k < kBatch; k++) f[k] = c[k] >= 0 ? ld_relaxed_u32(a.flag + c[k]) : ep;
 #pragma unroll
-            for (int k = 0; k < kBatch; k++) t = acc_sub<VT, EXACT>(t, v[k], o[k]);
+                for (int k = 0; k < kBatch; k++)
+                    if (f[k] != ep) wait_flag(a.flag, c[k], ep, flags);
+                fence_acq_rel_gpu();  // the flags were released after the values
+#pragma unroll
+                for (int k = 0; k < kBatch; k++)
+                    if (c[k] >= 0) t = acc_sub<VT, EXACT>(t, v[k], ld_relaxed_f64((const double *)out + c[k]));
+            } else {
+                unsigned long long w[kBatch];
+#pragma unroll
+                for (int k = 0; k < kBatch; k++) w[k] = c[k] >= 0 ? ld_relaxed_u64(a.pk + c[k]) : 0ull;
+#pragma unroll
+                for (int k = 0; k < kBatch; k++) {
+                    if (c[k] < 0) continue;
+                    if ((unsigned)(w[k] >> 32) != ep) w[k] = wait_packed(a.pk, c[k], ep, flags);
+                    V o;
+                    if constexpr (VT == VT_I32) o = (int)(unsigned)w[k];
+                    else o = __uint_as_float((unsigned)w[k]);
+                    t = acc_sub<VT, EXACT>(t, v[k], o);
+                }
+            }
         }
     }
     t = acc_reduce<VT>(t, G);
-    if (valid && g == 0) out[r.row] = acc_finish<VT>(t, r.dinv, a.bit, a.dbit, ovf);
+    if (valid && g == 0) {
+        const V r = acc_finish<VT>(t, __ldg((const V *)a.dinv + p), a.bit, a.dbit, ovf);
+        out[row] = r;
+        if constexpr (VT == VT_F64) {
+            st_release_u32(a.flag + row, ep);
+        } else if constexpr (VT == VT_I32) {
+            st_relaxed_u64(a.pk + row, ((unsigned long long)ep << 32) | (unsigned)r);
+        } else {
+            st_relaxed_u64(a.pk + row, ((unsigned long long)ep << 32) | __float_as_uint(r));
+        }
+    }
 }
 
 template <int VT, int G, bool EXACT>
-__global__ void __launch_bounds__(kTriThreads) k_tri(TriArgs a, const void *in_, void *out_, unsigned *flags) {
-    using V = vt_t<VT>;
-    const V *in = (const V *)in_;
-    V *out = (V *)out_;
+__global__ void __launch_bounds__(kTriThreads) k_tri(TriArgs a, const void *in, void *out, unsigned *flags) {
     __shared__ int s_chunk;
     __shared__ unsigned s_epoch;
     if (threadIdx.x == 0) s_epoch = ld_acquire_u32(&a.sync->epoch) + 1;
     __syncthreads();
-    const unsigned long long ep = s_epoch;
+    const unsigned ep = s_epoch;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     constexpr int RPW = 32 / G;  // rows per warp per pass
     constexpr int NW = kTriThreads / 32;
     const int g = lane % G, sub = lane / G;
     bool ovf = false;
-    RowRegs<VT, G> r;
     for (;;) {
         if (threadIdx.x == 0) s_chunk = aborted(flags) ? a.nchunks : (int)atomicAdd(&a.sync->ticket, 1u);
         __syncthreads();
         const int ch = s_chunk;
         if (ch >= a.nchunks) break;
         const int s0 = __ldg(a.chunk_lv + ch), s1 = __ldg(a.chunk_lv + ch + 1);
-        const int L0 = __ldg(a.sub_level + s0);
-        // row data of the first pass does not depend on the sweep: load it
-        // while the previous level completes
-        int p0 = __ldg(a.sub_bound + s0), p1 = __ldg(a.sub_bound + s0 + 1);
-        load_row<VT, G>(r, a, p0 + warp * RPW + sub, p0 + warp * RPW + sub < p1, g, in);
-        if (threadIdx.x == 0 && L0 > 0) {
-            const unsigned long long size = (unsigned long long)(__ldg(a.lvl_ptr + L0) - __ldg(a.lvl_ptr + L0 - 1));
-            wait_count(a.lvl_done + L0 - 1, ep * size, flags);
-        }
-        __syncthreads();
         for (int s = s0; s < s1; s++) {
-            if (s > s0) {
-                p0 = p1;
-                p1 = __ldg(a.sub_bound + s + 1);
-                __syncthreads();  // earlier sub-level of this chunk written
-            }
-            bool first = true;
+            const int p0 = __ldg(a.sub_bound + s), p1 = __ldg(a.sub_bound + s + 1);
             for (int base = p0 + warp * RPW; base < p1; base += NW * RPW) {
                 const int p = base + sub;
-                if (!first || s > s0) load_row<VT, G>(r, a, p, p < p1, g, in);
-                first = false;
-                compute_row<VT, G, EXACT>(r, a, p < p1, g, out, ovf);
+                tri_row<VT, G, EXACT>(a, p, p < p1, g, ep, in, out, flags, ovf);
             }
+            if (s + 1 < s1) __syncthreads();
         }
         __syncthreads();
-        if (threadIdx.x == 0) {
-            __threadfence();
-            for (int s = s0; s < s1; s++)
-                atomicAdd(a.lvl_done + __ldg(a.sub_level + s),
-                          (unsigned long long)(__ldg(a.sub_bound + s + 1) - __ldg(a.sub_bound + s)));
-        }
     }
     if (ovf) atomicOr(flags, ST_OVERFLOW);
     if (threadIdx.x == 0) {
@@ -249,7 +236,7 @@ __global__ void __launch_bounds__(kTriThreads) k_tri(TriArgs a, const void *in_,
             a.sync->ticket = 0;
             a.sync->done = 0;
             __threadfence();
-            st_release_u32(&a.sync->epoch, (unsigned)ep);
+            st_release_u32(&a.sync->epoch, ep);
         }
     }
 }
@@ -291,7 +278,7 @@ __device__ __forceinline__ void cta_level(const unsigned char *blk, vt_t<VT> *s_
 
 template <int VT, int G, bool EXACT>
 __global__ void __launch_bounds__(kCtaThreads, 1)
-k_tri_cta(const unsigned char *__restrict__ blocks, const long long *__restrict__ blk_off, int nlev, int n,
+k_tri_cta(const unsigned char *__restrict__ blocks, const unsigned *__restrict__ blk_off, int nlev, int n,
           int bit, int dbit, int stage_bytes, const void *in_, void *out_, unsigned *flags) {
     using V = vt_t<VT>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -299,6 +286,7 @@ k_tri_cta(const unsigned char *__restrict__ blocks, const long long *__restrict_
     const size_t vec_bytes = ((size_t)n * sizeof(V) + 15) & ~(size_t)15;
     unsigned char *stage = smem_raw + vec_bytes;
     unsigned long long *bar = (unsigned long long *)(stage + (size_t)kStages * stage_bytes);
+    unsigned *s_off = (unsigned *)(bar + kStages);  // block offsets in 16-byte units
     const V *in = (const V *)in_;
     V *out = (V *)out_;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -310,25 +298,25 @@ k_tri_cta(const unsigned char *__restrict__ blocks, const long long *__restrict_
         fence_mbar_init();
     }
     for (int i = threadIdx.x; i < n; i += kCtaThreads) s_out[i] = in[i];
+    for (int i = threadIdx.x; i <= nlev; i += kCtaThreads) s_off[i] = __ldg(blk_off + i);
     __syncthreads();
+    auto fits = [&](int d) { return (int)(s_off[d + 1] - s_off[d]) * 16 <= stage_bytes; };
     auto issue = [&](int d) {  // thread 0: bring level d's block into its stage
-        const long long o0 = __ldg(blk_off + d), o1 = __ldg(blk_off + d + 1);
-        const unsigned bytes = (unsigned)(o1 - o0);
-        if ((int)bytes > stage_bytes) return;
+        if (!fits(d)) return;
         const int s = d % kStages;
         fence_proxy_async_smem();
+        const unsigned bytes = (s_off[d + 1] - s_off[d]) * 16u;
         mbar_expect_tx(bar + s, bytes);
-        bulk_g2s(stage + (size_t)s * stage_bytes, blocks + o0, bytes, bar + s);
+        bulk_g2s(stage + (size_t)s * stage_bytes, blocks + (size_t)s_off[d] * 16, bytes, bar + s);
     };
     if (threadIdx.x == 0)
         for (int d = 0; d < nlev && d < kStages; d++) issue(d);
     unsigned phase = 0;  // bit s: parity of stage s's next completion
     int stuck = -1;      // level whose copy did not arrive in time
     for (int d = 0; d < nlev; d++) {
-        const long long o0 = __ldg(blk_off + d), o1 = __ldg(blk_off + d + 1);
-        const bool staged = (int)(o1 - o0) <= stage_bytes;
+        const bool staged = fits(d);
         const int s = d % kStages;
-        const unsigned char *blk = blocks + o0;
+        const unsigned char *blk = blocks + (size_t)s_off[d] * 16;
         bool timed_out = false;
         if (staged) {
             // bounded wait for the bulk copy of this level
@@ -342,15 +330,15 @@ k_tri_cta(const unsigned char *__restrict__ blocks, const long long *__restrict_
                     }
                 }
             }
+            phase ^= 1u << s;
             blk = stage + (size_t)s * stage_bytes;
         }
+        if (!timed_out) cta_level<VT, G, EXACT>(blk, s_out, bit, dbit, warp, sub, g, ovf);
+        // one barrier per level: results visible, stage free for reuse
         if (__syncthreads_or(timed_out)) {
             stuck = d;
             break;
         }
-        if (staged) phase ^= 1u << s;
-        cta_level<VT, G, EXACT>(blk, s_out, bit, dbit, warp, sub, g, ovf);
-        __syncthreads();
         if (threadIdx.x == 0 && d + kStages < nlev) issue(d + kStages);
     }
     if (stuck >= 0) {
@@ -360,11 +348,12 @@ k_tri_cta(const unsigned char *__restrict__ blocks, const long long *__restrict_
             atomicOr(flags, ST_TIMEOUT);
             const unsigned long long t0 = globaltimer_ns();
             for (int dd = stuck; dd < nlev && dd < stuck + kStages; dd++) {
-                if ((int)(__ldg(blk_off + dd + 1) - __ldg(blk_off + dd)) > stage_bytes) continue;
+                if (!fits(dd)) continue;
                 const int s = dd % kStages;
-                while (!mbar_try_wait(bar + s, (phase >> s) & 1u) && globaltimer_ns() - t0 < kSpinLimitNs) {
+                // the stuck level's wait already flipped its parity bit
+                const unsigned par = ((phase >> s) & 1u) ^ (dd == stuck ? 1u : 0u);
+                while (!mbar_try_wait(bar + s, par) && globaltimer_ns() - t0 < kSpinLimitNs) {
                 }
-                phase ^= 1u << s;
             }
         }
         __syncthreads();
@@ -384,15 +373,15 @@ void DevTri::release() {
     dfree(dinv);
     dfree(chunk_lv);
     dfree(sub_bound);
-    dfree(chunk_level);
-    dfree(lvl_ptr);
-    dfree(lvl_done);
+    dfree(pk);
+    dfree(flag);
     dfree(sync);
     dfree(blocks);
     dfree(blk_off);
-    perm = prp = pci = chunk_lv = sub_bound = chunk_level = lvl_ptr = nullptr;
+    perm = prp = pci = chunk_lv = sub_bound = nullptr;
     pval = dinv = nullptr;
-    lvl_done = nullptr;
+    pk = nullptr;
+    flag = nullptr;
     sync = nullptr;
     blocks = nullptr;
     blk_off = nullptr;
@@ -488,23 +477,31 @@ DevTri upload_tri(const Ctx &c, int n, const int *rptr, const int *cind, const v
     else put_vals(float());
     if (d.one_cta) {
         d.blocks = blob.empty() ? (unsigned char *)dmalloc(16) : dupload(blob);
-        d.blk_off = dupload(off);
-        const size_t avail = kSmemMax - vec_bytes - 64;
+        std::vector<unsigned> off16(off.size());
+        for (size_t i = 0; i < off.size(); i++) off16[i] = (unsigned)(off[i] / 16);
+        d.blk_off = dupload(off16);
+        const size_t offs_bytes = up(4 * ((size_t)s.nlev + 1), 16);
+        if (vec_bytes + offs_bytes + 8 * kStages + (size_t)kStages * 1024 > kSmemMax)
+            throw CudaError{"sweep schedule too large for the single-CTA kernel"};
+        const size_t avail = kSmemMax - vec_bytes - offs_bytes - 8 * kStages;
         d.stage_bytes = (int)std::min<size_t>(avail / kStages / 16 * 16, 64 * 1024);
-        d.cta_smem = vec_bytes + (size_t)kStages * d.stage_bytes + 8 * kStages;
+        d.cta_smem = vec_bytes + (size_t)kStages * d.stage_bytes + 8 * kStages + offs_bytes;
     } else {
         d.perm = dupload(s.perm);
         d.prp = dupload(s.prp);
         d.pci = s.pci.empty() ? (int *)dmalloc(16) : dupload(s.pci);
         d.chunk_lv = dupload(s.chunk_lv);
         d.sub_bound = dupload(s.sub_bound);
-        d.chunk_level = dupload(s.sub_level);
-        d.lvl_ptr = dupload(s.lvl_ptr);
-        d.lvl_done = (unsigned long long *)dmalloc(sizeof(unsigned long long) * std::max(s.nlev, 1));
-        SAGB_CUDA(cudaMemset(d.lvl_done, 0, sizeof(unsigned long long) * std::max(s.nlev, 1)));
+        if (vt == VT_F64) {
+            d.flag = (unsigned *)dmalloc(sizeof(unsigned) * std::max(n, 1));
+            SAGB_CUDA(cudaMemset(d.flag, 0, sizeof(unsigned) * std::max(n, 1)));
+        } else {
+            d.pk = (unsigned long long *)dmalloc(sizeof(unsigned long long) * std::max(n, 1));
+            SAGB_CUDA(cudaMemset(d.pk, 0, sizeof(unsigned long long) * std::max(n, 1)));
+        }
         d.sync = (TriSync *)dmalloc(sizeof(TriSync));
         SAGB_CUDA(cudaMemset(d.sync, 0, sizeof(TriSync)));
-        d.grid = std::max(1, std::min(d.nchunks, c.num_sms * 2));
+        d.grid = std::max(1, std::min(d.nchunks, c.num_sms));
     }
     return d;
 }
@@ -516,7 +513,7 @@ static void launch_tri(Ctx &c, const DevTri &T, const void *in, void *out) {
             T.blocks, T.blk_off, T.nlev, T.n, T.bit, T.dbit, T.stage_bytes, in, out, c.d_flags);
     } else {
         TriArgs a{T.n, T.nchunks, T.bit, T.dbit, T.perm, T.prp, T.pci, T.pval, T.dinv,
-                  T.chunk_lv, T.sub_bound, T.chunk_level, T.lvl_ptr, T.lvl_done, T.sync};
+                  T.chunk_lv, T.sub_bound, T.pk, T.flag, T.sync};
         k_tri<VT, G, EXACT><<<T.grid, kTriThreads, 0, c.stream>>>(a, in, out, c.d_flags);
     }
     c.launches++;

@@ -89,15 +89,14 @@ struct DevTri {
     int *perm = nullptr, *prp = nullptr, *pci = nullptr;
     void *pval = nullptr, *dinv = nullptr;
     int *chunk_lv = nullptr, *sub_bound = nullptr;
-    int *chunk_level = nullptr;        // level of each chunk's first sub-level
-    int *lvl_ptr = nullptr;            // level boundaries
-    unsigned long long *lvl_done = nullptr;  // rows completed per level, summed over all sweeps
+    unsigned long long *pk = nullptr;  // packed {epoch, value} per row (int32 / f32)
+    unsigned *flag = nullptr;          // ready epoch per row (f64)
     TriSync *sync = nullptr;
     // single-CTA mode: the result vector in shared memory, each level's row
     // data in one 16-byte aligned block fetched ahead by bulk copies
     bool one_cta = false;
     unsigned char *blocks = nullptr;
-    long long *blk_off = nullptr;      // byte offset of each level's block (nlev + 1)
+    unsigned *blk_off = nullptr;       // offset of each level's block in 16-byte units (nlev + 1)
     int stage_bytes = 0;               // largest block that goes through the staging ring
     size_t cta_smem = 0;
     void release();
