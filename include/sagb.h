@@ -187,6 +187,18 @@ int sa_amg_smooth(sa_ctx ctx, sa_amg M, int level, const void *in, void *out, in
 /* ldtri::SpMat<T>::SpTRSV of level l's smoother (one Gauss-Seidel sweep)
  *                                   Library/matrix/trimat/ldtri.hpp:49-58, 172-183, 398-412, 511-525 */
 int sa_amg_sweep(sa_ctx ctx, sa_amg M, int level, const void *in, void *out);
+/* No counterpart in the reference.  The same sweep as sa_amg_sweep, but it
+ * allocates no device memory: for callers that cannot call cudaMalloc while
+ * they solve -- their GPU memory is already claimed by another allocator (a
+ * framework's caching allocator, a fixed pool), or they cannot afford the
+ * device-wide synchronisation that allocating and freeing imply.  in and out
+ * must be device buffers.  The fine-level sweep kernel's scratch comes from a
+ * static device array sized for 262,144 rows (2 MiB, held by every GPU that
+ * loads the library until the process exits); a level with more rows is
+ * rejected with SA_ERR_ARG.  The first call on a device looks up that array's
+ * address, so make the first call before any stream capture.  Every call
+ * shares the array: calls that overlap on the GPU race. */
+int sa_amg_sweep_noalloc(sa_ctx ctx, sa_amg M, int level, const void *in, void *out);
 /* direct::LUflex::Solve / LU<T>::Solve   Library/solver/lu.hpp:30-33, 91-94 */
 int sa_amg_coarse_solve(sa_ctx ctx, sa_amg M, const void *in, void *out);
 /* SpMV with one operator of the hierarchy (SA_OP_A0, _CA, _P, _R, _U) */

@@ -667,6 +667,20 @@ extern "C" int sa_amg_sweep(sa_ctx ctx, sa_amg M, int level, const void *in, voi
     SA_GUARD_END
 }
 
+// The sweep of sa_amg_sweep without any device allocation (see the header):
+// device buffers only, scratch from the sweep kernels' static array.
+extern "C" int sa_amg_sweep_noalloc(sa_ctx ctx, sa_amg M, int level, const void *in, void *out) {
+    if (!ctx || !M || !in || !out) return fail(SA_ERR_ARG, "null argument");
+    if (level < 0 || level >= M->M->depth) return fail(SA_ERR_ARG, "no such level");
+    if (!is_device_ptr(in) || !is_device_ptr(out))
+        return fail(SA_ERR_ARG, "sa_amg_sweep_noalloc needs device buffers (host buffers would need staging)");
+    SA_GUARD_BEGIN
+    trsv_noalloc(ctx->c, M->M->LD[level], in, out);
+    SAGB_CUDA(cudaGetLastError());
+    return SA_OK;
+    SA_GUARD_END
+}
+
 extern "C" int sa_amg_coarse_solve(sa_ctx ctx, sa_amg M, const void *in, void *out) {
     if (!ctx || !M || !in || !out) return fail(SA_ERR_ARG, "null argument");
     SA_GUARD_BEGIN

@@ -27,6 +27,7 @@
 // the last CTA, so both kernels replay from a CUDA graph.
 #include <algorithm>
 #include <cstring>
+#include <mutex>
 #include <type_traits>
 
 #include "../sagb_internal.hpp"
@@ -540,6 +541,64 @@ void trsv(Ctx &c, const DevTri &T, const void *in, void *out) {
     }
     if (c.fp_exact) return tri_by_group<VT_F32, true>(c, T, in, out);
     return tri_by_group<VT_F32, false>(c, T, in, out);
+}
+
+// ================================================ sweep without allocation
+//
+// For callers that cannot allocate device memory while they solve (their GPU
+// memory is already claimed by another allocator, or they cannot afford the
+// device-wide synchronisation cudaMalloc/cudaFree imply).  The fine-level sweep
+// kernel needs per-row scratch (the packed {epoch, value} words and the
+// ticket/epoch block); this variant takes it from the file-scope array below
+// instead of the schedule's own allocation.  The array is sized for
+// kNoAllocRows rows (2 MiB) and every GPU that loads the library holds it
+// until the process exits.  All calls share it and it keeps the last call's
+// contents, so before each call the words of this level's rows and the
+// ticket/done counters are cleared (a previous call may have left words of
+// another precision there); the epoch keeps counting across calls.  Calls that
+// overlap on the GPU race on this array.
+constexpr int kNoAllocRows = 262144;
+static __device__ __align__(256) unsigned long long g_noalloc_scratch[kNoAllocRows + 2];
+
+static std::mutex g_noalloc_mu;
+static void *g_noalloc_addr[64];
+
+// The array's device address, looked up once per device with that device
+// current (in host code the symbol is only a host-side stand-in).
+static unsigned long long *noalloc_scratch(int device) {
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (device < 0 || device >= 64) throw CudaError{"device index out of range"};
+    if (!g_noalloc_addr[device]) {
+        int cur = -1;
+        SAGB_CUDA(cudaGetDevice(&cur));
+        if (cur != device) SAGB_CUDA(cudaSetDevice(device));
+        void *p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (cur != device) cudaSetDevice(cur);
+        if (e != cudaSuccess || !p) throw CudaError{std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e)};
+        g_noalloc_addr[device] = p;
+    }
+    return (unsigned long long *)g_noalloc_addr[device];
+}
+
+void trsv_noalloc(Ctx &c, const DevTri &T, const void *in, void *out) {
+    if (T.n == 0 || T.one_cta) return trsv(c, T, in, out);  // shared memory only: no scratch
+    if (T.n > kNoAllocRows)
+        throw CudaError{"level has more than 262144 rows, the limit of the no-allocation sweep"};
+    unsigned long long *s = noalloc_scratch(c.device);
+    DevTri U = T;  // same schedule and operator, scratch from the static array
+    U.pk = s;
+    U.flag = (unsigned *)s;
+    U.sync = (TriSync *)(s + kNoAllocRows);
+    SAGB_CUDA(cudaMemsetAsync(s, 0, sizeof(unsigned long long) * (size_t)T.n, c.stream));
+    SAGB_CUDA(cudaMemsetAsync(U.sync, 0, 2 * sizeof(unsigned), c.stream));  // ticket, done
+    if (U.vt == VT_I32) return tri_by_group<VT_I32, false>(c, U, in, out);
+    if (U.vt == VT_F64) {
+        if (c.fp_exact) return tri_by_group<VT_F64, true>(c, U, in, out);
+        return tri_by_group<VT_F64, false>(c, U, in, out);
+    }
+    if (c.fp_exact) return tri_by_group<VT_F32, true>(c, U, in, out);
+    return tri_by_group<VT_F32, false>(c, U, in, out);
 }
 
 // ======================================================== dense coarse LU

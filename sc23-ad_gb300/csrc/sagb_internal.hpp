@@ -107,6 +107,8 @@ struct DevTri {
 DevTri upload_tri(const Ctx &c, int n, const int *rptr, const int *cind, const void *vals, int vt, int kind,
                   int bit, int dbit);
 void trsv(Ctx &c, const DevTri &T, const void *in, void *out);
+// the same sweep with its scratch in a static device array (no allocation)
+void trsv_noalloc(Ctx &c, const DevTri &T, const void *in, void *out);
 
 // Dense coarsest-level LU: strict lower L (unit), strict upper U and D^-1,
 // row-major n x n, solved by one block.

@@ -87,6 +87,7 @@ SIGNATURES = {
     "sa_amg_precondition": (C.c_int, [VP, VP, VP, VP]),
     "sa_amg_smooth": (C.c_int, [VP, VP, C.c_int, VP, VP, C.c_int]),
     "sa_amg_sweep": (C.c_int, [VP, VP, C.c_int, VP, VP]),
+    "sa_amg_sweep_noalloc": (C.c_int, [VP, VP, C.c_int, VP, VP]),
     "sa_amg_coarse_solve": (C.c_int, [VP, VP, VP, VP]),
     "sa_amg_level_spmv": (C.c_int, [VP, VP, C.c_int, C.c_int, VP, VP]),
     "sa_amg_level_info": (C.c_int, [VP, C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
