@@ -60,6 +60,7 @@ extern "C" {
 #define SA_OP_LUL 6 /* coarsest LU, unit lower factor (ltri)           */
 #define SA_OP_LUU 7 /* coarsest LU, D^-1 U (dutri)                     */
 #define SA_OP_BJ 8  /* block boundaries of a BlockSOR smoother (rptr)  */
+#define SA_OP_COLOR 9 /* colour of each row of a multicolour smoother (view.rptr, n rows) */
 
 /* synthetic systems for sa_gen */
 #define SA_GEN_POISSON2D 0  /* 5-point, 4/-1                             */
@@ -91,6 +92,8 @@ typedef struct {
     int smoother_blocks; /* 0: SOR, >0: BlockSOR with this many blocks  Library/parameters.hpp:223-241 */
     double omega;        /* SORParam::omega (1.0)                                                     */
     int smooth_iter;     /* SORParam::iter (1)                                                        */
+    int multicolor;      /* 1: SOR in greedy-colour order (ldtri::MCCSR, matrix/trispmat.hpp:597-640,
+                            colouring helper/helper_graph.hpp:191-219); 0: natural order (default) */
 } sa_amg_params;
 
 typedef struct {

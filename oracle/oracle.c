@@ -57,17 +57,25 @@ int or_spmv_i32(const or_csr_i32 *A, const int32_t *in, int32_t *out) {
 /* ldtri::CSRflex::SpTRSV (matrix/trimat/ldtri.hpp:172-183): forward Gauss-Seidel
  * row with the inverse diagonal stored last in the row.  With bj != NULL the
  * same sweep runs inside each block independently (BJCSRflex, ldtri.hpp:511-525). */
-static int ldtri_rows(const or_csr_i32 *LD, int r0, int r1, const int32_t *in, int32_t *out) {
+static int ldtri_row(const or_csr_i32 *LD, int i, const int32_t *in, int32_t *out) {
     const int bit = LD->bit, dbit = LD->dbit;
+    int64_t t = wshl((int64_t)in[i], bit);
+    int j;
+    for (j = LD->rptr[i]; j < LD->rptr[i + 1] - 1; j++) t = wsub(t, (int64_t)LD->val[j] * (int64_t)out[LD->cind[j]]);
+    int64_t s = wmul(t >> bit, (int64_t)LD->val[j]) >> dbit;
+    out[i] = lo32(s);
+    return s != (int64_t)lo32(s);
+}
+
+static int ldtri_rows(const or_csr_i32 *LD, int r0, int r1, const int32_t *in, int32_t *out) {
     int ovf = 0;
-    for (int i = r0; i < r1; i++) {
-        int64_t t = wshl((int64_t)in[i], bit);
-        int j;
-        for (j = LD->rptr[i]; j < LD->rptr[i + 1] - 1; j++) t = wsub(t, (int64_t)LD->val[j] * (int64_t)out[LD->cind[j]]);
-        int64_t s = wmul(t >> bit, (int64_t)LD->val[j]) >> dbit;
-        out[i] = lo32(s);
-        ovf |= (s != (int64_t)lo32(s));
-    }
+    for (int i = r0; i < r1; i++) ovf |= ldtri_row(LD, i, in, out);
+    return ovf;
+}
+
+int or_ldtri_order_i32(const or_csr_i32 *LD, const int32_t *order, const int32_t *in, int32_t *out) {
+    int ovf = 0;
+    for (int k = 0; k < LD->n; k++) ovf |= ldtri_row(LD, order[k], in, out);
     return ovf;
 }
 
@@ -190,21 +198,26 @@ void or_trsv_i32(const int64_t *H, double e0, const int64_t *e, double *y, int l
  * (smoother/stationary.hpp:415-430, 997-1012):
  *   isInited: repeat iter times { tmp = in - U*out; out = LD^-1 tmp }
  *   else:     out = LD^-1 in; repeat iter-1 times { ... } */
+static void sweep_i32(const or_amg_i32 *h, int l, const int32_t *in, int32_t *out) {
+    const int32_t *order = h->order ? h->order[l] : NULL;
+    if (order) or_ldtri_order_i32(&h->LD[l], order, in, out);
+    else or_ldtri_i32(&h->LD[l], h->bj ? h->bj[l] : NULL, h->nbj, in, out);
+}
+
 void or_smooth_i32(const or_amg_i32 *h, int l, const int32_t *in, int32_t *out, int inited) {
-    const or_csr_i32 *LD = &h->LD[l], *U = &h->U[l];
-    const int32_t *bj = h->bj ? h->bj[l] : NULL;
-    const int n = LD->n;
+    const or_csr_i32 *U = &h->U[l];
+    const int n = h->LD[l].n;
     int32_t *tmp = (int32_t *)malloc(sizeof(int32_t) * (size_t)n);
     int k0 = 0;
     if (!inited) {
-        or_ldtri_i32(LD, bj, h->nbj, in, out);
+        sweep_i32(h, l, in, out);
         k0 = 1;
     }
     for (int k = k0; k < h->smooth_iter; k++) {
         or_spmv_i32(U, out, tmp);
 #pragma omp parallel for num_threads(g_threads) schedule(static)
         for (int i = 0; i < n; i++) tmp[i] = sub32(in[i], tmp[i]); /* Axpby<int>(1,in,-1,tmp) */
-        or_ldtri_i32(LD, bj, h->nbj, tmp, out);
+        sweep_i32(h, l, tmp, out);
     }
     free(tmp);
 }
@@ -363,13 +376,18 @@ int or_ir_solve_i32(const or_csr_f64 *dA, const or_csr_i32 *A, const or_amg_i32 
         return 0;                                                                                   \
     }                                                                                               \
     /* ldtri::CSR<T>::SpTRSV (ldtri.hpp:49-58); BJCSR<T> (ldtri.hpp:398-412) */                  \
+    static void ldtri_row_##SFX(const or_csr_##SFX *LD, int i, const T *in, T *out) {             \
+        T t = in[i];                                                                                \
+        int j;                                                                                      \
+        for (j = LD->rptr[i]; j < LD->rptr[i + 1] - 1; j++) t -= LD->val[j] * out[LD->cind[j]];     \
+        out[i] = t * LD->val[j];                                                                    \
+    }                                                                                               \
     static void ldtri_rows_##SFX(const or_csr_##SFX *LD, int r0, int r1, const T *in, T *out) {   \
-        for (int i = r0; i < r1; i++) {                                                             \
-            T t = in[i];                                                                            \
-            int j;                                                                                  \
-            for (j = LD->rptr[i]; j < LD->rptr[i + 1] - 1; j++) t -= LD->val[j] * out[LD->cind[j]]; \
-            out[i] = t * LD->val[j];                                                                \
-        }                                                                                           \
+        for (int i = r0; i < r1; i++) ldtri_row_##SFX(LD, i, in, out);                              \
+    }                                                                                               \
+    int or_ldtri_order_##SFX(const or_csr_##SFX *LD, const int32_t *order, const T *in, T *out) { \
+        for (int k = 0; k < LD->n; k++) ldtri_row_##SFX(LD, order[k], in, out);                     \
+        return 0;                                                                                   \
     }                                                                                               \
     int or_ldtri_##SFX(const or_csr_##SFX *LD, const int32_t *bj, int nbj, const T *in, T *out) { \
         if (!bj) { ldtri_rows_##SFX(LD, 0, LD->n, in, out); return 0; }                             \
@@ -397,17 +415,21 @@ int or_ir_solve_i32(const or_csr_f64 *dA, const or_csr_i32 *A, const or_amg_i32 
         return 0;                                                                                   \
     }                                                                                               \
     /* SOR<ClassLD<T>,ClassU<T>>::Smooth (stationary.hpp:238-255) */                              \
+    static void sweep_##SFX(const or_amg_##SFX *h, int l, const T *in, T *out) {                 \
+        const int32_t *order = h->order ? h->order[l] : NULL;                                       \
+        if (order) or_ldtri_order_##SFX(&h->LD[l], order, in, out);                                 \
+        else or_ldtri_##SFX(&h->LD[l], h->bj ? h->bj[l] : NULL, h->nbj, in, out);                   \
+    }                                                                                               \
     static void smooth_##SFX(const or_amg_##SFX *h, int l, const T *in, T *out, int inited) {     \
-        const or_csr_##SFX *LD = &h->LD[l], *U = &h->U[l];                                           \
-        const int32_t *bj = h->bj ? h->bj[l] : NULL;                                                \
-        const int n = LD->n;                                                                        \
+        const or_csr_##SFX *U = &h->U[l];                                                           \
+        const int n = h->LD[l].n;                                                                   \
         T *tmp = (T *)malloc(sizeof(T) * (size_t)n);                                                \
         int k0 = 0;                                                                                 \
-        if (!inited) { or_ldtri_##SFX(LD, bj, h->nbj, in, out); k0 = 1; }                            \
+        if (!inited) { sweep_##SFX(h, l, in, out); k0 = 1; }                                        \
         for (int k = k0; k < h->smooth_iter; k++) {                                                 \
             or_spmv_##SFX(U, out, tmp);                                                             \
             for (int i = 0; i < n; i++) tmp[i] = (T)1 * in[i] + (T)(-1) * tmp[i];                   \
-            or_ldtri_##SFX(LD, bj, h->nbj, tmp, out);                                               \
+            sweep_##SFX(h, l, tmp, out);                                                            \
         }                                                                                           \
         free(tmp);                                                                                  \
     }                                                                                               \

@@ -32,7 +32,10 @@ typedef struct { int n, m; const int32_t *rptr, *cind; const float *val; } or_cs
  * depth coarse levels, CA[0..depth-2], P[0..depth-1] (Intrpl), R[0..depth-1]
  * (Intrpl_t), smoother of level l = (LD[l], U[l]) for l in 0..depth-1, with
  * optional block-Jacobi boundaries bj[l] (nbj blocks) for BlockSORflex, and the
- * coarsest LU factors (ltri LUL, dutri LUU). */
+ * coarsest LU factors (ltri LUL, dutri LUU).  order (optional, may be NULL or
+ * hold NULL levels) gives, per level, the row order of the smoother's forward
+ * sweep: the multicolour variant sweeps the rows colour by colour
+ * (ldtri::MCCSR, matrix/trispmat.hpp:597-640, after the MC renumbering). */
 typedef struct {
     int depth;
     or_csr_i32 A0;
@@ -41,6 +44,7 @@ typedef struct {
     int nbj;
     int smooth_iter;
     or_csr_i32 LUL, LUU;
+    const int32_t *const *order;
 } or_amg_i32;
 
 typedef struct {
@@ -51,6 +55,7 @@ typedef struct {
     int nbj;
     int smooth_iter;
     or_csr_f64 LUL, LUU;
+    const int32_t *const *order;
 } or_amg_f64;
 
 typedef struct {
@@ -61,6 +66,7 @@ typedef struct {
     int nbj;
     int smooth_iter;
     or_csr_f32 LUL, LUU;
+    const int32_t *const *order;
 } or_amg_f32;
 
 /* Threads used by the parallel loops (SpMV rows, integer reductions).  FP
@@ -71,6 +77,8 @@ int or_get_threads(void);
 /* --- integer kernels --- */
 int or_spmv_i32(const or_csr_i32 *A, const int32_t *in, int32_t *out);
 int or_ldtri_i32(const or_csr_i32 *LD, const int32_t *bj, int nbj, const int32_t *in, int32_t *out);
+/* the same forward sweep, rows visited in the given order (a permutation) */
+int or_ldtri_order_i32(const or_csr_i32 *LD, const int32_t *order, const int32_t *in, int32_t *out);
 int or_ltri_i32(const or_csr_i32 *L, const int32_t *in, int32_t *out);
 int or_dutri_i32(const or_csr_i32 *U, const int32_t *in, int32_t *out);
 int64_t or_lsqrt(int64_t x);
@@ -103,6 +111,7 @@ int or_ir_solve_i32(const or_csr_f64 *dA, const or_csr_i32 *A, const or_amg_i32 
 /* --- FP64 / FP32 siblings --- */
 int or_spmv_f64(const or_csr_f64 *A, const double *in, double *out);
 int or_ldtri_f64(const or_csr_f64 *LD, const int32_t *bj, int nbj, const double *in, double *out);
+int or_ldtri_order_f64(const or_csr_f64 *LD, const int32_t *order, const double *in, double *out);
 int or_ltri_f64(const or_csr_f64 *L, const double *in, double *out);
 int or_dutri_f64(const or_csr_f64 *U, const double *in, double *out);
 void or_vcycle_f64(const or_amg_f64 *h, const double *in, double *out);
@@ -111,6 +120,7 @@ int or_ir_solve_f64(const or_csr_f64 *dA, const or_amg_f64 *M, int m, double eps
 
 int or_spmv_f32(const or_csr_f32 *A, const float *in, float *out);
 int or_ldtri_f32(const or_csr_f32 *LD, const int32_t *bj, int nbj, const float *in, float *out);
+int or_ldtri_order_f32(const or_csr_f32 *LD, const int32_t *order, const float *in, float *out);
 void or_vcycle_f32(const or_amg_f32 *h, const float *in, float *out);
 int or_ir_solve_f32(const or_csr_f64 *dA, const or_csr_f32 *fA, const or_amg_f32 *M, int m, double eps,
                     const double *b, double nrm_b, double *x, int max_outer, int print);

@@ -37,7 +37,7 @@ def _amg_struct(csr_t):
         _fields_ = [("depth", C.c_int), ("A0", csr_t), ("CA", C.POINTER(csr_t)), ("P", C.POINTER(csr_t)),
                     ("R", C.POINTER(csr_t)), ("LD", C.POINTER(csr_t)), ("U", C.POINTER(csr_t)),
                     ("bj", C.POINTER(i32p)), ("nbj", C.c_int), ("smooth_iter", C.c_int),
-                    ("LUL", csr_t), ("LUU", csr_t)]
+                    ("LUL", csr_t), ("LUU", csr_t), ("order", C.POINTER(i32p))]
     return Amg
 
 
@@ -64,6 +64,7 @@ def lib():
             "or_set_threads": (None, [C.c_int]),
             "or_spmv_i32": (C.c_int, [ci, i32p, i32p]),
             "or_ldtri_i32": (C.c_int, [ci, i32p, C.c_int, i32p, i32p]),
+            "or_ldtri_order_i32": (C.c_int, [ci, i32p, i32p, i32p]),
             "or_ltri_i32": (C.c_int, [ci, i32p, i32p]),
             "or_dutri_i32": (C.c_int, [ci, i32p, i32p]),
             "or_lsqrt": (C.c_int64, [C.c_int64]),
@@ -84,12 +85,14 @@ def lib():
                                           C.c_int, C.c_int]),
             "or_spmv_f64": (C.c_int, [cf, f64p, f64p]),
             "or_ldtri_f64": (C.c_int, [cf, i32p, C.c_int, f64p, f64p]),
+            "or_ldtri_order_f64": (C.c_int, [cf, i32p, f64p, f64p]),
             "or_ltri_f64": (C.c_int, [cf, f64p, f64p]),
             "or_dutri_f64": (C.c_int, [cf, f64p, f64p]),
             "or_vcycle_f64": (None, [af, f64p, f64p]),
             "or_ir_solve_f64": (C.c_int, [cf, af, C.c_int, C.c_double, f64p, C.c_double, f64p, C.c_int, C.c_int]),
             "or_spmv_f32": (C.c_int, [cs, f32p, f32p]),
             "or_ldtri_f32": (C.c_int, [cs, i32p, C.c_int, f32p, f32p]),
+            "or_ldtri_order_f32": (C.c_int, [cs, i32p, f32p, f32p]),
             "or_vcycle_f32": (None, [as_, f32p, f32p]),
             "or_ir_solve_f32": (C.c_int, [cf, cs, as_, C.c_int, C.c_double, f64p, C.c_double, f64p, C.c_int,
                                           C.c_int]),
@@ -169,6 +172,20 @@ def golden_amg_i32(keep, g, bj=False):
     h.smooth_iter = 1
     h.LUL = g_csr_i32(keep, g, "LU_L")
     h.LUU = g_csr_i32(keep, g, "LU_U")
+    return h
+
+
+def colour_order(colour):
+    """Rows colour by colour, increasing inside a colour (the MC renumbering)."""
+    return np.argsort(np.asarray(colour), kind="stable").astype(np.int32)
+
+
+def set_orders(keep, h, orders):
+    """Attach per-level sweep orders (arrays or None) to an oracle hierarchy."""
+    arrs = [None if o is None else keep.arr(o, np.int32) for o in orders]
+    op = (i32p * len(arrs))(*[ptr(a, i32p) if a is not None else i32p() for a in arrs])
+    keep.refs.append(op)
+    h.order = op
     return h
 
 

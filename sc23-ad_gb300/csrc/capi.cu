@@ -457,6 +457,7 @@ extern "C" void sa_amg_params_default(sa_amg_params *p) {
     p->smoother_blocks = 0;
     p->omega = 1.0;
     p->smooth_iter = 1;
+    p->multicolor = 0;
 }
 
 static void build_setup(sa_hierarchy &s, const CsrD &A) {
@@ -467,6 +468,7 @@ static void build_setup(sa_hierarchy &s, const CsrD &A) {
     sm.block = s.p.smoother_blocks;
     sm.omega = s.p.omega;
     sm.iter = s.p.smooth_iter;
+    sm.multicolor = s.p.multicolor;
     if (s.precision == SA_INT) s.hi = std::make_shared<IntHierarchy>(build_int_hierarchy(A, chain, sm));
     else if (s.precision == SA_F64) s.hd = std::make_shared<FpHierarchy<double>>(build_f64_hierarchy(A, chain, sm));
     else s.hf = std::make_shared<FpHierarchy<float>>(build_f32_hierarchy(A, chain, sm));
@@ -481,7 +483,8 @@ extern "C" int sa_setup_create(int precision, const sa_amg_params *p, int n, con
     s->precision = precision;
     if (p) s->p = *p;
     else sa_amg_params_default(&s->p);
-    if (s->p.smooth_iter < 1 || s->p.max_levels < 1 || s->p.smoother_blocks < 0) {
+    if (s->p.smooth_iter < 1 || s->p.max_levels < 1 || s->p.smoother_blocks < 0 ||
+        s->p.multicolor < 0 || s->p.multicolor > 1 || (s->p.multicolor && s->p.smoother_blocks)) {
         delete s;
         return fail(SA_ERR_ARG, "invalid AMG parameters");
     }
@@ -565,6 +568,16 @@ static int view_hier(const H &h, int op, int level, sa_csr_view *o, B bits) {
             o->m = 0;
             o->nnz = 0;
             o->rptr = h.bj[level].data();
+            o->cind = nullptr;
+            o->val = nullptr;
+            o->bit = o->dbit = 0;
+            return SA_OK;
+        case SA_OP_COLOR:
+            if (level < 0 || level >= D || h.colour[level].empty()) return bad();
+            o->n = (int)h.colour[level].size();
+            o->m = 0;
+            o->nnz = 0;
+            o->rptr = h.colour[level].data();
             o->cind = nullptr;
             o->val = nullptr;
             o->bit = o->dbit = 0;

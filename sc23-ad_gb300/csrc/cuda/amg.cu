@@ -52,8 +52,12 @@ std::unique_ptr<DevAmg> upload_amg_int(Ctx &c, std::shared_ptr<IntHierarchy> h) 
     for (auto &m : h->P) M->P.push_back(upload_csr_i32(m));
     for (auto &m : h->R) M->R.push_back(upload_csr_i32(m));
     for (auto &m : h->U) M->U.push_back(upload_csr_i32(m));
-    for (auto &m : h->LD)
-        M->LD.push_back(upload_tri(c, m.n, m.rptr.data(), m.cind.data(), m.val.data(), VT_I32, TRI_LD, m.bit, m.dbit));
+    for (int l = 0; l < h->depth; l++) {
+        const CsrI &m = h->LD[l];
+        const int *hint = h->colour[l].empty() ? nullptr : h->colour[l].data();
+        M->LD.push_back(
+            upload_tri(c, m.n, m.rptr.data(), m.cind.data(), m.val.data(), VT_I32, TRI_LD, m.bit, m.dbit, hint));
+    }
     M->nbj = h->bj.empty() || h->bj[0].empty() ? 0 : (int)h->bj[0].size() - 1;
     M->LU = upload_dense_lu(h->LUL.rptr.data(), h->LUL.cind.data(), h->LUL.val.data(), h->LUU.rptr.data(),
                             h->LUU.cind.data(), h->LUU.val.data(), h->LUL.n, VT_I32, h->LUL.bit, h->LUU.bit,
@@ -74,8 +78,11 @@ static std::unique_ptr<DevAmg> upload_amg_fp(Ctx &c, const FpHierarchy<T> &h, in
     for (auto &m : h.P) M->P.push_back(upload_csr_fp<T>(m));
     for (auto &m : h.R) M->R.push_back(upload_csr_fp<T>(m));
     for (auto &m : h.U) M->U.push_back(upload_csr_fp<T>(m));
-    for (auto &m : h.LD)
-        M->LD.push_back(upload_tri(c, m.n, m.rptr.data(), m.cind.data(), m.val.data(), vt, TRI_LD, 0, 0));
+    for (int l = 0; l < h.depth; l++) {
+        const auto &m = h.LD[l];
+        const int *hint = h.colour[l].empty() ? nullptr : h.colour[l].data();
+        M->LD.push_back(upload_tri(c, m.n, m.rptr.data(), m.cind.data(), m.val.data(), vt, TRI_LD, 0, 0, hint));
+    }
     M->nbj = h.bj.empty() || h.bj[0].empty() ? 0 : (int)h.bj[0].size() - 1;
     M->LU = upload_dense_lu(h.LUL.rptr.data(), h.LUL.cind.data(), h.LUL.val.data(), h.LUU.rptr.data(),
                             h.LUU.cind.data(), h.LUU.val.data(), h.LUL.n, vt, 0, 0, 0);

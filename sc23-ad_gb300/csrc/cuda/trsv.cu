@@ -438,7 +438,7 @@ static int pow2_at_least(double x) {
 }
 
 DevTri upload_tri(const Ctx &c, int n, const int *rptr, const int *cind, const void *vals, int vt, int kind,
-                  int bit, int dbit) {
+                  int bit, int dbit, const int *level_hint) {
     if (kind != TRI_LD) throw CudaError{"only LD sweeps are uploaded as sparse triangles"};
     DevTri d;
     d.n = n;
@@ -455,7 +455,7 @@ DevTri upload_tri(const Ctx &c, int n, const int *rptr, const int *cind, const v
     if (vt != VT_I32 && c.fp_exact) G = 1;  // sequential order inside a row
     d.group = G;
     const int rows_per_chunk = 2 * kTriThreads / G;
-    TriSchedule s = build_tri_schedule(rptr, cind, n, kind, rows_per_chunk, 1 << 20);
+    TriSchedule s = build_tri_schedule(rptr, cind, n, kind, rows_per_chunk, 1 << 20, level_hint);
     d.nlev = s.nlev;
     d.max_level_rows = s.max_level_rows;
     d.nnz_off = (int64_t)s.pci.size();

@@ -658,12 +658,103 @@ CsrI to_dutri_flex(const CsrD &DinvU) {
 
 // ================================================================= hierarchies
 
-static void smoother_split(const CsrD &A, const SmootherSpec &sm, CsrD &LD, CsrD &U, std::vector<int> &bj) {
-    if (sm.block > 0) {
+std::vector<int> greedy_colouring(const CsrD &A, int *ncolors) {
+    const int N = A.n;
+    // symmetrised adjacency without the diagonal
+    std::vector<int> deg(N, 0);
+    for (int i = 0; i < N; i++)
+        for (int j = A.rptr[i]; j < A.rptr[i + 1]; j++)
+            if (A.cind[j] != i) {
+                deg[i]++;
+                deg[A.cind[j]]++;
+            }
+    std::vector<int> ap(N + 1, 0);
+    for (int i = 0; i < N; i++) ap[i + 1] = ap[i] + deg[i];
+    std::vector<int> adj(ap[N]), fill(ap.begin(), ap.end() - 1);
+    for (int i = 0; i < N; i++)
+        for (int j = A.rptr[i]; j < A.rptr[i + 1]; j++) {
+            const int c = A.cind[j];
+            if (c == i) continue;
+            adj[fill[i]++] = c;
+            adj[fill[c]++] = i;
+        }
+    // colour k: sweep the rows in order, take every uncoloured row that has no
+    // neighbour of colour k yet
+    std::vector<int> col(N, -1);
+    int k = 0, left = N;
+    while (left > 0) {
+        for (int i = 0; i < N; i++) {
+            if (col[i] >= 0) continue;
+            bool adjacent = false;
+            for (int t = ap[i]; t < ap[i + 1]; t++)
+                if (col[adj[t]] == k) {
+                    adjacent = true;
+                    break;
+                }
+            if (adjacent) continue;
+            col[i] = k;
+            left--;
+        }
+        k++;
+    }
+    if (ncolors) *ncolors = k;
+    return col;
+}
+
+void mc_sor_split(const CsrD &A, double omega, const std::vector<int> &col, CsrD &LD, CsrD &U) {
+    const int N = A.n;
+    LD.n = LD.m = U.n = U.m = N;
+    LD.rptr.assign(N + 1, 0);
+    U.rptr.assign(N + 1, 0);
+    LD.cind.clear(); LD.val.clear(); U.cind.clear(); U.val.clear();
+    for (int i = 0; i < N; i++) {
+        double d = 0;
+        for (int j = A.rptr[i]; j < A.rptr[i + 1]; j++) {
+            const int c = A.cind[j];
+            if (c == i) {
+                d = A.val[j];
+            } else if (col[c] < col[i]) {
+                LD.cind.push_back(c);
+                LD.val.push_back(A.val[j]);
+            }
+        }
+        LD.cind.push_back(i);
+        LD.val.push_back(1.0 / omega * d);
+        U.cind.push_back(i);
+        U.val.push_back((1 - 1.0 / omega) * d);
+        for (int j = A.rptr[i]; j < A.rptr[i + 1]; j++) {
+            const int c = A.cind[j];
+            if (c != i && col[c] >= col[i]) {
+                U.cind.push_back(c);
+                U.val.push_back(A.val[j]);
+            }
+        }
+        LD.rptr[i + 1] = (int)LD.cind.size();
+        U.rptr[i + 1] = (int)U.cind.size();
+    }
+}
+
+// LD with its diagonal (the last entry of each row) inverted: extractLDinv for a
+// split whose couplings may lie on either side of the diagonal (colour order).
+static CsrD invert_last(const CsrD &LD) {
+    CsrD B = LD;
+    for (int i = 0; i < B.n; i++)
+        if (B.rptr[i + 1] > B.rptr[i]) B.val[B.rptr[i + 1] - 1] = 1 / B.val[B.rptr[i + 1] - 1];
+    return B;
+}
+
+static void smoother_split(const CsrD &A, const SmootherSpec &sm, CsrD &LD, CsrD &U, std::vector<int> &bj,
+                           std::vector<int> &colour) {
+    colour.clear();
+    bj.clear();
+    if (sm.multicolor) {
+        int nc = 0;
+        colour = greedy_colouring(A, &nc);
+        mc_sor_split(A, sm.omega, colour, LD, U);
+    } else if (sm.block > 0) {
         block_sor_split(A, sm.omega, sm.block, LD, U, bj);
     } else {
         sor_split(A, sm.omega, LD, U);
-        bj.clear();
     }
 }
 
@@ -700,11 +791,12 @@ IntHierarchy build_int_hierarchy(const CsrD &A, const RsChain &chain, const Smoo
     h.LD.resize(D);
     h.U.resize(D);
     h.bj.resize(D);
+    h.colour.resize(D);
     for (int l = 0; l < D; l++) {
         const CsrD &Al = l == 0 ? A : CA[l - 1];
         CsrD LD, U;
-        smoother_split(Al, sm, LD, U, h.bj[l]);
-        h.LD[l] = to_ldtri_flex(extract_ldinv(LD));
+        smoother_split(Al, sm, LD, U, h.bj[l], h.colour[l]);
+        h.LD[l] = to_ldtri_flex(sm.multicolor ? invert_last(LD) : extract_ldinv(LD));
         h.U[l] = to_flex(U);
     }
     for (int i = 0; i < D; i++) {
@@ -740,11 +832,12 @@ static FpHierarchy<T> build_fp(const CsrD &A, const RsChain &chain, const Smooth
     h.LD.resize(D);
     h.U.resize(D);
     h.bj.resize(D);
+    h.colour.resize(D);
     for (int l = 0; l < D; l++) {
         const CsrD &Al = l == 0 ? A : chain.CA[l - 1];
         CsrD LD, U;
-        smoother_split(Al, sm, LD, U, h.bj[l]);
-        h.LD[l] = convert<T>(extract_ldinv(LD));
+        smoother_split(Al, sm, LD, U, h.bj[l], h.colour[l]);
+        h.LD[l] = convert<T>(sm.multicolor ? invert_last(LD) : extract_ldinv(LD));
         h.U[l] = convert<T>(U);
     }
     for (int i = 0; i < D; i++) {

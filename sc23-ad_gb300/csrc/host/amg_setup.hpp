@@ -72,7 +72,17 @@ struct SmootherSpec {
     int block = 0;       // 0: SOR, else BlockSOR with this many blocks
     double omega = 1.0;
     int iter = 1;
+    int multicolor = 0;  // 1: SOR in colour order (the multicolour variant)
 };
+
+// Greedy colouring, colour by colour, on the symmetrised pattern (the
+// reference's coloring_greedy, Library/helper/helper_graph.hpp:191-219).
+// Returns 0-based colours; *ncolors set.
+std::vector<int> greedy_colouring(const CsrD &A, int *ncolors);
+// SOR split in colour order: LD = couplings to earlier colours + diag/omega
+// (diagonal last), U = (1 - 1/omega) diag first + couplings to later colours.
+// GS with this split is ldtri::MCCSRflex (ldtri.hpp:635-700) without renumbering.
+void mc_sor_split(const CsrD &A, double omega, const std::vector<int> &colour, CsrD &LD, CsrD &U);
 
 struct IntHierarchy {
     int depth = 0;
@@ -81,6 +91,7 @@ struct IntHierarchy {
     std::vector<CsrI> CA, P, R;  // C_A[depth-1], Intrpl[depth], Intrpl_t[depth]
     std::vector<CsrI> LD, U;     // smoother of level l, l = 0..depth-1
     std::vector<std::vector<int>> bj;
+    std::vector<std::vector<int>> colour;  // multicolour variant: 0-based colour per row
     CsrI LUL, LUU;
 };
 
@@ -91,6 +102,7 @@ struct FpHierarchy {
     CsrT<T> A0;
     std::vector<CsrT<T>> CA, P, R, LD, U;
     std::vector<std::vector<int>> bj;
+    std::vector<std::vector<int>> colour;
     CsrT<T> LUL, LUU;
 };
 

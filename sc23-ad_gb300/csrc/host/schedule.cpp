@@ -5,7 +5,7 @@
 namespace sagb {
 
 TriSchedule build_tri_schedule(const int *rptr, const int *cind, int n, int kind, int rows_per_chunk,
-                               int max_run_levels) {
+                               int max_run_levels, const int *level_hint) {
     TriSchedule s;
     s.n = n;
     s.kind = kind;
@@ -20,7 +20,16 @@ TriSchedule build_tri_schedule(const int *rptr, const int *cind, int n, int kind
         if (b < a) b = a;
     };
     int nlev = 0;
-    if (kind == TRI_DU) {
+    if (level_hint) {
+        for (int i = 0; i < n; i++) {
+            int a, b;
+            off_range(i, a, b);
+            for (int j = a; j < b; j++)
+                if (level_hint[cind[j]] >= level_hint[i]) throw SetupError{"level hint violates a dependency"};
+            level[i] = level_hint[i];
+            nlev = std::max(nlev, level[i] + 1);
+        }
+    } else if (kind == TRI_DU) {
         for (int i = n - 1; i >= 0; i--) {
             int a, b, lv = 0;
             off_range(i, a, b);

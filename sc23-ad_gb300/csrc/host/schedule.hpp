@@ -42,7 +42,9 @@ struct TriSchedule {
 
 // rows_per_chunk: maximum rows of one chunk; also the threshold below which a
 // level is merged with its neighbours into a run chunk.
+// level_hint (optional): a level per row in which every dependency has a lower
+// level (the colour index of a multicolour sweep); the DAG levels otherwise.
 TriSchedule build_tri_schedule(const int *rptr, const int *cind, int n, int kind, int rows_per_chunk,
-                               int max_run_levels);
+                               int max_run_levels, const int *level_hint = nullptr);
 
 }  // namespace sagb

@@ -104,8 +104,9 @@ struct DevTri {
 
 // Builds the schedule from a triangular CSR (kind: TRI_LD / TRI_L / TRI_DU) and
 // uploads it.  vals points at int32 / double / float values of the source CSR.
+// level_hint (optional): the level of each row (colours of a multicolour split).
 DevTri upload_tri(const Ctx &c, int n, const int *rptr, const int *cind, const void *vals, int vt, int kind,
-                  int bit, int dbit);
+                  int bit, int dbit, const int *level_hint = nullptr);
 void trsv(Ctx &c, const DevTri &T, const void *in, void *out);
 // the same sweep with its scratch in a static device array (no allocation)
 void trsv_noalloc(Ctx &c, const DevTri &T, const void *in, void *out);

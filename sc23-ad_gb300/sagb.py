@@ -16,7 +16,7 @@ SA_OK, SA_ERR_ARG, SA_ERR_CUDA, SA_ERR_SETUP, SA_ERR_NUMERIC = 0, 1, 2, 3, 4
 FLAG_OVERFLOW, FLAG_TIMEOUT, FLAG_DIVZERO, FLAG_NORM_OVERFLOW = 1, 2, 4, 8
 INT, F64, F32 = 0, 1, 2
 MAT_FIXED, MAT_FLEX, MAT_F64, MAT_F32 = 0, 1, 2, 3
-OP_A0, OP_CA, OP_P, OP_R, OP_LD, OP_U, OP_LUL, OP_LUU, OP_BJ = range(9)
+OP_A0, OP_CA, OP_P, OP_R, OP_LD, OP_U, OP_LUL, OP_LUU, OP_BJ, OP_COLOR = range(10)
 GEN_POISSON2D, GEN_POISSON3D, GEN_ANISO2D, GEN_STENCIL27, GEN_CONVDIFF3D, GEN_VARCOEF3D = range(6)
 OPT_FP_EXACT, OPT_GRAPHS = 0, 1
 
@@ -32,7 +32,7 @@ class CsrView(C.Structure):
 
 class AmgParams(C.Structure):
     _fields_ = [("max_levels", C.c_int), ("theta", C.c_double), ("smoother_blocks", C.c_int),
-                ("omega", C.c_double), ("smooth_iter", C.c_int)]
+                ("omega", C.c_double), ("smooth_iter", C.c_int), ("multicolor", C.c_int)]
 
 
 class SolverParams(C.Structure):
@@ -212,8 +212,8 @@ class HostCsr:
     __del__ = close
 
 
-def amg_params(max_levels=20, theta=0.8, smoother_blocks=0, omega=1.0, smooth_iter=1):
-    return AmgParams(max_levels, theta, smoother_blocks, omega, smooth_iter)
+def amg_params(max_levels=20, theta=0.8, smoother_blocks=0, omega=1.0, smooth_iter=1, multicolor=0):
+    return AmgParams(max_levels, theta, smoother_blocks, omega, smooth_iter, multicolor)
 
 
 class Setup:
@@ -247,6 +247,8 @@ class Setup:
         check(lib().sa_setup_view(self.h, op, level, C.byref(v)))
         if op == OP_BJ:
             return np.ctypeslib.as_array(v.rptr, shape=(v.n + 1,)).copy()
+        if op == OP_COLOR:
+            return np.ctypeslib.as_array(v.rptr, shape=(v.n,)).copy()
         kind = {INT: "i32", F64: "f64", F32: "f32"}[self.precision]
         r, c, val = view_arrays(v, kind)
         return r, c, val, v.bit, v.dbit, v.m

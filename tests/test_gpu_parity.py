@@ -13,6 +13,7 @@ import pytest
 
 import oracle_ffi as of
 import sagb
+import setup_views as sv
 
 pytestmark = pytest.mark.gpu
 
@@ -193,30 +194,6 @@ def test_fp32_full_solve(ctx, case):
     S.close()
 
 
-def _oracle_amg(keep, setup):
-    """An oracle hierarchy struct over the product's host setup arrays."""
-    g = {"depth": np.array([setup.depth])}
-    D = setup.depth
-
-    def put(pfx, op, level=0):
-        r, c, v, bit, dbit, m = setup.view(op, level)
-        n = len(r) - 1
-        g[pfx + "_rptr"], g[pfx + "_cind"], g[pfx + "_val"] = r, c, v
-        g[pfx + "_meta"] = np.array([n, m, bit, dbit])
-    put("A0", sagb.OP_A0)
-    for i in range(D):
-        if i < D - 1:
-            put(f"L{i}_CA", sagb.OP_CA, i)
-        put(f"L{i}_P", sagb.OP_P, i)
-        put(f"L{i}_R", sagb.OP_R, i)
-        put(f"S{i}_LD", sagb.OP_LD, i)
-        put(f"S{i}_U", sagb.OP_U, i)
-    put("LU_L", sagb.OP_LUL)
-    put("LU_U", sagb.OP_LUU)
-    g["A0_meta"][2] = 30
-    return of.golden_amg_i32(keep, g)
-
-
 @pytest.mark.parametrize("n", [48])
 def test_int_vcycle_vs_oracle_3d(ctx, n):
     """A deeper hierarchy (3D 7-point n^3): GPU V-cycle == oracle V-cycle."""
@@ -227,7 +204,7 @@ def test_int_vcycle_vs_oracle_3d(ctx, n):
     setup = sagb.Setup(sagb.INT, r, c, v)
     M = sagb.Amg(ctx, sagb.INT, setup=setup)
     keep = of.Keep()
-    h = _oracle_amg(keep, setup)
+    h = sv.oracle_amg(keep, setup)
     rng = np.random.default_rng(5)
     vin = rng.integers(-(1 << 29), 1 << 29, size=len(r) - 1).astype(np.int32)
     ref = np.zeros_like(vin)
