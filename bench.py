@@ -416,8 +416,13 @@ def main_ours(a):
         ach = sw["bytes_per_vcycle"] / (sw["ms_per_vcycle"] * 1e-3) / 1e9
         line["roofline"] = {"kernel": "k_tri (level-scheduled int Gauss-Seidel sweeps, all levels)",
                             "bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
-                            "peak_kind": peak_kind, "traffic": ncu_traffic("k_tri"),
+                            "peak_kind": peak_kind, "traffic": ncu_traffic("k_tri_all_levels"),
                             "share_of_vcycle": sw["ms_per_vcycle"] / k["vcycle"]["ms"]}
+        # the level-0 launch alone (the one kernel with a committed ncu capture)
+        l0 = sw["per_level"][0]
+        a0 = l0["bytes"] / (l0["ms"] * 1e-3) / 1e9
+        line["roofline"]["level0"] = {"kernel": "k_tri level 0", "achieved": a0, "frac": a0 / peak,
+                                      "bytes": l0["bytes"], "ms": l0["ms"], "traffic": ncu_traffic("k_tri_level0")}
         spa = sp["bytes"] / (sp["ms"] * 1e-3) / 1e9
         line["spmv_A0"] = {"achieved": spa, "peak": peak, "unit": "GB/s", "frac": spa / peak, "ms": sp["ms"],
                            "bytes": sp["bytes"], "traffic": ncu_traffic("k_spmv_i32")}
