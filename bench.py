@@ -288,6 +288,10 @@ def multicolor_row(ctx, a, r, c, v, b, nrm_b, dA, A0, db, dx, N):
     e1.record(ctx)
     ctx.sync()
     row["vcycle_ms"] = e0.elapsed_ms(e1) / 10
+    k = kernel_rooflines(ctx, Mm, A0, N, a)
+    row["sweep_ms_per_vcycle"] = k["sweeps"]["ms_per_vcycle"]
+    row["coarse_lu_ms"] = k["coarse_lu"]["ms"]
+    row["sweep_levels"] = [(p["level"], p["n"], p["levels"], round(p["ms"], 4)) for p in k["sweeps"]["per_level"]]
     Sm.close()
     Mm.close()
     Mm64.close()

@@ -232,6 +232,74 @@ int sa_solver_history(sa_solver S, double *hist, int cap, int *n, unsigned *flag
 
 /* Work/main.cpp:153-161: one FP64 V-cycle on b, F = rule(max|c| / ||b||) */
 int sa_rule_bits(sa_ctx ctx, sa_amg M_f64, const double *b, double nrm_b, int *frac_bits);
+/* the same V-cycle; *ratio = max|c| / ||b||, the number the rule maps to F */
+int sa_rule_ratio(sa_ctx ctx, sa_amg M_f64, const double *b, double nrm_b, double *ratio);
+
+/* ------------------------------------------------ learned bit selector
+ * No counterpart in the reference, which picks F by the rule above or by a
+ * manual sweep (Work/sub.cpp:36-102).  A 3-layer FP32 MLP (n_in -> hidden ->
+ * hidden -> n_out, ReLU) maps SA_NUM_FEATURES matrix features to a predicted
+ * cost (log2 iterations) for each candidate F = f_lo + k; the selector takes
+ * the argmin.  Training and inference run in this library's own CUDA kernels.
+ * Arrays are row-major (one sample per row); host or device pointers. */
+#define SA_NUM_FEATURES 20
+typedef struct sa_mlp_net *sa_mlp;
+/* features of an integer setup; ratio = sa_rule_ratio's value */
+int sa_setup_features(sa_setup s_int, double ratio, float *feat);
+int sa_mlp_create(sa_ctx ctx, int n_in, int hidden, int n_out, uint64_t seed, sa_mlp *out);
+int sa_mlp_destroy(sa_mlp m);
+/* flat parameters W1[h][in] b1[h] W2[h][h] b2[h] W3[out][h] b3[out] */
+int sa_mlp_nparams(sa_mlp m, int64_t *n);
+int sa_mlp_get_params(sa_mlp m, float *out);
+int sa_mlp_set_params(sa_mlp m, const float *in);
+/* input standardisation x -> (x - mu) / sd applied before the first layer */
+int sa_mlp_set_norm(sa_mlp m, const float *mu, const float *sd);
+int sa_mlp_predict(sa_ctx ctx, sa_mlp m, const float *X, int n, float *Y);
+/* masked MSE loss sum M (Y - T)^2 / sum M over all n rows and its gradient
+ * with respect to the flat parameters (no update) */
+int sa_mlp_gradient(sa_ctx ctx, sa_mlp m, const float *X, const float *T, const float *M, int n, float *grad,
+                    float *loss);
+/* mini-batch Adam (lr, beta 0.9/0.999, eps 1e-8), rows shuffled per epoch by
+ * seed; loss_hist[epoch] (optional) = mean batch loss */
+int sa_mlp_train(sa_ctx ctx, sa_mlp m, const float *X, const float *T, const float *M, int n, int epochs,
+                 int batch, float lr, uint64_t seed, float *loss_hist);
+/* argmin over the predicted costs of one feature row: *bits = f_lo + k */
+int sa_mlp_select_bits(sa_ctx ctx, sa_mlp m, const float *feat, int f_lo, int *frac_bits);
+
+/* ------------------------------------------------------ batched solver
+ * No counterpart in the reference, which solves one system per process.  Many
+ * independent systems (already LMax1-scaled, uneven sizes), nrhs right-hand
+ * sides each (1, 2 or 4), are set up with the multicolour SOR smoother and
+ * solved together: every operation of the V-cycle and of FGMRESflex is one
+ * launch over the whole batch, each Arnoldi step is one CUDA graph.  Per
+ * system and right-hand side the integer arithmetic is that of the
+ * single-system solver with a multicolour setup (sa_amg_params.multicolor = 1).
+ * Vectors (b, x, precondition in/out) hold the systems' rows one after the
+ * other (sa_batch_offsets) with the right-hand sides interleaved:
+ * v[(offset[s] + i) * nrhs + r].  Per-pair arrays are indexed s * nrhs + r. */
+typedef struct sa_batch_set *sa_batch;
+/* threads: host threads for the per-system setup (0: all) */
+int sa_batch_create(sa_ctx ctx, int nsys, const int *n, const int32_t *const *rptr, const int32_t *const *cind,
+                    const double *const *val, int nrhs, const sa_amg_params *p, int threads, sa_batch *out);
+int sa_batch_destroy(sa_batch B);
+int sa_batch_info(sa_batch B, int *nsys, int *nrhs, int *depth_max, int64_t *rows);
+/* offsets[nsys + 1]: first row of each system in the batch vectors */
+int sa_batch_offsets(sa_batch B, int64_t *offsets);
+/* the integer setup of one system (a new handle sharing the batch's arrays;
+ * release it with sa_setup_destroy) */
+int sa_batch_system_setup(sa_batch B, int sys, sa_setup *out);
+/* intAMGflex::Precondition of every system and right-hand side at once */
+int sa_batch_precondition(sa_ctx ctx, sa_batch B, const int32_t *in, int32_t *out);
+/* time every candidate lanes-per-row value of each level operator and keep the fastest */
+int sa_batch_autotune(sa_ctx ctx, sa_batch B, int reps);
+/* the chosen lanes per row of one operator (op: 0 A, 1 LD sweep, 2 U, 3 P, 4 R) */
+int sa_batch_group(sa_batch B, int level, int op, int *group);
+/* Work/main.cpp:153-161 per system and right-hand side: max|M_f64 b| / ||b|| */
+int sa_batch_rule_ratios(sa_ctx ctx, sa_batch B, const double *b, const double *nrm_b, double *ratio);
+/* Restarted(FGMRESflex) per pair; bits: F_G per system; nrm_b per pair;
+ * iters / converged / final_bits (after overflow fallbacks) per pair, optional */
+int sa_batch_solve(sa_ctx ctx, sa_batch B, const sa_solver_params *p, const int *bits, const double *b,
+                   const double *nrm_b, double *x, int *iters, int *converged, int *final_bits);
 
 #ifdef __cplusplus
 }

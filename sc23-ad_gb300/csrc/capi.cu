@@ -6,9 +6,11 @@
 #include <cstring>
 #include <memory>
 #include <string>
+#include <thread>
 
 #include "../../include/sagb.h"
 #include "cuda/common.cuh"
+#include "host/features.hpp"
 #include "host/generators.hpp"
 #include "sagb_internal.hpp"
 
@@ -74,6 +76,15 @@ struct sa_host_csr {
 };
 struct sa_timer {
     cudaEvent_t e;
+};
+struct sa_mlp_net {
+    std::unique_ptr<Mlp> net;
+};
+struct sa_batch_set {
+    sa_context *ctx;
+    sa_amg_params p;
+    std::shared_ptr<BatchHierarchy> h;
+    std::unique_ptr<BatchEngine> eng;
 };
 
 // ------------------------------------------------------------------ helpers
@@ -906,6 +917,27 @@ extern "C" int sa_solver_history(sa_solver S, double *hist, int cap, int *n, uns
     return SA_OK;
 }
 
+extern "C" int sa_rule_ratio(sa_ctx ctx, sa_amg M, const double *b, double nrm_b, double *ratio) {
+    if (!ctx || !M || !b || !ratio) return fail(SA_ERR_ARG, "null argument");
+    if (M->precision != SA_F64) return fail(SA_ERR_ARG, "the bit rule uses the FP64 preconditioner");
+    SA_GUARD_BEGIN
+    Ctx &c = ctx->c;
+    const int N = M->M->A0.n;
+    std::vector<double> ch(N);
+    Staged sb(c, b, sizeof(double) * N, true, false);
+    double *dc = (double *)dmalloc(sizeof(double) * N);
+    vcycle(c, *M->M, sb.get(), dc);
+    SAGB_CUDA(cudaMemcpyAsync(ch.data(), dc, sizeof(double) * N, cudaMemcpyDeviceToHost, c.stream));
+    SAGB_CUDA(cudaStreamSynchronize(c.stream));
+    dfree(dc);
+    double cmax = 0;
+    for (int i = 0; i < N; i++)
+        if (std::fabs(ch[i]) > cmax) cmax = std::fabs(ch[i]);
+    *ratio = cmax / nrm_b;
+    return SA_OK;
+    SA_GUARD_END
+}
+
 extern "C" int sa_rule_bits(sa_ctx ctx, sa_amg M, const double *b, double nrm_b, int *bits) {
     if (!ctx || !M || !b || !bits) return fail(SA_ERR_ARG, "null argument");
     if (M->precision != SA_F64) return fail(SA_ERR_ARG, "the bit rule uses the FP64 preconditioner");
@@ -923,6 +955,279 @@ extern "C" int sa_rule_bits(sa_ctx ctx, sa_amg M, const double *b, double nrm_b,
     for (int i = 0; i < N; i++)
         if (std::fabs(ch[i]) > cmax) cmax = std::fabs(ch[i]);
     *bits = rule_frac_bits(cmax, nrm_b);
+    return SA_OK;
+    SA_GUARD_END
+}
+
+// ------------------------------------------------------ learned bit selector
+
+extern "C" int sa_setup_features(sa_setup s, double ratio, float *feat) {
+    if (!s || !feat) return fail(SA_ERR_ARG, "null argument");
+    if (!s->hi || !s->A) return fail(SA_ERR_ARG, "features need an integer setup");
+    SA_GUARD_BEGIN
+    bit_features(*s->A, *s->hi, ratio, feat);
+    return SA_OK;
+    SA_GUARD_END
+}
+
+extern "C" int sa_mlp_create(sa_ctx ctx, int n_in, int hidden, int n_out, uint64_t seed, sa_mlp *out) {
+    if (!ctx || !out) return fail(SA_ERR_ARG, "null argument");
+    if (n_in < 1 || hidden < 1 || n_out < 1 || n_in > 4096 || hidden > 4096 || n_out > 4096)
+        return fail(SA_ERR_ARG, "invalid MLP shape");
+    SA_GUARD_BEGIN
+    SAGB_CUDA(cudaSetDevice(ctx->c.device));
+    auto *m = new sa_mlp_net();
+    m->net = std::make_unique<Mlp>(n_in, hidden, n_out, seed);
+    *out = m;
+    return SA_OK;
+    SA_GUARD_END
+}
+
+extern "C" int sa_mlp_destroy(sa_mlp m) {
+    delete m;
+    return SA_OK;
+}
+
+extern "C" int sa_mlp_nparams(sa_mlp m, int64_t *n) {
+    if (!m || !n) return fail(SA_ERR_ARG, "null argument");
+    *n = (int64_t)m->net->nparams();
+    return SA_OK;
+}
+
+extern "C" int sa_mlp_get_params(sa_mlp m, float *out) {
+    if (!m || !out) return fail(SA_ERR_ARG, "null argument");
+    SA_GUARD_BEGIN
+    m->net->get_params(out);
+    return SA_OK;
+    SA_GUARD_END
+}
+
+extern "C" int sa_mlp_set_params(sa_mlp m, const float *in) {
+    if (!m || !in) return fail(SA_ERR_ARG, "null argument");
+    SA_GUARD_BEGIN
+    m->net->set_params(in);
+    return SA_OK;
+    SA_GUARD_END
+}
+
+extern "C" int sa_mlp_set_norm(sa_mlp m, const float *mu, const float *sd) {
+    if (!m || !mu || !sd) return fail(SA_ERR_ARG, "null argument");
+    SA_GUARD_BEGIN
+    m->net->set_norm(mu, sd);
+    return SA_OK;
+    SA_GUARD_END
+}
+
+extern "C" int sa_mlp_predict(sa_ctx ctx, sa_mlp m, const float *X, int n, float *Y) {
+    if (!ctx || !m || !X || !Y || n < 1) return fail(SA_ERR_ARG, "invalid argument");
+    SA_GUARD_BEGIN
+    m->net->predict(ctx->c, X, n, Y);
+    return SA_OK;
+    SA_GUARD_END
+}
+
+extern "C" int sa_mlp_gradient(sa_ctx ctx, sa_mlp m, const float *X, const float *T, const float *M, int n,
+                               float *grad, float *loss) {
+    if (!ctx || !m || !X || !T || !M || n < 1) return fail(SA_ERR_ARG, "invalid argument");
+    SA_GUARD_BEGIN
+    const float l = m->net->gradient(ctx->c, X, T, M, n, grad);
+    if (loss) *loss = l;
+    return SA_OK;
+    SA_GUARD_END
+}
+
+extern "C" int sa_mlp_train(sa_ctx ctx, sa_mlp m, const float *X, const float *T, const float *M, int n,
+                            int epochs, int batch, float lr, uint64_t seed, float *loss_hist) {
+    if (!ctx || !m || !X || !T || !M || n < 1 || epochs < 1 || batch < 1 || !(lr > 0))
+        return fail(SA_ERR_ARG, "invalid argument");
+    SA_GUARD_BEGIN
+    m->net->train(ctx->c, X, T, M, n, epochs, batch, lr, seed, loss_hist);
+    return SA_OK;
+    SA_GUARD_END
+}
+
+extern "C" int sa_mlp_select_bits(sa_ctx ctx, sa_mlp m, const float *feat, int f_lo, int *bits) {
+    if (!ctx || !m || !feat || !bits) return fail(SA_ERR_ARG, "null argument");
+    SA_GUARD_BEGIN
+    std::vector<float> y(m->net->nout);
+    m->net->predict(ctx->c, feat, 1, y.data());
+    int k = 0;
+    for (int i = 1; i < (int)y.size(); i++)
+        if (y[i] < y[k]) k = i;
+    *bits = f_lo + k;
+    return SA_OK;
+    SA_GUARD_END
+}
+
+// ------------------------------------------------------------ batched solver
+
+extern "C" int sa_batch_create(sa_ctx ctx, int nsys, const int *n, const int32_t *const *rptr,
+                               const int32_t *const *cind, const double *const *val, int nrhs,
+                               const sa_amg_params *p, int threads, sa_batch *out) {
+    if (!ctx || !n || !rptr || !cind || !val || !out || nsys < 1) return fail(SA_ERR_ARG, "invalid argument");
+    if (nrhs != 1 && nrhs != 2 && nrhs != 4) return fail(SA_ERR_ARG, "nrhs must be 1, 2 or 4");
+    for (int s = 0; s < nsys; s++)
+        if (int e = check_csr(n[s], n[s], rptr[s], cind[s])) return e;
+    sa_amg_params q;
+    if (p) q = *p;
+    else sa_amg_params_default(&q);
+    if (q.smooth_iter < 1 || q.max_levels < 1 || q.smoother_blocks != 0 || q.theta <= 0 || q.theta > 1)
+        return fail(SA_ERR_ARG, "invalid AMG parameters (the batch uses the multicolour SOR smoother)");
+    q.multicolor = 1;
+    SA_GUARD_BEGIN
+    std::vector<CsrD> sys(nsys);
+    for (int s = 0; s < nsys; s++) {
+        sys[s].n = sys[s].m = n[s];
+        sys[s].rptr.assign(rptr[s], rptr[s] + n[s] + 1);
+        sys[s].cind.assign(cind[s], cind[s] + rptr[s][n[s]]);
+        sys[s].val.assign(val[s], val[s] + rptr[s][n[s]]);
+    }
+    if (threads < 1) threads = (int)std::max(1u, std::thread::hardware_concurrency());
+    auto *B = new sa_batch_set();
+    B->ctx = ctx;
+    B->p = q;
+    try {
+        B->h = std::make_shared<BatchHierarchy>(
+            build_batch(sys, q.theta, q.max_levels, q.omega, q.smooth_iter, threads));
+        SAGB_CUDA(cudaSetDevice(ctx->c.device));
+        B->eng = std::make_unique<BatchEngine>(ctx->c, B->h, nrhs);
+        SAGB_CUDA(cudaDeviceSynchronize());
+    } catch (...) {
+        delete B;
+        throw;
+    }
+    *out = B;
+    return SA_OK;
+    SA_GUARD_END
+}
+
+extern "C" int sa_batch_destroy(sa_batch B) {
+    delete B;
+    return SA_OK;
+}
+
+extern "C" int sa_batch_info(sa_batch B, int *nsys, int *nrhs, int *depth_max, int64_t *rows) {
+    if (!B) return fail(SA_ERR_ARG, "null argument");
+    if (nsys) *nsys = B->h->S;
+    if (nrhs) *nrhs = B->eng->nrhs();
+    if (depth_max) *depth_max = B->h->Dmax;
+    if (rows) *rows = (int64_t)B->eng->rows();
+    return SA_OK;
+}
+
+extern "C" int sa_batch_offsets(sa_batch B, int64_t *offsets) {
+    if (!B || !offsets) return fail(SA_ERR_ARG, "null argument");
+    for (int s = 0; s < B->h->S; s++) offsets[s] = B->h->offset[0][s];
+    offsets[B->h->S] = B->h->n_level[0];
+    return SA_OK;
+}
+
+extern "C" int sa_batch_system_setup(sa_batch B, int sys, sa_setup *out) {
+    if (!B || !out || sys < 0 || sys >= B->h->S) return fail(SA_ERR_ARG, "invalid argument");
+    SA_GUARD_BEGIN
+    auto *s = new sa_hierarchy();
+    s->precision = SA_INT;
+    s->p = B->p;
+    s->A = B->h->A_sys[sys];
+    s->chain = B->h->chain[sys];
+    s->hi = B->h->hi[sys];
+    *out = s;
+    return SA_OK;
+    SA_GUARD_END
+}
+
+extern "C" int sa_batch_precondition(sa_ctx ctx, sa_batch B, const int32_t *in, int32_t *out) {
+    if (!ctx || !B || !in || !out) return fail(SA_ERR_ARG, "null argument");
+    SA_GUARD_BEGIN
+    Ctx &c = ctx->c;
+    const size_t bytes = sizeof(int32_t) * B->eng->rows() * B->eng->nrhs();
+    Staged si(c, in, bytes, true, false);
+    Staged so(c, out, bytes, false, true);
+    B->eng->precondition((const int *)si.get(), (int *)so.get());
+    so.finish();
+    return SA_OK;
+    SA_GUARD_END
+}
+
+extern "C" int sa_batch_autotune(sa_ctx ctx, sa_batch B, int reps) {
+    if (!ctx || !B || reps < 1) return fail(SA_ERR_ARG, "invalid argument");
+    SA_GUARD_BEGIN
+    B->eng->autotune(reps);
+    return SA_OK;
+    SA_GUARD_END
+}
+
+extern "C" int sa_batch_group(sa_batch B, int level, int op, int *group) {
+    if (!B || !group || level < 0 || level >= B->h->Dmax || op < 0 || op > 4) return fail(SA_ERR_ARG, "invalid argument");
+    *group = B->eng->group(level, op);
+    return SA_OK;
+}
+
+extern "C" int sa_batch_rule_ratios(sa_ctx ctx, sa_batch B, const double *b, const double *nrm_b, double *ratio) {
+    if (!ctx || !B || !b || !nrm_b || !ratio) return fail(SA_ERR_ARG, "null argument");
+    SA_GUARD_BEGIN
+    Ctx &c = ctx->c;
+    const int S = B->h->S, R = B->eng->nrhs();
+    const size_t N0 = B->eng->rows();
+    std::vector<double> hb(N0 * R), hn((size_t)S * R);
+    SAGB_CUDA(cudaMemcpy(hb.data(), b, sizeof(double) * hb.size(), cudaMemcpyDefault));
+    SAGB_CUDA(cudaMemcpy(hn.data(), nrm_b, sizeof(double) * hn.size(), cudaMemcpyDefault));
+    SmootherSpec sm;
+    sm.omega = B->p.omega;
+    sm.iter = B->p.smooth_iter;
+    sm.multicolor = 1;
+    for (int s = 0; s < S; s++) {
+        // Work/main.cpp:153-161 per system: one FP64 V-cycle of its own hierarchy
+        auto hd = std::make_shared<FpHierarchy<double>>(build_f64_hierarchy(*B->h->A_sys[s], *B->h->chain[s], sm));
+        auto M = upload_amg_f64(c, hd);
+        const int n = B->h->n_sys[s];
+        const size_t off = (size_t)B->h->offset[0][s];
+        std::vector<double> col(n), out(n);
+        double *db = (double *)dmalloc(sizeof(double) * n), *dc = (double *)dmalloc(sizeof(double) * n);
+        for (int r = 0; r < R; r++) {
+            for (int i = 0; i < n; i++) col[i] = hb[(off + i) * R + r];
+            SAGB_CUDA(cudaMemcpyAsync(db, col.data(), sizeof(double) * n, cudaMemcpyHostToDevice, c.stream));
+            vcycle(c, *M, db, dc);
+            SAGB_CUDA(cudaMemcpyAsync(out.data(), dc, sizeof(double) * n, cudaMemcpyDeviceToHost, c.stream));
+            SAGB_CUDA(cudaStreamSynchronize(c.stream));
+            double cmax = 0;
+            for (int i = 0; i < n; i++) cmax = std::max(cmax, std::fabs(out[i]));
+            ratio[(size_t)s * R + r] = cmax / hn[(size_t)s * R + r];
+        }
+        dfree(db);
+        dfree(dc);
+        M->release();
+    }
+    return SA_OK;
+    SA_GUARD_END
+}
+
+extern "C" int sa_batch_solve(sa_ctx ctx, sa_batch B, const sa_solver_params *p, const int *bits, const double *b,
+                              const double *nrm_b, double *x, int *iters, int *converged, int *final_bits) {
+    if (!ctx || !B || !p || !bits || !b || !nrm_b || !x) return fail(SA_ERR_ARG, "null argument");
+    if (p->m < 1 || p->m > 64 || p->max_outer < 1 || !(p->eps > 0)) return fail(SA_ERR_ARG, "invalid solver parameters");
+    const int S = B->h->S, R = B->eng->nrhs();
+    for (int s = 0; s < S; s++)
+        if (bits[s] < 1 || bits[s] > 30) return fail(SA_ERR_ARG, "fractional bits out of range");
+    SA_GUARD_BEGIN
+    Ctx &c = ctx->c;
+    KrylovParams kp;
+    kp.m = p->m;
+    kp.eps = p->eps;
+    kp.max_outer = p->max_outer;
+    kp.fallback = p->overflow_fallback;
+    kp.explicit_check = p->explicit_stop;
+    const size_t bytes = sizeof(double) * B->eng->rows() * R;
+    Staged sb(c, b, bytes, true, false);
+    Staged sx(c, x, bytes, true, true);
+    BatchStats st;
+    B->eng->solve(kp, bits, (const double *)sb.get(), nrm_b, (double *)sx.get(), st);
+    sx.finish();
+    for (int q = 0; q < S * R; q++) {
+        if (iters) iters[q] = st.iters[q];
+        if (converged) converged[q] = st.converged[q];
+        if (final_bits) final_bits[q] = st.final_bit[q];
+    }
     return SA_OK;
     SA_GUARD_END
 }

@@ -1,0 +1,1280 @@
+// Batched int-AMG-FGMRES: many independent systems of uneven size, each with
+// R right-hand sides, advanced together so that every operation is one launch
+// over the whole batch.
+//
+// Layout.  The systems' level operators are block-diagonal batch matrices
+// (host/batch_setup.hpp) with one shift per row.  Vectors interleave the R
+// right-hand sides of a row (x[row * R + r]), so a row's R values are one
+// 4/8/16-byte load and every matrix entry is read once for all R of them.
+//
+// Per system and right-hand side ("pair"), the arithmetic is exactly that of
+// the single-system solver with the multicolour smoother:
+//   * V-cycle: intAMGflex::Precondition (INTAMG.hpp:269-293); the down pass of
+//     all systems runs level by level, the coarsest LU of every system is one
+//     launch (one CTA per system), then the up pass.
+//   * sweeps: ldtri::MCCSR order (matrix/trispmat.hpp:597-640): one launch per
+//     colour; the rows of a colour read only earlier colours.
+//   * FGMRESflex::Solve (gmres.hpp:225-271) per pair: dots and norms are exact
+//     int64 sums per pair (segmented by system), the Givens/e update and the
+//     convergence test run one thread per pair, pairs that converge stop while
+//     the others continue.
+//   * Restarted::Solve (irsolver.hpp:27-43) per pair on the host, with the FP64
+//     residual of every pair from one launch.
+// Each Arnoldi step of the whole batch is captured once into a CUDA graph and
+// replayed; the per-pair state lives in device memory, so the graph does not
+// change when pairs stop or change fractional bits.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <type_traits>
+
+#include "../sagb_internal.hpp"
+#include "common.cuh"
+
+namespace sagb {
+
+constexpr int kBThreads = 256;
+constexpr int kTileRows = 2048;
+constexpr int kBLuThreads = 512;  // 16 warps: room for 128 registers a thread
+
+struct DBCsr {
+    int n;
+    const int *rptr, *cind, *val;
+    const signed char *bit, *dbit;
+};
+
+template <int R>
+__device__ __forceinline__ void load_r(const int *__restrict__ x, int row, int (&v)[R]) {
+    if constexpr (R == 4) {
+        const int4 q = __ldg(reinterpret_cast<const int4 *>(x) + row);
+        v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
+    } else if constexpr (R == 2) {
+        const int2 q = __ldg(reinterpret_cast<const int2 *>(x) + row);
+        v[0] = q.x; v[1] = q.y;
+    } else {
+        v[0] = __ldg(x + row);
+    }
+}
+// plain (coherent) load: for vectors written earlier in the same sweep
+template <int R>
+__device__ __forceinline__ void load_rw(const int *x, int row, int (&v)[R]) {
+    if constexpr (R == 4) {
+        const int4 q = reinterpret_cast<const int4 *>(x)[row];
+        v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
+    } else if constexpr (R == 2) {
+        const int2 q = reinterpret_cast<const int2 *>(x)[row];
+        v[0] = q.x; v[1] = q.y;
+    } else {
+        v[0] = x[row];
+    }
+}
+template <int R>
+__device__ __forceinline__ void store_r(int *x, int row, const int (&v)[R]) {
+    if constexpr (R == 4) reinterpret_cast<int4 *>(x)[row] = make_int4(v[0], v[1], v[2], v[3]);
+    else if constexpr (R == 2) reinterpret_cast<int2 *>(x)[row] = make_int2(v[0], v[1]);
+    else x[row] = v[0];
+}
+
+// ------------------------------------------------------------------ SpMV
+// y = A x (SET), y = z - A x (RESID) or y = A x + y (ADD), per row shift;
+// the same integer results as k_spmv_i32 for every right-hand side.
+template <int R, int G, int MODE>
+__global__ void __launch_bounds__(kBThreads)
+k_bspmv(DBCsr A, const int *__restrict__ x, int *__restrict__ y, const int *__restrict__ z,
+        const int *__restrict__ row_sys, unsigned *__restrict__ pflag, unsigned *__restrict__ flags) {
+    const long long tid = (long long)blockIdx.x * kBThreads + threadIdx.x;
+    const int row = (int)(tid / G), lane = (int)(tid % G);
+    long long acc[R];
+#pragma unroll
+    for (int r = 0; r < R; r++) acc[r] = 0;
+    if (row < A.n) {
+        const int a = __ldg(A.rptr + row), b = __ldg(A.rptr + row + 1);
+        for (int j = a + lane; j < b; j += G) {
+            const long long v = __ldg(A.val + j);
+            int xv[R];
+            load_r<R>(x, __ldg(A.cind + j), xv);
+#pragma unroll
+            for (int r = 0; r < R; r++) acc[r] = wadd(acc[r], v * (long long)xv[r]);
+        }
+    }
+#pragma unroll
+    for (int r = 0; r < R; r++)
+#pragma unroll
+        for (int o = G / 2; o > 0; o >>= 1) acc[r] = wadd(acc[r], shfl_xor(acc[r], o));
+    if (lane == 0 && row < A.n) {
+        const int bit = A.bit[row];
+        int out[R], zz[R], yy[R];
+        if (MODE == SPMV_RESID) load_r<R>(z, row, zz);
+        if (MODE == SPMV_ADD) load_rw<R>(y, row, yy);
+        bool any = false;
+#pragma unroll
+        for (int r = 0; r < R; r++) {
+            const long long s = acc[r] >> bit;
+            bool ovf = !fits32(s);
+            long long v = (long long)lo32(s);
+            if (MODE == SPMV_RESID) v = (long long)zz[r] - v;
+            if (MODE == SPMV_ADD) v = v + (long long)yy[r];
+            ovf |= !fits32(v);
+            out[r] = lo32(v);
+            if (ovf) {
+                atomicOr(pflag + (size_t)row_sys[row] * R + r, ST_OVERFLOW);
+                any = true;
+            }
+        }
+        store_r<R>(y, row, out);
+        if (any) atomicOr(flags, ST_OVERFLOW);
+    }
+}
+
+// --------------------------------------------------------- colour sweep
+// One colour of the multicolour Gauss-Seidel sweep (ldtri::CSRflex row rule,
+// ldtri.hpp:172-183): t = in << b; t -= sum l_ij out_j; out = (int)((t >> b) * dinv >> db).
+template <int R, int G>
+__global__ void __launch_bounds__(kBThreads)
+k_bcolour(int cnt, const int *__restrict__ rows, DBCsr LD, const int *__restrict__ in, int *out,
+          const int *__restrict__ row_sys, unsigned *__restrict__ pflag, unsigned *__restrict__ flags) {
+    const long long tid = (long long)blockIdx.x * kBThreads + threadIdx.x;
+    const int k = (int)(tid / G), lane = (int)(tid % G);
+    long long acc[R];
+#pragma unroll
+    for (int r = 0; r < R; r++) acc[r] = 0;
+    int row = -1, dpos = 0;
+    if (k < cnt) {
+        row = __ldg(rows + k);
+        const int a = __ldg(LD.rptr + row);
+        dpos = __ldg(LD.rptr + row + 1) - 1;
+        for (int j = a + lane; j < dpos; j += G) {
+            const long long v = __ldg(LD.val + j);
+            int ov[R];
+            load_rw<R>(out, __ldg(LD.cind + j), ov);
+#pragma unroll
+            for (int r = 0; r < R; r++) acc[r] = wsub(acc[r], v * (long long)ov[r]);
+        }
+    }
+#pragma unroll
+    for (int r = 0; r < R; r++)
+#pragma unroll
+        for (int o = G / 2; o > 0; o >>= 1) acc[r] = wadd(acc[r], shfl_xor(acc[r], o));
+    if (lane == 0 && k < cnt) {
+        const int bit = LD.bit[row], dbit = LD.dbit[row];
+        const long long dinv = __ldg(LD.val + dpos);
+        int iv[R], res[R];
+        load_rw<R>(in, row, iv);
+        bool any = false;
+#pragma unroll
+        for (int r = 0; r < R; r++) {
+            const long long t = wadd(wshl((long long)iv[r], bit), acc[r]);
+            const long long s = wmul(t >> bit, dinv) >> dbit;
+            res[r] = lo32(s);
+            if (!fits32(s)) {
+                atomicOr(pflag + (size_t)row_sys[row] * R + r, ST_OVERFLOW);
+                any = true;
+            }
+        }
+        store_r<R>(out, row, res);
+        if (any) atomicOr(flags, ST_OVERFLOW);
+    }
+}
+
+// ------------------------------------------------------------ coarse LU
+struct BLuDesc {
+    int n, sys;
+    int bitL, bitU, dbitU;
+    long long mat_off, d_off;  // offsets into the concatenated L/U and dinv arrays
+    const int *in;             // the system's rows of its LU level (interleaved)
+    int *out;
+};
+
+// LUflex::Solve (solver/lu.hpp:91-94) for every system of the batch: one CTA
+// per system, R right-hand sides at once.  Same panel algorithm as the
+// single-system dense LU kernel: 32-row panels, warps reduce a panel row
+// against the solved part, warp 0 solves the diagonal block from registers.
+template <int R>
+__global__ void __launch_bounds__(kBLuThreads, 1)
+k_blu(const BLuDesc *__restrict__ desc, const int *__restrict__ Lcat, const int *__restrict__ Ucat,
+      const int *__restrict__ dcat, unsigned *__restrict__ pflag, unsigned *__restrict__ flags) {
+    const BLuDesc d = desc[blockIdx.x];
+    const int n = d.n;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    long long *t = (long long *)smem_raw;              // n * R accumulators
+    int *x = (int *)(smem_raw + sizeof(long long) * (size_t)n * R);  // n * R values
+    const int *L = Lcat + d.mat_off, *U = Ucat + d.mat_off, *dinv = dcat + d.d_off;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    unsigned ovf = 0;
+    for (int i = tid; i < n * R; i += kBLuThreads) t[i] = wshl((long long)d.in[i], d.bitL);
+    __syncthreads();
+    for (int k0 = 0; k0 < n; k0 += 32) {
+        const int kb = min(32, n - k0);
+        for (int pr = warp; k0 > 0 && pr < kb; pr += kBLuThreads / 32) {
+            const int *row = L + (size_t)(k0 + pr) * n;
+            long long acc[R];
+#pragma unroll
+            for (int r = 0; r < R; r++) acc[r] = 0;
+            for (int c = lane; c < k0; c += 32) {
+                const long long v = __ldg(row + c);
+#pragma unroll
+                for (int r = 0; r < R; r++) acc[r] = wsub(acc[r], v * (long long)x[c * R + r]);
+            }
+#pragma unroll
+            for (int r = 0; r < R; r++) {
+                for (int o = 16; o > 0; o >>= 1) acc[r] = wadd(acc[r], shfl_xor(acc[r], o));
+                if (lane == 0) t[(k0 + pr) * R + r] = wadd(t[(k0 + pr) * R + r], acc[r]);
+            }
+        }
+        __syncthreads();
+        if (warp == 0) {
+            int dblk[32];
+            const int *row = L + (size_t)(k0 + lane) * n + k0;
+#pragma unroll
+            for (int c = 0; c < 32; c++) dblk[c] = (lane < kb && c < lane) ? __ldg(row + c) : 0;
+            long long tr[R];
+#pragma unroll
+            for (int r = 0; r < R; r++) tr[r] = lane < kb ? t[(k0 + lane) * R + r] : 0;
+#pragma unroll
+            for (int c = 0; c < 32; c++) {
+                if (c < kb) {
+#pragma unroll
+                    for (int r = 0; r < R; r++) {
+                        const long long s = tr[r] >> d.bitL;
+                        if (lane == c && !fits32(s)) ovf |= 1u << r;
+                        const int xc = __shfl_sync(0xffffffffu, lo32(s), c);
+                        if (lane > c) tr[r] = wsub(tr[r], (long long)dblk[c] * xc);
+                        if (lane == c) x[(k0 + c) * R + r] = xc;
+                    }
+                }
+            }
+        }
+        __syncthreads();
+    }
+    for (int i = tid; i < n * R; i += kBLuThreads) t[i] = wshl((long long)x[i], d.bitU);
+    __syncthreads();
+    for (int k1 = n; k1 > 0; k1 -= 32) {
+        const int kb = min(32, k1);
+        const int k0 = k1 - kb;
+        for (int pr = warp; k1 < n && pr < kb; pr += kBLuThreads / 32) {
+            const int *row = U + (size_t)(k0 + pr) * n;
+            long long acc[R];
+#pragma unroll
+            for (int r = 0; r < R; r++) acc[r] = 0;
+            for (int c = k1 + lane; c < n; c += 32) {
+                const long long v = __ldg(row + c);
+#pragma unroll
+                for (int r = 0; r < R; r++) acc[r] = wsub(acc[r], v * (long long)x[c * R + r]);
+            }
+#pragma unroll
+            for (int r = 0; r < R; r++) {
+                for (int o = 16; o > 0; o >>= 1) acc[r] = wadd(acc[r], shfl_xor(acc[r], o));
+                if (lane == 0) t[(k0 + pr) * R + r] = wadd(t[(k0 + pr) * R + r], acc[r]);
+            }
+        }
+        __syncthreads();
+        if (warp == 0) {
+            int dblk[32];
+            const int *row = U + (size_t)(k0 + lane) * n + k0;
+#pragma unroll
+            for (int c = 0; c < 32; c++) dblk[c] = (lane < kb && c > lane && c < kb) ? __ldg(row + c) : 0;
+            long long tr[R];
+#pragma unroll
+            for (int r = 0; r < R; r++) tr[r] = lane < kb ? t[(k0 + lane) * R + r] : 0;
+            const long long dv = lane < kb ? (long long)__ldg(dinv + k0 + lane) : 0;
+#pragma unroll
+            for (int c = 31; c >= 0; c--) {
+                if (c < kb) {
+#pragma unroll
+                    for (int r = 0; r < R; r++) {
+                        int xc = 0;
+                        if (lane == c) {
+                            const long long s = wmul(tr[r] >> d.bitU, dv) >> d.dbitU;
+                            if (!fits32(s)) ovf |= 1u << r;
+                            xc = lo32(s);
+                        }
+                        xc = __shfl_sync(0xffffffffu, xc, c);
+                        if (lane < c) tr[r] = wsub(tr[r], (long long)dblk[c] * xc);
+                        if (lane == c) x[(k0 + c) * R + r] = xc;
+                    }
+                }
+            }
+        }
+        __syncthreads();
+    }
+    for (int i = tid; i < n * R; i += kBLuThreads) d.out[i] = x[i];
+    if (ovf) {
+        for (int r = 0; r < R; r++)
+            if (ovf & (1u << r)) atomicOr(pflag + (size_t)d.sys * R + r, ST_OVERFLOW);
+        atomicOr(flags, ST_OVERFLOW);
+    }
+}
+
+// ============================================================== Krylov
+
+struct BTile {
+    int sys, row0, row1, first;  // rows [row0, row1) of one system; first tile of that system
+};
+
+struct BPair {
+    double e0, e_inv, nrm_b, relres;
+    long long criteria, hinv;
+    int bit, active, jn, conv;
+    unsigned bad;  // status bits seen while the pair was active (the cycle is discarded)
+    int pad;
+};
+
+struct BInfo {
+    int n_active;
+    unsigned flags;
+};
+
+// fixed-order block sum of R int64 partials (wrapping); result valid in thread 0
+template <int R>
+__device__ __forceinline__ void bsum_i64(long long (&v)[R], long long (*sh)[R]) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int r = 0; r < R; r++)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v[r] = wadd(v[r], shfl_xor(v[r], o));
+    if (lane == 0)
+#pragma unroll
+        for (int r = 0; r < R; r++) sh[warp][r] = v[r];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int r = 0; r < R; r++) {
+            long long s = 0;
+            for (int w = 0; w < kBThreads / 32; w++) s = wadd(s, sh[w][r]);
+            v[r] = s;
+        }
+    }
+    __syncthreads();
+}
+
+template <int R>
+__device__ __forceinline__ void bsum_f64(double (&v)[R], double (*sh)[R]) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int r = 0; r < R; r++)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v[r] += __shfl_xor_sync(0xffffffffu, v[r], o);
+    if (lane == 0)
+#pragma unroll
+        for (int r = 0; r < R; r++) sh[warp][r] = v[r];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int r = 0; r < R; r++) {
+            double s = 0;
+            for (int w = 0; w < kBThreads / 32; w++) s += sh[w][r];
+            v[r] = s;
+        }
+    }
+    __syncthreads();
+}
+
+// FGMRESflex::Solve prologue per pair (gmres.hpp:228-233)
+__global__ void k_bbegin(int P, const double *__restrict__ e0, double eps, BPair *pairs, long long *e,
+                         unsigned long long *acc, int m) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= P) return;
+    BPair &q = pairs[p];
+    q.jn = 0;
+    q.conv = 0;
+    q.bad = 0;
+    for (int k = 0; k <= m + 1; k++) acc[(size_t)p * (m + 2) + k] = 0;
+    if (!q.active) return;
+    const double fact = (double)(1LL << q.bit);
+    q.e0 = e0[p];
+    q.e_inv = 1.0 / q.e0;
+    q.criteria = d2l_x86(__dmul_rn(__dmul_rn(__dmul_rn(q.nrm_b, eps), q.e_inv), fact));
+    e[(size_t)p * (m + 1)] = 1LL << q.bit;
+}
+
+template <int R>
+__global__ void k_bv0(const BTile *__restrict__ tiles, const double *__restrict__ rv, const BPair *__restrict__ pairs,
+                      int *__restrict__ V0) {
+    const BTile t = tiles[blockIdx.x];
+    for (int i = t.row0 + threadIdx.x; i < t.row1; i += blockDim.x) {
+#pragma unroll
+        for (int r = 0; r < R; r++) {
+            const BPair &q = pairs[t.sys * R + r];
+            if (!q.active) continue;
+            const double fact = (double)(1LL << q.bit);
+            V0[(size_t)i * R + r] = d2i_x86(__dmul_rn(__dmul_rn(rv[(size_t)i * R + r], q.e_inv), fact));
+        }
+    }
+}
+
+// w = A z on the tile's rows and acc[p][0] += V0 . w
+template <int R, int G>
+__global__ void __launch_bounds__(kBThreads)
+k_bspmv_dot(const BTile *__restrict__ tiles, DBCsr A, const int *__restrict__ z, int *__restrict__ w,
+            const int *__restrict__ v0, const BPair *__restrict__ pairs, unsigned long long *acc, int m,
+            unsigned *__restrict__ pflag, unsigned *__restrict__ flags) {
+    __shared__ long long sh[kBThreads / 32][R];
+    const BTile t = tiles[blockIdx.x];
+    const int lane = threadIdx.x % G;
+    long long dot[R];
+#pragma unroll
+    for (int r = 0; r < R; r++) dot[r] = 0;
+    unsigned ovf = 0;
+    for (int row0 = t.row0; row0 < t.row1; row0 += kBThreads / G) {
+        const int row = row0 + threadIdx.x / G;
+        long long a[R];
+#pragma unroll
+        for (int r = 0; r < R; r++) a[r] = 0;
+        if (row < t.row1) {
+            const int b0 = __ldg(A.rptr + row), b1 = __ldg(A.rptr + row + 1);
+            for (int j = b0 + lane; j < b1; j += G) {
+                const long long v = __ldg(A.val + j);
+                int zv[R];
+                load_r<R>(z, __ldg(A.cind + j), zv);
+#pragma unroll
+                for (int r = 0; r < R; r++) a[r] = wadd(a[r], v * (long long)zv[r]);
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < R; r++)
+#pragma unroll
+            for (int o = G / 2; o > 0; o >>= 1) a[r] = wadd(a[r], shfl_xor(a[r], o));
+        if (lane == 0 && row < t.row1) {
+            const int bit = A.bit[row];
+            int y[R], vv[R];
+            load_r<R>(v0, row, vv);
+#pragma unroll
+            for (int r = 0; r < R; r++) {
+                const long long s = a[r] >> bit;
+                if (!fits32(s)) ovf |= 1u << r;
+                y[r] = lo32(s);
+                dot[r] = wadd(dot[r], (long long)vv[r] * y[r]);
+            }
+            store_r<R>(w, row, y);
+        }
+    }
+    bsum_i64<R>(dot, sh);
+    if (threadIdx.x == 0)
+#pragma unroll
+        for (int r = 0; r < R; r++) atomicAdd(acc + (size_t)(t.sys * R + r) * (m + 2), (unsigned long long)dot[r]);
+    if (ovf) {
+#pragma unroll
+        for (int r = 0; r < R; r++)
+            if (ovf & (1u << r)) atomicOr(pflag + (size_t)t.sys * R + r, ST_OVERFLOW);
+        atomicOr(flags, ST_OVERFLOW);
+    }
+}
+
+// MGS pass k of step j for every active pair: h = acc[k] >> bit, H[j][k] = h,
+// w += (int)((-h) V_k >> bit), then acc[k+1] += V_{k+1} . w (or w . w).
+template <int R, bool LAST>
+__global__ void __launch_bounds__(kBThreads)
+k_bmgs(const BTile *__restrict__ tiles, int k, int j, int m, size_t vstride, const int *__restrict__ V,
+       int *__restrict__ w, const BPair *__restrict__ pairs, unsigned long long *acc, long long *H) {
+    __shared__ long long sh[kBThreads / 32][R];
+    const BTile t = tiles[blockIdx.x];
+    long long a[R];
+    int bit[R];
+    bool act[R];
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+        const int p = t.sys * R + r;
+        act[r] = pairs[p].active != 0;
+        bit[r] = pairs[p].bit;
+        const long long h = ((long long)acc[(size_t)p * (m + 2) + k]) >> bit[r];
+        if (t.first && threadIdx.x == 0 && act[r]) H[(size_t)p * (m + 1) * m + (size_t)j * (m + 1) + k] = h;
+        a[r] = wsub(0, h);
+    }
+    const int *vk = V + (size_t)k * vstride;
+    const int *vk1 = V + (size_t)(k + 1) * vstride;
+    long long part[R];
+#pragma unroll
+    for (int r = 0; r < R; r++) part[r] = 0;
+    for (int i = t.row0 + threadIdx.x; i < t.row1; i += kBThreads) {
+        int wv[R], v[R], v1[R];
+        load_rw<R>(w, i, wv);
+        load_r<R>(vk, i, v);
+        if (!LAST) load_r<R>(vk1, i, v1);
+#pragma unroll
+        for (int r = 0; r < R; r++) {
+            if (!act[r]) continue;
+            wv[r] = (int)((unsigned)wv[r] + (unsigned)lo32(wmul(a[r], (long long)v[r]) >> bit[r]));
+            part[r] = wadd(part[r], LAST ? (long long)wv[r] * wv[r] : (long long)v1[r] * wv[r]);
+        }
+        store_r<R>(w, i, wv);
+    }
+    bsum_i64<R>(part, sh);
+    if (threadIdx.x == 0)
+#pragma unroll
+        for (int r = 0; r < R; r++)
+            if (act[r])
+                atomicAdd(acc + (size_t)(t.sys * R + r) * (m + 2) + (LAST ? m + 1 : k + 1),
+                          (unsigned long long)part[r]);
+}
+
+__device__ long long bggen(long long a, long long b, long long *c, long long *s, int bit, unsigned *pf) {
+    const long long r = lsqrt_dev(wadd(wmul(a, a), wmul(b, b)));
+    long long inv_r = 0;
+    if (r == 0) *pf |= ST_DIVZERO;
+    else inv_r = ((1LL << 62) / r) >> (62 - bit - bit);
+    *c = wmul(a, inv_r) >> bit;
+    *s = wsub(0, wmul(b, inv_r)) >> bit;
+    return r;
+}
+
+// per pair: H_{j+1,j} = lsqrt(w.w), its reciprocal, Givens, e update and the
+// convergence test (gmres.hpp:240-262); converged pairs leave the cycle
+__global__ void k_bgivens(int P, int j, int m, BPair *pairs, long long *Hall, long long *call, long long *sall,
+                          long long *eall, unsigned long long *acc, unsigned *pflag, BInfo *info) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < P && pairs[p].active) {
+        BPair &q = pairs[p];
+        const int bit = q.bit;
+        long long *Hj = Hall + (size_t)p * (m + 1) * m + (size_t)j * (m + 1);
+        long long *c = call + (size_t)p * m, *s = sall + (size_t)p * m, *e = eall + (size_t)p * (m + 1);
+        unsigned long long *ac = acc + (size_t)p * (m + 2);
+        unsigned pf = 0;
+        const long long nsq = (long long)ac[m + 1];
+        if (nsq < 0) pf |= ST_NORM_OVF;
+        Hj[j + 1] = lsqrt_dev(nsq);
+        long long hinv = 0;
+        if (Hj[j + 1] == 0) pf |= ST_DIVZERO;
+        else hinv = ((1LL << 62) / Hj[j + 1]) >> (62 - bit - bit);
+        q.hinv = hinv;
+        for (int k = 0; k < j; k++) {
+            const long long tt = Hj[k];
+            Hj[k] = wsub(wmul(c[k], tt), wmul(s[k], Hj[k + 1])) >> bit;
+            Hj[k + 1] = wadd(wmul(s[k], tt), wmul(c[k], Hj[k + 1])) >> bit;
+        }
+        Hj[j] = bggen(Hj[j], Hj[j + 1], &c[j], &s[j], bit, &pf);
+        Hj[j + 1] = 0;
+        e[j + 1] = wmul(s[j], e[j]) >> bit;
+        e[j] = wmul(c[j], e[j]) >> bit;
+        const double fact = (double)(1LL << bit);
+        q.relres = fabs(__ddiv_rn(__dmul_rn(q.e0, (double)e[j + 1]), fact)) / q.nrm_b;
+        const long long en = e[j + 1];
+        const long long aen = en < 0 ? wsub(0, en) : en;
+        q.jn = j + 1;
+        for (int k = 0; k <= m + 1; k++) ac[k] = 0;
+        // status raised while this pair was active: the V-cycle, SpMV and LU
+        // of this step (pflag) or the scalars above (pf)
+        const unsigned bad = pf | (pflag[p] & (ST_OVERFLOW | ST_DIVZERO | ST_NORM_OVF));
+        if (bad) {
+            q.bad = bad;
+            q.active = 0;
+        } else if (aen <= q.criteria) {
+            q.conv = 1;
+            q.active = 0;
+        } else if (j + 1 < m) {
+            atomicAdd(&info->n_active, 1);
+        }
+    }
+}
+
+// V_{j+1} = (int)(hinv * w >> bit) for the pairs that took step j
+template <int R>
+__global__ void k_bscal(const BTile *__restrict__ tiles, int j, const BPair *__restrict__ pairs, int *__restrict__ w) {
+    const BTile t = tiles[blockIdx.x];
+    long long a[R];
+    int bit[R];
+    bool act[R];
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+        const BPair &q = pairs[t.sys * R + r];
+        act[r] = q.jn == j + 1;
+        a[r] = q.hinv;
+        bit[r] = q.bit;
+    }
+    for (int i = t.row0 + threadIdx.x; i < t.row1; i += blockDim.x) {
+        int wv[R];
+        load_rw<R>(w, i, wv);
+#pragma unroll
+        for (int r = 0; r < R; r++)
+            if (act[r]) wv[r] = lo32(wmul(a[r], (long long)wv[r]) >> bit[r]);
+        store_r<R>(w, i, wv);
+    }
+}
+
+__global__ void k_binfo_reset(BInfo *info) {
+    info->n_active = 0;
+}
+
+// blas2::int32::Trsv per pair (blas2.hpp:366-376); skipped for discarded pairs
+__global__ void k_btrsv(int P, int m, const BPair *__restrict__ pairs, const long long *Hall, const long long *eall,
+                        double *yall) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= P) return;
+    const BPair &q = pairs[p];
+    const int jn = q.jn;
+    if (jn == 0 || q.bad) return;
+    const long long *H = Hall + (size_t)p * (m + 1) * m;
+    const long long *e = eall + (size_t)p * (m + 1);
+    double *y = yall + (size_t)p * m;
+    const double fact = (double)(1LL << q.bit);
+    for (int i = jn - 1; i >= 0; i--) {
+        double t = __ddiv_rn(__dmul_rn(q.e0, (double)e[i]), fact);
+        for (int k = jn - 1; k > i; k--) t = __dsub_rn(t, __dmul_rn(__ddiv_rn((double)H[(size_t)k * (m + 1) + i], fact), y[k]));
+        y[i] = __ddiv_rn(t, __ddiv_rn((double)H[(size_t)i * (m + 1) + i], fact));
+    }
+}
+
+// x += y_k Z_k 2^-bit, k = 0..jn-1 in order (Axpy_D, blas1.hpp:252-258)
+template <int R>
+__global__ void k_bxupd(const BTile *__restrict__ tiles, int m, size_t vstride, const BPair *__restrict__ pairs,
+                        const double *__restrict__ yall, const int *__restrict__ Z, double *__restrict__ x) {
+    const BTile t = tiles[blockIdx.x];
+    __shared__ double sy[R][64];
+    __shared__ int sjn[R];
+    __shared__ double sfi[R];
+    if (threadIdx.x < R) {
+        const int p = t.sys * R + threadIdx.x;
+        const BPair &q = pairs[p];
+        const bool ok = q.jn > 0 && !q.bad;
+        sjn[threadIdx.x] = ok ? q.jn : 0;
+        sfi[threadIdx.x] = 1.0 / (double)(1LL << q.bit);
+    }
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < R * m; idx += blockDim.x) {
+        const int r = idx / m, k = idx % m;
+        sy[r][k] = k < sjn[r] ? yall[(size_t)(t.sys * R + r) * m + k] : 0.0;
+    }
+    __syncthreads();
+    for (int i = t.row0 + threadIdx.x; i < t.row1; i += blockDim.x) {
+#pragma unroll
+        for (int r = 0; r < R; r++) {
+            const int jn = sjn[r];
+            if (!jn) continue;
+            double xi = x[(size_t)i * R + r];
+            for (int k = 0; k < jn; k++)
+                xi = __dadd_rn(xi, __dmul_rn(__dmul_rn(sy[r][k], (double)Z[(size_t)k * vstride + (size_t)i * R + r]), sfi[r]));
+            x[(size_t)i * R + r] = xi;
+        }
+    }
+}
+
+// r = b - A x per row in the reference's order (row-sequential FP64 SpMV,
+// then Axpby(1, b, -1, r)), every right-hand side
+template <int R>
+__global__ void k_bresid_f64(int n, const int *__restrict__ rptr, const int *__restrict__ cind,
+                             const double *__restrict__ val, const double *__restrict__ x, const double *__restrict__ b,
+                             double *__restrict__ rv) {
+    const int row = blockIdx.x * blockDim.x + threadIdx.x;
+    if (row >= n) return;
+    double acc[R];
+#pragma unroll
+    for (int r = 0; r < R; r++) acc[r] = 0.0;
+    for (int j = rptr[row]; j < rptr[row + 1]; j++) {
+        const double a = val[j];
+        const size_t c = (size_t)cind[j] * R;
+#pragma unroll
+        for (int r = 0; r < R; r++) acc[r] = __dadd_rn(acc[r], __dmul_rn(a, x[c + r]));
+    }
+#pragma unroll
+    for (int r = 0; r < R; r++) rv[(size_t)row * R + r] = __dsub_rn(b[(size_t)row * R + r], acc[r]);
+}
+
+// per-tile sums of squares (fixed order), then per pair in tile order
+template <int R>
+__global__ void k_bnorm_part(const BTile *__restrict__ tiles, const double *__restrict__ v, double *__restrict__ part) {
+    __shared__ double sh[kBThreads / 32][R];
+    const BTile t = tiles[blockIdx.x];
+    double s[R];
+#pragma unroll
+    for (int r = 0; r < R; r++) s[r] = 0;
+    for (int i = t.row0 + threadIdx.x; i < t.row1; i += kBThreads)
+#pragma unroll
+        for (int r = 0; r < R; r++) {
+            const double q = v[(size_t)i * R + r];
+            s[r] += q * q;
+        }
+    bsum_f64<R>(s, sh);
+    if (threadIdx.x == 0)
+#pragma unroll
+        for (int r = 0; r < R; r++) part[(size_t)blockIdx.x * R + r] = s[r];
+}
+
+__global__ void k_bnorm_fin(int S, int R, const int *__restrict__ tile_ptr, const double *__restrict__ part,
+                            double *__restrict__ out) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= S * R) return;
+    const int s = p / R, r = p % R;
+    double acc = 0;
+    for (int k = tile_ptr[s]; k < tile_ptr[s + 1]; k++) acc += part[(size_t)k * R + r];
+    out[p] = sqrt(acc);
+}
+
+// ============================================================== host side
+
+static DBCsr dview(const BatchCsr &M, int *&rp, int *&ci, int *&va, signed char *&bi, signed char *&db) {
+    rp = dupload(M.rptr);
+    ci = M.cind.empty() ? nullptr : dupload(M.cind);
+    va = M.val.empty() ? nullptr : dupload(M.val);
+    bi = M.bit.empty() ? nullptr : dupload(M.bit);
+    db = M.dbit.empty() ? nullptr : dupload(M.dbit);
+    return DBCsr{M.n, rp, ci, va, bi, db};
+}
+
+struct DevBMat {
+    DBCsr d{};
+    int group = 1;
+    int *rp = nullptr, *ci = nullptr, *va = nullptr;
+    signed char *bi = nullptr, *db = nullptr;
+    void up(const BatchCsr &M) {
+        d = dview(M, rp, ci, va, bi, db);
+        group = pick_group(M.n ? (double)M.nnz() / M.n : 1.0);
+    }
+    void release() {
+        dfree(rp); dfree(ci); dfree(va); dfree(bi); dfree(db);
+        rp = ci = va = nullptr;
+        bi = db = nullptr;
+    }
+};
+
+struct DevBLevel {
+    int n_all = 0, n_smooth = 0;
+    DevBMat A, LD, U, P, R;
+    int *colour_rows = nullptr;
+    std::vector<int> colour_ptr;
+    int *row_sys = nullptr;       // system of each row of this level
+    int *row_sys_next = nullptr;  // ... and of level l+1 (rows of R)
+};
+
+struct BatchEngine::Impl {
+    Ctx &c;
+    int S, Rn, Dmax, smooth_iter, m = 0;
+    std::shared_ptr<BatchHierarchy> h;
+    std::vector<DevBLevel> lv;
+    std::vector<int> n_level;
+    std::vector<int *> ee, xx, rr, tmp;  // per level (ee/xx index l = 0 unused)
+    std::vector<int *> row_sys;          // per level 0 .. Dmax
+    BLuDesc *d_lu = nullptr;
+    int nlu = 0;
+    size_t lu_smem = 0;
+    int *Lcat = nullptr, *Ucat = nullptr, *dcat = nullptr;
+    DevCsr Af;
+    std::vector<BTile> tiles_h;
+    BTile *tiles = nullptr;
+    int *tile_ptr = nullptr;
+    int ntiles = 0;
+    unsigned *pflag = nullptr;
+    // Krylov state (allocated for the largest m used)
+    int *V = nullptr, *Z = nullptr;
+    long long *H = nullptr, *cs = nullptr, *sn = nullptr, *e = nullptr;
+    double *y = nullptr, *rvec = nullptr, *nrm = nullptr, *npart = nullptr, *e0 = nullptr;
+    unsigned long long *acc = nullptr;
+    BPair *pairs = nullptr;
+    BInfo *info_d = nullptr, *info_h = nullptr;
+    std::vector<cudaGraphExec_t> graphs;
+    std::vector<long long> graph_launches;
+    size_t N0 = 0;  // level-0 rows
+
+    Impl(Ctx &ctx, std::shared_ptr<BatchHierarchy> hh, int nrhs) : c(ctx), h(hh) {
+        S = h->S;
+        Rn = nrhs;
+        Dmax = h->Dmax;
+        smooth_iter = h->hi.empty() ? 1 : h->hi[0]->smooth_iter;
+        n_level = h->n_level;
+        N0 = (size_t)n_level[0];
+        lv.resize(Dmax);
+        for (int l = 0; l < Dmax; l++) {
+            const BatchLevel &L = h->lv[l];
+            DevBLevel &d = lv[l];
+            d.n_all = L.n_all;
+            d.n_smooth = L.n_smooth;
+            d.A.up(L.A);
+            d.LD.up(L.LD);
+            d.U.up(L.U);
+            d.P.up(L.P);
+            d.R.up(L.R);
+            // the colour pass reads a row's LD entries minus the diagonal
+            d.LD.group = pick_group(L.LD.n ? (double)(L.LD.nnz() - L.LD.n) / L.LD.n : 1.0);
+            d.colour_rows = L.colour_rows.empty() ? nullptr : dupload(L.colour_rows);
+            d.colour_ptr = L.colour_ptr;
+        }
+        for (int l = 0; l <= Dmax; l++) row_sys.push_back(dupload(h->row_sys[l]));
+        for (int l = 0; l < Dmax; l++) {
+            lv[l].row_sys = row_sys[l];
+            lv[l].row_sys_next = row_sys[l + 1];
+        }
+        auto vec = [&](int rows) { return (int *)dmalloc(sizeof(int) * (size_t)std::max(rows, 1) * Rn); };
+        ee.assign(Dmax + 1, nullptr);
+        xx.assign(Dmax + 1, nullptr);
+        rr.assign(Dmax, nullptr);
+        tmp.assign(Dmax, nullptr);
+        for (int l = 1; l <= Dmax; l++) {
+            ee[l] = vec(n_level[l]);
+            xx[l] = vec(n_level[l]);
+        }
+        for (int l = 0; l < Dmax; l++) {
+            rr[l] = vec(n_level[l]);
+            tmp[l] = vec(n_level[l]);
+        }
+        // coarsest LU factors of every system, concatenated
+        std::vector<BLuDesc> desc;
+        std::vector<int> Lh, Uh, dh;
+        size_t maxn = 0;
+        for (const BatchLU &lu : h->lu) {
+            BLuDesc d{};
+            d.n = lu.n;
+            d.sys = lu.sys;
+            d.bitL = lu.bitL;
+            d.bitU = lu.bitU;
+            d.dbitU = lu.dbitU;
+            d.mat_off = (long long)Lh.size();
+            d.d_off = (long long)dh.size();
+            d.in = ee[lu.level] + (size_t)lu.offset * Rn;
+            d.out = xx[lu.level] + (size_t)lu.offset * Rn;
+            Lh.insert(Lh.end(), lu.L.begin(), lu.L.end());
+            Uh.insert(Uh.end(), lu.U.begin(), lu.U.end());
+            dh.insert(dh.end(), lu.dinv.begin(), lu.dinv.end());
+            maxn = std::max(maxn, (size_t)lu.n);
+            desc.push_back(d);
+        }
+        nlu = (int)desc.size();
+        lu_smem = (sizeof(long long) + sizeof(int)) * maxn * Rn;
+        if (lu_smem > 227 * 1024) throw CudaError{"a coarsest level is too large for the batched LU kernel"};
+        Lcat = dupload(Lh);
+        Ucat = dupload(Uh);
+        dcat = dupload(dh);
+        d_lu = dupload(desc);
+        Af = upload_csr_f64(h->Af);
+        // tiles over the level-0 rows, never straddling two systems
+        std::vector<int> tp(1, 0);
+        for (int s = 0; s < S; s++) {
+            const int off = h->offset[0][s], n = h->n_sys[s];
+            for (int r0 = 0; r0 < n; r0 += kTileRows)
+                tiles_h.push_back(BTile{s, off + r0, off + std::min(n, r0 + kTileRows), r0 == 0});
+            tp.push_back((int)tiles_h.size());
+        }
+        ntiles = (int)tiles_h.size();
+        tiles = dupload(tiles_h);
+        tile_ptr = dupload(tp);
+        pflag = (unsigned *)dmalloc(sizeof(unsigned) * (size_t)S * Rn);
+        SAGB_CUDA(cudaMemset(pflag, 0, sizeof(unsigned) * (size_t)S * Rn));
+        rvec = (double *)dmalloc(sizeof(double) * N0 * Rn);
+        nrm = (double *)dmalloc(sizeof(double) * (size_t)S * Rn);
+        e0 = (double *)dmalloc(sizeof(double) * (size_t)S * Rn);
+        npart = (double *)dmalloc(sizeof(double) * (size_t)ntiles * Rn);
+        pairs = (BPair *)dmalloc(sizeof(BPair) * (size_t)S * Rn);
+        SAGB_CUDA(cudaMemset(pairs, 0, sizeof(BPair) * (size_t)S * Rn));
+        info_d = (BInfo *)dmalloc(sizeof(BInfo));
+        SAGB_CUDA(cudaMallocHost(&info_h, sizeof(BInfo)));
+        static bool attr = false;
+        if (!attr) {
+            SAGB_CUDA(cudaFuncSetAttribute(k_blu<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
+            SAGB_CUDA(cudaFuncSetAttribute(k_blu<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
+            SAGB_CUDA(cudaFuncSetAttribute(k_blu<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
+            attr = true;
+        }
+    }
+
+    void free_krylov() {
+        dfree(V); dfree(Z); dfree(H); dfree(cs); dfree(sn); dfree(e); dfree(y); dfree(acc);
+        V = Z = nullptr;
+        H = cs = sn = e = nullptr;
+        y = nullptr;
+        acc = nullptr;
+        clear_graphs();
+    }
+
+    void clear_graphs() {
+        for (auto g : graphs)
+            if (g) cudaGraphExecDestroy(g);
+        graphs.clear();
+        graph_launches.clear();
+    }
+
+    ~Impl() {
+        free_krylov();
+        for (auto &d : lv) {
+            d.A.release(); d.LD.release(); d.U.release(); d.P.release(); d.R.release();
+            dfree(d.colour_rows);
+        }
+        for (auto p : row_sys) dfree(p);
+        for (auto p : ee) dfree(p);
+        for (auto p : xx) dfree(p);
+        for (auto p : rr) dfree(p);
+        for (auto p : tmp) dfree(p);
+        dfree(d_lu); dfree(Lcat); dfree(Ucat); dfree(dcat);
+        Af.release();
+        dfree(tiles); dfree(tile_ptr); dfree(pflag); dfree(rvec); dfree(nrm); dfree(e0); dfree(npart);
+        dfree(pairs); dfree(info_d);
+        if (info_h) cudaFreeHost(info_h);
+    }
+
+    // ------------------------------------------------------- dispatch helpers
+    template <typename F>
+    void by_r(F &&f) {
+        if (Rn == 4) f(std::integral_constant<int, 4>());
+        else if (Rn == 2) f(std::integral_constant<int, 2>());
+        else f(std::integral_constant<int, 1>());
+    }
+    template <typename F>
+    static void by_g(int G, F &&f) {
+        switch (G) {
+            case 1: f(std::integral_constant<int, 1>()); break;
+            case 2: f(std::integral_constant<int, 2>()); break;
+            case 4: f(std::integral_constant<int, 4>()); break;
+            case 8: f(std::integral_constant<int, 8>()); break;
+            case 16: f(std::integral_constant<int, 16>()); break;
+            default: f(std::integral_constant<int, 32>()); break;
+        }
+    }
+
+    void bspmv(const DevBMat &M, const int *x, int *y, int mode, const int *z, const int *row_sys) {
+        if (M.d.n == 0) return;
+        const long long threads = (long long)M.d.n * M.group;
+        const int blocks = (int)((threads + kBThreads - 1) / kBThreads);
+        by_r([&](auto RR) {
+            constexpr int R = decltype(RR)::value;
+            by_g(M.group, [&](auto GG) {
+                constexpr int G = decltype(GG)::value;
+                if (mode == SPMV_SET)
+                    k_bspmv<R, G, SPMV_SET><<<blocks, kBThreads, 0, c.stream>>>(M.d, x, y, z, row_sys, pflag, c.d_flags);
+                else if (mode == SPMV_RESID)
+                    k_bspmv<R, G, SPMV_RESID><<<blocks, kBThreads, 0, c.stream>>>(M.d, x, y, z, row_sys, pflag, c.d_flags);
+                else
+                    k_bspmv<R, G, SPMV_ADD><<<blocks, kBThreads, 0, c.stream>>>(M.d, x, y, z, row_sys, pflag, c.d_flags);
+            });
+        });
+        c.launches++;
+    }
+
+    void sweep(int l, const int *in, int *out) {
+        const DevBLevel &L = lv[l];
+        const int nc = (int)L.colour_ptr.size() - 1;
+        for (int k = 0; k < nc; k++) {
+            const int a = L.colour_ptr[k], cnt = L.colour_ptr[k + 1] - a;
+            if (cnt == 0) continue;
+            const long long threads = (long long)cnt * L.LD.group;
+            const int blocks = (int)((threads + kBThreads - 1) / kBThreads);
+            by_r([&](auto RR) {
+                constexpr int R = decltype(RR)::value;
+                by_g(L.LD.group, [&](auto GG) {
+                    constexpr int G = decltype(GG)::value;
+                    k_bcolour<R, G><<<blocks, kBThreads, 0, c.stream>>>(cnt, L.colour_rows + a, L.LD.d, in, out,
+                                                                       L.row_sys, pflag, c.d_flags);
+                });
+            });
+            c.launches++;
+        }
+    }
+
+    void smooth(int l, const int *in, int *out, bool inited) {
+        int k0 = 0;
+        if (!inited) {
+            sweep(l, in, out);
+            k0 = 1;
+        }
+        for (int k = k0; k < smooth_iter; k++) {
+            bspmv(lv[l].U, out, tmp[l], SPMV_RESID, in, lv[l].row_sys);
+            sweep(l, tmp[l], out);
+        }
+    }
+
+    // intAMGflex::Precondition (INTAMG.hpp:269-293) for the whole batch
+    void vcycle(const int *in, int *out) {
+        for (int l = 0; l < Dmax; l++) {
+            const int *e_l = l == 0 ? in : ee[l];
+            int *x_l = l == 0 ? out : xx[l];
+            smooth(l, e_l, x_l, false);
+            bspmv(lv[l].A, x_l, rr[l], SPMV_RESID, e_l, lv[l].row_sys);
+            bspmv(lv[l].R, rr[l], ee[l + 1], SPMV_SET, nullptr, lv[l].row_sys_next);
+        }
+        if (nlu) {
+            by_r([&](auto RR) {
+                constexpr int R = decltype(RR)::value;
+                k_blu<R><<<nlu, kBLuThreads, lu_smem, c.stream>>>(d_lu, Lcat, Ucat, dcat, pflag, c.d_flags);
+            });
+            c.launches++;
+        }
+        for (int l = Dmax - 1; l >= 0; l--) {
+            const int *e_l = l == 0 ? in : ee[l];
+            int *x_l = l == 0 ? out : xx[l];
+            bspmv(lv[l].P, xx[l + 1], x_l, SPMV_ADD, nullptr, lv[l].row_sys);
+            smooth(l, e_l, x_l, true);
+        }
+    }
+
+    // ----------------------------------------------------------- Krylov
+    void ensure_krylov(int mm) {
+        if (mm == m && V) return;
+        free_krylov();
+        m = mm;
+        const size_t P = (size_t)S * Rn;
+        V = (int *)dmalloc(sizeof(int) * N0 * Rn * (m + 1));
+        Z = (int *)dmalloc(sizeof(int) * N0 * Rn * (m + 1));
+        H = (long long *)dmalloc(sizeof(long long) * P * (m + 1) * m);
+        cs = (long long *)dmalloc(sizeof(long long) * P * m);
+        sn = (long long *)dmalloc(sizeof(long long) * P * m);
+        e = (long long *)dmalloc(sizeof(long long) * P * (m + 1));
+        y = (double *)dmalloc(sizeof(double) * P * m);
+        acc = (unsigned long long *)dmalloc(sizeof(unsigned long long) * P * (m + 2));
+        SAGB_CUDA(cudaMemset(H, 0, sizeof(long long) * P * (m + 1) * m));
+        SAGB_CUDA(cudaMemset(V, 0, sizeof(int) * N0 * Rn * (m + 1)));
+        SAGB_CUDA(cudaMemset(Z, 0, sizeof(int) * N0 * Rn * (m + 1)));
+    }
+
+    void pair_norms(const double *v) {
+        by_r([&](auto RR) {
+            constexpr int R = decltype(RR)::value;
+            k_bnorm_part<R><<<ntiles, kBThreads, 0, c.stream>>>(tiles, v, npart);
+        });
+        const int P = S * Rn;
+        k_bnorm_fin<<<(P + 127) / 128, 128, 0, c.stream>>>(S, Rn, tile_ptr, npart, nrm);
+        c.launches += 2;
+    }
+
+    void arnoldi_step(int j) {
+        const int P = S * Rn;
+        const size_t vs = N0 * Rn;
+        int *Vj = V + (size_t)j * vs, *Zj = Z + (size_t)j * vs, *w = V + (size_t)(j + 1) * vs;
+        k_binfo_reset<<<1, 1, 0, c.stream>>>(info_d);
+        vcycle(Vj, Zj);
+        const DevBMat &A0 = lv[0].A;
+        by_r([&](auto RR) {
+            constexpr int R = decltype(RR)::value;
+            by_g(A0.group, [&](auto GG) {
+                constexpr int G = decltype(GG)::value;
+                k_bspmv_dot<R, G><<<ntiles, kBThreads, 0, c.stream>>>(tiles, A0.d, Zj, w, V, pairs, acc, m, pflag,
+                                                                     c.d_flags);
+            });
+            for (int k = 0; k <= j; k++) {
+                if (k < j)
+                    k_bmgs<R, false><<<ntiles, kBThreads, 0, c.stream>>>(tiles, k, j, m, vs, V, w, pairs, acc, H);
+                else
+                    k_bmgs<R, true><<<ntiles, kBThreads, 0, c.stream>>>(tiles, k, j, m, vs, V, w, pairs, acc, H);
+            }
+        });
+        k_bgivens<<<(P + 127) / 128, 128, 0, c.stream>>>(P, j, m, pairs, H, cs, sn, e, acc, pflag, info_d);
+        by_r([&](auto RR) {
+            constexpr int R = decltype(RR)::value;
+            k_bscal<R><<<ntiles, kBThreads, 0, c.stream>>>(tiles, j, pairs, w);
+        });
+        c.launches += j + 5;
+        SAGB_CUDA(cudaMemcpyAsync(info_h, info_d, sizeof(BInfo), cudaMemcpyDeviceToHost, c.stream));
+    }
+
+    void step(int j) {
+        if (!c.use_graphs) {
+            arnoldi_step(j);
+        } else {
+            if ((int)graphs.size() <= j) {
+                graphs.resize(j + 1, nullptr);
+                graph_launches.resize(j + 1, 0);
+            }
+            if (!graphs[j]) {
+                cudaGraph_t g;
+                const long long before = c.launches;
+                SAGB_CUDA(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
+                try {
+                    arnoldi_step(j);
+                } catch (...) {
+                    cudaStreamEndCapture(c.stream, &g);
+                    throw;
+                }
+                SAGB_CUDA(cudaStreamEndCapture(c.stream, &g));
+                SAGB_CUDA(cudaGraphInstantiate(&graphs[j], g, 0));
+                cudaGraphDestroy(g);
+                graph_launches[j] = c.launches - before;
+                c.launches = before;
+            }
+            SAGB_CUDA(cudaGraphLaunch(graphs[j], c.stream));
+            c.launches += graph_launches[j];
+        }
+        SAGB_CUDA(cudaStreamSynchronize(c.stream));
+    }
+
+    void residual(const double *b, const double *x) {
+        const int n = (int)N0;
+        by_r([&](auto RR) {
+            constexpr int R = decltype(RR)::value;
+            k_bresid_f64<R><<<(n + 127) / 128, 128, 0, c.stream>>>(n, Af.rptr, Af.cind, (const double *)Af.val, x, b,
+                                                                  rvec);
+        });
+        c.launches++;
+        pair_norms(rvec);
+    }
+
+    // Restarted::Solve per pair (irsolver.hpp:27-43), all pairs in lockstep
+    void solve(const KrylovParams &kp, const int *bits_sys, const double *b, const double *nrm_b, double *x,
+               BatchStats &st) {
+        const int P = S * Rn;
+        ensure_krylov(kp.m);
+        st = BatchStats();
+        st.iters.assign(P, 0);
+        st.converged.assign(P, 0);
+        st.fallbacks.assign(P, 0);
+        st.final_bit.assign(P, 0);
+        st.explicit_res.assign(P, 0.0);
+        std::vector<BPair> hp(P);
+        std::vector<double> nb(P);
+        SAGB_CUDA(cudaMemcpy(nb.data(), nrm_b, sizeof(double) * P, cudaMemcpyDefault));
+        std::vector<int> bit(P), done(P, 0), discarded(P, 0);
+        std::vector<double> prev(P, 0.0), hn(P);
+        if (kp.m > 64) throw CudaError{"restart length above 64"};
+        for (int p = 0; p < P; p++) bit[p] = bits_sys[p / Rn];
+        SAGB_CUDA(cudaMemsetAsync(pflag, 0, sizeof(unsigned) * P, c.stream));
+        for (int outer = 0; outer < kp.max_outer; outer++) {
+            residual(b, x);
+            SAGB_CUDA(cudaMemcpyAsync(hn.data(), nrm, sizeof(double) * P, cudaMemcpyDeviceToHost, c.stream));
+            SAGB_CUDA(cudaStreamSynchronize(c.stream));
+            int ncycle = 0;
+            for (int p = 0; p < P; p++) {
+                hp[p] = BPair();
+                hp[p].bit = bit[p];
+                hp[p].nrm_b = nb[p];
+                if (done[p]) continue;
+                const double nr = hn[p];
+                st.explicit_res[p] = nr / nb[p];
+                if (kp.explicit_check && outer > 0 && !discarded[p] && nr <= kp.eps * nb[p]) {
+                    done[p] = 1;
+                    st.converged[p] = 1;
+                    continue;
+                }
+                if (!discarded[p] && std::fabs(nr - prev[p]) / nr < 1.0e-8) {  // stagnation (irsolver.hpp:35)
+                    done[p] = 1;
+                    st.iters[p] = 0;
+                    continue;
+                }
+                prev[p] = nr;
+                discarded[p] = 0;
+                hp[p].active = 1;
+                ncycle++;
+            }
+            if (ncycle == 0) break;
+            st.restarts++;
+            // status bits of the previous cycle (including those raised on
+            // the vectors of pairs that had already stopped) are dropped
+            SAGB_CUDA(cudaMemsetAsync(pflag, 0, sizeof(unsigned) * P, c.stream));
+            SAGB_CUDA(cudaMemcpyAsync(pairs, hp.data(), sizeof(BPair) * P, cudaMemcpyHostToDevice, c.stream));
+            SAGB_CUDA(cudaMemcpyAsync(e0, nrm, sizeof(double) * P, cudaMemcpyDeviceToDevice, c.stream));
+            k_bbegin<<<(P + 127) / 128, 128, 0, c.stream>>>(P, e0, kp.eps, pairs, e, acc, m);
+            by_r([&](auto RR) {
+                constexpr int R = decltype(RR)::value;
+                k_bv0<R><<<ntiles, kBThreads, 0, c.stream>>>(tiles, rvec, pairs, V);
+            });
+            c.launches += 2;
+            for (int j = 0; j < m; j++) {
+                step(j);
+                if (info_h->n_active == 0) break;
+            }
+            k_btrsv<<<(P + 127) / 128, 128, 0, c.stream>>>(P, m, pairs, H, e, y);
+            by_r([&](auto RR) {
+                constexpr int R = decltype(RR)::value;
+                k_bxupd<R><<<ntiles, kBThreads, 0, c.stream>>>(tiles, m, N0 * Rn, pairs, y, Z, x);
+            });
+            c.launches += 2;
+            SAGB_CUDA(cudaMemcpyAsync(hp.data(), pairs, sizeof(BPair) * P, cudaMemcpyDeviceToHost, c.stream));
+            SAGB_CUDA(cudaStreamSynchronize(c.stream));
+            for (int p = 0; p < P; p++) {
+                if (done[p] || !(hp[p].jn > 0)) continue;
+                if (hp[p].bad) {
+                    // cycle discarded (x untouched): one fractional bit less
+                    st.flags |= hp[p].bad;
+                    discarded[p] = 1;
+                    if (!kp.fallback || bit[p] <= 1) {
+                        done[p] = 1;
+                        continue;
+                    }
+                    bit[p]--;
+                    st.fallbacks[p]++;
+                    continue;
+                }
+                st.iters[p] += hp[p].jn;
+                if (hp[p].conv && !kp.explicit_check) {
+                    done[p] = 1;
+                    st.converged[p] = 1;
+                }
+            }
+        }
+        // the last cycle's update has not been checked yet
+        residual(b, x);
+        SAGB_CUDA(cudaMemcpyAsync(hn.data(), nrm, sizeof(double) * P, cudaMemcpyDeviceToHost, c.stream));
+        SAGB_CUDA(cudaStreamSynchronize(c.stream));
+        for (int p = 0; p < P; p++) {
+            st.explicit_res[p] = hn[p] / nb[p];
+            st.final_bit[p] = bit[p];
+            if (!done[p] && kp.explicit_check && hn[p] <= kp.eps * nb[p]) st.converged[p] = 1;
+            if (!st.converged[p]) st.iters[p] = 0;
+        }
+    }
+};
+
+BatchEngine::BatchEngine(Ctx &c, std::shared_ptr<BatchHierarchy> h, int nrhs)
+    : impl_(new Impl(c, std::move(h), nrhs)) {}
+BatchEngine::~BatchEngine() { delete impl_; }
+int BatchEngine::nrhs() const { return impl_->Rn; }
+size_t BatchEngine::rows() const { return impl_->N0; }
+void BatchEngine::precondition(const int *in, int *out) { impl_->vcycle(in, out); }
+void BatchEngine::pair_norms(const double *v, double *out_dev) {
+    impl_->pair_norms(v);
+    SAGB_CUDA(cudaMemcpyAsync(out_dev, impl_->nrm, sizeof(double) * (size_t)impl_->S * impl_->Rn,
+                              cudaMemcpyDefault, impl_->c.stream));
+}
+void BatchEngine::solve(const KrylovParams &kp, const int *bits_sys, const double *b, const double *nrm_b, double *x,
+                        BatchStats &st) {
+    impl_->solve(kp, bits_sys, b, nrm_b, x, st);
+}
+void BatchEngine::set_groups(int level, int op, int group) {
+    if (level < 0 || level >= impl_->Dmax) throw CudaError{"no such level"};
+    DevBLevel &L = impl_->lv[level];
+    DevBMat *M = op == 0 ? &L.A : op == 1 ? &L.LD : op == 2 ? &L.U : op == 3 ? &L.P : &L.R;
+    M->group = group;
+    impl_->clear_graphs();
+}
+int BatchEngine::group(int level, int op) const {
+    const DevBLevel &L = impl_->lv[level];
+    const DevBMat *M = op == 0 ? &L.A : op == 1 ? &L.LD : op == 2 ? &L.U : op == 3 ? &L.P : &L.R;
+    return M->group;
+}
+int BatchEngine::depth() const { return impl_->Dmax; }
+
+// Autotuner: for every level operator, time each candidate lanes-per-row
+// value on the current vectors and keep the fastest (the SpMV and the colour
+// sweep have the same results for every value).
+void BatchEngine::autotune(int reps) {
+    Impl &I = *impl_;
+    Ctx &c = I.c;
+    cudaEvent_t e0, e1;
+    SAGB_CUDA(cudaEventCreate(&e0));
+    SAGB_CUDA(cudaEventCreate(&e1));
+    int *xa = (int *)dmalloc(sizeof(int) * I.N0 * I.Rn), *xb = (int *)dmalloc(sizeof(int) * I.N0 * I.Rn);
+    SAGB_CUDA(cudaMemset(xa, 0, sizeof(int) * I.N0 * I.Rn));
+    SAGB_CUDA(cudaMemset(xb, 0, sizeof(int) * I.N0 * I.Rn));
+    const int cand[] = {1, 2, 4, 8, 16, 32};
+    for (int l = 0; l < I.Dmax; l++) {
+        DevBLevel &L = I.lv[l];
+        for (int op = 0; op < 5; op++) {
+            DevBMat *M = op == 0 ? &L.A : op == 1 ? &L.LD : op == 2 ? &L.U : op == 3 ? &L.P : &L.R;
+            if (M->d.n == 0) continue;
+            float best = 1e30f;
+            int bestg = M->group;
+            for (int g : cand) {
+                M->group = g;
+                auto run = [&] {
+                    if (op == 1) I.sweep(l, xa, xb);
+                    else I.bspmv(*M, xa, xb, SPMV_SET, nullptr, L.row_sys);
+                };
+                run();
+                SAGB_CUDA(cudaEventRecord(e0, c.stream));
+                for (int k = 0; k < reps; k++) run();
+                SAGB_CUDA(cudaEventRecord(e1, c.stream));
+                SAGB_CUDA(cudaEventSynchronize(e1));
+                float ms = 0;
+                SAGB_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+                if (ms < best) {
+                    best = ms;
+                    bestg = g;
+                }
+            }
+            M->group = bestg;
+        }
+    }
+    SAGB_CUDA(cudaMemsetAsync(I.pflag, 0, sizeof(unsigned) * (size_t)I.S * I.Rn, c.stream));
+    SAGB_CUDA(cudaMemsetAsync(c.d_flags, 0, sizeof(unsigned), c.stream));
+    SAGB_CUDA(cudaStreamSynchronize(c.stream));
+    dfree(xa);
+    dfree(xb);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    I.clear_graphs();
+}
+
+}  // namespace sagb

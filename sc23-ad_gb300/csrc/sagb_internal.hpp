@@ -8,6 +8,7 @@
 #include <vector>
 
 #include "host/amg_setup.hpp"
+#include "host/batch_setup.hpp"
 #include "host/csr.hpp"
 #include "host/schedule.hpp"
 
@@ -195,5 +196,78 @@ class Solver {
 // FP64 norm of a device vector (deterministic reduction order)
 double nrm2_f64(Ctx &c, const double *x, int n);
 void nrm2_f64_dev(Ctx &c, const double *x, int n, double *d_out);
+
+// ------------------------------------------------------------ batched solver
+struct BatchStats {
+    std::vector<int> iters, converged, fallbacks, final_bit;  // per pair (system * nrhs + rhs)
+    std::vector<double> explicit_res;
+    int restarts = 0;
+    unsigned flags = 0;
+};
+
+// Many systems, nrhs right-hand sides each, solved together (cuda/batch.cu).
+// Vectors are level-0 rows with the right-hand sides interleaved.
+class BatchEngine {
+  public:
+    BatchEngine(Ctx &c, std::shared_ptr<BatchHierarchy> h, int nrhs);
+    ~BatchEngine();
+    int nrhs() const;
+    size_t rows() const;
+    int depth() const;
+    void precondition(const int *in, int *out);  // device pointers
+    void pair_norms(const double *v, double *out);
+    // b, x: device; nrm_b: per pair (host or device); bits_sys: host, per system
+    void solve(const KrylovParams &kp, const int *bits_sys, const double *b, const double *nrm_b, double *x,
+               BatchStats &st);
+    void autotune(int reps);
+    void set_groups(int level, int op, int group);  // op: 0 A, 1 LD, 2 U, 3 P, 4 R
+    int group(int level, int op) const;
+
+  private:
+    struct Impl;
+    Impl *impl_;
+};
+
+// ------------------------------------------------------ learned bit selector
+// 3-layer FP32 MLP (nin -> hid -> hid -> nout, ReLU on the hidden layers),
+// trained with a masked MSE loss and Adam.  Inputs are standardised on the
+// device with (x - mu) / sd.  Host pointers or device pointers are accepted.
+struct Mlp {
+    int nin, hid, nout;
+    float *p = nullptr, *g = nullptr, *m1 = nullptr, *m2 = nullptr;  // params, grads, Adam moments
+    float *norm = nullptr;                                            // mu[nin], sd[nin]
+    float *ws = nullptr;                                              // per-batch activations
+    int ws_batch = 0;
+    float *data = nullptr;  // loaded X, T, M
+    int data_n = 0, loaded_n = 0;
+    int *perm_d = nullptr;
+    long long t = 0;  // Adam step
+    Mlp(int in, int hidden, int out, uint64_t seed);
+    ~Mlp();
+    size_t off_w1() const { return 0; }
+    size_t off_b1() const { return off_w1() + (size_t)hid * nin; }
+    size_t off_w2() const { return off_b1() + hid; }
+    size_t off_b2() const { return off_w2() + (size_t)hid * hid; }
+    size_t off_w3() const { return off_b2() + hid; }
+    size_t off_b3() const { return off_w3() + (size_t)nout * hid; }
+    size_t nparams() const { return off_b3() + nout; }
+    void set_norm(const float *mu, const float *sd);
+    void predict(Ctx &c, const float *X, int n, float *Y);
+    // loss and flat gradient of the whole set as one batch (no update)
+    float gradient(Ctx &c, const float *X, const float *T, const float *M, int n, float *grad);
+    // mini-batch Adam; loss_hist[epoch] = mean batch loss of that epoch
+    void train(Ctx &c, const float *X, const float *T, const float *M, int n, int epochs, int batch, float lr,
+               uint64_t seed, float *loss_hist);
+    void get_params(float *out) const;
+    void set_params(const float *in);
+
+  private:
+    void reserve(int B);
+    void load(Ctx &c, const float *X, const float *T, const float *M, int n);
+    void gather(Ctx &c, const int *perm, int off, int B, bool targets);
+    void forward_batch(Ctx &c, int B);
+    void backward_batch(Ctx &c, int B);
+    float *loss_slot();
+};
 
 }  // namespace sagb

@@ -23,6 +23,7 @@ OPT_FP_EXACT, OPT_GRAPHS = 0, 1
 VP = C.c_void_p
 I32P = C.POINTER(C.c_int32)
 F64P = C.POINTER(C.c_double)
+F32P = C.POINTER(C.c_float)
 
 
 class CsrView(C.Structure):
@@ -102,6 +103,31 @@ SIGNATURES = {
     "sa_solver_bits": (C.c_int, [VP, C.POINTER(C.c_int)]),
     "sa_solver_history": (C.c_int, [VP, F64P, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_uint)]),
     "sa_rule_bits": (C.c_int, [VP, VP, VP, C.c_double, C.POINTER(C.c_int)]),
+    "sa_rule_ratio": (C.c_int, [VP, VP, VP, C.c_double, C.POINTER(C.c_double)]),
+    "sa_setup_features": (C.c_int, [VP, C.c_double, F32P]),
+    "sa_mlp_create": (C.c_int, [VP, C.c_int, C.c_int, C.c_int, C.c_uint64, C.POINTER(VP)]),
+    "sa_mlp_destroy": (C.c_int, [VP]),
+    "sa_mlp_nparams": (C.c_int, [VP, C.POINTER(C.c_int64)]),
+    "sa_mlp_get_params": (C.c_int, [VP, F32P]),
+    "sa_mlp_set_params": (C.c_int, [VP, F32P]),
+    "sa_mlp_set_norm": (C.c_int, [VP, F32P, F32P]),
+    "sa_mlp_predict": (C.c_int, [VP, VP, F32P, C.c_int, F32P]),
+    "sa_mlp_gradient": (C.c_int, [VP, VP, F32P, F32P, F32P, C.c_int, F32P, C.POINTER(C.c_float)]),
+    "sa_mlp_train": (C.c_int, [VP, VP, F32P, F32P, F32P, C.c_int, C.c_int, C.c_int, C.c_float, C.c_uint64,
+                               F32P]),
+    "sa_mlp_select_bits": (C.c_int, [VP, VP, F32P, C.c_int, C.POINTER(C.c_int)]),
+    "sa_batch_create": (C.c_int, [VP, C.c_int, I32P, C.POINTER(I32P), C.POINTER(I32P), C.POINTER(F64P), C.c_int,
+                                  C.POINTER(AmgParams), C.c_int, C.POINTER(VP)]),
+    "sa_batch_destroy": (C.c_int, [VP]),
+    "sa_batch_info": (C.c_int, [VP, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                C.POINTER(C.c_int64)]),
+    "sa_batch_offsets": (C.c_int, [VP, C.POINTER(C.c_int64)]),
+    "sa_batch_system_setup": (C.c_int, [VP, C.c_int, C.POINTER(VP)]),
+    "sa_batch_precondition": (C.c_int, [VP, VP, VP, VP]),
+    "sa_batch_autotune": (C.c_int, [VP, VP, C.c_int]),
+    "sa_batch_group": (C.c_int, [VP, C.c_int, C.c_int, C.POINTER(C.c_int)]),
+    "sa_batch_rule_ratios": (C.c_int, [VP, VP, VP, VP, F64P]),
+    "sa_batch_solve": (C.c_int, [VP, VP, C.POINTER(SolverParams), I32P, VP, VP, VP, I32P, I32P, I32P]),
 }
 
 _lib = None
@@ -512,6 +538,151 @@ class Solver:
         if self.h:
             lib().sa_solver_destroy(self.h)
             self.h = None
+
+
+def rule_ratio(ctx, M64, b, nrm_b):
+    """max|M b| / ||b|| of one FP64 V-cycle (the rule's input, Work/main.cpp:153-161)."""
+    q = C.c_double()
+    check(lib().sa_rule_ratio(ctx.h, M64.h, _arg(b), nrm_b, C.byref(q)))
+    return q.value
+
+
+NUM_FEATURES = 20
+
+
+def setup_features(setup_int, ratio):
+    f = np.zeros(NUM_FEATURES, np.float32)
+    check(lib().sa_setup_features(setup_int.h, ratio, _ptr(f, F32P)))
+    return f
+
+
+class Mlp:
+    """The bit selector's 3-layer FP32 MLP (trained and run by this library's kernels)."""
+
+    def __init__(self, ctx, n_in, hidden, n_out, seed=0):
+        self.ctx, self.n_in, self.n_out = ctx, n_in, n_out
+        self.h = VP()
+        check(lib().sa_mlp_create(ctx.h, n_in, hidden, n_out, seed, C.byref(self.h)))
+
+    @property
+    def nparams(self):
+        n = C.c_int64()
+        check(lib().sa_mlp_nparams(self.h, C.byref(n)))
+        return n.value
+
+    def params(self):
+        p = np.zeros(self.nparams, np.float32)
+        check(lib().sa_mlp_get_params(self.h, _ptr(p, F32P)))
+        return p
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, np.float32)
+        assert p.size == self.nparams
+        check(lib().sa_mlp_set_params(self.h, _ptr(p, F32P)))
+
+    def set_norm(self, mu, sd):
+        mu = np.ascontiguousarray(mu, np.float32)
+        sd = np.ascontiguousarray(sd, np.float32)
+        check(lib().sa_mlp_set_norm(self.h, _ptr(mu, F32P), _ptr(sd, F32P)))
+
+    def predict(self, X):
+        X = np.ascontiguousarray(np.atleast_2d(X), np.float32)
+        Y = np.zeros((X.shape[0], self.n_out), np.float32)
+        check(lib().sa_mlp_predict(self.ctx.h, self.h, _ptr(X, F32P), X.shape[0], _ptr(Y, F32P)))
+        return Y
+
+    def gradient(self, X, T, M):
+        X, T, M = (np.ascontiguousarray(a, np.float32) for a in (X, T, M))
+        g = np.zeros(self.nparams, np.float32)
+        loss = C.c_float()
+        check(lib().sa_mlp_gradient(self.ctx.h, self.h, _ptr(X, F32P), _ptr(T, F32P), _ptr(M, F32P), X.shape[0],
+                                    _ptr(g, F32P), C.byref(loss)))
+        return loss.value, g
+
+    def train(self, X, T, M, epochs, batch, lr, seed=0):
+        X, T, M = (np.ascontiguousarray(a, np.float32) for a in (X, T, M))
+        hist = np.zeros(epochs, np.float32)
+        check(lib().sa_mlp_train(self.ctx.h, self.h, _ptr(X, F32P), _ptr(T, F32P), _ptr(M, F32P), X.shape[0],
+                                 epochs, batch, lr, seed, _ptr(hist, F32P)))
+        return hist
+
+    def select_bits(self, feat, f_lo):
+        f = np.ascontiguousarray(feat, np.float32)
+        b = C.c_int()
+        check(lib().sa_mlp_select_bits(self.ctx.h, self.h, _ptr(f, F32P), f_lo, C.byref(b)))
+        return b.value
+
+    def close(self):
+        if self.h:
+            lib().sa_mlp_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+
+class Batch:
+    """Many systems (already scaled), nrhs right-hand sides each, solved together."""
+
+    def __init__(self, ctx, systems, nrhs=1, params=None, threads=0):
+        self.ctx = ctx
+        S = len(systems)
+        self._keep = [(np.ascontiguousarray(r, np.int32), np.ascontiguousarray(c, np.int32),
+                       np.ascontiguousarray(v, np.float64)) for r, c, v in systems]
+        n = np.array([len(r) - 1 for r, _, _ in self._keep], np.int32)
+        rp = (I32P * S)(*[_ptr(r, I32P) for r, _, _ in self._keep])
+        cp = (I32P * S)(*[_ptr(c, I32P) for _, c, _ in self._keep])
+        vp = (F64P * S)(*[_ptr(v, F64P) for _, _, v in self._keep])
+        p = params or amg_params()
+        self.h = VP()
+        check(lib().sa_batch_create(ctx.h, S, _ptr(n, I32P), rp, cp, vp, nrhs, C.byref(p), threads,
+                                    C.byref(self.h)))
+        self._keep = None
+        ns, nr, d, rows = C.c_int(), C.c_int(), C.c_int(), C.c_int64()
+        check(lib().sa_batch_info(self.h, C.byref(ns), C.byref(nr), C.byref(d), C.byref(rows)))
+        self.nsys, self.nrhs, self.depth, self.rows = ns.value, nr.value, d.value, rows.value
+        off = np.zeros(self.nsys + 1, np.int64)
+        check(lib().sa_batch_offsets(self.h, _ptr(off, C.POINTER(C.c_int64))))
+        self.offsets = off
+
+    def system_setup(self, s):
+        h = VP()
+        check(lib().sa_batch_system_setup(self.h, s, C.byref(h)))
+        return Setup(INT, _handle=h)
+
+    def precondition(self, x, out=None):
+        out = np.zeros(self.rows * self.nrhs, np.int32) if out is None else out
+        check(lib().sa_batch_precondition(self.ctx.h, self.h, _arg(x), _arg(out)))
+        return out
+
+    def autotune(self, reps=3):
+        check(lib().sa_batch_autotune(self.ctx.h, self.h, reps))
+
+    def group(self, level, op):
+        g = C.c_int()
+        check(lib().sa_batch_group(self.h, level, op, C.byref(g)))
+        return g.value
+
+    def rule_ratios(self, b, nrm_b):
+        q = np.zeros(self.nsys * self.nrhs)
+        check(lib().sa_batch_rule_ratios(self.ctx.h, self.h, _arg(b), _arg(np.ascontiguousarray(nrm_b, np.float64)),
+                                         _ptr(q, F64P)))
+        return q
+
+    def solve(self, params, bits, b, nrm_b, x):
+        P = self.nsys * self.nrhs
+        bits = np.ascontiguousarray(bits, np.int32)
+        it, cv, fb = np.zeros(P, np.int32), np.zeros(P, np.int32), np.zeros(P, np.int32)
+        check(lib().sa_batch_solve(self.ctx.h, self.h, C.byref(params), _ptr(bits, I32P), _arg(b),
+                                   _arg(np.ascontiguousarray(nrm_b, np.float64)), _arg(x), _ptr(it, I32P),
+                                   _ptr(cv, I32P), _ptr(fb, I32P)))
+        return it, cv, fb
+
+    def close(self):
+        if self.h:
+            lib().sa_batch_destroy(self.h)
+            self.h = None
+
+    __del__ = close
 
 
 def rule_bits(ctx, M64, b, nrm_b):

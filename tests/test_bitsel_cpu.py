@@ -1,0 +1,90 @@
+"""Learned bit selector on the host: the MLP oracle and the matrix features.
+
+The oracle (oracle/mlp_oracle.py) is pinned by central finite differences in
+float64, since the reference has no learned component to compare with.  The
+features are host computations over the integer setup."""
+import numpy as np
+import pytest
+
+import mlp_oracle as mo
+import sagb
+
+
+def _toy(n=37, nin=20, hid=64, nout=21, seed=1):
+    rng = np.random.default_rng(seed)
+    X = rng.standard_normal((n, nin))
+    T = rng.standard_normal((n, nout))
+    M = (rng.random((n, nout)) > 0.2).astype(np.float64)
+    p = mo.init_params(nin, hid, nout, seed) + 0.01 * rng.standard_normal(
+        sum(int(np.prod(s)) for _, s in mo.shapes(nin, hid, nout)))
+    return X, T, M, p
+
+
+def test_oracle_gradient_matches_finite_differences():
+    nin, hid, nout = 6, 8, 5
+    X, T, M, p = _toy(n=11, nin=nin, hid=hid, nout=nout)
+    loss, g = mo.loss_grad(p, X, T, M, nin, hid, nout)
+    rng = np.random.default_rng(0)
+    h = 1e-6
+    for i in rng.choice(p.size, 60, replace=False):
+        e = np.zeros_like(p)
+        e[i] = h
+        lp, _ = mo.loss_grad(p + e, X, T, M, nin, hid, nout)
+        lm, _ = mo.loss_grad(p - e, X, T, M, nin, hid, nout)
+        assert abs((lp - lm) / (2 * h) - g[i]) <= 1e-6 * max(1.0, abs(g[i])), i
+
+
+def test_oracle_normalisation_and_mask():
+    nin, hid, nout = 4, 8, 3
+    X, T, M, p = _toy(n=9, nin=nin, hid=hid, nout=nout)
+    mu, sd = X.mean(0), X.std(0) + 0.5
+    y1, _ = mo.forward(p, X, nin, hid, nout, mu, sd)
+    y2, _ = mo.forward(p, (X - mu) / sd, nin, hid, nout)
+    np.testing.assert_allclose(y1, y2, rtol=1e-12)
+    # a masked-out target does not change the loss or the gradient
+    T2 = T.copy()
+    T2[M == 0] += 100.0
+    l1, g1 = mo.loss_grad(p, X, T, M, nin, hid, nout)
+    l2, g2 = mo.loss_grad(p, X, T2, M, nin, hid, nout)
+    assert l1 == pytest.approx(l2, rel=1e-12)
+    np.testing.assert_allclose(g1, g2, rtol=1e-12, atol=1e-15)
+
+
+def test_oracle_training_reduces_loss():
+    nin, hid, nout = 5, 16, 4
+    rng = np.random.default_rng(2)
+    X = rng.standard_normal((64, nin))
+    W = rng.standard_normal((nout, nin))
+    T = np.tanh(X @ W.T)
+    M = np.ones_like(T)
+    p0 = mo.init_params(nin, hid, nout, 7)
+    p, hist = mo.train(p0, X, T, M, nin, hid, nout, epochs=30, batch=16, lr=3e-3, seed=5)
+    assert hist[-1] < 0.3 * hist[0]
+
+
+def test_features_of_a_setup():
+    A = sagb.HostCsr.generate(sagb.GEN_POISSON3D, 14)
+    xs, b = A.rhs(1)
+    A.lmax1_scaling(b)
+    r, c, v = A.arrays()
+    s = sagb.Setup(sagb.INT, r, c, v)
+    for ratio in (0.5, 3.7, 1000.0):
+        f = sagb.setup_features(s, ratio)
+        assert f.shape == (sagb.NUM_FEATURES,) and np.isfinite(f).all()
+        assert f[0] == pytest.approx(np.log2(len(r) - 1))
+        assert f[1] == pytest.approx(c.size / (len(r) - 1), rel=1e-6)
+        assert f[3] == s.depth
+        q = ratio
+        rule = 29 if q < 1 else 31 - (int(np.ceil(np.log2(int(q) + 1))) + 1)
+        assert f[7] == rule
+        assert f[10] == pytest.approx(0.0, abs=1e-7)  # symmetric operator
+    # convection makes the operator nonsymmetric
+    B = sagb.HostCsr.generate(sagb.GEN_CONVDIFF3D, 10, 50.0)
+    xs, b = B.rhs(1)
+    B.lmax1_scaling(b)
+    rb, cb, vb = B.arrays()
+    f = sagb.setup_features(sagb.Setup(sagb.INT, rb, cb, vb), 1.0)
+    assert f[10] > 0.01
+    # a floating-point setup has no integer operators to describe
+    with pytest.raises(sagb.SagbError):
+        sagb.setup_features(sagb.Setup(sagb.F64, r, c, v), 1.0)

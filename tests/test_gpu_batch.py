@@ -1,0 +1,136 @@
+"""GPU parity of the batched solver: many systems of uneven size, several
+right-hand sides each, one launch per operation.
+
+Per system and right-hand side the batch must compute what the system's own
+multicolour hierarchy computes: the batched V-cycle is compared bit for bit
+with the C oracle's V-cycle on each system (colour-ordered sweeps), and with
+the single-system GPU path; whole solves are compared by convergence, explicit
+residual and iteration count with the single-system solver."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import oracle_ffi as of
+import sagb
+import setup_views as sv
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    c = sagb.Context(0)
+    yield c
+    c.close()
+
+
+SYSTEMS = [(sagb.GEN_POISSON3D, 12, 0.0), (sagb.GEN_STENCIL27, 10, 0.0), (sagb.GEN_CONVDIFF3D, 14, 20.0),
+           (sagb.GEN_POISSON2D, 40, 0.0), (sagb.GEN_POISSON3D, 17, 0.0), (sagb.GEN_VARCOEF3D, 13, 1.0)]
+
+
+def _systems(specs, nrhs, seed=1):
+    out, bs = [], []
+    for k, (kind, n, prm) in enumerate(specs):
+        A = sagb.HostCsr.generate(kind, n, prm, seed=k + 1)
+        cols = []
+        for r in range(nrhs):
+            xs, b = A.rhs(seed + 100 * k + r)
+            cols.append(b)
+        B = np.stack(cols, 1)
+        # LMax1Scaling scales A and one b; the other columns by the same row maxima
+        r0, c0, v0 = A.arrays()
+        rows = np.repeat(np.arange(len(r0) - 1), np.diff(r0))
+        rmax = np.zeros(len(r0) - 1)
+        np.maximum.at(rmax, rows, np.abs(v0))
+        b0 = B[:, 0].copy()
+        A.lmax1_scaling(b0)
+        out.append(A.arrays())
+        bs.append(B / rmax[:, None])
+    return out, bs
+
+
+def _interleave(batch, cols):
+    v = np.zeros((batch.rows, batch.nrhs), cols[0].dtype)
+    for s, c in enumerate(cols):
+        v[batch.offsets[s]:batch.offsets[s + 1]] = c
+    return v.ravel()
+
+
+@pytest.mark.parametrize("nrhs", [1, 2, 4])
+def test_batched_vcycle_bit_exact(ctx, nrhs):
+    systems, _ = _systems(SYSTEMS, nrhs)
+    B = sagb.Batch(ctx, systems, nrhs)
+    assert B.nsys == len(SYSTEMS) and B.offsets[-1] == B.rows
+    rng = np.random.default_rng(nrhs)
+    vin = rng.integers(-(1 << 28), 1 << 28, size=B.rows * nrhs).astype(np.int32)
+    out = B.precondition(vin).reshape(B.rows, nrhs)
+    vin2 = vin.reshape(B.rows, nrhs)
+    for s in range(B.nsys):
+        setup = B.system_setup(s)
+        keep = of.Keep()
+        h = sv.oracle_amg(keep, setup)
+        M = sagb.Amg(ctx, sagb.INT, setup=setup)
+        a, b = B.offsets[s], B.offsets[s + 1]
+        for r in range(nrhs):
+            x = np.ascontiguousarray(vin2[a:b, r])
+            ref = np.zeros_like(x)
+            of.lib().or_vcycle_i32(C.byref(h), of.ptr(x, of.i32p), of.ptr(ref, of.i32p))
+            np.testing.assert_array_equal(out[a:b, r], ref, err_msg=f"system {s} rhs {r}")
+            np.testing.assert_array_equal(M.precondition(x), ref)
+        M.close()
+    # the autotuner changes launch shapes only, never results
+    B.autotune(2)
+    np.testing.assert_array_equal(B.precondition(vin).reshape(B.rows, nrhs), out)
+    B.close()
+
+
+def test_batched_solve_matches_single_system(ctx):
+    nrhs = 2
+    systems, bs = _systems(SYSTEMS, nrhs)
+    B = sagb.Batch(ctx, systems, nrhs)
+    b = _interleave(B, bs)
+    nrm_b = np.array([np.linalg.norm(bs[s][:, r]) for s in range(B.nsys) for r in range(nrhs)])
+    ratios = B.rule_ratios(b, nrm_b)
+    bits = []
+    for s in range(B.nsys):
+        q = ratios[s * nrhs]
+        bits.append(29 if q < 1 else 31 - (int(np.ceil(np.log2(int(q) + 1))) + 1))
+    params = sagb.solver_params(m=20, explicit_stop=1)
+    x = np.zeros(B.rows * nrhs)
+    it, cv, fb = B.solve(params, bits, b, nrm_b, x)
+    X = x.reshape(B.rows, nrhs)
+    for s, (r, c, v) in enumerate(systems):
+        rows = np.repeat(np.arange(len(r) - 1), np.diff(r))
+        a, e = B.offsets[s], B.offsets[s + 1]
+        setup = B.system_setup(s)
+        M = sagb.Amg(ctx, sagb.INT, setup=setup)
+        dA = sagb.Matrix(ctx, sagb.MAT_F64, r, c, v)
+        iA = sagb.Matrix(ctx, sagb.MAT_FIXED, r, c, v, bit=30)
+        S1 = sagb.Solver(ctx, sagb.INT, dA, iA, M, sagb.solver_params(m=20, frac_bits=bits[s], explicit_stop=1))
+        for q in range(nrhs):
+            p = s * nrhs + q
+            xs = X[a:e, q]
+            res = np.linalg.norm(bs[s][:, q] - np.bincount(rows, weights=v * xs[c], minlength=len(r) - 1))
+            assert cv[p] == 1 and res / nrm_b[p] <= 1e-10, (s, q, it[p], res / nrm_b[p])
+            x1 = np.zeros(len(r) - 1)
+            it1, cv1 = S1.solve(np.ascontiguousarray(bs[s][:, q]), float(nrm_b[p]), x1)
+            assert cv1 == 1 and abs(int(it[p]) - it1) <= 2, (s, q, it[p], it1)
+        S1.close(); M.close()
+    B.close()
+
+
+def test_batched_overflow_falls_back_per_pair(ctx):
+    """A pair whose fractional bits overflow is redone with fewer bits while the
+    other systems of the batch are not disturbed."""
+    specs = [(sagb.GEN_POISSON3D, 12, 0.0), (sagb.GEN_ANISO2D, 64, 1e-3)]
+    systems, bs = _systems(specs, 1)
+    B = sagb.Batch(ctx, systems, 1)
+    b = _interleave(B, bs)
+    nrm_b = np.array([np.linalg.norm(x[:, 0]) for x in bs])
+    params = sagb.solver_params(m=20, explicit_stop=1)
+    x = np.zeros(B.rows)
+    it, cv, fb = B.solve(params, [29, 30], b, nrm_b, x)
+    assert cv.all(), (it, cv, fb)
+    assert fb[0] == 29 and fb[1] < 30
+    B.close()
