@@ -44,6 +44,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-multicolor", action="store_true", help="skip the multicolour-smoother row")
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched-engine rows")
     ap.add_argument("--profile", action="store_true", help="skip extras (for profilers)")
     return ap.parse_args()
 
@@ -249,7 +250,72 @@ def run_ours(a, dist):
     # ---- the multicolour smoother variant (same solver, colour-ordered GS)
     if not a.no_multicolor:
         out["multicolor"] = multicolor_row(ctx, a, r, c, v, b, nrm_b, dA, A0, db, dx, N)
+    # ---- the batched engine on the same system (1 and 4 right-hand sides)
+    if not a.no_batched:
+        out["batched"] = batched_rows(ctx, a, r, c, v, b, nrm_b, dist)
     return sec, out, ctx, (s_int, r, c, v, b, bits)
+
+
+def batched_rows(ctx, a, r, c, v, b, nrm_b, dist):
+    """The batched engine (multicolour colour-pass sweeps, graph-captured
+    Arnoldi steps, autotuned lanes per row) on the same 128^3 system: one
+    right-hand side, and four right-hand sides solved together."""
+    import sagb
+    N = len(b)
+    rows = {}
+    for nrhs in (1, 4):
+        t0 = time.time()
+        B = sagb.Batch(ctx, [(r, c, v)], nrhs)
+        t_setup = time.time() - t0
+        t0 = time.time()
+        B.autotune(2)
+        t_tune = time.time() - t0
+        cols = [b] + [build_system(a.n, seed=1 + dist.rank + 1000 * k)[3] for k in range(1, nrhs)]
+        bb = np.stack(cols, 1).ravel()
+        nb = np.array([np.linalg.norm(col) for col in cols])
+        q = B.rule_ratios(bb, nb)
+        bits = [29 if q[0] < 1 else 31 - (int(np.ceil(np.log2(int(q[0]) + 1))) + 1)]
+        params = sagb.solver_params(m=a.m, explicit_stop=1)
+        db = sagb.DeviceArray.from_host(ctx, bb)
+        dx = sagb.DeviceArray(ctx, N * nrhs, np.float64)
+        zeros = sagb.DeviceArray.from_host(ctx, np.zeros(N * nrhs))
+
+        def one():
+            sagb.check(sagb.lib().sa_memcpy(ctx.h, dx.ptr, zeros.ptr, 8 * N * nrhs))
+            return B.solve(params, bits, db, nb, dx)
+
+        one()
+        e0, e1 = sagb.Event(), sagb.Event()
+        reps = 3
+        ctx.sync()
+        l0 = ctx.launches()
+        e0.record(ctx)
+        for _ in range(reps):
+            it, cv, fb = one()
+        e1.record(ctx)
+        ctx.sync()
+        sec = e0.elapsed_ms(e1) / 1000.0 / reps
+        X = dx.download().reshape(N, nrhs)
+        res = [explicit_res(r, c, v, cols[k], np.ascontiguousarray(X[:, k])) for k in range(nrhs)]
+        vin = sagb.DeviceArray.from_host(ctx, np.random.default_rng(3).integers(
+            -(1 << 28), 1 << 28, size=N * nrhs).astype(np.int32))
+        vout = sagb.DeviceArray(ctx, N * nrhs, np.int32)
+        B.precondition(vin, vout)
+        ctx.sync()
+        e0.record(ctx)
+        for _ in range(5):
+            B.precondition(vin, vout)
+        e1.record(ctx)
+        ctx.sync()
+        rows[f"nrhs{nrhs}"] = {"value": sec, "per_rhs": sec / nrhs, "iters": [int(i) for i in it],
+                               "converged": bool(cv.all()), "explicit_res": max(res), "frac_bits": bits[0],
+                               "final_bits": [int(f) for f in fb], "vcycle_ms": e0.elapsed_ms(e1) / 5,
+                               "setup_s": t_setup, "autotune_s": t_tune,
+                               "launches_per_solve": (ctx.launches() - l0) // reps}
+        for arr in (db, dx, zeros, vin, vout):
+            arr.close()
+        B.close()
+    return rows
 
 
 def multicolor_row(ctx, a, r, c, v, b, nrm_b, dA, A0, db, dx, N):
@@ -436,6 +502,8 @@ def main_ours(a):
         line["sweep_levels"] = [(p["level"], p["n"], p["levels"], round(p["ms"], 4)) for p in sw["per_level"]]
     if "multicolor" in out:
         line["multicolor"] = out["multicolor"]
+    if "batched" in out:
+        line["batched"] = out["batched"]
     if "fp64_gpu_s" in out:
         line["fp64_gpu"] = {"value": out["fp64_gpu_s"], "iters": out["fp64_gpu_iters"],
                             "explicit_res": out["fp64_gpu_res"]}

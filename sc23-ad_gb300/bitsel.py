@@ -1,0 +1,235 @@
+"""Learned fractional-bit selector for int-AMG-FGMRES.
+
+The reference chooses F_G with a fixed rule (Work/main.cpp:153-161) or by a
+manual sweep (Work/sub.cpp, Work/run_sub.sh).  Here the integer solver itself
+runs the sweep on synthetic matrices (F = 8..29), a 3-layer 64-wide FP32 MLP
+(trained by the library's own CUDA kernels, sagb.Mlp) learns the log2
+iteration count of every F from matrix features (sagb.setup_features), and
+the selector takes the F with the smallest prediction.  A solve with the
+selected F that overflows, or does not converge, is redone with the rule's F.
+
+Training mixture: 5-point 2D (anisotropy 1e-4..1), 7-point 3D Poisson,
+27-point, lognormal-coefficient diffusion (sigma 0..3) and upwinded
+convection-diffusion (Peclet 0..100); cube sides from a range.
+"""
+import json
+import os
+import time
+
+import numpy as np
+
+import sagb
+
+F_LO, F_HI = 8, 29  # the config's 8..28 plus 29, the top value of the rule
+N_OUT = F_HI - F_LO + 1
+PENALTY = float(np.log2(2000.0))  # target of a sweep point that did not converge
+HERE = os.path.dirname(os.path.abspath(__file__))
+DATA = os.path.join(HERE, "data")
+WEIGHTS = os.path.join(DATA, "bitsel_mlp.npz")
+DATASET = os.path.join(DATA, "bitsel_dataset.npz")
+
+
+def rule_of(ratio):
+    """Work/main.cpp:160."""
+    return 29 if ratio < 1 else 31 - (int(np.ceil(np.log2(int(ratio) + 1))) + 1)
+
+
+def training_specs(count, seed, side=(24, 48)):
+    """(kind, nx, param, seed) of `count` matrices from the training mixture."""
+    rng = np.random.default_rng(seed)
+    specs = []
+    for k in range(count):
+        fam = int(rng.integers(0, 5))
+        s3 = int(rng.integers(side[0], side[1] + 1))
+        if fam == 0:    # 5-point 2D, anisotropy 1e-4..1 (side^1.5 rows ~ a 3D cube's)
+            n2 = int(round(s3 ** 1.5))
+            specs.append((sagb.GEN_ANISO2D, n2, float(10 ** rng.uniform(-4, 0)), k + 1))
+        elif fam == 1:  # 7-point 3D Poisson
+            specs.append((sagb.GEN_POISSON3D, s3, 0.0, k + 1))
+        elif fam == 2:  # 27-point
+            specs.append((sagb.GEN_STENCIL27, s3, 0.0, k + 1))
+        elif fam == 3:  # lognormal coefficients
+            specs.append((sagb.GEN_VARCOEF3D, s3, float(rng.uniform(0, 3)), k + 1))
+        else:           # upwinded convection-diffusion
+            specs.append((sagb.GEN_CONVDIFF3D, s3, float(rng.uniform(0, 100)), k + 1))
+    return specs
+
+
+def make_system(spec):
+    kind, nx, prm, sd = spec
+    A = sagb.HostCsr.generate(kind, nx, prm, seed=sd)
+    xs, b = A.rhs(sd)
+    A.lmax1_scaling(b)
+    r, c, v = A.arrays()
+    return r, c, v, b
+
+
+class Prepared:
+    """Setup, GPU operators, rule ratio and features of one system."""
+
+    def __init__(self, ctx, r, c, v, b, multicolor=1):
+        self.r, self.c, self.v, self.b = r, c, v, b
+        self.nrm_b = float(np.linalg.norm(b))
+        t0 = time.time()
+        self.s_int = sagb.Setup(sagb.INT, r, c, v, sagb.amg_params(multicolor=multicolor))
+        s64 = self.s_int.derive(sagb.F64)
+        self.setup_s = time.time() - t0
+        self.M = sagb.Amg(ctx, sagb.INT, setup=self.s_int)
+        M64 = sagb.Amg(ctx, sagb.F64, setup=s64)
+        self.dA = sagb.Matrix(ctx, sagb.MAT_F64, r, c, v)
+        self.iA = sagb.Matrix(ctx, sagb.MAT_FIXED, r, c, v, bit=30)
+        self.ratio = sagb.rule_ratio(ctx, M64, b, self.nrm_b)
+        self.rule = rule_of(self.ratio)
+        self.features = sagb.setup_features(self.s_int, self.ratio)
+        M64.close()
+        self.ctx = ctx
+
+    def solve(self, bit, m=30, max_outer=33, fallback=0):
+        """One solve at F = bit: (iterations, converged, explicit residual, seconds, flags)."""
+        ctx = self.ctx
+        p = sagb.solver_params(m=m, frac_bits=bit, explicit_stop=1, overflow_fallback=fallback,
+                               max_outer=max_outer)
+        S = sagb.Solver(ctx, sagb.INT, self.dA, self.iA, self.M, p)
+        x = sagb.DeviceArray.from_host(ctx, np.zeros(len(self.b)))
+        db = sagb.DeviceArray.from_host(ctx, self.b)
+        e0, e1 = sagb.Event(), sagb.Event()
+        ctx.flags(clear=True)
+        e0.record(ctx)
+        it, conv = S.solve(db, self.nrm_b, x)
+        e1.record(ctx)
+        ctx.sync()
+        sec = e0.elapsed_ms(e1) / 1000.0
+        _, flags = S.history()
+        xs = x.download()
+        rows = np.repeat(np.arange(len(self.r) - 1), np.diff(self.r))
+        res = float(np.linalg.norm(self.b - np.bincount(rows, weights=self.v * xs[self.c], minlength=len(self.b)))
+                    / self.nrm_b)
+        S.close()
+        x.close()
+        db.close()
+        return int(it), int(conv), res, sec, int(flags)
+
+    def close(self):
+        for o in (self.M, self.dA, self.iA):
+            o.close()
+
+
+def sweep(ctx, prep, bits=range(F_LO, F_HI + 1), m=30, max_outer=4):
+    """Iterations of the integer solver for every F (no overflow fallback, so an
+    overflowing F counts as a failure)."""
+    out = []
+    for f in bits:
+        it, conv, res, sec, flags = prep.solve(f, m=m, max_outer=max_outer, fallback=0)
+        out.append({"bit": f, "iters": it, "converged": int(conv and res <= 1e-10), "res": res, "seconds": sec,
+                    "flags": flags})
+    return out
+
+
+def targets(rows):
+    T = np.full(N_OUT, PENALTY, np.float32)
+    for q in rows:
+        if q["converged"] and q["iters"] > 0:
+            T[q["bit"] - F_LO] = np.log2(q["iters"])
+    return T
+
+
+def build_dataset(ctx, specs, chunk=16, m=30, max_outer=4, log=None):
+    """Sweep every F of every matrix with the batched solver: the copies of one
+    matrix (one per F) share one setup, and `chunk` matrices run together.
+    A point counts as converged when the explicit residual reaches 1e-10 within
+    max_outer restarts without overflow (no fallback)."""
+    bits = list(range(F_LO, F_HI + 1))
+    nb = len(bits)
+    X, T, meta = [], [], []
+    for k0 in range(0, len(specs), chunk):
+        t0 = time.time()
+        part = specs[k0:k0 + chunk]
+        mats = [make_system(sp) for sp in part]
+        systems = []
+        for r, c, v, b in mats:
+            systems += [(r, c, v)] * nb
+        B = sagb.Batch(ctx, systems, 1)
+        t_setup = time.time() - t0
+        feats, rules, ratios = [], [], []
+        for i, (r, c, v, b) in enumerate(mats):
+            s_int = B.system_setup(i * nb)
+            M64 = sagb.Amg(ctx, sagb.F64, setup=s_int.derive(sagb.F64))
+            q = sagb.rule_ratio(ctx, M64, b, float(np.linalg.norm(b)))
+            M64.close()
+            feats.append(sagb.setup_features(s_int, q))
+            ratios.append(q)
+            rules.append(rule_of(q))
+        bvec = np.concatenate([np.tile(b, 1) for r, c, v, b in mats for _ in range(nb)])
+        nrm_b = np.array([np.linalg.norm(b) for r, c, v, b in mats for _ in range(nb)])
+        x = np.zeros(B.rows)
+        p = sagb.solver_params(m=m, max_outer=max_outer, explicit_stop=1, overflow_fallback=0)
+        t1 = time.time()
+        it, cv, fb = B.solve(p, bits * len(mats), bvec, nrm_b, x)
+        t_solve = time.time() - t1
+        for i, (r, c, v, b) in enumerate(mats):
+            rows_i = np.repeat(np.arange(len(r) - 1), np.diff(r))
+            out = []
+            for j, f in enumerate(bits):
+                s = i * nb + j
+                xs = x[B.offsets[s]:B.offsets[s + 1]]
+                res = float(np.linalg.norm(b - np.bincount(rows_i, weights=v * xs[c], minlength=len(b)))
+                            / np.linalg.norm(b))
+                out.append({"bit": f, "iters": int(it[s]), "converged": int(cv[s] and res <= 1e-10), "res": res})
+            X.append(feats[i])
+            T.append(targets(out))
+            meta.append({"spec": [int(part[i][0]), int(part[i][1]), float(part[i][2]), int(part[i][3])],
+                         "rule": rules[i], "ratio": ratios[i], "rows": len(r) - 1, "sweep": out})
+            if log:
+                best = min(out, key=lambda q: (not q["converged"], q["iters"]))
+                rule_pt = next((q for q in out if q["bit"] == rules[i]), None)
+                log(f"[{k0 + i + 1}/{len(specs)}] spec={part[i]} rule={rules[i]} "
+                    f"({rule_pt['iters'] if rule_pt else '-'} it) best={best['bit']} ({best['iters']} it)")
+        B.close()
+        if log:
+            log(f"  chunk setup {t_setup:.1f}s solve {t_solve:.1f}s")
+    return np.array(X, np.float32), np.array(T, np.float32), meta
+
+
+def train(ctx, X, T, epochs=400, batch=64, lr=2e-3, seed=1, hidden=64):
+    M = np.ones_like(T)
+    mu = X.mean(0)
+    sd = X.std(0)
+    sd[sd < 1e-6] = 1.0
+    net = sagb.Mlp(ctx, X.shape[1], hidden, T.shape[1], seed=seed)
+    net.set_norm(mu, sd)
+    hist = net.train(X, T, M, epochs=epochs, batch=batch, lr=lr, seed=seed)
+    return net, mu, sd, hist
+
+
+def save(path, net, mu, sd, info=None):
+    os.makedirs(os.path.dirname(path), exist_ok=True)
+    np.savez(path, params=net.params(), mu=mu, sd=sd, n_in=net.n_in, n_out=net.n_out, hidden=64,
+             f_lo=F_LO, info=json.dumps(info or {}))
+
+
+def load(ctx, path=WEIGHTS):
+    z = np.load(path)
+    net = sagb.Mlp(ctx, int(z["n_in"]), int(z["hidden"]), int(z["n_out"]))
+    net.set_params(z["params"])
+    net.set_norm(z["mu"], z["sd"])
+    return net, int(z["f_lo"])
+
+
+class Selector:
+    """Learned F with the rule as fallback."""
+
+    def __init__(self, ctx, path=WEIGHTS):
+        self.net, self.f_lo = load(ctx, path)
+
+    def choose(self, features):
+        return self.net.select_bits(features, self.f_lo)
+
+    def solve(self, prep, m=30):
+        """Solve with the learned F; on overflow or failure, with the rule's F.
+        Returns (bit used, iterations, converged, residual, seconds, fell_back)."""
+        f = self.choose(prep.features)
+        it, conv, res, sec, flags = prep.solve(f, m=m, fallback=0)
+        if conv and res <= 1e-10:
+            return f, it, conv, res, sec, False
+        it2, conv2, res2, sec2, _ = prep.solve(prep.rule, m=m, fallback=1)
+        return prep.rule, it + it2, conv2, res2, sec + sec2, True

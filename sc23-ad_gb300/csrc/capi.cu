@@ -1075,8 +1075,20 @@ extern "C" int sa_batch_create(sa_ctx ctx, int nsys, const int *n, const int32_t
         return fail(SA_ERR_ARG, "invalid AMG parameters (the batch uses the multicolour SOR smoother)");
     q.multicolor = 1;
     SA_GUARD_BEGIN
+    // systems passed with the same arrays share one setup
     std::vector<CsrD> sys(nsys);
+    std::vector<int> src(nsys);
     for (int s = 0; s < nsys; s++) {
+        src[s] = s;
+        for (int t = 0; t < s; t++)
+            if (src[t] == t && n[t] == n[s] && rptr[t] == rptr[s] && cind[t] == cind[s] && val[t] == val[s]) {
+                src[s] = t;
+                break;
+            }
+        if (src[s] != s) {
+            sys[s].n = sys[s].m = n[s];
+            continue;
+        }
         sys[s].n = sys[s].m = n[s];
         sys[s].rptr.assign(rptr[s], rptr[s] + n[s] + 1);
         sys[s].cind.assign(cind[s], cind[s] + rptr[s][n[s]]);
@@ -1088,7 +1100,7 @@ extern "C" int sa_batch_create(sa_ctx ctx, int nsys, const int *n, const int32_t
     B->p = q;
     try {
         B->h = std::make_shared<BatchHierarchy>(
-            build_batch(sys, q.theta, q.max_levels, q.omega, q.smooth_iter, threads));
+            build_batch(sys, q.theta, q.max_levels, q.omega, q.smooth_iter, threads, src));
         SAGB_CUDA(cudaSetDevice(ctx->c.device));
         B->eng = std::make_unique<BatchEngine>(ctx->c, B->h, nrhs);
         SAGB_CUDA(cudaDeviceSynchronize());

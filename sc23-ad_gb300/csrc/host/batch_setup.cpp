@@ -29,10 +29,16 @@ static void start(BatchCsr &B, int m) {
 static int level_size(const IntHierarchy &h, int l) { return l == 0 ? h.A0.n : h.R[l - 1].n; }
 
 BatchHierarchy build_batch(const std::vector<CsrD> &systems, double theta, int max_levels, double omega,
-                           int smooth_iter, int threads) {
+                           int smooth_iter, int threads, const std::vector<int> &src_in) {
     BatchHierarchy B;
     const int S = (int)systems.size();
     if (S == 0) throw SetupError{"empty batch"};
+    std::vector<int> src(S);
+    for (int s = 0; s < S; s++) {
+        src[s] = src_in.empty() ? s : src_in[s];
+        if (src[s] < 0 || src[s] > s || (src[s] != s && src[src[s]] != src[s]))
+            throw SetupError{"invalid repeated-system index"};
+    }
     B.S = S;
     B.chain.resize(S);
     B.hi.resize(S);
@@ -51,6 +57,7 @@ BatchHierarchy build_batch(const std::vector<CsrD> &systems, double theta, int m
         for (;;) {
             const int s = next.fetch_add(1);
             if (s >= S) return;
+            if (src[s] != s) continue;  // a copy: shares the hierarchy below
             try {
                 B.A_sys[s] = std::make_shared<CsrD>(systems[s]);
                 B.chain[s] = std::make_shared<RsChain>(rs_chain(systems[s], theta, max_levels));
@@ -67,6 +74,12 @@ BatchHierarchy build_batch(const std::vector<CsrD> &systems, double theta, int m
     for (auto &t : pool) t.join();
     for (int s = 0; s < S; s++)
         if (!errs[s].empty()) throw SetupError{"system " + std::to_string(s) + ": " + errs[s]};
+    for (int s = 0; s < S; s++)
+        if (src[s] != s) {
+            B.A_sys[s] = B.A_sys[src[s]];
+            B.chain[s] = B.chain[src[s]];
+            B.hi[s] = B.hi[src[s]];
+        }
     int Dmax = 0;
     for (int s = 0; s < S; s++) {
         B.depth[s] = B.hi[s]->depth;
@@ -172,7 +185,7 @@ BatchHierarchy build_batch(const std::vector<CsrD> &systems, double theta, int m
     B.Af.n = B.Af.m = B.n_level[0];
     B.Af.rptr.assign(1, 0);
     for (int s : order[0]) {
-        const CsrD &A = systems[s];
+        const CsrD &A = *B.A_sys[s];
         const int off = B.offset[0][s];
         for (int i = 0; i < A.n; i++) {
             for (int j = A.rptr[i]; j < A.rptr[i + 1]; j++) {

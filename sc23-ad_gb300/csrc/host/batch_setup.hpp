@@ -62,8 +62,11 @@ struct BatchHierarchy {
 };
 
 // Build the hierarchies of all systems (threads over systems) and assemble the
-// batch.  The systems must already be scaled (LMax1Scaling).
+// batch.  The systems must already be scaled (LMax1Scaling).  src[s] (optional)
+// names the system whose matrix and hierarchy system s repeats (src[s] <= s),
+// so copies of one matrix, e.g. solved with different fractional bits, share
+// one setup.
 BatchHierarchy build_batch(const std::vector<CsrD> &systems, double theta, int max_levels, double omega,
-                           int smooth_iter, int threads);
+                           int smooth_iter, int threads, const std::vector<int> &src = {});
 
 }  // namespace sagb

@@ -134,3 +134,27 @@ def test_batched_overflow_falls_back_per_pair(ctx):
     assert cv.all(), (it, cv, fb)
     assert fb[0] == 29 and fb[1] < 30
     B.close()
+
+
+def test_copies_share_one_setup(ctx):
+    """Copies of one matrix (the same arrays) share a setup; solved with
+    different fractional bits, each copy matches the single-system solver."""
+    systems, bs = _systems([(sagb.GEN_POISSON3D, 14, 0.0)], 1)
+    r, c, v = systems[0]
+    bits = [20, 25, 29]
+    B = sagb.Batch(ctx, [(r, c, v)] * len(bits), 1)
+    b = np.concatenate([bs[0][:, 0]] * len(bits))
+    nrm = np.linalg.norm(bs[0][:, 0])
+    x = np.zeros(B.rows)
+    it, cv, fb = B.solve(sagb.solver_params(m=20, explicit_stop=1), bits, b, np.full(len(bits), nrm), x)
+    setup = B.system_setup(0)
+    M = sagb.Amg(ctx, sagb.INT, setup=setup)
+    dA = sagb.Matrix(ctx, sagb.MAT_F64, r, c, v)
+    iA = sagb.Matrix(ctx, sagb.MAT_FIXED, r, c, v, bit=30)
+    for k, f in enumerate(bits):
+        S1 = sagb.Solver(ctx, sagb.INT, dA, iA, M, sagb.solver_params(m=20, frac_bits=f, explicit_stop=1))
+        x1 = np.zeros(len(r) - 1)
+        it1, cv1 = S1.solve(np.ascontiguousarray(bs[0][:, 0]), float(nrm), x1)
+        assert cv[k] == cv1 and abs(int(it[k]) - it1) <= 2, (f, it[k], it1)
+        S1.close()
+    B.close()
