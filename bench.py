@@ -29,8 +29,9 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(ROOT, "sc23-ad_gb300"))
 
-WORKLOAD = ("3D 7-point Poisson 128^3, int-AMG-FGMRES(30) with FP64 refinement, reference bit rule, "
-            "level-scheduled bit-exact SOR smoother")
+WORKLOAD = ("3D 7-point Poisson 128^3, one right-hand side: batched int-AMG-FGMRES(30) with FP64 refinement, "
+            "multicolour SOR smoother, learned fractional bits (rule as fallback); the plain drop-in (rule bits, "
+            "bit-exact level-scheduled SOR) and FP64-AMG-FGMRES on the same GPU reported beside it")
 
 
 def parse():
@@ -46,6 +47,10 @@ def parse():
     ap.add_argument("--no-multicolor", action="store_true", help="skip the multicolour-smoother row")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-engine rows")
     ap.add_argument("--profile", action="store_true", help="skip extras (for profilers)")
+    ap.add_argument("--workload", choices=["poisson128", "batch256", "convdiff128"], default="poisson128",
+                    help="poisson128: the headline; batch256: 256 27-point systems x 4 right-hand sides; "
+                         "convdiff128: learned vs rule bits on convection-diffusion 128^3, Pe 50")
+    ap.add_argument("--nsys", type=int, default=256)
     return ap.parse_args()
 
 
@@ -159,7 +164,23 @@ def ncu_traffic(kernel):
 
 # ------------------------------------------------------------------ our arm
 
+def learned_bits(ctx, setup_int, ratio):
+    """F from the trained selector (sc23-ad_gb300/data/bitsel_mlp.npz), or None."""
+    import bitsel
+    import sagb
+    if not os.path.exists(bitsel.WEIGHTS):
+        return None
+    sel = bitsel.Selector(ctx)
+    f = sel.choose(sagb.setup_features(setup_int, ratio))
+    sel.net.close()
+    return f
+
+
 def run_ours(a, dist):
+    """Headline: the batched engine (multicolour colour-pass sweeps, autotuned
+    lanes per row, graph-captured Arnoldi steps) with the learned F and the
+    rule's F as fallback, on one 128^3 system and one right-hand side."""
+    import bitsel
     import sagb
     dev = dist.local
     ctx = sagb.Context(dev)
@@ -167,24 +188,32 @@ def run_ours(a, dist):
     N = len(b)
     nrm_b = float(np.linalg.norm(b))
     t0 = time.time()
-    s_int = sagb.Setup(sagb.INT, r, c, v)
-    s_f64 = s_int.derive(sagb.F64)
+    B = sagb.Batch(ctx, [(r, c, v)], 1)
     t_setup = time.time() - t0
-    M = sagb.Amg(ctx, sagb.INT, setup=s_int)
-    M64 = sagb.Amg(ctx, sagb.F64, setup=s_f64)
-    dA = sagb.Matrix(ctx, sagb.MAT_F64, r, c, v)
-    A0 = sagb.Matrix(ctx, sagb.MAT_FIXED, r, c, v, bit=30)
-    bits = sagb.rule_bits(ctx, M64, b, nrm_b)
-    # explicit_stop: the metric is the explicit residual; the reference's inner
-    # estimate alone stops above 1e-10 on this system
-    S = sagb.Solver(ctx, sagb.INT, dA, A0, M, sagb.solver_params(m=a.m, frac_bits=bits, explicit_stop=1))
+    t0 = time.time()
+    B.autotune(2)
+    t_tune = time.time() - t0
+    ratio = float(B.rule_ratios(b, [nrm_b])[0])
+    rule = bitsel.rule_of(ratio)
+    s0 = B.system_setup(0)
+    learned = learned_bits(ctx, s0, ratio)
+    bits = learned if learned is not None else rule
+    params = sagb.solver_params(m=a.m, explicit_stop=1)
     db = sagb.DeviceArray.from_host(ctx, b)
     dx = sagb.DeviceArray(ctx, N, np.float64)
     zeros = sagb.DeviceArray.from_host(ctx, np.zeros(N))
+    nb = np.array([nrm_b])
+    state = {"fallbacks": 0}
 
     def one_solve():
         sagb.check(sagb.lib().sa_memcpy(ctx.h, dx.ptr, zeros.ptr, 8 * N))
-        return S.solve(db, nrm_b, dx)
+        it, cv, fb = B.solve(params, [bits], db, nb, dx)
+        if not cv[0]:  # the learned F failed: the rule's F (part of the method, timed)
+            state["fallbacks"] += 1
+            sagb.check(sagb.lib().sa_memcpy(ctx.h, dx.ptr, zeros.ptr, 8 * N))
+            it2, cv, fb = B.solve(params, [rule], db, nb, dx)
+            it = it + it2
+        return int(it[0]), int(cv[0]), int(fb[0])
 
     for _ in range(a.warmup):
         one_solve()
@@ -206,15 +235,13 @@ def run_ours(a, dist):
     dist.barrier()
     sec = dist.max(ms / 1000.0 / a.steps)
     x = dx.download()
-    res = explicit_res(r, c, v, b, x)
-    iters = its[-1][0]
-    conv = all(cv for _, cv in its)
-    hist, flags = S.history()
-    out = {"iters": iters, "converged": bool(conv), "explicit_res": res, "frac_bits": bits,
-           "setup_s": t_setup, "launches": launches, "clocks": clk, "flags": flags}
+    out = {"iters": its[-1][0], "converged": all(q[1] for q in its), "explicit_res": explicit_res(r, c, v, b, x),
+           "frac_bits": bits, "rule_bits": rule, "learned_bits": learned, "final_bits": its[-1][2],
+           "selector_fallbacks": state["fallbacks"], "setup_s": t_setup, "autotune_s": t_tune,
+           "launches": launches, "clocks": clk}
     if a.profile:
         return sec, out, ctx, None
-    # ---- end to end through the C ABI with page-locked host buffers
+    # ---- end to end through the C ABI with page-locked host b and x
     if not a.no_e2e:
         hb = sagb.PinnedArray(N, np.float64)
         hx = sagb.PinnedArray(N, np.float64)
@@ -223,117 +250,193 @@ def run_ours(a, dist):
         for k in range(max(2, a.steps // 2) + 1):
             hx.a[:] = 0
             t = time.perf_counter()
-            S.solve(hb, nrm_b, hx)
+            it, cv, fb = B.solve(params, [bits], hb, nb, hx)
             ts.append(time.perf_counter() - t)
         out["e2e_s"] = dist.max(float(np.mean(ts[1:])))
         out["e2e_res"] = explicit_res(r, c, v, b, np.array(hx.a))
         hb.close()
         hx.close()
-    # ---- kernel roofline: level-0 sweep family and the fine SpMV, timed alone
-    out["kernels"] = kernel_rooflines(ctx, M, A0, N, a)
-    # ---- FP64-AMG-FGMRES on the same GPU (comparison row)
-    S64 = sagb.Solver(ctx, sagb.F64, dA, dA, M64, sagb.solver_params(m=a.m, explicit_stop=1))
-    dx.upload(np.zeros(N))
-    S64.solve(db, nrm_b, dx)
-    e0.record(ctx)
-    nrep = 2
-    it64 = None
-    for _ in range(nrep):
-        dx.upload(np.zeros(N))
-        it64 = S64.solve(db, nrm_b, dx)
-    e1.record(ctx)
-    ctx.sync()
-    out["fp64_gpu_s"] = e0.elapsed_ms(e1) / 1000.0 / nrep
-    out["fp64_gpu_iters"] = it64[0]
-    out["fp64_gpu_res"] = explicit_res(r, c, v, b, dx.download())
-    S64.close()
-    # ---- the multicolour smoother variant (same solver, colour-ordered GS)
+    out["kernels"] = batch_rooflines(ctx, B, a)
+    for arr in (db, dx, zeros):
+        arr.close()
+    B.close()
+    # ---- comparison rows on the same GPU
+    out["plain"] = plain_row(ctx, a, r, c, v, b, nrm_b)
     if not a.no_multicolor:
-        out["multicolor"] = multicolor_row(ctx, a, r, c, v, b, nrm_b, dA, A0, db, dx, N)
-    # ---- the batched engine on the same system (1 and 4 right-hand sides)
+        out["multicolor"] = multicolor_row(ctx, a, r, c, v, b, nrm_b)
     if not a.no_batched:
-        out["batched"] = batched_rows(ctx, a, r, c, v, b, nrm_b, dist)
-    return sec, out, ctx, (s_int, r, c, v, b, bits)
+        out["batched"] = batched_rows(ctx, a, r, c, v, b, nrm_b, dist, bits, rule)
+    return sec, out, ctx, out["plain"].pop("state")
 
 
-def batched_rows(ctx, a, r, c, v, b, nrm_b, dist):
-    """The batched engine (multicolour colour-pass sweeps, graph-captured
-    Arnoldi steps, autotuned lanes per row) on the same 128^3 system: one
-    right-hand side, and four right-hand sides solved together."""
+def plain_row(ctx, a, r, c, v, b, nrm_b):
+    """The plain drop-in: bit-exact level-scheduled SOR sweeps, the rule's F
+    (the reference's algorithm on the GPU), and the FP64 solver beside it."""
     import sagb
     N = len(b)
-    rows = {}
-    for nrhs in (1, 4):
-        t0 = time.time()
-        B = sagb.Batch(ctx, [(r, c, v)], nrhs)
-        t_setup = time.time() - t0
-        t0 = time.time()
-        B.autotune(2)
-        t_tune = time.time() - t0
-        cols = [b] + [build_system(a.n, seed=1 + dist.rank + 1000 * k)[3] for k in range(1, nrhs)]
-        bb = np.stack(cols, 1).ravel()
-        nb = np.array([np.linalg.norm(col) for col in cols])
-        q = B.rule_ratios(bb, nb)
-        bits = [29 if q[0] < 1 else 31 - (int(np.ceil(np.log2(int(q[0]) + 1))) + 1)]
-        params = sagb.solver_params(m=a.m, explicit_stop=1)
-        db = sagb.DeviceArray.from_host(ctx, bb)
-        dx = sagb.DeviceArray(ctx, N * nrhs, np.float64)
-        zeros = sagb.DeviceArray.from_host(ctx, np.zeros(N * nrhs))
+    t0 = time.time()
+    s_int = sagb.Setup(sagb.INT, r, c, v)
+    s_f64 = s_int.derive(sagb.F64)
+    t_setup = time.time() - t0
+    M = sagb.Amg(ctx, sagb.INT, setup=s_int)
+    M64 = sagb.Amg(ctx, sagb.F64, setup=s_f64)
+    dA = sagb.Matrix(ctx, sagb.MAT_F64, r, c, v)
+    A0 = sagb.Matrix(ctx, sagb.MAT_FIXED, r, c, v, bit=30)
+    bits = sagb.rule_bits(ctx, M64, b, nrm_b)
+    S = sagb.Solver(ctx, sagb.INT, dA, A0, M, sagb.solver_params(m=a.m, frac_bits=bits, explicit_stop=1))
+    db = sagb.DeviceArray.from_host(ctx, b)
+    dx = sagb.DeviceArray(ctx, N, np.float64)
+    e0, e1 = sagb.Event(), sagb.Event()
 
-        def one():
-            sagb.check(sagb.lib().sa_memcpy(ctx.h, dx.ptr, zeros.ptr, 8 * N * nrhs))
-            return B.solve(params, bits, db, nb, dx)
-
-        one()
-        e0, e1 = sagb.Event(), sagb.Event()
-        reps = 3
-        ctx.sync()
-        l0 = ctx.launches()
+    def timed(solver, reps):
+        dx.upload(np.zeros(N))
+        solver.solve(db, nrm_b, dx)
+        it = None
         e0.record(ctx)
         for _ in range(reps):
-            it, cv, fb = one()
+            dx.upload(np.zeros(N))
+            it = solver.solve(db, nrm_b, dx)
         e1.record(ctx)
         ctx.sync()
-        sec = e0.elapsed_ms(e1) / 1000.0 / reps
-        X = dx.download().reshape(N, nrhs)
-        res = [explicit_res(r, c, v, cols[k], np.ascontiguousarray(X[:, k])) for k in range(nrhs)]
-        vin = sagb.DeviceArray.from_host(ctx, np.random.default_rng(3).integers(
-            -(1 << 28), 1 << 28, size=N * nrhs).astype(np.int32))
-        vout = sagb.DeviceArray(ctx, N * nrhs, np.int32)
-        B.precondition(vin, vout)
+        return e0.elapsed_ms(e1) / 1000.0 / reps, it
+    sec, it = timed(S, 2)
+    row = {"value": sec, "iters": it[0], "converged": bool(it[1]), "explicit_res": explicit_res(r, c, v, b, dx.download()),
+           "frac_bits": bits, "setup_s": t_setup}
+    k = kernel_rooflines(ctx, M, A0, N, a)
+    row["vcycle_ms"] = k["vcycle"]["ms"]
+    row["sweep_ms_per_vcycle"] = k["sweeps"]["ms_per_vcycle"]
+    row["coarse_lu_ms"] = k["coarse_lu"]["ms"]
+    row["sweep_levels"] = [(p["level"], p["n"], p["levels"], round(p["ms"], 4)) for p in k["sweeps"]["per_level"]]
+    l0 = k["sweeps"]["per_level"][0]
+    row["sweep_level0"] = {"ms": l0["ms"], "bytes": l0["bytes"], "traffic": ncu_traffic("k_tri_level0")}
+    row["spmv_A0"] = k["spmv_A0"]
+    S.close()
+    S64 = sagb.Solver(ctx, sagb.F64, dA, dA, M64, sagb.solver_params(m=a.m, explicit_stop=1))
+    sec64, it64 = timed(S64, 2)
+    row["fp64_gpu"] = {"value": sec64, "iters": it64[0], "explicit_res": explicit_res(r, c, v, b, dx.download())}
+    S64.close()
+    row["state"] = (s_int, r, c, v, b, bits)
+    for o in (db, dx):
+        o.close()
+    return row
+
+
+def batch_rooflines(ctx, B, a):
+    """Average launch time (CUDA events on the library stream) and algorithmic
+    bytes of every batched level operator, and the V-cycle they make up."""
+    import sagb
+    R = B.nrhs
+    rng = np.random.default_rng(3)
+    big = B.rows * R
+    xin = sagb.DeviceArray.from_host(ctx, rng.integers(-(1 << 28), 1 << 28, size=big).astype(np.int32))
+    xout = sagb.DeviceArray(ctx, big, np.int32)
+    e0, e1 = sagb.Event(), sagb.Event()
+    reps = 10
+
+    def timed(fn):
+        fn()
         ctx.sync()
         e0.record(ctx)
-        for _ in range(5):
-            B.precondition(vin, vout)
+        for _ in range(reps):
+            fn()
         e1.record(ctx)
-        ctx.sync()
-        rows[f"nrhs{nrhs}"] = {"value": sec, "per_rhs": sec / nrhs, "iters": [int(i) for i in it],
-                               "converged": bool(cv.all()), "explicit_res": max(res), "frac_bits": bits[0],
-                               "final_bits": [int(f) for f in fb], "vcycle_ms": e0.elapsed_ms(e1) / 5,
-                               "setup_s": t_setup, "autotune_s": t_tune,
-                               "launches_per_solve": (ctx.launches() - l0) // reps}
-        for arr in (db, dx, zeros, vin, vout):
-            arr.close()
-        B.close()
-    return rows
+        return e0.elapsed_ms(e1) / reps
+
+    fam = {"spmv": [0.0, 0], "sweep": [0.0, 0]}
+    per = []
+    for l in range(B.depth):
+        for op, name in ((0, "A"), (1, "LD"), (2, "U"), (3, "P"), (4, "R")):
+            n, m, nnz, ncol = B.level_info(l, op)
+            if n == 0:
+                continue
+            t = timed(lambda: sagb.check(sagb.lib().sa_batch_level_op(ctx.h, B.h, l, op, xin.ptr, xout.ptr)))
+            if op == 1:
+                # LD entries, row pointers, two shifts, the colour row list, in once, out written once
+                by = 8 * nnz + 4 * (n + 1) + 2 * n + 4 * n + 8 * R * n
+                calls = 2  # pre- and post-smoothing
+            else:
+                # entries, row pointers, the shift, x once, y once (and z for the residuals)
+                by = 8 * nnz + 4 * (n + 1) + n + 4 * R * m + 4 * R * n
+                calls = 2 if op in (0, 2) else 1
+            per.append({"level": l, "op": name, "n": n, "nnz": nnz, "colours": ncol if op == 1 else None,
+                        "ms": t, "bytes": by, "per_vcycle": calls})
+            key = "sweep" if op == 1 else "spmv"
+            fam[key][0] += calls * t
+            fam[key][1] += calls * by
+    t_lu = timed(lambda: B.coarse_solve())
+    vin = sagb.DeviceArray.from_host(ctx, rng.integers(-(1 << 28), 1 << 28, size=big).astype(np.int32))
+    t_v = timed(lambda: B.precondition(vin, xout))
+    for o in (xin, xout, vin):
+        o.close()
+    return {"per_op": per, "families": fam, "coarse_lu_ms": t_lu, "vcycle_ms": t_v}
 
 
-def multicolor_row(ctx, a, r, c, v, b, nrm_b, dA, A0, db, dx, N):
-    """int-AMG-FGMRES with the multicolour Gauss-Seidel smoother: solve time,
-    iterations and the V-cycle time, beside the natural-order numbers."""
+def batched_rows(ctx, a, r, c, v, b, nrm_b, dist, bits, rule):
+    """Four right-hand sides of the same 128^3 system solved together (the
+    matrix entries are read once for all four)."""
     import sagb
+    N = len(b)
+    nrhs = 4
+    t0 = time.time()
+    B = sagb.Batch(ctx, [(r, c, v)], nrhs)
+    t_setup = time.time() - t0
+    B.autotune(2)
+    cols = [b] + [build_system(a.n, seed=1 + dist.rank + 1000 * k)[3] for k in range(1, nrhs)]
+    bb = np.stack(cols, 1).ravel()
+    nb = np.array([np.linalg.norm(col) for col in cols])
+    params = sagb.solver_params(m=a.m, explicit_stop=1)
+    db = sagb.DeviceArray.from_host(ctx, bb)
+    dx = sagb.DeviceArray(ctx, N * nrhs, np.float64)
+    zeros = sagb.DeviceArray.from_host(ctx, np.zeros(N * nrhs))
+
+    def one():
+        sagb.check(sagb.lib().sa_memcpy(ctx.h, dx.ptr, zeros.ptr, 8 * N * nrhs))
+        return B.solve(params, [bits], db, nb, dx)
+
+    one()
+    e0, e1 = sagb.Event(), sagb.Event()
+    reps = 3
+    ctx.sync()
+    e0.record(ctx)
+    for _ in range(reps):
+        it, cv, fb = one()
+    e1.record(ctx)
+    ctx.sync()
+    sec = e0.elapsed_ms(e1) / 1000.0 / reps
+    X = dx.download().reshape(N, nrhs)
+    res = [explicit_res(r, c, v, cols[k], np.ascontiguousarray(X[:, k])) for k in range(nrhs)]
+    k = batch_rooflines(ctx, B, a)
+    row = {"nrhs": nrhs, "value": sec, "per_rhs": sec / nrhs, "iters": [int(i) for i in it],
+           "converged": bool(cv.all()), "explicit_res": max(res), "frac_bits": bits,
+           "final_bits": [int(f) for f in fb], "vcycle_ms": k["vcycle_ms"], "setup_s": t_setup,
+           "spmv_A0": next(p for p in k["per_op"] if p["level"] == 0 and p["op"] == "A")}
+    for arr in (db, dx, zeros):
+        arr.close()
+    B.close()
+    return row
+
+
+def multicolor_row(ctx, a, r, c, v, b, nrm_b):
+    """The single-system solver with the multicolour split (level-scheduled
+    sweep kernels with the colours as levels), rule's F."""
+    import sagb
+    N = len(b)
     t0 = time.time()
     s_mc = sagb.Setup(sagb.INT, r, c, v, sagb.amg_params(multicolor=1))
     s_mc64 = s_mc.derive(sagb.F64)
     t_setup = time.time() - t0
     Mm = sagb.Amg(ctx, sagb.INT, setup=s_mc)
     Mm64 = sagb.Amg(ctx, sagb.F64, setup=s_mc64)
+    dA = sagb.Matrix(ctx, sagb.MAT_F64, r, c, v)
+    A0 = sagb.Matrix(ctx, sagb.MAT_FIXED, r, c, v, bit=30)
     bits = sagb.rule_bits(ctx, Mm64, b, nrm_b)
     Sm = sagb.Solver(ctx, sagb.INT, dA, A0, Mm, sagb.solver_params(m=a.m, frac_bits=bits, explicit_stop=1))
+    db = sagb.DeviceArray.from_host(ctx, b)
+    dx = sagb.DeviceArray(ctx, N, np.float64)
     e0, e1 = sagb.Event(), sagb.Event()
     dx.upload(np.zeros(N))
     Sm.solve(db, nrm_b, dx)
-    nrep = 3
+    nrep = 2
     itm = None
     e0.record(ctx)
     for _ in range(nrep):
@@ -344,23 +447,12 @@ def multicolor_row(ctx, a, r, c, v, b, nrm_b, dA, A0, db, dx, N):
     row = {"value": e0.elapsed_ms(e1) / 1000.0 / nrep, "iters": itm[0], "converged": bool(itm[1]),
            "explicit_res": explicit_res(r, c, v, b, dx.download()), "frac_bits": bits, "setup_s": t_setup,
            "colours": [int(s_mc.view(sagb.OP_COLOR, l).max()) + 1 for l in range(s_mc.depth)]}
-    rng = np.random.default_rng(3)
-    vin = sagb.DeviceArray.from_host(ctx, rng.integers(-(1 << 28), 1 << 28, size=N).astype(np.int32))
-    vout = sagb.DeviceArray(ctx, N, np.int32)
-    sagb.check(sagb.lib().sa_amg_precondition(ctx.h, Mm.h, vin.ptr, vout.ptr))
-    e0.record(ctx)
-    for _ in range(10):
-        sagb.check(sagb.lib().sa_amg_precondition(ctx.h, Mm.h, vin.ptr, vout.ptr))
-    e1.record(ctx)
-    ctx.sync()
-    row["vcycle_ms"] = e0.elapsed_ms(e1) / 10
     k = kernel_rooflines(ctx, Mm, A0, N, a)
+    row["vcycle_ms"] = k["vcycle"]["ms"]
     row["sweep_ms_per_vcycle"] = k["sweeps"]["ms_per_vcycle"]
-    row["coarse_lu_ms"] = k["coarse_lu"]["ms"]
     row["sweep_levels"] = [(p["level"], p["n"], p["levels"], round(p["ms"], 4)) for p in k["sweeps"]["per_level"]]
-    Sm.close()
-    Mm.close()
-    Mm64.close()
+    for o in (Sm, Mm, Mm64, dA, A0, db, dx):
+        o.close()
     return row
 
 
@@ -456,6 +548,9 @@ def oracle_hierarchy(of, keep, setup):
     return of.golden_amg_i32(keep, g)
 
 
+METRIC = "time to 1e-10 rel. residual: batched+learned-bits vs plain int-AMG-FGMRES on GB300"
+
+
 def main_ours(a):
     dist = Dist(a.gpus)
     sec, out, ctx, state = run_ours(a, dist)
@@ -465,54 +560,54 @@ def main_ours(a):
     N = a.n ** 3
     peak, peak_kind = measured_peak()
     line = {
-        "metric": "time to 1e-10 explicit relative residual, int-AMG-FGMRES(30), 3D Poisson 128^3",
+        "metric": METRIC,
         "value": sec, "unit": "s", "n_gpus": dist.world, "steps": a.steps, "warmup": a.warmup,
         "ms_per_step": sec * 1000.0, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
         "dtype": "int32", "data": "synthetic (b = A x*, x* ~ U[-1,1] seeded; SuiteSparse inputs not shipped)",
         "config": {"workload": WORKLOAD, "rows": N, "m": a.m, "eps": 1e-10, "parallelism": f"replicas{dist.world}",
-                   "l2": "inputs larger than L2 (hierarchy ~1.4 GB, Krylov basis 0.5 GB per solve)"},
+                   "l2": "inputs larger than L2 (hierarchy ~1.5 GB, Krylov basis 0.5 GB per solve)"},
         "iters": out["iters"], "converged": out["converged"], "explicit_res": out["explicit_res"],
-        "frac_bits": out["frac_bits"], "setup_s": out["setup_s"], "status_flags": out["flags"],
+        "frac_bits": out["frac_bits"], "rule_bits": out["rule_bits"], "learned_bits": out["learned_bits"],
+        "final_bits": out["final_bits"], "selector_fallbacks": out["selector_fallbacks"],
+        "setup_s": out["setup_s"], "autotune_s": out["autotune_s"],
         "gpu_launches": out["launches"], "clocks": out["clocks"],
     }
     if "e2e_s" in out:
-        line["e2e"] = {"value": out["e2e_s"], "unit": "s", "h2d_bytes_per_step": 2 * 8 * N,
+        line["e2e"] = {"value": out["e2e_s"], "unit": "s", "h2d_bytes_per_step": 8 * N + 8,
                        "d2h_bytes_per_step": 8 * N, "explicit_res": out["e2e_res"]}
     if "kernels" in out:
         k = out["kernels"]
-        sw = k["sweeps"]
-        sp = k["spmv_A0"]
-        # dominant kernel family: the level-scheduled Gauss-Seidel sweeps
-        ach = sw["bytes_per_vcycle"] / (sw["ms_per_vcycle"] * 1e-3) / 1e9
-        line["roofline"] = {"kernel": "k_tri (level-scheduled int Gauss-Seidel sweeps, all levels)",
-                            "bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
-                            "peak_kind": peak_kind, "traffic": ncu_traffic("k_tri_all_levels"),
-                            "share_of_vcycle": sw["ms_per_vcycle"] / k["vcycle"]["ms"]}
-        # the level-0 launch alone (the one kernel with a committed ncu capture)
-        l0 = sw["per_level"][0]
-        a0 = l0["bytes"] / (l0["ms"] * 1e-3) / 1e9
-        line["roofline"]["level0"] = {"kernel": "k_tri level 0", "achieved": a0, "frac": a0 / peak,
-                                      "bytes": l0["bytes"], "ms": l0["ms"], "traffic": ncu_traffic("k_tri_level0")}
+        fam = k["families"]
+        # dominant kernel family of the V-cycle: the colour-pass sweeps or the SpMVs
+        name = max(fam, key=lambda f: fam[f][0])
+        ms, by = fam[name]
+        ach = by / (ms * 1e-3) / 1e9
+        kern = "k_bcolour (multicolour Gauss-Seidel colour passes, all levels)" if name == "sweep" else \
+            "k_bspmv / k_bspmv_stream (level SpMVs, all levels)"
+        line["roofline"] = {"kernel": kern, "bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
+                            "frac": ach / peak, "peak_kind": peak_kind, "traffic": ncu_traffic(name + "_per_vcycle"),
+                            "bytes_per_vcycle": by, "ms_per_vcycle": ms, "share_of_vcycle": ms / k["vcycle_ms"]}
+        sp = next(p for p in k["per_op"] if p["level"] == 0 and p["op"] == "A")
         spa = sp["bytes"] / (sp["ms"] * 1e-3) / 1e9
-        line["spmv_A0"] = {"achieved": spa, "peak": peak, "unit": "GB/s", "frac": spa / peak, "ms": sp["ms"],
-                           "bytes": sp["bytes"], "traffic": ncu_traffic("k_spmv_i32")}
-        line["vcycle_ms"] = k["vcycle"]["ms"]
-        line["sweep_ms_per_vcycle"] = sw["ms_per_vcycle"]
-        line["coarse_lu_ms"] = k["coarse_lu"]["ms"]
-        line["sweep_levels"] = [(p["level"], p["n"], p["levels"], round(p["ms"], 4)) for p in sw["per_level"]]
-    if "multicolor" in out:
-        line["multicolor"] = out["multicolor"]
-    if "batched" in out:
-        line["batched"] = out["batched"]
-    if "fp64_gpu_s" in out:
-        line["fp64_gpu"] = {"value": out["fp64_gpu_s"], "iters": out["fp64_gpu_iters"],
-                            "explicit_res": out["fp64_gpu_res"]}
+        line["spmv_A0"] = {"kernel": "k_bspmv_stream level 0", "achieved": spa, "peak": peak, "unit": "GB/s",
+                           "frac": spa / peak, "ms": sp["ms"], "bytes": sp["bytes"], "traffic": ncu_traffic("spmv_A0")}
+        line["vcycle_ms"] = k["vcycle_ms"]
+        line["coarse_lu_ms"] = k["coarse_lu_ms"]
+        line["families_ms_per_vcycle"] = {f: fam[f][0] for f in fam}
+        line["ops"] = [(p["level"], p["op"], p["n"], p["colours"], round(p["ms"], 4)) for p in k["per_op"]]
+    for key in ("plain", "multicolor", "batched"):
+        if key in out:
+            line[key] = out[key]
+    if "plain" in out:
+        line["speedup_vs_plain"] = out["plain"]["value"] / sec
+        line["speedup_vs_fp64_gpu"] = out["plain"]["fp64_gpu"]["value"] / sec
     if state is not None and not a.no_cpu_baseline and dist.world == 1:
         threads = os.cpu_count() or 1
         t, it, res = cpu_baseline(state, threads, a.m)
         line["cpu_baseline"] = {"value": t, "unit": "s", "cores": threads, "kind": "port",
-                                "sample": "one full solve of the same 128^3 system (same hierarchy and bit), "
-                                          f"oracle C restatement, {threads} threads; iters={it} res={res:.2e}"}
+                                "sample": "one full plain int solve of the same 128^3 system (same hierarchy and "
+                                          f"rule bit), oracle C restatement, {threads} threads; iters={it} "
+                                          f"res={res:.2e}"}
     print(json.dumps(line), flush=True)
     dist.close()
 
@@ -554,7 +649,7 @@ def main_reference(a):
     val = float(np.mean(ts))
     line = {
         "impl": "reference",
-        "metric": "time to 1e-10 explicit relative residual, int-AMG-FGMRES(30), 3D Poisson 128^3",
+        "metric": METRIC,
         "value": val, "unit": "s", "n_gpus": dist.world, "steps": a.steps, "warmup": a.warmup,
         "ms_per_step": val * 1000, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
         "dtype": "int32", "data": "synthetic (b = A x*, x* ~ U[-1,1] seeded)",
@@ -594,9 +689,185 @@ def fp64_oracle_hierarchy(of, keep, s, r, c, v):
     return h
 
 
+# ----------------------------------------------------------- other workloads
+
+def batch_systems(nsys, nrhs, seed=2024):
+    """256 SPD 27-point systems (diagonal 26 + U[0.1, 1], off-diagonals -1),
+    cube sides uniform in 16..64, nrhs right-hand sides U[-1, 1] each; rows and
+    right-hand sides scaled by the row maxima (LMax1Scaling)."""
+    import sagb
+    rng = np.random.default_rng(seed)
+    sides = rng.integers(16, 65, size=nsys)
+    systems, bs = [], []
+    for s, n in enumerate(sides):
+        A = sagb.HostCsr.generate(sagb.GEN_STENCIL27, int(n), 0.0, seed=int(seed + s))
+        r, c, v = A.arrays()
+        rows = np.repeat(np.arange(len(r) - 1), np.diff(r))
+        rmax = np.zeros(len(r) - 1)
+        np.maximum.at(rmax, rows, np.abs(v))
+        B = rng.uniform(-1.0, 1.0, size=(len(r) - 1, nrhs))
+        b0 = B[:, 0].copy()
+        A.lmax1_scaling(b0)
+        systems.append(A.arrays())
+        bs.append(B / rmax[:, None])
+    return systems, bs, sides
+
+
+def main_batch(a):
+    import bitsel
+    import sagb
+    dist = Dist(a.gpus)
+    ctx = sagb.Context(dist.local)
+    nrhs = 4
+    t0 = time.time()
+    systems, bs, sides = batch_systems(a.nsys, nrhs, seed=2024 + dist.rank)
+    t_gen = time.time() - t0
+    t0 = time.time()
+    B = sagb.Batch(ctx, systems, nrhs)
+    t_setup = time.time() - t0
+    t0 = time.time()
+    B.autotune(2)
+    t_tune = time.time() - t0
+    bvec = np.zeros((B.rows, nrhs))
+    for s in range(B.nsys):
+        bvec[B.offsets[s]:B.offsets[s + 1]] = bs[s]
+    bvec = bvec.ravel()
+    nrm_b = np.array([np.linalg.norm(bs[s][:, r]) for s in range(B.nsys) for r in range(nrhs)])
+    t0 = time.time()
+    ratios = B.rule_ratios(bvec, nrm_b)
+    t_rule = time.time() - t0
+    rule = [min(bitsel.rule_of(q) for q in ratios[s * nrhs:(s + 1) * nrhs]) for s in range(B.nsys)]
+    bits = list(rule)
+    learned = None
+    if os.path.exists(bitsel.WEIGHTS):
+        sel = bitsel.Selector(ctx)
+        learned = [sel.choose(sagb.setup_features(B.system_setup(s), float(ratios[s * nrhs])))
+                   for s in range(B.nsys)]
+        sel.net.close()
+        bits = learned
+    params = sagb.solver_params(m=20, explicit_stop=1)
+    db = sagb.DeviceArray.from_host(ctx, bvec)
+    dx = sagb.DeviceArray(ctx, B.rows * nrhs, np.float64)
+    zeros = sagb.DeviceArray.from_host(ctx, np.zeros(B.rows * nrhs))
+
+    def one(bb):
+        sagb.check(sagb.lib().sa_memcpy(ctx.h, dx.ptr, zeros.ptr, 8 * B.rows * nrhs))
+        return B.solve(params, bb, db, nrm_b, dx)
+
+    for _ in range(a.warmup):
+        one(bits)
+    clocks = Clocks(dist.local)
+    e0, e1 = sagb.Event(), sagb.Event()
+    dist.barrier()
+    ctx.sync()
+    l0 = ctx.launches()
+    clocks.start()
+    e0.record(ctx)
+    for _ in range(a.steps):
+        it, cv, fb = one(bits)
+    e1.record(ctx)
+    ctx.sync()
+    clk = clocks.stop()
+    launches = ctx.launches() - l0
+    sec = dist.max(e0.elapsed_ms(e1) / 1000.0 / a.steps)
+    X = dx.download().reshape(B.rows, nrhs)
+    worst = 0.0
+    for s, (r, c, v) in enumerate(systems):
+        rows = np.repeat(np.arange(len(r) - 1), np.diff(r))
+        xs = X[B.offsets[s]:B.offsets[s + 1]]
+        for q in range(nrhs):
+            res = np.linalg.norm(bs[s][:, q] - np.bincount(rows, weights=v * xs[c, q], minlength=len(r) - 1))
+            worst = max(worst, res / nrm_b[s * nrhs + q])
+    # the rule's bits on the same batch, for comparison
+    rule_row = None
+    if learned is not None:
+        one(rule)
+        e0.record(ctx)
+        itr, cvr, fbr = one(rule)
+        e1.record(ctx)
+        ctx.sync()
+        rule_row = {"value": e0.elapsed_ms(e1) / 1000.0, "iters_total": int(itr.sum()),
+                    "iters_max": int(itr.max()), "converged": int(cvr.sum())}
+    k = batch_rooflines(ctx, B, a)
+    peak, peak_kind = measured_peak()
+    sp = next(p for p in k["per_op"] if p["level"] == 0 and p["op"] == "A")
+    spa = sp["bytes"] / (sp["ms"] * 1e-3) / 1e9
+    fam = k["families"]
+    name = max(fam, key=lambda f: fam[f][0])
+    ach = fam[name][1] / (fam[name][0] * 1e-3) / 1e9
+    if dist.rank == 0:
+        line = {
+            "metric": "time to 1e-10 explicit relative residual, 256 x 4 batched solves, int-AMG-FGMRES(20)",
+            "value": sec, "unit": "s", "n_gpus": dist.world, "steps": a.steps, "warmup": a.warmup,
+            "ms_per_step": sec * 1000, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+            "dtype": "int32", "data": "synthetic 27-point SPD systems, sides U{16..64}, b ~ U[-1,1]",
+            "config": {"workload": "batch of 27-point systems x 4 right-hand sides", "nsys": B.nsys,
+                       "rows": int(B.rows), "nrhs": nrhs, "m": 20, "depth_max": B.depth,
+                       "sides_min_max": [int(sides.min()), int(sides.max())]},
+            "pairs_converged": int(cv.sum()), "pairs": int(len(cv)), "iters_total": int(it.sum()),
+            "iters_max": int(it.max()), "worst_explicit_res": worst,
+            "bits": "learned" if learned is not None else "rule", "rule_row": rule_row,
+            "gen_s": t_gen, "setup_s": t_setup, "autotune_s": t_tune, "rule_s": t_rule,
+            "gpu_launches": launches, "clocks": clk, "vcycle_ms": k["vcycle_ms"], "coarse_lu_ms": k["coarse_lu_ms"],
+            "roofline": {"kernel": name, "bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
+                         "frac": ach / peak, "peak_kind": peak_kind, "traffic": None},
+            "spmv_A0": {"achieved": spa, "frac": spa / peak, "ms": sp["ms"], "bytes": sp["bytes"]},
+            "families_ms_per_vcycle": {f: fam[f][0] for f in fam},
+        }
+        print(json.dumps(line), flush=True)
+    dist.close()
+
+
+def main_convdiff(a):
+    """Learned against rule bits on 3D convection-diffusion 128^3, Pe = 50,
+    through the batched engine (one system, one right-hand side)."""
+    import bitsel
+    import sagb
+    dist = Dist(a.gpus)
+    ctx = sagb.Context(dist.local)
+    A = sagb.HostCsr.generate(sagb.GEN_CONVDIFF3D, a.n, 50.0)
+    xs, b = A.rhs(1)
+    A.lmax1_scaling(b)
+    r, c, v = A.arrays()
+    nrm_b = float(np.linalg.norm(b))
+    B = sagb.Batch(ctx, [(r, c, v)], 1)
+    B.autotune(2)
+    ratio = float(B.rule_ratios(b, [nrm_b])[0])
+    rule = bitsel.rule_of(ratio)
+    learned = learned_bits(ctx, B.system_setup(0), ratio)
+    rows = {}
+    for name, f in (("rule", rule), ("learned", learned)):
+        if f is None:
+            continue
+        x = sagb.DeviceArray(ctx, len(b), np.float64)
+        db = sagb.DeviceArray.from_host(ctx, b)
+        p = sagb.solver_params(m=a.m, explicit_stop=1)
+        x.upload(np.zeros(len(b)))
+        B.solve(p, [f], db, [nrm_b], x)
+        e0, e1 = sagb.Event(), sagb.Event()
+        x.upload(np.zeros(len(b)))
+        e0.record(ctx)
+        it, cv, fb = B.solve(p, [f], db, [nrm_b], x)
+        e1.record(ctx)
+        ctx.sync()
+        rows[name] = {"bits": f, "final_bits": int(fb[0]), "iters": int(it[0]), "converged": int(cv[0]),
+                      "seconds": e0.elapsed_ms(e1) / 1000.0,
+                      "explicit_res": explicit_res(r, c, v, b, x.download())}
+        x.close()
+        db.close()
+    if dist.rank == 0:
+        print(json.dumps({"workload": f"3D convection-diffusion {a.n}^3, Pe 50, batched engine, m={a.m}",
+                          "ratio": ratio, **rows}), flush=True)
+    dist.close()
+
+
 if __name__ == "__main__":
     args = parse()
     if args.impl == "reference":
         main_reference(args)
+    elif args.workload == "batch256":
+        main_batch(args)
+    elif args.workload == "convdiff128":
+        main_convdiff(args)
     else:
         main_ours(args)

@@ -296,6 +296,14 @@ int sa_batch_autotune(sa_ctx ctx, sa_batch B, int reps);
 int sa_batch_group(sa_batch B, int level, int op, int *group);
 /* Work/main.cpp:153-161 per system and right-hand side: max|M_f64 b| / ||b|| */
 int sa_batch_rule_ratios(sa_ctx ctx, sa_batch B, const double *b, const double *nrm_b, double *ratio);
+/* one operator of one batch level on interleaved vectors: op 0 A, 2 U, 3 P,
+ * 4 R (y = M x), or op 1 the multicolour sweep (out = LD^-1 in; out is read
+ * and written) */
+int sa_batch_level_op(sa_ctx ctx, sa_batch B, int level, int op, const int32_t *in, int32_t *out);
+/* the batched coarsest LU solve on the batch's own level vectors (for timing) */
+int sa_batch_coarse_solve(sa_ctx ctx, sa_batch B);
+/* rows, columns, entries and colour count of one batch level operator */
+int sa_batch_level_info(sa_batch B, int level, int op, int *n, int *m, int64_t *nnz, int *ncolours);
 /* Restarted(FGMRESflex) per pair; bits: F_G per system; nrm_b per pair;
  * iters / converged / final_bits (after overflow fallbacks) per pair, optional */
 int sa_batch_solve(sa_ctx ctx, sa_batch B, const sa_solver_params *p, const int *bits, const double *b,

@@ -1,6 +1,7 @@
 // C ABI (include/sagb.h) over the host setup and the CUDA kernels.
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -1188,10 +1189,37 @@ extern "C" int sa_batch_rule_ratios(sa_ctx ctx, sa_batch B, const double *b, con
     sm.omega = B->p.omega;
     sm.iter = B->p.smooth_iter;
     sm.multicolor = 1;
+    // FP64 hierarchies of all systems on host threads (copies of one matrix share one)
+    std::vector<std::shared_ptr<FpHierarchy<double>>> hds(S);
+    {
+        std::atomic<int> next{0};
+        auto work = [&]() {
+            for (;;) {
+                const int s = next.fetch_add(1);
+                if (s >= S) return;
+                bool copy = false;
+                for (int t = 0; t < s && !copy; t++) copy = B->h->hi[t] == B->h->hi[s];
+                if (!copy)
+                    hds[s] = std::make_shared<FpHierarchy<double>>(
+                        build_f64_hierarchy(*B->h->A_sys[s], *B->h->chain[s], sm));
+            }
+        };
+        const int T = std::max(1, std::min(S, (int)std::thread::hardware_concurrency()));
+        std::vector<std::thread> pool;
+        for (int t = 1; t < T; t++) pool.emplace_back(work);
+        work();
+        for (auto &t : pool) t.join();
+        for (int s = 0; s < S; s++)
+            if (!hds[s])
+                for (int t = 0; t < s; t++)
+                    if (B->h->hi[t] == B->h->hi[s] && hds[t]) {
+                        hds[s] = hds[t];
+                        break;
+                    }
+    }
     for (int s = 0; s < S; s++) {
         // Work/main.cpp:153-161 per system: one FP64 V-cycle of its own hierarchy
-        auto hd = std::make_shared<FpHierarchy<double>>(build_f64_hierarchy(*B->h->A_sys[s], *B->h->chain[s], sm));
-        auto M = upload_amg_f64(c, hd);
+        auto M = upload_amg_f64(c, hds[s]);
         const int n = B->h->n_sys[s];
         const size_t off = (size_t)B->h->offset[0][s];
         std::vector<double> col(n), out(n);
@@ -1209,6 +1237,7 @@ extern "C" int sa_batch_rule_ratios(sa_ctx ctx, sa_batch B, const double *b, con
         dfree(db);
         dfree(dc);
         M->release();
+        if (s + 1 < S && hds[s + 1] != hds[s]) hds[s].reset();
     }
     return SA_OK;
     SA_GUARD_END
@@ -1240,6 +1269,39 @@ extern "C" int sa_batch_solve(sa_ctx ctx, sa_batch B, const sa_solver_params *p,
         if (converged) converged[q] = st.converged[q];
         if (final_bits) final_bits[q] = st.final_bit[q];
     }
+    return SA_OK;
+    SA_GUARD_END
+}
+
+extern "C" int sa_batch_level_op(sa_ctx ctx, sa_batch B, int level, int op, const int32_t *in, int32_t *out) {
+    if (!ctx || !B || !in || !out) return fail(SA_ERR_ARG, "null argument");
+    if (level < 0 || level >= B->h->Dmax || op < 0 || op > 4) return fail(SA_ERR_ARG, "no such operator/level");
+    SA_GUARD_BEGIN
+    Ctx &c = ctx->c;
+    int n = 0, m = 0;
+    B->eng->level_info(level, op, &n, &m, nullptr, nullptr);
+    const int R = B->eng->nrhs();
+    const size_t rows_in = (size_t)(op == 1 ? n : m), rows_out = (size_t)n;
+    Staged si(c, in, sizeof(int32_t) * std::max<size_t>(rows_in, 1) * R, true, false);
+    Staged so(c, out, sizeof(int32_t) * std::max<size_t>(rows_out, 1) * R, op == 1, true);
+    B->eng->level_op(level, op, (const int *)si.get(), (int *)so.get());
+    so.finish();
+    return SA_OK;
+    SA_GUARD_END
+}
+
+extern "C" int sa_batch_coarse_solve(sa_ctx ctx, sa_batch B) {
+    if (!ctx || !B) return fail(SA_ERR_ARG, "null argument");
+    SA_GUARD_BEGIN
+    B->eng->coarse_solve();
+    return SA_OK;
+    SA_GUARD_END
+}
+
+extern "C" int sa_batch_level_info(sa_batch B, int level, int op, int *n, int *m, int64_t *nnz, int *ncolours) {
+    if (!B || level < 0 || level >= B->h->Dmax || op < 0 || op > 4) return fail(SA_ERR_ARG, "no such operator/level");
+    SA_GUARD_BEGIN
+    B->eng->level_info(level, op, n, m, nnz, ncolours);
     return SA_OK;
     SA_GUARD_END
 }

@@ -31,6 +31,7 @@
 
 #include "../sagb_internal.hpp"
 #include "common.cuh"
+#include "stream.cuh"
 
 namespace sagb {
 
@@ -79,6 +80,32 @@ __device__ __forceinline__ void store_r(int *x, int row, const int (&v)[R]) {
 // ------------------------------------------------------------------ SpMV
 // y = A x (SET), y = z - A x (RESID) or y = A x + y (ADD), per row shift;
 // the same integer results as k_spmv_i32 for every right-hand side.
+template <int R, int MODE>
+__device__ __forceinline__ void bspmv_finish(const DBCsr &A, int row, const long long (&acc)[R], int *y,
+                                             const int *z, const int *row_sys, unsigned *pflag, unsigned *flags) {
+    const int bit = A.bit[row];
+    int out[R], zz[R], yy[R];
+    if (MODE == SPMV_RESID) load_r<R>(z, row, zz);
+    if (MODE == SPMV_ADD) load_rw<R>(y, row, yy);
+    bool any = false;
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+        const long long s = acc[r] >> bit;
+        bool ovf = !fits32(s);
+        long long v = (long long)lo32(s);
+        if (MODE == SPMV_RESID) v = (long long)zz[r] - v;
+        if (MODE == SPMV_ADD) v = v + (long long)yy[r];
+        ovf |= !fits32(v);
+        out[r] = lo32(v);
+        if (ovf) {
+            atomicOr(pflag + (size_t)row_sys[row] * R + r, ST_OVERFLOW);
+            any = true;
+        }
+    }
+    store_r<R>(y, row, out);
+    if (any) atomicOr(flags, ST_OVERFLOW);
+}
+
 template <int R, int G, int MODE>
 __global__ void __launch_bounds__(kBThreads)
 k_bspmv(DBCsr A, const int *__restrict__ x, int *__restrict__ y, const int *__restrict__ z,
@@ -102,29 +129,21 @@ k_bspmv(DBCsr A, const int *__restrict__ x, int *__restrict__ y, const int *__re
     for (int r = 0; r < R; r++)
 #pragma unroll
         for (int o = G / 2; o > 0; o >>= 1) acc[r] = wadd(acc[r], shfl_xor(acc[r], o));
-    if (lane == 0 && row < A.n) {
-        const int bit = A.bit[row];
-        int out[R], zz[R], yy[R];
-        if (MODE == SPMV_RESID) load_r<R>(z, row, zz);
-        if (MODE == SPMV_ADD) load_rw<R>(y, row, yy);
-        bool any = false;
+    if (lane == 0 && row < A.n) bspmv_finish<R, MODE>(A, row, acc, y, z, row_sys, pflag, flags);
+}
+
+// the same rows through the tile-staged stream (short rows, group 0)
+template <int R, int MODE>
+__global__ void __launch_bounds__(kStreamThreads)
+k_bspmv_stream(DBCsr A, const int *__restrict__ x, int *__restrict__ y, const int *__restrict__ z,
+               const int *__restrict__ row_sys, unsigned *__restrict__ pflag, unsigned *__restrict__ flags) {
+    long long acc[R];
 #pragma unroll
-        for (int r = 0; r < R; r++) {
-            const long long s = acc[r] >> bit;
-            bool ovf = !fits32(s);
-            long long v = (long long)lo32(s);
-            if (MODE == SPMV_RESID) v = (long long)zz[r] - v;
-            if (MODE == SPMV_ADD) v = v + (long long)yy[r];
-            ovf |= !fits32(v);
-            out[r] = lo32(v);
-            if (ovf) {
-                atomicOr(pflag + (size_t)row_sys[row] * R + r, ST_OVERFLOW);
-                any = true;
-            }
-        }
-        store_r<R>(y, row, out);
-        if (any) atomicOr(flags, ST_OVERFLOW);
-    }
+    for (int r = 0; r < R; r++) acc[r] = 0;
+    const int r0 = blockIdx.x * kStreamThreads;
+    stream_rows<R>(r0, min(A.n, r0 + kStreamThreads), A.rptr, A.cind, A.val, x, acc);
+    const int row = r0 + threadIdx.x;
+    if (row < A.n) bspmv_finish<R, MODE>(A, row, acc, y, z, row_sys, pflag, flags);
 }
 
 // --------------------------------------------------------- colour sweep
@@ -461,6 +480,46 @@ k_bspmv_dot(const BTile *__restrict__ tiles, DBCsr A, const int *__restrict__ z,
     }
 }
 
+// w = A z and acc[p][0] += V0 . w through the tile-staged stream; one CTA per
+// tile of at most kStreamThreads rows of one system
+template <int R>
+__global__ void __launch_bounds__(kStreamThreads)
+k_bspmv_dot_stream(const BTile *__restrict__ tiles, DBCsr A, const int *__restrict__ z, int *__restrict__ w,
+                   const int *__restrict__ v0, unsigned long long *acc, int m, unsigned *__restrict__ pflag,
+                   unsigned *__restrict__ flags) {
+    __shared__ long long sh[kStreamThreads / 32][R];
+    const BTile t = tiles[blockIdx.x];
+    long long a[R], dot[R];
+#pragma unroll
+    for (int r = 0; r < R; r++) a[r] = dot[r] = 0;
+    stream_rows<R>(t.row0, t.row1, A.rptr, A.cind, A.val, z, a);
+    const int row = t.row0 + threadIdx.x;
+    unsigned ovf = 0;
+    if (row < t.row1) {
+        const int bit = A.bit[row];
+        int y[R], vv[R];
+        load_r<R>(v0, row, vv);
+#pragma unroll
+        for (int r = 0; r < R; r++) {
+            const long long s = a[r] >> bit;
+            if (!fits32(s)) ovf |= 1u << r;
+            y[r] = lo32(s);
+            dot[r] = (long long)vv[r] * y[r];
+        }
+        store_r<R>(w, row, y);
+    }
+    bsum_i64<R>(dot, sh);
+    if (threadIdx.x == 0)
+#pragma unroll
+        for (int r = 0; r < R; r++) atomicAdd(acc + (size_t)(t.sys * R + r) * (m + 2), (unsigned long long)dot[r]);
+    if (ovf) {
+#pragma unroll
+        for (int r = 0; r < R; r++)
+            if (ovf & (1u << r)) atomicOr(pflag + (size_t)t.sys * R + r, ST_OVERFLOW);
+        atomicOr(flags, ST_OVERFLOW);
+    }
+}
+
 // MGS pass k of step j for every active pair: h = acc[k] >> bit, H[j][k] = h,
 // w += (int)((-h) V_k >> bit), then acc[k+1] += V_{k+1} . w (or w . w).
 template <int R, bool LAST>
@@ -717,7 +776,8 @@ struct DevBMat {
     signed char *bi = nullptr, *db = nullptr;
     void up(const BatchCsr &M) {
         d = dview(M, rp, ci, va, bi, db);
-        group = pick_group(M.n ? (double)M.nnz() / M.n : 1.0);
+        const double avg = M.n ? (double)M.nnz() / M.n : 1.0;
+        group = avg <= 32.0 ? 0 : pick_group(avg);  // 0: tile-staged stream
     }
     void release() {
         dfree(rp); dfree(ci); dfree(va); dfree(bi); dfree(db);
@@ -750,6 +810,8 @@ struct BatchEngine::Impl {
     DevCsr Af;
     std::vector<BTile> tiles_h;
     BTile *tiles = nullptr;
+    BTile *stiles = nullptr;  // tiles of at most kStreamThreads rows (stream SpMV + dot)
+    int nstiles = 0;
     int *tile_ptr = nullptr;
     int ntiles = 0;
     unsigned *pflag = nullptr;
@@ -782,7 +844,7 @@ struct BatchEngine::Impl {
             d.U.up(L.U);
             d.P.up(L.P);
             d.R.up(L.R);
-            // the colour pass reads a row's LD entries minus the diagonal
+            // the colour pass reads a row's LD entries minus the diagonal (no stream form)
             d.LD.group = pick_group(L.LD.n ? (double)(L.LD.nnz() - L.LD.n) / L.LD.n : 1.0);
             d.colour_rows = L.colour_rows.empty() ? nullptr : dupload(L.colour_rows);
             d.colour_ptr = L.colour_ptr;
@@ -844,6 +906,14 @@ struct BatchEngine::Impl {
         }
         ntiles = (int)tiles_h.size();
         tiles = dupload(tiles_h);
+        std::vector<BTile> st;
+        for (int s = 0; s < S; s++) {
+            const int off = h->offset[0][s], n = h->n_sys[s];
+            for (int r0 = 0; r0 < n; r0 += kStreamThreads)
+                st.push_back(BTile{s, off + r0, off + std::min(n, r0 + kStreamThreads), r0 == 0});
+        }
+        nstiles = (int)st.size();
+        stiles = dupload(st);
         tile_ptr = dupload(tp);
         pflag = (unsigned *)dmalloc(sizeof(unsigned) * (size_t)S * Rn);
         SAGB_CUDA(cudaMemset(pflag, 0, sizeof(unsigned) * (size_t)S * Rn));
@@ -893,7 +963,7 @@ struct BatchEngine::Impl {
         for (auto p : tmp) dfree(p);
         dfree(d_lu); dfree(Lcat); dfree(Ucat); dfree(dcat);
         Af.release();
-        dfree(tiles); dfree(tile_ptr); dfree(pflag); dfree(rvec); dfree(nrm); dfree(e0); dfree(npart);
+        dfree(tiles); dfree(stiles); dfree(tile_ptr); dfree(pflag); dfree(rvec); dfree(nrm); dfree(e0); dfree(npart);
         dfree(pairs); dfree(info_d);
         if (info_h) cudaFreeHost(info_h);
     }
@@ -919,6 +989,23 @@ struct BatchEngine::Impl {
 
     void bspmv(const DevBMat &M, const int *x, int *y, int mode, const int *z, const int *row_sys) {
         if (M.d.n == 0) return;
+        if (M.group == 0) {
+            const int blocks = (M.d.n + kStreamThreads - 1) / kStreamThreads;
+            by_r([&](auto RR) {
+                constexpr int R = decltype(RR)::value;
+                if (mode == SPMV_SET)
+                    k_bspmv_stream<R, SPMV_SET><<<blocks, kStreamThreads, 0, c.stream>>>(M.d, x, y, z, row_sys, pflag,
+                                                                                     c.d_flags);
+                else if (mode == SPMV_RESID)
+                    k_bspmv_stream<R, SPMV_RESID><<<blocks, kStreamThreads, 0, c.stream>>>(M.d, x, y, z, row_sys,
+                                                                                       pflag, c.d_flags);
+                else
+                    k_bspmv_stream<R, SPMV_ADD><<<blocks, kStreamThreads, 0, c.stream>>>(M.d, x, y, z, row_sys, pflag,
+                                                                                     c.d_flags);
+            });
+            c.launches++;
+            return;
+        }
         const long long threads = (long long)M.d.n * M.group;
         const int blocks = (int)((threads + kBThreads - 1) / kBThreads);
         by_r([&](auto RR) {
@@ -1030,11 +1117,16 @@ struct BatchEngine::Impl {
         const DevBMat &A0 = lv[0].A;
         by_r([&](auto RR) {
             constexpr int R = decltype(RR)::value;
-            by_g(A0.group, [&](auto GG) {
-                constexpr int G = decltype(GG)::value;
-                k_bspmv_dot<R, G><<<ntiles, kBThreads, 0, c.stream>>>(tiles, A0.d, Zj, w, V, pairs, acc, m, pflag,
-                                                                     c.d_flags);
-            });
+            if (A0.group == 0) {
+                k_bspmv_dot_stream<R><<<nstiles, kStreamThreads, 0, c.stream>>>(stiles, A0.d, Zj, w, V, acc, m, pflag,
+                                                                              c.d_flags);
+            } else {
+                by_g(A0.group, [&](auto GG) {
+                    constexpr int G = decltype(GG)::value;
+                    k_bspmv_dot<R, G><<<ntiles, kBThreads, 0, c.stream>>>(tiles, A0.d, Zj, w, V, pairs, acc, m,
+                                                                         pflag, c.d_flags);
+                });
+            }
             for (int k = 0; k <= j; k++) {
                 if (k < j)
                     k_bmgs<R, false><<<ntiles, kBThreads, 0, c.stream>>>(tiles, k, j, m, vs, V, w, pairs, acc, H);
@@ -1226,6 +1318,36 @@ int BatchEngine::group(int level, int op) const {
 }
 int BatchEngine::depth() const { return impl_->Dmax; }
 
+void BatchEngine::level_op(int level, int op, const int *in, int *out) {
+    Impl &I = *impl_;
+    if (level < 0 || level >= I.Dmax || op < 0 || op > 4) throw CudaError{"no such operator"};
+    DevBLevel &L = I.lv[level];
+    if (op == 1) return I.sweep(level, in, out);
+    const DevBMat &M = op == 0 ? L.A : op == 2 ? L.U : op == 3 ? L.P : L.R;
+    I.bspmv(M, in, out, SPMV_SET, nullptr, op == 4 ? L.row_sys_next : L.row_sys);
+}
+
+void BatchEngine::coarse_solve() {
+    Impl &I = *impl_;
+    if (!I.nlu) return;
+    I.by_r([&](auto RR) {
+        constexpr int R = decltype(RR)::value;
+        k_blu<R><<<I.nlu, kBLuThreads, I.lu_smem, I.c.stream>>>(I.d_lu, I.Lcat, I.Ucat, I.dcat, I.pflag, I.c.d_flags);
+    });
+    I.c.launches++;
+}
+
+void BatchEngine::level_info(int level, int op, int *n, int *m, int64_t *nnz, int *ncolours) const {
+    const Impl &I = *impl_;
+    if (level < 0 || level >= I.Dmax || op < 0 || op > 4) throw CudaError{"no such operator"};
+    const BatchLevel &L = I.h->lv[level];
+    const BatchCsr &M = op == 0 ? L.A : op == 1 ? L.LD : op == 2 ? L.U : op == 3 ? L.P : L.R;
+    if (n) *n = M.n;
+    if (m) *m = M.m;
+    if (nnz) *nnz = M.nnz();
+    if (ncolours) *ncolours = (int)L.colour_ptr.size() - 1;
+}
+
 // Autotuner: for every level operator, time each candidate lanes-per-row
 // value on the current vectors and keep the fastest (the SpMV and the colour
 // sweep have the same results for every value).
@@ -1238,7 +1360,7 @@ void BatchEngine::autotune(int reps) {
     int *xa = (int *)dmalloc(sizeof(int) * I.N0 * I.Rn), *xb = (int *)dmalloc(sizeof(int) * I.N0 * I.Rn);
     SAGB_CUDA(cudaMemset(xa, 0, sizeof(int) * I.N0 * I.Rn));
     SAGB_CUDA(cudaMemset(xb, 0, sizeof(int) * I.N0 * I.Rn));
-    const int cand[] = {1, 2, 4, 8, 16, 32};
+    const int cand[] = {0, 1, 2, 4, 8, 16, 32};  // 0: tile-staged stream (not for the colour sweep)
     for (int l = 0; l < I.Dmax; l++) {
         DevBLevel &L = I.lv[l];
         for (int op = 0; op < 5; op++) {
@@ -1247,6 +1369,7 @@ void BatchEngine::autotune(int reps) {
             float best = 1e30f;
             int bestg = M->group;
             for (int g : cand) {
+                if (g == 0 && op == 1) continue;
                 M->group = g;
                 auto run = [&] {
                     if (op == 1) I.sweep(l, xa, xb);

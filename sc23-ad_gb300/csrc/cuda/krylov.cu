@@ -20,6 +20,7 @@
 
 #include "../sagb_internal.hpp"
 #include "common.cuh"
+#include "stream.cuh"
 
 namespace sagb {
 
@@ -174,6 +175,28 @@ k_spmv_dot_i32(int n, const int *__restrict__ rptr, const int *__restrict__ cind
     long long d = 0;
     if (lane == 0 && row < n) {
         const long long s = a >> bit;
+        const int y = lo32(s);
+        if (!fits32(s)) atomicOr(flags, ST_OVERFLOW);
+        w[row] = y;
+        d = (long long)__ldg(v0 + row) * y;
+    }
+    d = block_sum(d, sh);
+    if (threadIdx.x == 0) atomicAdd(acc, (unsigned long long)d);
+}
+
+// the same through the tile-staged stream (short rows)
+__global__ void __launch_bounds__(kStreamThreads)
+k_spmv_dot_stream_i32(int n, const int *__restrict__ rptr, const int *__restrict__ cind, const int *__restrict__ val,
+                      const int *__restrict__ z, int *__restrict__ w, const int *__restrict__ v0, int bit,
+                      unsigned long long *acc, unsigned *flags) {
+    __shared__ long long sh[32];
+    long long a[1] = {0};
+    const int r0 = blockIdx.x * kStreamThreads;
+    stream_rows<1>(r0, min(n, r0 + kStreamThreads), rptr, cind, val, z, a);
+    const int row = r0 + threadIdx.x;
+    long long d = 0;
+    if (row < n) {
+        const long long s = a[0] >> bit;
         const int y = lo32(s);
         if (!fits32(s)) atomicOr(flags, ST_OVERFLOW);
         w[row] = y;
@@ -643,12 +666,18 @@ class IntSolver : public SolverBase {
             int *vj = V_ + (size_t)j * N, *zj = Z_ + (size_t)j * N, *w = V_ + (size_t)(j + 1) * N;
             StepInfo inf = step(j, [&] {
                 vcycle(c_, *M_, vj, zj);
-                by_group(A_->group, [&](auto G) {
-                    const long long thr = (long long)N * G.value;
-                    const int blocks = (int)((thr + kRedThreads - 1) / kRedThreads);
-                    k_spmv_dot_i32<G.value><<<blocks, kRedThreads, 0, c_.stream>>>(
-                        N, A_->rptr, A_->cind, (const int *)A_->val, zj, w, V_, A_->bit, acc_, c_.d_flags);
-                });
+                if (A_->group == 0) {
+                    k_spmv_dot_stream_i32<<<(N + kStreamThreads - 1) / kStreamThreads, kStreamThreads, 0,
+                                            c_.stream>>>(N, A_->rptr, A_->cind, (const int *)A_->val, zj, w, V_,
+                                                         A_->bit, acc_, c_.d_flags);
+                } else {
+                    by_group(A_->group, [&](auto G) {
+                        const long long thr = (long long)N * G.value;
+                        const int blocks = (int)((thr + kRedThreads - 1) / kRedThreads);
+                        k_spmv_dot_i32<G.value><<<blocks, kRedThreads, 0, c_.stream>>>(
+                            N, A_->rptr, A_->cind, (const int *)A_->val, zj, w, V_, A_->bit, acc_, c_.d_flags);
+                    });
+                }
                 for (int k = 0; k < j; k++)
                     k_mgs_i32<false><<<gb, kRedThreads, 0, c_.stream>>>(N, k, j, m, bit, V_, w, acc_, H_);
                 k_mgs_i32<true><<<gb, kRedThreads, 0, c_.stream>>>(N, j, j, m, bit, V_, w, acc_, H_);

@@ -11,6 +11,7 @@
 
 #include "../sagb_internal.hpp"
 #include "common.cuh"
+#include "stream.cuh"
 
 namespace sagb {
 
@@ -36,6 +37,10 @@ void DevCsr::release() {
     val = nullptr;
 }
 
+// integer matrices with at most this many entries per row on average use the
+// tile-staged stream kernel (group 0)
+constexpr double kStreamMaxAvg = 32.0;
+
 int pick_group(double avg) {
     // lanes per row: about the average row length, within [1, 32]
     int g = 1;
@@ -54,6 +59,7 @@ DevCsr upload_csr_i32(const CsrI &A) {
     d.cind = A.cind.empty() ? (int *)dmalloc(16) : dupload(A.cind);
     d.val = A.val.empty() ? dmalloc(16) : (void *)dupload(A.val);
     d.group = pick_group(A.n ? (double)d.nnz / A.n : 1.0);
+    if (A.n && (double)d.nnz / A.n <= kStreamMaxAvg) d.group = 0;  // tile-staged stream
     return d;
 }
 
@@ -148,6 +154,41 @@ k_spmv_fp(int n, const int *__restrict__ rptr, const int *__restrict__ cind, con
     }
 }
 
+// the same rows through the tile-staged stream (short rows)
+template <int MODE>
+__global__ void __launch_bounds__(kStreamThreads)
+k_spmv_stream_i32(int n, const int *__restrict__ rptr, const int *__restrict__ cind, const int *__restrict__ val,
+                  const int *__restrict__ x, int *__restrict__ y, const int *__restrict__ z, int bit,
+                  unsigned *__restrict__ flags) {
+    long long acc[1] = {0};
+    const int r0 = blockIdx.x * kStreamThreads;
+    stream_rows<1>(r0, min(n, r0 + kStreamThreads), rptr, cind, val, x, acc);
+    const int row = r0 + threadIdx.x;
+    if (row < n) {
+        const long long s = acc[0] >> bit;
+        bool ovf = !fits32(s);
+        long long v = (long long)lo32(s);
+        if (MODE == SPMV_RESID) v = (long long)z[row] - v;
+        if (MODE == SPMV_ADD) v = v + (long long)y[row];
+        ovf |= !fits32(v);
+        y[row] = lo32(v);
+        if (ovf) atomicOr(flags, ST_OVERFLOW);
+    }
+}
+
+static void launch_stream_i32(Ctx &c, const DevCsr &A, const void *x, void *y, int mode, const void *z) {
+    const int blocks = (A.n + kStreamThreads - 1) / kStreamThreads;
+    if (blocks == 0) return;
+    auto args = [&](auto kern) {
+        kern<<<blocks, kStreamThreads, 0, c.stream>>>(A.n, A.rptr, A.cind, (const int *)A.val, (const int *)x,
+                                                        (int *)y, (const int *)z, A.bit, c.d_flags);
+    };
+    if (mode == SPMV_SET) args(k_spmv_stream_i32<SPMV_SET>);
+    else if (mode == SPMV_RESID) args(k_spmv_stream_i32<SPMV_RESID>);
+    else args(k_spmv_stream_i32<SPMV_ADD>);
+    c.launches++;
+}
+
 template <int G>
 static void launch_i32(Ctx &c, const DevCsr &A, const void *x, void *y, int mode, const void *z) {
     const long long threads = (long long)A.n * G;
@@ -194,6 +235,7 @@ static void dispatch_fp(Ctx &c, const DevCsr &A, const void *x, void *y, int mod
 void spmv(Ctx &c, const DevCsr &A, const void *x, void *y, int mode, const void *z) {
     if (A.vt == VT_I32) {
         switch (A.group) {
+            case 0: return launch_stream_i32(c, A, x, y, mode, z);
             case 1: return launch_i32<1>(c, A, x, y, mode, z);
             case 2: return launch_i32<2>(c, A, x, y, mode, z);
             case 4: return launch_i32<4>(c, A, x, y, mode, z);

@@ -222,6 +222,10 @@ class BatchEngine {
     void autotune(int reps);
     void set_groups(int level, int op, int group);  // op: 0 A, 1 LD, 2 U, 3 P, 4 R
     int group(int level, int op) const;
+    // one operator of one level on caller vectors (op 1: the colour sweep LD^-1 in)
+    void level_op(int level, int op, const int *in, int *out);
+    void coarse_solve();  // the batched LU on the engine's own level vectors
+    void level_info(int level, int op, int *n, int *m, int64_t *nnz, int *ncolours) const;
 
   private:
     struct Impl;

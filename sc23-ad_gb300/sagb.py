@@ -128,6 +128,10 @@ SIGNATURES = {
     "sa_batch_group": (C.c_int, [VP, C.c_int, C.c_int, C.POINTER(C.c_int)]),
     "sa_batch_rule_ratios": (C.c_int, [VP, VP, VP, VP, F64P]),
     "sa_batch_solve": (C.c_int, [VP, VP, C.POINTER(SolverParams), I32P, VP, VP, VP, I32P, I32P, I32P]),
+    "sa_batch_level_op": (C.c_int, [VP, VP, C.c_int, C.c_int, VP, VP]),
+    "sa_batch_coarse_solve": (C.c_int, [VP, VP]),
+    "sa_batch_level_info": (C.c_int, [VP, C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                      C.POINTER(C.c_int64), C.POINTER(C.c_int)]),
 }
 
 _lib = None
@@ -653,6 +657,21 @@ class Batch:
         out = np.zeros(self.rows * self.nrhs, np.int32) if out is None else out
         check(lib().sa_batch_precondition(self.ctx.h, self.h, _arg(x), _arg(out)))
         return out
+
+    def level_info(self, level, op):
+        n, m, nnz, nc = C.c_int(), C.c_int(), C.c_int64(), C.c_int()
+        check(lib().sa_batch_level_info(self.h, level, op, C.byref(n), C.byref(m), C.byref(nnz), C.byref(nc)))
+        return n.value, m.value, nnz.value, nc.value
+
+    def level_op(self, level, op, x, out=None):
+        n, m, _, _ = self.level_info(level, op)
+        if out is None:
+            out = np.zeros(n * self.nrhs, np.int32)
+        check(lib().sa_batch_level_op(self.ctx.h, self.h, level, op, _arg(x), _arg(out)))
+        return out
+
+    def coarse_solve(self):
+        check(lib().sa_batch_coarse_solve(self.ctx.h, self.h))
 
     def autotune(self, reps=3):
         check(lib().sa_batch_autotune(self.ctx.h, self.h, reps))
