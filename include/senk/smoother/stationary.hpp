@@ -1,0 +1,3 @@
+// The reference header of the same path (Library/smoother/stationary.hpp) maps to the GPU facade.
+#pragma once
+#include "senk_gb300.hpp"
