@@ -47,7 +47,8 @@ def parse():
     ap.add_argument("--no-multicolor", action="store_true", help="skip the multicolour-smoother row")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-engine rows")
     ap.add_argument("--profile", action="store_true", help="skip extras (for profilers)")
-    ap.add_argument("--workload", choices=["poisson128", "batch256", "convdiff128"], default="poisson128",
+    ap.add_argument("--workload", choices=["poisson128", "batch256", "convdiff128", "precision"],
+                    default="poisson128",
                     help="poisson128: the headline; batch256: 256 27-point systems x 4 right-hand sides; "
                          "convdiff128: learned vs rule bits on convection-diffusion 128^3, Pe 50")
     ap.add_argument("--nsys", type=int, default=256)
@@ -861,6 +862,70 @@ def main_convdiff(a):
     dist.close()
 
 
+def main_precision(a):
+    """Precision split: int32 fixed-point inner solve with FP64 refinement,
+    FP32-mixed and FP64 AMG-FGMRES(30) (all with the bit-exact SOR smoother and
+    the reference's algorithms) on the two systems of the precision config.
+    Each solution is compared with the exact x* (b = A x*) and with an FP64
+    solve run to 1e-14."""
+    import sagb
+    dist = Dist(a.gpus)
+    ctx = sagb.Context(dist.local)
+    cases = [("varcoef3d_96_sigma2", sagb.GEN_VARCOEF3D, 96, 2.0), ("aniso2d_1024_eps1e-3", sagb.GEN_ANISO2D, 1024, 1e-3)]
+    rows = {}
+    for name, kind, n, prm in cases:
+        A = sagb.HostCsr.generate(kind, n, prm, seed=7)
+        xs, b = A.rhs(11)
+        A.lmax1_scaling(b)
+        r, c, v = A.arrays()
+        N = len(b)
+        nrm_b = float(np.linalg.norm(b))
+        t0 = time.time()
+        s_int = sagb.Setup(sagb.INT, r, c, v)
+        s64, s32 = s_int.derive(sagb.F64), s_int.derive(sagb.F32)
+        t_setup = time.time() - t0
+        M, M64, M32 = (sagb.Amg(ctx, p, setup=st) for p, st in ((sagb.INT, s_int), (sagb.F64, s64), (sagb.F32, s32)))
+        dA = sagb.Matrix(ctx, sagb.MAT_F64, r, c, v)
+        iA = sagb.Matrix(ctx, sagb.MAT_FIXED, r, c, v, bit=30)
+        fA = sagb.Matrix(ctx, sagb.MAT_F32, r, c, v)
+        bits = sagb.rule_bits(ctx, M64, b, nrm_b)
+        db = sagb.DeviceArray.from_host(ctx, b)
+        dx = sagb.DeviceArray(ctx, N, np.float64)
+
+        def run(prec, A_, M_, eps, fb=1):
+            S = sagb.Solver(ctx, prec, dA, A_, M_, sagb.solver_params(m=a.m, eps=eps, frac_bits=bits,
+                                                                      explicit_stop=1, overflow_fallback=fb))
+            dx.upload(np.zeros(N))
+            e0, e1 = sagb.Event(), sagb.Event()
+            e0.record(ctx)
+            it, cv = S.solve(db, nrm_b, dx)
+            e1.record(ctx)
+            ctx.sync()
+            _, flags = S.history()
+            nb = C.c_int()
+            sagb.check(sagb.lib().sa_solver_bits(S.h, C.byref(nb)))
+            S.close()
+            return it, cv, e0.elapsed_ms(e1) / 1000.0, dx.download(), flags, nb.value
+
+        *_, x_ref, _, _ = run(sagb.F64, dA, M64, 1e-14)
+        row = {"rows": N, "setup_s": t_setup, "rule_bits": bits}
+        for label, prec, A_, M_ in (("int_fp64ir", sagb.INT, iA, M), ("fp32_mixed", sagb.F32, fA, M32),
+                                    ("fp64", sagb.F64, dA, M64)):
+            it, cv, sec, x, flags, fbits = run(prec, A_, M_, 1e-10)
+            row[label] = {"iters": it, "converged": bool(cv), "seconds": sec,
+                          "explicit_res": explicit_res(r, c, v, b, x),
+                          "err_vs_xstar": float(np.linalg.norm(x - xs) / np.linalg.norm(xs)),
+                          "err_vs_fp64": float(np.linalg.norm(x - x_ref) / np.linalg.norm(x_ref)),
+                          "status_flags": flags, "final_bits": fbits if prec == sagb.INT else None}
+        rows[name] = row
+        for o in (M, M64, M32, dA, iA, fA, db, dx):
+            o.close()
+    if dist.rank == 0:
+        print(json.dumps({"workload": "precision split (int + FP64 IR / FP32-mixed / FP64), m=%d" % a.m, **rows}),
+              flush=True)
+    dist.close()
+
+
 if __name__ == "__main__":
     args = parse()
     if args.impl == "reference":
@@ -869,5 +934,7 @@ if __name__ == "__main__":
         main_batch(args)
     elif args.workload == "convdiff128":
         main_convdiff(args)
+    elif args.workload == "precision":
+        main_precision(args)
     else:
         main_ours(args)

@@ -88,3 +88,35 @@ def test_features_of_a_setup():
     # a floating-point setup has no integer operators to describe
     with pytest.raises(sagb.SagbError):
         sagb.setup_features(sagb.Setup(sagb.F64, r, c, v), 1.0)
+
+
+def test_trained_selector_gains_on_heldout_sweeps():
+    """The committed network, evaluated by the oracle's forward pass on the
+    held-out 20 % of the GPU sweep dataset, needs fewer integer iterations than
+    the reference's rule (a failed F costs the sweep's cap plus the rule)."""
+    import json
+    import os
+    d = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "sc23-ad_gb300", "data")
+    z = np.load(os.path.join(d, "bitsel_mlp.npz"))
+    ds = np.load(os.path.join(d, "bitsel_dataset.npz"))
+    X, meta = ds["X"].astype(np.float64), json.loads(str(ds["meta"]))
+    nin, hid, nout, f_lo = int(z["n_in"]), int(z["hidden"]), int(z["n_out"]), int(z["f_lo"])
+    ntr = int(round(0.8 * len(X)))
+    Y, _ = mo.forward(z["params"].astype(np.float64), X[ntr:], nin, hid, nout, z["mu"].astype(np.float64),
+                      z["sd"].astype(np.float64))
+    sel_it = rule_it = 0
+    fails_sel = fails_rule = 0
+    for k, y in enumerate(Y):
+        sw = {q["bit"]: q for q in meta[ntr + k]["sweep"]}
+        f = f_lo + int(np.argmin(y))
+        rule = sw[meta[ntr + k]["rule"]]
+        r_it = rule["iters"] if rule["converged"] else 120
+        fails_rule += not rule["converged"]
+        if sw[f]["converged"]:
+            sel_it += sw[f]["iters"]
+        else:
+            fails_sel += 1
+            sel_it += 120 + r_it
+        rule_it += r_it
+    assert fails_sel < fails_rule
+    assert sel_it < 0.95 * rule_it, (sel_it, rule_it)
