@@ -41,7 +41,7 @@ def _write_mm(path, r, c, v):
         f.write(f"{n} {n} {len(c)}\n")
         rows = np.repeat(np.arange(n), np.diff(r))
         for i, j, x in zip(rows, c, v):
-            f.write(f"{i + 1} {j + 1} {x!r}\n")
+            f.write(f"{int(i) + 1} {int(j) + 1} {float(x)!r}\n")
 
 
 @pytest.mark.gpu
