@@ -172,7 +172,7 @@ def learned_bits(ctx, setup_int, ratio):
     if not os.path.exists(bitsel.WEIGHTS):
         return None
     sel = bitsel.Selector(ctx)
-    f = sel.choose(sagb.setup_features(setup_int, ratio))
+    f = sel.choose(sagb.setup_features(setup_int, ratio), bitsel.rule_of(ratio))
     sel.net.close()
     return f
 
@@ -742,7 +742,7 @@ def main_batch(a):
     learned = None
     if os.path.exists(bitsel.WEIGHTS):
         sel = bitsel.Selector(ctx)
-        learned = [sel.choose(sagb.setup_features(B.system_setup(s), float(ratios[s * nrhs])))
+        learned = [sel.choose(sagb.setup_features(B.system_setup(s), float(ratios[s * nrhs])), rule[s])
                    for s in range(B.nsys)]
         sel.net.close()
         bits = learned

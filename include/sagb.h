@@ -38,6 +38,7 @@ extern "C" {
 #define SA_FLAG_TIMEOUT 2u        /* a bounded device-side wait ran out                          */
 #define SA_FLAG_DIVZERO 4u        /* zero Hessenberg / Givens denominator                        */
 #define SA_FLAG_NORM_OVERFLOW 8u  /* int64 sum of squares wrapped                                */
+#define SA_FLAG_PRECOND_OVERFLOW 16u /* an int32 result wrapped inside the V-cycle (FGMRES continues) */
 
 /* precisions */
 #define SA_INT 0 /* int32 fixed point, int64 accumulation (FGMRESflex/intAMGflex) */

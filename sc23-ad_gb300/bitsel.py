@@ -215,19 +215,30 @@ def load(ctx, path=WEIGHTS):
     return net, int(z["f_lo"])
 
 
+# the selector leaves the rule's F only when the network predicts at least this
+# much (log2 iterations) fewer iterations: on the held-out sweeps this keeps the
+# rule where it is already near best and still removes its failures
+MARGIN = 0.5
+
+
 class Selector:
-    """Learned F with the rule as fallback."""
+    """Learned F with the rule as default and as fallback."""
 
-    def __init__(self, ctx, path=WEIGHTS):
+    def __init__(self, ctx, path=WEIGHTS, margin=MARGIN):
         self.net, self.f_lo = load(ctx, path)
+        self.margin = margin
 
-    def choose(self, features):
-        return self.net.select_bits(features, self.f_lo)
+    def choose(self, features, rule=None):
+        y = self.net.predict(features)[0]
+        f = self.f_lo + int(np.argmin(y))
+        if rule is not None and F_LO <= rule <= F_HI and y[rule - self.f_lo] - y[f - self.f_lo] < self.margin:
+            return rule
+        return f
 
     def solve(self, prep, m=30):
         """Solve with the learned F; on overflow or failure, with the rule's F.
         Returns (bit used, iterations, converged, residual, seconds, fell_back)."""
-        f = self.choose(prep.features)
+        f = self.choose(prep.features, prep.rule)
         it, conv, res, sec, flags = prep.solve(f, m=m, fallback=0)
         if conv and res <= 1e-10:
             return f, it, conv, res, sec, False

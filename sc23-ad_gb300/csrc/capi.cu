@@ -154,6 +154,8 @@ extern "C" int sa_ctx_create(int device, sa_ctx *out) {
     SAGB_CUDA(cudaStreamCreateWithFlags(&h->c.stream, cudaStreamNonBlocking));
     h->c.d_flags = (unsigned *)dmalloc(sizeof(unsigned) * 4);
     SAGB_CUDA(cudaMemset(h->c.d_flags, 0, sizeof(unsigned) * 4));
+    h->c.d_flags_main = h->c.d_flags;
+    h->c.d_flags_prec = h->c.d_flags + 1;
     SAGB_CUDA(cudaMallocHost(&h->c.h_flags, sizeof(unsigned) * 4));
     init_kernel_attributes();
     *out = h;
@@ -164,7 +166,7 @@ extern "C" int sa_ctx_create(int device, sa_ctx *out) {
 extern "C" int sa_ctx_destroy(sa_ctx ctx) {
     if (!ctx) return SA_OK;
     cudaStreamSynchronize(ctx->c.stream);
-    dfree(ctx->c.d_flags);
+    dfree(ctx->c.d_flags_main);
     cudaFreeHost(ctx->c.h_flags);
     cudaStreamDestroy(ctx->c.stream);
     delete ctx;
@@ -182,12 +184,14 @@ extern "C" int sa_ctx_set_option(sa_ctx ctx, int option, int value) {
 extern "C" int sa_ctx_flags(sa_ctx ctx, unsigned *flags, int clear) {
     if (!ctx) return fail(SA_ERR_ARG, "null context");
     SA_GUARD_BEGIN
-    SAGB_CUDA(cudaMemcpyAsync(ctx->c.h_flags, ctx->c.d_flags, sizeof(unsigned), cudaMemcpyDeviceToHost,
+    SAGB_CUDA(cudaMemcpyAsync(ctx->c.h_flags, ctx->c.d_flags_main, 2 * sizeof(unsigned), cudaMemcpyDeviceToHost,
                               ctx->c.stream));
     SAGB_CUDA(cudaStreamSynchronize(ctx->c.stream));
-    if (flags) *flags = ctx->c.h_flags[0];
+    // word 1 (the V-cycle's kernels): an int32 wrap there is SA_FLAG_PRECOND_OVERFLOW
+    const unsigned w1 = ctx->c.h_flags[1];
+    if (flags) *flags = ctx->c.h_flags[0] | (w1 & ~ST_OVERFLOW) | ((w1 & ST_OVERFLOW) ? ST_PREC_OVF : 0u);
     if (clear) {
-        SAGB_CUDA(cudaMemsetAsync(ctx->c.d_flags, 0, sizeof(unsigned), ctx->c.stream));
+        SAGB_CUDA(cudaMemsetAsync(ctx->c.d_flags_main, 0, 2 * sizeof(unsigned), ctx->c.stream));
         SAGB_CUDA(cudaStreamSynchronize(ctx->c.stream));
     }
     return SA_OK;
@@ -855,7 +859,7 @@ extern "C" int sa_solver_solve(sa_solver S, const double *b, double nrm_b, doubl
         SAGB_CUDA(cudaMemcpyAsync(S->dx, x, bytes, cudaMemcpyHostToDevice, c.stream));
         dx = S->dx;
     }
-    SAGB_CUDA(cudaMemsetAsync(c.d_flags, 0, sizeof(unsigned), c.stream));
+    SAGB_CUDA(cudaMemsetAsync(c.d_flags_main, 0, 2 * sizeof(unsigned), c.stream));
     int it = S->S->solve(db, nrm_b, dx, S->last);
     if (hx) SAGB_CUDA(cudaMemcpyAsync(x, dx, bytes, cudaMemcpyDeviceToHost, c.stream));
     SAGB_CUDA(cudaStreamSynchronize(c.stream));
@@ -877,7 +881,7 @@ extern "C" int sa_solver_cycle(sa_solver S, const double *r, double nrm_b, doubl
     Staged sr(c, r, bytes, true, false);
     Staged sx(c, x, bytes, true, true);
     int conv = 0;
-    SAGB_CUDA(cudaMemsetAsync(c.d_flags, 0, sizeof(unsigned), c.stream));
+    SAGB_CUDA(cudaMemsetAsync(c.d_flags_main, 0, 2 * sizeof(unsigned), c.stream));
     int it = S->S->cycle((const double *)sr.get(), nrm_b, (double *)sx.get(), e0, &conv, dumps);
     if (it < 0) {
         sx.finish();

@@ -114,6 +114,7 @@ void smooth(Ctx &c, DevAmg &M, int l, const void *in, void *out, bool inited) {
 }
 
 void vcycle(Ctx &c, DevAmg &M, const void *in, void *out) {
+    PrecFlags pf(c);
     const int D = M.depth;
     smooth(c, M, 0, in, out, false);
     spmv(c, M.A0, out, M.r, SPMV_RESID, in);

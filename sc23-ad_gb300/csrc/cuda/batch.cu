@@ -196,6 +196,90 @@ k_bcolour(int cnt, const int *__restrict__ rows, DBCsr LD, const int *__restrict
     }
 }
 
+// ------------------------------------------------ cluster sweep (many colours)
+// The whole sweep of one level in one launch: cluster g (kClusterCtas CTAs on
+// as many SMs) owns a group of systems and walks their colours in order; the
+// hardware cluster barrier (release / acquire) separates consecutive colours,
+// so a level with hundreds of small colours costs one launch instead of one
+// per colour.  Dependencies are read through L2 (ld.global.cg): another SM of
+// the cluster wrote them in an earlier colour.
+constexpr int kClusterCtas = 8;
+
+__device__ __forceinline__ void cluster_barrier() {
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
+template <int R>
+__device__ __forceinline__ void load_cg(const int *x, int row, int (&v)[R]) {
+    if constexpr (R == 4) {
+        const int4 q = __ldcg(reinterpret_cast<const int4 *>(x) + row);
+        v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
+    } else if constexpr (R == 2) {
+        const int2 q = __ldcg(reinterpret_cast<const int2 *>(x) + row);
+        v[0] = q.x; v[1] = q.y;
+    } else {
+        v[0] = __ldcg(x + row);
+    }
+}
+
+template <int R, int G>
+__global__ void __launch_bounds__(kBThreads)
+k_bsweep_cluster(const int *__restrict__ gc_ptr, const int *__restrict__ cbound, const int *__restrict__ grows,
+                 DBCsr LD, const int *__restrict__ in, int *out, const int *__restrict__ row_sys,
+                 unsigned *__restrict__ pflag, unsigned *__restrict__ flags) {
+    const int g = blockIdx.x / kClusterCtas, rank = blockIdx.x % kClusterCtas;
+    const int t = rank * kBThreads + threadIdx.x;  // thread index inside the cluster
+    const int lane = t % G, slot = t / G;
+    constexpr int kSlots = kClusterCtas * kBThreads / G;  // rows in flight per pass
+    const int c0 = gc_ptr[g], c1 = gc_ptr[g + 1];
+    for (int k = c0; k + 1 < c1; k++) {
+        const int a = cbound[k], b = cbound[k + 1];
+        for (int base = a; base < b; base += kSlots) {
+            const int idx = base + slot;
+            long long acc[R];
+#pragma unroll
+            for (int r = 0; r < R; r++) acc[r] = 0;
+            int row = -1, dpos = 0;
+            if (idx < b) {
+                row = __ldg(grows + idx);
+                const int e0 = __ldg(LD.rptr + row);
+                dpos = __ldg(LD.rptr + row + 1) - 1;
+                for (int j = e0 + lane; j < dpos; j += G) {
+                    const long long v = __ldg(LD.val + j);
+                    int ov[R];
+                    load_cg<R>(out, __ldg(LD.cind + j), ov);
+#pragma unroll
+                    for (int r = 0; r < R; r++) acc[r] = wsub(acc[r], v * (long long)ov[r]);
+                }
+            }
+#pragma unroll
+            for (int r = 0; r < R; r++)
+#pragma unroll
+                for (int o = G / 2; o > 0; o >>= 1) acc[r] = wadd(acc[r], shfl_xor(acc[r], o));
+            if (lane == 0 && idx < b) {
+                const int bit = LD.bit[row], dbit = LD.dbit[row];
+                const long long dinv = __ldg(LD.val + dpos);
+                int iv[R], res[R];
+                load_rw<R>(in, row, iv);
+                bool any = false;
+#pragma unroll
+                for (int r = 0; r < R; r++) {
+                    const long long tt = wadd(wshl((long long)iv[r], bit), acc[r]);
+                    const long long sv = wmul(tt >> bit, dinv) >> dbit;
+                    res[r] = lo32(sv);
+                    if (!fits32(sv)) {
+                        atomicOr(pflag + (size_t)row_sys[row] * R + r, ST_OVERFLOW);
+                        any = true;
+                    }
+                }
+                store_r<R>(out, row, res);
+                if (any) atomicOr(flags, ST_OVERFLOW);
+            }
+        }
+        cluster_barrier();
+    }
+}
+
 // ------------------------------------------------------------ coarse LU
 struct BLuDesc {
     int n, sys;
@@ -793,6 +877,9 @@ struct DevBLevel {
     std::vector<int> colour_ptr;
     int *row_sys = nullptr;       // system of each row of this level
     int *row_sys_next = nullptr;  // ... and of level l+1 (rows of R)
+    // cluster sweep: groups of systems, each walking its own colours
+    int use_cluster = 0, ngroups = 0;
+    int *gc_ptr = nullptr, *cbound = nullptr, *grows = nullptr;
 };
 
 struct BatchEngine::Impl {
@@ -814,7 +901,9 @@ struct BatchEngine::Impl {
     int nstiles = 0;
     int *tile_ptr = nullptr;
     int ntiles = 0;
-    unsigned *pflag = nullptr;
+    unsigned *pflag = nullptr;       // per pair: status raised outside the preconditioner (fatal for a cycle)
+    unsigned *pflag_prec = nullptr;  // per pair: int32 wraps inside the V-cycle (reported)
+    unsigned *cur_pflag = nullptr;   // the array the launches of the moment report into
     // Krylov state (allocated for the largest m used)
     int *V = nullptr, *Z = nullptr;
     long long *H = nullptr, *cs = nullptr, *sn = nullptr, *e = nullptr;
@@ -849,6 +938,7 @@ struct BatchEngine::Impl {
             d.colour_rows = L.colour_rows.empty() ? nullptr : dupload(L.colour_rows);
             d.colour_ptr = L.colour_ptr;
         }
+        for (int l = 0; l < Dmax; l++) build_cluster_groups(l);
         for (int l = 0; l <= Dmax; l++) row_sys.push_back(dupload(h->row_sys[l]));
         for (int l = 0; l < Dmax; l++) {
             lv[l].row_sys = row_sys[l];
@@ -915,8 +1005,10 @@ struct BatchEngine::Impl {
         nstiles = (int)st.size();
         stiles = dupload(st);
         tile_ptr = dupload(tp);
-        pflag = (unsigned *)dmalloc(sizeof(unsigned) * (size_t)S * Rn);
-        SAGB_CUDA(cudaMemset(pflag, 0, sizeof(unsigned) * (size_t)S * Rn));
+        pflag = (unsigned *)dmalloc(sizeof(unsigned) * (size_t)S * Rn * 2);
+        SAGB_CUDA(cudaMemset(pflag, 0, sizeof(unsigned) * (size_t)S * Rn * 2));
+        pflag_prec = pflag + (size_t)S * Rn;
+        cur_pflag = pflag;
         rvec = (double *)dmalloc(sizeof(double) * N0 * Rn);
         nrm = (double *)dmalloc(sizeof(double) * (size_t)S * Rn);
         e0 = (double *)dmalloc(sizeof(double) * (size_t)S * Rn);
@@ -932,6 +1024,56 @@ struct BatchEngine::Impl {
             SAGB_CUDA(cudaFuncSetAttribute(k_blu<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
             attr = true;
         }
+    }
+
+    // Groups of the systems that smooth at level l, balanced by LD entries, one
+    // cluster each; rows of a group listed colour by colour.  The cluster sweep
+    // is the default where colours are small (many colours per row count).
+    void build_cluster_groups(int l) {
+        const BatchLevel &L = h->lv[l];
+        DevBLevel &d = lv[l];
+        std::vector<int> sys;
+        for (int s = 0; s < S; s++)
+            if (h->depth[s] > l) sys.push_back(s);
+        if (sys.empty()) return;
+        std::vector<long long> work(sys.size());
+        for (size_t k = 0; k < sys.size(); k++) work[k] = h->hi[sys[k]]->LD[l].nnz();
+        std::vector<size_t> idx(sys.size());
+        for (size_t k = 0; k < idx.size(); k++) idx[k] = k;
+        std::sort(idx.begin(), idx.end(), [&](size_t a, size_t b) { return work[a] > work[b]; });
+        const int G = std::max(1, std::min((int)sys.size(), 2 * c.num_sms / kClusterCtas));
+        std::vector<long long> load(G, 0);
+        std::vector<std::vector<int>> members(G);
+        for (size_t k : idx) {
+            const int g = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+            load[g] += work[k];
+            members[g].push_back(sys[k]);
+        }
+        std::vector<int> gc(1, 0), cb, rows;
+        for (int g = 0; g < G; g++) {
+            std::sort(members[g].begin(), members[g].end());
+            int nc = 0;
+            for (int s : members[g])
+                for (int cc : h->hi[s]->colour[l]) nc = std::max(nc, cc + 1);
+            for (int k = 0; k < nc; k++) {
+                cb.push_back((int)rows.size());
+                for (int s : members[g]) {
+                    const std::vector<int> &col = h->hi[s]->colour[l];
+                    const int off = h->offset[l][s];
+                    for (int i = 0; i < (int)col.size(); i++)
+                        if (col[i] == k) rows.push_back(off + i);
+                }
+            }
+            cb.push_back((int)rows.size());
+            gc.push_back((int)cb.size());
+        }
+        // gc[g]..gc[g+1]-1 index cb; colours of group g = gc[g+1] - gc[g] - 1
+        d.ngroups = G;
+        d.gc_ptr = dupload(gc);
+        d.cbound = dupload(cb);
+        d.grows = dupload(rows);
+        const int ncol = (int)L.colour_ptr.size() - 1;
+        d.use_cluster = ncol > 0 && (double)L.n_smooth / ncol < 16384.0;
     }
 
     void free_krylov() {
@@ -955,6 +1097,9 @@ struct BatchEngine::Impl {
         for (auto &d : lv) {
             d.A.release(); d.LD.release(); d.U.release(); d.P.release(); d.R.release();
             dfree(d.colour_rows);
+            dfree(d.gc_ptr);
+            dfree(d.cbound);
+            dfree(d.grows);
         }
         for (auto p : row_sys) dfree(p);
         for (auto p : ee) dfree(p);
@@ -994,13 +1139,13 @@ struct BatchEngine::Impl {
             by_r([&](auto RR) {
                 constexpr int R = decltype(RR)::value;
                 if (mode == SPMV_SET)
-                    k_bspmv_stream<R, SPMV_SET><<<blocks, kStreamThreads, 0, c.stream>>>(M.d, x, y, z, row_sys, pflag,
+                    k_bspmv_stream<R, SPMV_SET><<<blocks, kStreamThreads, 0, c.stream>>>(M.d, x, y, z, row_sys, cur_pflag,
                                                                                      c.d_flags);
                 else if (mode == SPMV_RESID)
                     k_bspmv_stream<R, SPMV_RESID><<<blocks, kStreamThreads, 0, c.stream>>>(M.d, x, y, z, row_sys,
-                                                                                       pflag, c.d_flags);
+                                                                                       cur_pflag, c.d_flags);
                 else
-                    k_bspmv_stream<R, SPMV_ADD><<<blocks, kStreamThreads, 0, c.stream>>>(M.d, x, y, z, row_sys, pflag,
+                    k_bspmv_stream<R, SPMV_ADD><<<blocks, kStreamThreads, 0, c.stream>>>(M.d, x, y, z, row_sys, cur_pflag,
                                                                                      c.d_flags);
             });
             c.launches++;
@@ -1013,11 +1158,11 @@ struct BatchEngine::Impl {
             by_g(M.group, [&](auto GG) {
                 constexpr int G = decltype(GG)::value;
                 if (mode == SPMV_SET)
-                    k_bspmv<R, G, SPMV_SET><<<blocks, kBThreads, 0, c.stream>>>(M.d, x, y, z, row_sys, pflag, c.d_flags);
+                    k_bspmv<R, G, SPMV_SET><<<blocks, kBThreads, 0, c.stream>>>(M.d, x, y, z, row_sys, cur_pflag, c.d_flags);
                 else if (mode == SPMV_RESID)
-                    k_bspmv<R, G, SPMV_RESID><<<blocks, kBThreads, 0, c.stream>>>(M.d, x, y, z, row_sys, pflag, c.d_flags);
+                    k_bspmv<R, G, SPMV_RESID><<<blocks, kBThreads, 0, c.stream>>>(M.d, x, y, z, row_sys, cur_pflag, c.d_flags);
                 else
-                    k_bspmv<R, G, SPMV_ADD><<<blocks, kBThreads, 0, c.stream>>>(M.d, x, y, z, row_sys, pflag, c.d_flags);
+                    k_bspmv<R, G, SPMV_ADD><<<blocks, kBThreads, 0, c.stream>>>(M.d, x, y, z, row_sys, cur_pflag, c.d_flags);
             });
         });
         c.launches++;
@@ -1025,6 +1170,30 @@ struct BatchEngine::Impl {
 
     void sweep(int l, const int *in, int *out) {
         const DevBLevel &L = lv[l];
+        if (L.use_cluster && L.ngroups > 0) {
+            cudaLaunchConfig_t cfg = {};
+            cfg.gridDim = dim3(L.ngroups * kClusterCtas);
+            cfg.blockDim = dim3(kBThreads);
+            cfg.stream = c.stream;
+            cudaLaunchAttribute at[1];
+            at[0].id = cudaLaunchAttributeClusterDimension;
+            at[0].val.clusterDim.x = kClusterCtas;
+            at[0].val.clusterDim.y = 1;
+            at[0].val.clusterDim.z = 1;
+            cfg.attrs = at;
+            cfg.numAttrs = 1;
+            by_r([&](auto RR) {
+                constexpr int R = decltype(RR)::value;
+                by_g(L.LD.group, [&](auto GG) {
+                    constexpr int G = decltype(GG)::value;
+                    SAGB_CUDA(cudaLaunchKernelEx(&cfg, k_bsweep_cluster<R, G>, (const int *)L.gc_ptr,
+                                                 (const int *)L.cbound, (const int *)L.grows, L.LD.d, in, out,
+                                                 (const int *)L.row_sys, cur_pflag, c.d_flags));
+                });
+            });
+            c.launches++;
+            return;
+        }
         const int nc = (int)L.colour_ptr.size() - 1;
         for (int k = 0; k < nc; k++) {
             const int a = L.colour_ptr[k], cnt = L.colour_ptr[k + 1] - a;
@@ -1036,7 +1205,7 @@ struct BatchEngine::Impl {
                 by_g(L.LD.group, [&](auto GG) {
                     constexpr int G = decltype(GG)::value;
                     k_bcolour<R, G><<<blocks, kBThreads, 0, c.stream>>>(cnt, L.colour_rows + a, L.LD.d, in, out,
-                                                                       L.row_sys, pflag, c.d_flags);
+                                                                       L.row_sys, cur_pflag, c.d_flags);
                 });
             });
             c.launches++;
@@ -1055,8 +1224,17 @@ struct BatchEngine::Impl {
         }
     }
 
-    // intAMGflex::Precondition (INTAMG.hpp:269-293) for the whole batch
+    // intAMGflex::Precondition (INTAMG.hpp:269-293) for the whole batch; int32
+    // wraps inside it go to the preconditioner's status arrays (FGMRES is
+    // flexible, so they cost convergence speed, not correctness)
     void vcycle(const int *in, int *out) {
+        PrecFlags guard(c);
+        cur_pflag = pflag_prec;
+        vcycle_body(in, out);
+        cur_pflag = pflag;
+    }
+
+    void vcycle_body(const int *in, int *out) {
         for (int l = 0; l < Dmax; l++) {
             const int *e_l = l == 0 ? in : ee[l];
             int *x_l = l == 0 ? out : xx[l];
@@ -1067,7 +1245,7 @@ struct BatchEngine::Impl {
         if (nlu) {
             by_r([&](auto RR) {
                 constexpr int R = decltype(RR)::value;
-                k_blu<R><<<nlu, kBLuThreads, lu_smem, c.stream>>>(d_lu, Lcat, Ucat, dcat, pflag, c.d_flags);
+                k_blu<R><<<nlu, kBLuThreads, lu_smem, c.stream>>>(d_lu, Lcat, Ucat, dcat, cur_pflag, c.d_flags);
             });
             c.launches++;
         }
@@ -1202,7 +1380,7 @@ struct BatchEngine::Impl {
         std::vector<double> prev(P, 0.0), hn(P);
         if (kp.m > 64) throw CudaError{"restart length above 64"};
         for (int p = 0; p < P; p++) bit[p] = bits_sys[p / Rn];
-        SAGB_CUDA(cudaMemsetAsync(pflag, 0, sizeof(unsigned) * P, c.stream));
+        SAGB_CUDA(cudaMemsetAsync(pflag, 0, sizeof(unsigned) * P * 2, c.stream));
         for (int outer = 0; outer < kp.max_outer; outer++) {
             residual(b, x);
             SAGB_CUDA(cudaMemcpyAsync(hn.data(), nrm, sizeof(double) * P, cudaMemcpyDeviceToHost, c.stream));
@@ -1234,7 +1412,7 @@ struct BatchEngine::Impl {
             st.restarts++;
             // status bits of the previous cycle (including those raised on
             // the vectors of pairs that had already stopped) are dropped
-            SAGB_CUDA(cudaMemsetAsync(pflag, 0, sizeof(unsigned) * P, c.stream));
+            SAGB_CUDA(cudaMemsetAsync(pflag, 0, sizeof(unsigned) * P * 2, c.stream));
             SAGB_CUDA(cudaMemcpyAsync(pairs, hp.data(), sizeof(BPair) * P, cudaMemcpyHostToDevice, c.stream));
             SAGB_CUDA(cudaMemcpyAsync(e0, nrm, sizeof(double) * P, cudaMemcpyDeviceToDevice, c.stream));
             k_bbegin<<<(P + 127) / 128, 128, 0, c.stream>>>(P, e0, kp.eps, pairs, e, acc, m);
@@ -1275,6 +1453,13 @@ struct BatchEngine::Impl {
                     st.converged[p] = 1;
                 }
             }
+        }
+        {
+            std::vector<unsigned> pp(P);
+            SAGB_CUDA(cudaMemcpyAsync(pp.data(), pflag_prec, sizeof(unsigned) * P, cudaMemcpyDeviceToHost, c.stream));
+            SAGB_CUDA(cudaStreamSynchronize(c.stream));
+            for (unsigned f : pp)
+                if (f & ST_OVERFLOW) st.flags |= ST_PREC_OVF;
         }
         // the last cycle's update has not been checked yet
         residual(b, x);
@@ -1368,6 +1553,20 @@ void BatchEngine::autotune(int reps) {
             if (M->d.n == 0) continue;
             float best = 1e30f;
             int bestg = M->group;
+            if (op == 1) {
+                // the sweep form first: one cluster launch per level or one launch per colour
+                float bt[2] = {0, 0};
+                for (int uc = 0; uc < 2; uc++) {
+                    L.use_cluster = uc;
+                    I.sweep(l, xa, xb);
+                    SAGB_CUDA(cudaEventRecord(e0, c.stream));
+                    for (int k = 0; k < reps; k++) I.sweep(l, xa, xb);
+                    SAGB_CUDA(cudaEventRecord(e1, c.stream));
+                    SAGB_CUDA(cudaEventSynchronize(e1));
+                    SAGB_CUDA(cudaEventElapsedTime(&bt[uc], e0, e1));
+                }
+                L.use_cluster = bt[1] < bt[0];
+            }
             for (int g : cand) {
                 if (g == 0 && op == 1) continue;
                 M->group = g;
@@ -1390,7 +1589,7 @@ void BatchEngine::autotune(int reps) {
             M->group = bestg;
         }
     }
-    SAGB_CUDA(cudaMemsetAsync(I.pflag, 0, sizeof(unsigned) * (size_t)I.S * I.Rn, c.stream));
+    SAGB_CUDA(cudaMemsetAsync(I.pflag, 0, sizeof(unsigned) * (size_t)I.S * I.Rn * 2, c.stream));
     SAGB_CUDA(cudaMemsetAsync(c.d_flags, 0, sizeof(unsigned), c.stream));
     SAGB_CUDA(cudaStreamSynchronize(c.stream));
     dfree(xa);

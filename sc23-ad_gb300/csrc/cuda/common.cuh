@@ -11,6 +11,7 @@ enum : unsigned {
     ST_TIMEOUT = 2u,       // a bounded wait ran out (dependency never published)
     ST_DIVZERO = 4u,       // Hessenberg / Givens denominator was zero
     ST_NORM_OVF = 8u,      // int64 sum of squares wrapped (negative)
+    ST_PREC_OVF = 16u,     // an int32 result wrapped inside the preconditioner (V-cycle)
 };
 
 // Time limit of every spin wait in device code (nanoseconds).

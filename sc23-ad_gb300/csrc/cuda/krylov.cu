@@ -241,6 +241,13 @@ __device__ long long ggen_i32(long long a, long long b, long long *c, long long 
 
 // blas1::int32::Nrm2 / lsqrt, the H reciprocal, Grot/Ggen and the e update
 // (gmres.hpp:325-334), then the convergence test (gmres.hpp:339)
+// the step's status: the main word, plus the V-cycle's word with its int32
+// wraps reported as ST_PREC_OVF (flags[0], flags[1] of the context)
+__device__ __forceinline__ unsigned step_flags(const unsigned *flags) {
+    const unsigned w0 = *(volatile const unsigned *)flags, w1 = *(volatile const unsigned *)(flags + 1);
+    return w0 | (w1 & ~ST_OVERFLOW) | ((w1 & ST_OVERFLOW) ? ST_PREC_OVF : 0u);
+}
+
 __global__ void k_givens_i32(int j, int m, int bit, long long *H, long long *c, long long *s, long long *e,
                              IScal *sc, unsigned long long *acc, StepInfo *info, unsigned *flags) {
     long long *Hj = H + (size_t)j * (m + 1);
@@ -270,7 +277,7 @@ __global__ void k_givens_i32(int j, int m, int bit, long long *H, long long *c, 
     for (int k = 0; k <= m + 1; k++) acc[k] = 0;
     info->conv = conv;
     info->relres = relres;
-    info->flags = *(volatile unsigned *)flags;
+    info->flags = step_flags(flags);
 }
 
 __global__ void k_scal_i32(int n, const IScal *__restrict__ sc, int bit, int *__restrict__ w) {
@@ -409,7 +416,7 @@ __global__ void k_givens_fp(int j, int m, T *H, T *c, T *s, T *e, FScal<T> *sc, 
     sc->relres = relres;
     info->conv = conv;
     info->relres = relres;
-    info->flags = *(volatile unsigned *)flags;
+    info->flags = step_flags(flags);
 }
 
 template <typename T>
@@ -533,6 +540,7 @@ class SolverBase : public Solver {
         double prev = 0;
         int iter = 0;
         st = SolveStats();
+        SAGB_CUDA(cudaMemsetAsync(c_.d_flags_main, 0, 2 * sizeof(unsigned), c_.stream));
         for (int i = 0; i < p_.max_outer; i++) {
             spmv_resid_f64_exact(c_, *dA_, x, b, r_);
             nrm2_f64_dev(c_, r_, N_, nrm_);
@@ -566,7 +574,7 @@ class SolverBase : public Solver {
                 }
                 set_bit(p_.bit - 1);
                 st.fallbacks++;
-                SAGB_CUDA(cudaMemsetAsync(c_.d_flags, 0, sizeof(unsigned), c_.stream));
+                SAGB_CUDA(cudaMemsetAsync(c_.d_flags_main, 0, 2 * sizeof(unsigned), c_.stream));
                 it = run_cycle(r_, nrm_, nrm_b, x, &conv, nullptr, st);
             }
             st.final_bit = p_.bit;

@@ -29,12 +29,27 @@ struct Ctx {
     int device = 0;
     int num_sms = 0;
     cudaStream_t stream = nullptr;
-    unsigned *d_flags = nullptr;     // device status bits (ST_* in common.cuh)
+    unsigned *d_flags = nullptr;     // device status bits (ST_* in common.cuh) of the current launches
+    unsigned *d_flags_main = nullptr;  // word 0: everything outside the preconditioner
+    unsigned *d_flags_prec = nullptr;  // word 1: the V-cycle's kernels (see PrecFlags)
     unsigned *h_flags = nullptr;     // pinned mirror
     bool fp_exact = false;           // FP kernels in sequential order without FMA
     bool use_graphs = true;
     long long launches = 0;          // kernels launched by this context (for reporting)
     std::string err;
+};
+
+// While alive, kernels launched on the context report into the preconditioner's
+// status word.  FGMRES is flexible: a wrapped value inside the V-cycle gives a
+// different (poorer) direction Z_j but leaves the Arnoldi relation A Z = V H
+// exact, so the solvers report such overflow (SA_FLAG_PRECOND_OVERFLOW) and
+// keep going, while overflow in A Z_j, the Gram-Schmidt sums or the Givens step
+// discards the cycle.
+struct PrecFlags {
+    Ctx &c;
+    unsigned *saved;
+    explicit PrecFlags(Ctx &ctx) : c(ctx), saved(ctx.d_flags) { c.d_flags = c.d_flags_prec; }
+    ~PrecFlags() { c.d_flags = saved; }
 };
 
 void *dmalloc(size_t bytes);

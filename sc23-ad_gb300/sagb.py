@@ -14,6 +14,7 @@ LIB_PATH = os.path.join(HERE, "_build", "libsagb.so")
 
 SA_OK, SA_ERR_ARG, SA_ERR_CUDA, SA_ERR_SETUP, SA_ERR_NUMERIC = 0, 1, 2, 3, 4
 FLAG_OVERFLOW, FLAG_TIMEOUT, FLAG_DIVZERO, FLAG_NORM_OVERFLOW = 1, 2, 4, 8
+FLAG_PRECOND_OVERFLOW = 16  # an int32 wrap inside the V-cycle (FGMRES continues)
 INT, F64, F32 = 0, 1, 2
 MAT_FIXED, MAT_FLEX, MAT_F64, MAT_F32 = 0, 1, 2, 3
 OP_A0, OP_CA, OP_P, OP_R, OP_LD, OP_U, OP_LUL, OP_LUU, OP_BJ, OP_COLOR = range(10)

@@ -33,7 +33,7 @@ def test_selector_beats_rule(ctx):
         nrm = float(np.linalg.norm(b))
         q = float(B.rule_ratios(np.concatenate([b, b]), [nrm, nrm])[0])
         rule = bitsel.rule_of(q)
-        f = sel.choose(sagb.setup_features(B.system_setup(0), q))
+        f = sel.choose(sagb.setup_features(B.system_setup(0), q), rule)
         x = np.zeros(B.rows)
         p = sagb.solver_params(m=30, max_outer=4, explicit_stop=1, overflow_fallback=0)
         it, cv, fb = B.solve(p, [f, rule], np.concatenate([b, b]), [nrm, nrm], x)

@@ -142,7 +142,7 @@ def test_int_overflow_detected_and_recovered(ctx):
     x = np.zeros(len(g["b_scaled"]))
     it, conv = S.solve(g["b_scaled"], float(g["nrm_b"][0]), x)
     hist, flags = S.history()
-    assert flags & (sagb.FLAG_OVERFLOW | sagb.FLAG_NORM_OVERFLOW | sagb.FLAG_DIVZERO)
+    assert flags & (sagb.FLAG_OVERFLOW | sagb.FLAG_NORM_OVERFLOW | sagb.FLAG_DIVZERO | sagb.FLAG_PRECOND_OVERFLOW)
     bits = C.c_int()
     sagb.check(sagb.lib().sa_solver_bits(S.h, C.byref(bits)))
     assert bits.value < 29
