@@ -71,10 +71,70 @@ __device__ __forceinline__ void load_rw(const int *x, int row, int (&v)[R]) {
     }
 }
 template <int R>
+__device__ __forceinline__ void load_cg_r(const int *x, int row, int (&v)[R]) {
+    if constexpr (R == 4) {
+        const int4 q = __ldcg(reinterpret_cast<const int4 *>(x) + row);
+        v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
+    } else if constexpr (R == 2) {
+        const int2 q = __ldcg(reinterpret_cast<const int2 *>(x) + row);
+        v[0] = q.x; v[1] = q.y;
+    } else {
+        v[0] = __ldcg(x + row);
+    }
+}
+template <int R>
 __device__ __forceinline__ void store_r(int *x, int row, const int (&v)[R]) {
     if constexpr (R == 4) reinterpret_cast<int4 *>(x)[row] = make_int4(v[0], v[1], v[2], v[3]);
     else if constexpr (R == 2) reinterpret_cast<int2 *>(x)[row] = make_int2(v[0], v[1]);
     else x[row] = v[0];
+}
+
+// Row sums with four entries per lane in flight: the column indices and
+// values of four entries are loaded together, then their four vector values,
+// so a long row costs about a quarter of the dependent round trips.  Integer
+// sums wrap, so the grouping does not change any result.
+//   SUB = false: acc += a_ij x_j (x through the read-only cache)
+//   SUB = true:  acc -= a_ij x_j (x written by earlier launches or colours:
+//                plain loads, or L2 loads when CG)
+template <int R, int G, bool SUB, bool CG>
+__device__ __forceinline__ void row_accumulate(const int *__restrict__ cind, const int *__restrict__ val, int e0,
+                                               int e1, int lane, const int *x, long long (&acc)[R]) {
+    int j = e0 + lane;
+    for (; j + 3 * G < e1; j += 4 * G) {
+        int cc[4];
+        long long vv[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            cc[q] = __ldg(cind + j + q * G);
+            vv[q] = __ldg(val + j + q * G);
+        }
+        int xv[4][R];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            if constexpr (!SUB) load_r<R>(x, cc[q], xv[q]);
+            else if constexpr (CG) load_cg_r<R>(x, cc[q], xv[q]);
+            else load_rw<R>(x, cc[q], xv[q]);
+        }
+#pragma unroll
+        for (int q = 0; q < 4; q++)
+#pragma unroll
+            for (int r = 0; r < R; r++) {
+                if constexpr (SUB) acc[r] = wsub(acc[r], vv[q] * (long long)xv[q][r]);
+                else acc[r] = wadd(acc[r], vv[q] * (long long)xv[q][r]);
+            }
+    }
+    for (; j < e1; j += G) {
+        const long long v = __ldg(val + j);
+        int xv[R];
+        if constexpr (!SUB) load_r<R>(x, __ldg(cind + j), xv);
+        else if constexpr (CG) load_cg_r<R>(x, __ldg(cind + j), xv);
+        else load_rw<R>(x, __ldg(cind + j), xv);
+#pragma unroll
+        for (int r = 0; r < R; r++) {
+            if constexpr (SUB) acc[r] = wsub(acc[r], v * (long long)xv[r]);
+            else acc[r] = wadd(acc[r], v * (long long)xv[r]);
+        }
+    }
 }
 
 // ------------------------------------------------------------------ SpMV
@@ -115,16 +175,8 @@ k_bspmv(DBCsr A, const int *__restrict__ x, int *__restrict__ y, const int *__re
     long long acc[R];
 #pragma unroll
     for (int r = 0; r < R; r++) acc[r] = 0;
-    if (row < A.n) {
-        const int a = __ldg(A.rptr + row), b = __ldg(A.rptr + row + 1);
-        for (int j = a + lane; j < b; j += G) {
-            const long long v = __ldg(A.val + j);
-            int xv[R];
-            load_r<R>(x, __ldg(A.cind + j), xv);
-#pragma unroll
-            for (int r = 0; r < R; r++) acc[r] = wadd(acc[r], v * (long long)xv[r]);
-        }
-    }
+    if (row < A.n) row_accumulate<R, G, false, false>(A.cind, A.val, __ldg(A.rptr + row), __ldg(A.rptr + row + 1),
+                                                      lane, x, acc);
 #pragma unroll
     for (int r = 0; r < R; r++)
 #pragma unroll
@@ -161,15 +213,8 @@ k_bcolour(int cnt, const int *__restrict__ rows, DBCsr LD, const int *__restrict
     int row = -1, dpos = 0;
     if (k < cnt) {
         row = __ldg(rows + k);
-        const int a = __ldg(LD.rptr + row);
         dpos = __ldg(LD.rptr + row + 1) - 1;
-        for (int j = a + lane; j < dpos; j += G) {
-            const long long v = __ldg(LD.val + j);
-            int ov[R];
-            load_rw<R>(out, __ldg(LD.cind + j), ov);
-#pragma unroll
-            for (int r = 0; r < R; r++) acc[r] = wsub(acc[r], v * (long long)ov[r]);
-        }
+        row_accumulate<R, G, true, false>(LD.cind, LD.val, __ldg(LD.rptr + row), dpos, lane, out, acc);
     }
 #pragma unroll
     for (int r = 0; r < R; r++)
@@ -209,18 +254,6 @@ __device__ __forceinline__ void cluster_barrier() {
     asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
 }
 
-template <int R>
-__device__ __forceinline__ void load_cg(const int *x, int row, int (&v)[R]) {
-    if constexpr (R == 4) {
-        const int4 q = __ldcg(reinterpret_cast<const int4 *>(x) + row);
-        v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
-    } else if constexpr (R == 2) {
-        const int2 q = __ldcg(reinterpret_cast<const int2 *>(x) + row);
-        v[0] = q.x; v[1] = q.y;
-    } else {
-        v[0] = __ldcg(x + row);
-    }
-}
 
 template <int R, int G>
 __global__ void __launch_bounds__(kBThreads)
@@ -242,15 +275,8 @@ k_bsweep_cluster(const int *__restrict__ gc_ptr, const int *__restrict__ cbound,
             int row = -1, dpos = 0;
             if (idx < b) {
                 row = __ldg(grows + idx);
-                const int e0 = __ldg(LD.rptr + row);
                 dpos = __ldg(LD.rptr + row + 1) - 1;
-                for (int j = e0 + lane; j < dpos; j += G) {
-                    const long long v = __ldg(LD.val + j);
-                    int ov[R];
-                    load_cg<R>(out, __ldg(LD.cind + j), ov);
-#pragma unroll
-                    for (int r = 0; r < R; r++) acc[r] = wsub(acc[r], v * (long long)ov[r]);
-                }
+                row_accumulate<R, G, true, true>(LD.cind, LD.val, __ldg(LD.rptr + row), dpos, lane, out, acc);
             }
 #pragma unroll
             for (int r = 0; r < R; r++)
@@ -524,16 +550,8 @@ k_bspmv_dot(const BTile *__restrict__ tiles, DBCsr A, const int *__restrict__ z,
         long long a[R];
 #pragma unroll
         for (int r = 0; r < R; r++) a[r] = 0;
-        if (row < t.row1) {
-            const int b0 = __ldg(A.rptr + row), b1 = __ldg(A.rptr + row + 1);
-            for (int j = b0 + lane; j < b1; j += G) {
-                const long long v = __ldg(A.val + j);
-                int zv[R];
-                load_r<R>(z, __ldg(A.cind + j), zv);
-#pragma unroll
-                for (int r = 0; r < R; r++) a[r] = wadd(a[r], v * (long long)zv[r]);
-            }
-        }
+        if (row < t.row1)
+            row_accumulate<R, G, false, false>(A.cind, A.val, __ldg(A.rptr + row), __ldg(A.rptr + row + 1), lane, z, a);
 #pragma unroll
         for (int r = 0; r < R; r++)
 #pragma unroll

@@ -107,8 +107,17 @@ k_spmv_i32(int n, const int *__restrict__ rptr, const int *__restrict__ cind, co
     long long acc = 0;
     if (row < n) {
         const int a = __ldg(rptr + row), b = __ldg(rptr + row + 1);
-        for (int j = a + lane; j < b; j += G)
-            acc = wadd(acc, (long long)__ldg(val + j) * (long long)__ldg(x + __ldg(cind + j)));
+        int j = a + lane;
+        // four entries per lane in flight (integer sums wrap: any order gives the same result)
+        for (; j + 3 * G < b; j += 4 * G) {
+            const int c0 = __ldg(cind + j), c1 = __ldg(cind + j + G), c2 = __ldg(cind + j + 2 * G),
+                      c3 = __ldg(cind + j + 3 * G);
+            const long long v0 = __ldg(val + j), v1 = __ldg(val + j + G), v2 = __ldg(val + j + 2 * G),
+                            v3 = __ldg(val + j + 3 * G);
+            const long long x0 = __ldg(x + c0), x1 = __ldg(x + c1), x2 = __ldg(x + c2), x3 = __ldg(x + c3);
+            acc = wadd(acc, wadd(wadd(v0 * x0, v1 * x1), wadd(v2 * x2, v3 * x3)));
+        }
+        for (; j < b; j += G) acc = wadd(acc, (long long)__ldg(val + j) * (long long)__ldg(x + __ldg(cind + j)));
     }
 #pragma unroll
     for (int o = G / 2; o > 0; o >>= 1) acc = wadd(acc, shfl_xor(acc, o));
