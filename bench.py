@@ -47,7 +47,7 @@ def parse():
     ap.add_argument("--no-multicolor", action="store_true", help="skip the multicolour-smoother row")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-engine rows")
     ap.add_argument("--profile", action="store_true", help="skip extras (for profilers)")
-    ap.add_argument("--workload", choices=["poisson128", "batch256", "convdiff128", "precision"],
+    ap.add_argument("--workload", choices=["poisson128", "batch256", "convdiff128", "precision", "vcycle"],
                     default="poisson128",
                     help="poisson128: the headline; batch256: 256 27-point systems x 4 right-hand sides; "
                          "convdiff128: learned vs rule bits on convection-diffusion 128^3, Pe 50")
@@ -862,6 +862,31 @@ def main_convdiff(a):
     dist.close()
 
 
+def main_vcycle(a):
+    """Profiling aid: the headline's batched V-cycle (autotuned) on the 128^3
+    system (--n), --steps V-cycles inside a profiler collection range (run
+    under a profiler started with collection off)."""
+    import sagb
+    ctx = sagb.Context(0)
+    r, c, v, b = build_system(a.n, seed=1)
+    B = sagb.Batch(ctx, [(r, c, v)], 1)
+    B.autotune(2)
+    x = sagb.DeviceArray.from_host(ctx, np.random.default_rng(3).integers(-(1 << 28), 1 << 28, size=B.rows)
+                                   .astype(np.int32))
+    y = sagb.DeviceArray(ctx, B.rows, np.int32)
+    for _ in range(a.warmup):
+        B.precondition(x, y)
+    ctx.sync()
+    l0 = ctx.launches()
+    sagb.check(sagb.lib().sa_profiler_range(1))
+    for _ in range(a.steps):
+        B.precondition(x, y)
+    ctx.sync()
+    sagb.check(sagb.lib().sa_profiler_range(0))
+    print(json.dumps({"workload": f"batched V-cycle, Poisson {a.n}^3", "vcycles": a.steps,
+                      "launches": ctx.launches() - l0}), flush=True)
+
+
 def main_precision(a):
     """Precision split: int32 fixed-point inner solve with FP64 refinement,
     FP32-mixed and FP64 AMG-FGMRES(30) (all with the bit-exact SOR smoother and
@@ -936,5 +961,7 @@ if __name__ == "__main__":
         main_convdiff(args)
     elif args.workload == "precision":
         main_precision(args)
+    elif args.workload == "vcycle":
+        main_vcycle(args)
     else:
         main_ours(args)

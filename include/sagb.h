@@ -310,6 +310,10 @@ int sa_batch_level_info(sa_batch B, int level, int op, int *n, int *m, int64_t *
 int sa_batch_solve(sa_ctx ctx, sa_batch B, const sa_solver_params *p, const int *bits, const double *b,
                    const double *nrm_b, double *x, int *iters, int *converged, int *final_bits);
 
+/* start (on = 1) or stop (0) the profiler's collection range: a profiler
+ * started with collection off records only the launches in between */
+int sa_profiler_range(int on);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,4 +1,5 @@
 // C ABI (include/sagb.h) over the host setup and the CUDA kernels.
+#include <cuda_profiler_api.h>
 #include <cuda_runtime.h>
 
 #include <atomic>
@@ -1306,6 +1307,15 @@ extern "C" int sa_batch_level_info(sa_batch B, int level, int op, int *n, int *m
     if (!B || level < 0 || level >= B->h->Dmax || op < 0 || op > 4) return fail(SA_ERR_ARG, "no such operator/level");
     SA_GUARD_BEGIN
     B->eng->level_info(level, op, n, m, nnz, ncolours);
+    return SA_OK;
+    SA_GUARD_END
+}
+
+// ------------------------------------------------------------- profiling
+
+extern "C" int sa_profiler_range(int on) {
+    SA_GUARD_BEGIN
+    SAGB_CUDA(on ? cudaProfilerStart() : cudaProfilerStop());
     return SA_OK;
     SA_GUARD_END
 }

@@ -129,6 +129,7 @@ SIGNATURES = {
     "sa_batch_group": (C.c_int, [VP, C.c_int, C.c_int, C.POINTER(C.c_int)]),
     "sa_batch_rule_ratios": (C.c_int, [VP, VP, VP, VP, F64P]),
     "sa_batch_solve": (C.c_int, [VP, VP, C.POINTER(SolverParams), I32P, VP, VP, VP, I32P, I32P, I32P]),
+    "sa_profiler_range": (C.c_int, [C.c_int]),
     "sa_batch_level_op": (C.c_int, [VP, VP, C.c_int, C.c_int, VP, VP]),
     "sa_batch_coarse_solve": (C.c_int, [VP, VP]),
     "sa_batch_level_info": (C.c_int, [VP, C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
