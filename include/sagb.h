@@ -95,6 +95,8 @@ typedef struct {
     int smooth_iter;     /* SORParam::iter (1)                                                        */
     int multicolor;      /* 1: SOR in greedy-colour order (ldtri::MCCSR, matrix/trispmat.hpp:597-640,
                             colouring helper/helper_graph.hpp:191-219); 0: natural order (default) */
+    int max_colours;     /* multicolour: cap on the colours per level, rows beyond it join their least
+                            conflicting colour (Jacobi-like inside it); 0: no cap (default) */
 } sa_amg_params;
 
 typedef struct {

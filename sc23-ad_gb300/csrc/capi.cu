@@ -475,6 +475,7 @@ extern "C" void sa_amg_params_default(sa_amg_params *p) {
     p->omega = 1.0;
     p->smooth_iter = 1;
     p->multicolor = 0;
+    p->max_colours = 0;
 }
 
 static void build_setup(sa_hierarchy &s, const CsrD &A) {
@@ -486,6 +487,7 @@ static void build_setup(sa_hierarchy &s, const CsrD &A) {
     sm.omega = s.p.omega;
     sm.iter = s.p.smooth_iter;
     sm.multicolor = s.p.multicolor;
+    sm.max_colours = s.p.max_colours;
     if (s.precision == SA_INT) s.hi = std::make_shared<IntHierarchy>(build_int_hierarchy(A, chain, sm));
     else if (s.precision == SA_F64) s.hd = std::make_shared<FpHierarchy<double>>(build_f64_hierarchy(A, chain, sm));
     else s.hf = std::make_shared<FpHierarchy<float>>(build_f32_hierarchy(A, chain, sm));
@@ -501,7 +503,8 @@ extern "C" int sa_setup_create(int precision, const sa_amg_params *p, int n, con
     if (p) s->p = *p;
     else sa_amg_params_default(&s->p);
     if (s->p.smooth_iter < 1 || s->p.max_levels < 1 || s->p.smoother_blocks < 0 ||
-        s->p.multicolor < 0 || s->p.multicolor > 1 || (s->p.multicolor && s->p.smoother_blocks)) {
+        s->p.multicolor < 0 || s->p.multicolor > 1 || (s->p.multicolor && s->p.smoother_blocks) ||
+        s->p.max_colours < 0) {
         delete s;
         return fail(SA_ERR_ARG, "invalid AMG parameters");
     }
@@ -1106,7 +1109,7 @@ extern "C" int sa_batch_create(sa_ctx ctx, int nsys, const int *n, const int32_t
     B->p = q;
     try {
         B->h = std::make_shared<BatchHierarchy>(
-            build_batch(sys, q.theta, q.max_levels, q.omega, q.smooth_iter, threads, src));
+            build_batch(sys, q.theta, q.max_levels, q.omega, q.smooth_iter, threads, src, q.max_colours));
         SAGB_CUDA(cudaSetDevice(ctx->c.device));
         B->eng = std::make_unique<BatchEngine>(ctx->c, B->h, nrhs);
         SAGB_CUDA(cudaDeviceSynchronize());
@@ -1194,6 +1197,7 @@ extern "C" int sa_batch_rule_ratios(sa_ctx ctx, sa_batch B, const double *b, con
     sm.omega = B->p.omega;
     sm.iter = B->p.smooth_iter;
     sm.multicolor = 1;
+    sm.max_colours = B->p.max_colours;
     // FP64 hierarchies of all systems on host threads (copies of one matrix share one)
     std::vector<std::shared_ptr<FpHierarchy<double>>> hds(S);
     {

@@ -658,7 +658,7 @@ CsrI to_dutri_flex(const CsrD &DinvU) {
 
 // ================================================================= hierarchies
 
-std::vector<int> greedy_colouring(const CsrD &A, int *ncolors) {
+std::vector<int> greedy_colouring(const CsrD &A, int *ncolors, int max_colours) {
     const int N = A.n;
     // symmetrised adjacency without the diagonal
     std::vector<int> deg(N, 0);
@@ -682,7 +682,7 @@ std::vector<int> greedy_colouring(const CsrD &A, int *ncolors) {
     // neighbour of colour k yet
     std::vector<int> col(N, -1);
     int k = 0, left = N;
-    while (left > 0) {
+    while (left > 0 && (max_colours <= 0 || k < max_colours)) {
         for (int i = 0; i < N; i++) {
             if (col[i] >= 0) continue;
             bool adjacent = false;
@@ -696,6 +696,19 @@ std::vector<int> greedy_colouring(const CsrD &A, int *ncolors) {
             left--;
         }
         k++;
+    }
+    if (left > 0) {
+        // capped: every remaining row takes the colour with the fewest coloured
+        // neighbours (lowest colour on ties); its same-colour couplings then act
+        // through U, i.e. Jacobi-like within the colour
+        std::vector<int> cnt(k, 0);
+        for (int i = 0; i < N; i++) {
+            if (col[i] >= 0) continue;
+            std::fill(cnt.begin(), cnt.end(), 0);
+            for (int t = ap[i]; t < ap[i + 1]; t++)
+                if (col[adj[t]] >= 0) cnt[col[adj[t]]]++;
+            col[i] = (int)(std::min_element(cnt.begin(), cnt.end()) - cnt.begin());
+        }
     }
     if (ncolors) *ncolors = k;
     return col;
@@ -749,7 +762,7 @@ static void smoother_split(const CsrD &A, const SmootherSpec &sm, CsrD &LD, CsrD
     bj.clear();
     if (sm.multicolor) {
         int nc = 0;
-        colour = greedy_colouring(A, &nc);
+        colour = greedy_colouring(A, &nc, sm.max_colours);
         mc_sor_split(A, sm.omega, colour, LD, U);
     } else if (sm.block > 0) {
         block_sor_split(A, sm.omega, sm.block, LD, U, bj);

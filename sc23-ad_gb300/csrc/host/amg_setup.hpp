@@ -73,12 +73,16 @@ struct SmootherSpec {
     double omega = 1.0;
     int iter = 1;
     int multicolor = 0;  // 1: SOR in colour order (the multicolour variant)
+    int max_colours = 0; // multicolour: at most this many colours (0: as many as a proper colouring needs)
 };
 
 // Greedy colouring, colour by colour, on the symmetrised pattern (the
 // reference's coloring_greedy, Library/helper/helper_graph.hpp:191-219).
-// Returns 0-based colours; *ncolors set.
-std::vector<int> greedy_colouring(const CsrD &A, int *ncolors);
+// Returns 0-based colours; *ncolors set.  With max_colours > 0 the colouring
+// stops after that many colours and the remaining rows join the colour where
+// they have the fewest neighbours (no longer a proper colouring: within a
+// colour those couplings are then applied Jacobi-like through U).
+std::vector<int> greedy_colouring(const CsrD &A, int *ncolors, int max_colours = 0);
 // SOR split in colour order: LD = couplings to earlier colours + diag/omega
 // (diagonal last), U = (1 - 1/omega) diag first + couplings to later colours.
 // GS with this split is ldtri::MCCSRflex (ldtri.hpp:635-700) without renumbering.

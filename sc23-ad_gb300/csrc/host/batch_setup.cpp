@@ -29,7 +29,7 @@ static void start(BatchCsr &B, int m) {
 static int level_size(const IntHierarchy &h, int l) { return l == 0 ? h.A0.n : h.R[l - 1].n; }
 
 BatchHierarchy build_batch(const std::vector<CsrD> &systems, double theta, int max_levels, double omega,
-                           int smooth_iter, int threads, const std::vector<int> &src_in) {
+                           int smooth_iter, int threads, const std::vector<int> &src_in, int max_colours) {
     BatchHierarchy B;
     const int S = (int)systems.size();
     if (S == 0) throw SetupError{"empty batch"};
@@ -51,6 +51,7 @@ BatchHierarchy build_batch(const std::vector<CsrD> &systems, double theta, int m
     sm.omega = omega;
     sm.iter = smooth_iter;
     sm.multicolor = 1;
+    sm.max_colours = max_colours;
     std::atomic<int> next{0};
     std::vector<std::string> errs(S);
     auto work = [&]() {

@@ -34,7 +34,8 @@ class CsrView(C.Structure):
 
 class AmgParams(C.Structure):
     _fields_ = [("max_levels", C.c_int), ("theta", C.c_double), ("smoother_blocks", C.c_int),
-                ("omega", C.c_double), ("smooth_iter", C.c_int), ("multicolor", C.c_int)]
+                ("omega", C.c_double), ("smooth_iter", C.c_int), ("multicolor", C.c_int),
+                ("max_colours", C.c_int)]
 
 
 class SolverParams(C.Structure):
@@ -244,8 +245,8 @@ class HostCsr:
     __del__ = close
 
 
-def amg_params(max_levels=20, theta=0.8, smoother_blocks=0, omega=1.0, smooth_iter=1, multicolor=0):
-    return AmgParams(max_levels, theta, smoother_blocks, omega, smooth_iter, multicolor)
+def amg_params(max_levels=20, theta=0.8, smoother_blocks=0, omega=1.0, smooth_iter=1, multicolor=0, max_colours=0):
+    return AmgParams(max_levels, theta, smoother_blocks, omega, smooth_iter, multicolor, max_colours)
 
 
 class Setup:
@@ -627,7 +628,15 @@ class Mlp:
 
 
 class Batch:
-    """Many systems (already scaled), nrhs right-hand sides each, solved together."""
+    """Many systems (already scaled), nrhs right-hand sides each, solved together.
+
+    The default parameters cap the colours of every level at 8: coarse
+    operators need up to ~150 colours for a proper colouring, and each colour
+    is one dependent step of the sweep, while the capped split (rows beyond
+    the cap act Jacobi-like within their colour) keeps the iteration count
+    within about one iteration on the synthetic test families."""
+
+    DEFAULT_MAX_COLOURS = 8
 
     def __init__(self, ctx, systems, nrhs=1, params=None, threads=0):
         self.ctx = ctx
@@ -638,7 +647,7 @@ class Batch:
         rp = (I32P * S)(*[_ptr(r, I32P) for r, _, _ in self._keep])
         cp = (I32P * S)(*[_ptr(c, I32P) for _, c, _ in self._keep])
         vp = (F64P * S)(*[_ptr(v, F64P) for _, _, v in self._keep])
-        p = params or amg_params()
+        p = params or amg_params(max_colours=self.DEFAULT_MAX_COLOURS)
         self.h = VP()
         check(lib().sa_batch_create(ctx.h, S, _ptr(n, I32P), rp, cp, vp, nrhs, C.byref(p), threads,
                                     C.byref(self.h)))
