@@ -595,7 +595,9 @@ def main_ours(a):
         line["vcycle_ms"] = k["vcycle_ms"]
         line["coarse_lu_ms"] = k["coarse_lu_ms"]
         line["families_ms_per_vcycle"] = {f: fam[f][0] for f in fam}
-        line["ops"] = [(p["level"], p["op"], p["n"], p["colours"], round(p["ms"], 4)) for p in k["per_op"]]
+        # per level and operator: rows, colours (sweeps), ms per launch set, algorithmic GB/s
+        line["ops"] = [(p["level"], p["op"], p["n"], p["colours"], round(p["ms"], 4),
+                        round(p["bytes"] / (p["ms"] * 1e-3) / 1e9, 1)) for p in k["per_op"]]
     for key in ("plain", "multicolor", "batched"):
         if key in out:
             line[key] = out[key]

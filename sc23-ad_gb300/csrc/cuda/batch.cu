@@ -29,6 +29,8 @@
 #include <cstring>
 #include <type_traits>
 
+#include <cooperative_groups.h>
+
 #include "../sagb_internal.hpp"
 #include "common.cuh"
 #include "stream.cuh"
@@ -428,6 +430,175 @@ k_blu(const BLuDesc *__restrict__ desc, const int *__restrict__ Lcat, const int 
         __syncthreads();
     }
     for (int i = tid; i < n * R; i += kBLuThreads) d.out[i] = x[i];
+    if (ovf) {
+        for (int r = 0; r < R; r++)
+            if (ovf & (1u << r)) atomicOr(pflag + (size_t)d.sys * R + r, ST_OVERFLOW);
+        atomicOr(flags, ST_OVERFLOW);
+    }
+}
+
+// The same LU solves spread over a thread-block cluster (kLuCtas CTAs, one
+// system per cluster).  Panel p of 32 rows belongs to CTA p % kLuCtas, which
+// keeps the int64 accumulators of its rows in its own shared memory; every CTA
+// keeps a full copy of the solved values.  Per panel: the owner solves the
+// 32x32 diagonal block (warp 0, block in registers) and writes the 32 values
+// into every CTA's copy (distributed shared memory); one cluster barrier; then
+// each CTA subtracts the panel's columns from its own later rows (one thread
+// per row).  Each CTA thus reads only its own rows of L and U, so the factors
+// stream through kLuCtas SMs instead of one.  Integer sums wrap, so the
+// results are those of k_blu.
+constexpr int kLuCtas = 8;
+constexpr int kLuCThreads = 256;
+
+template <int R>
+__global__ void __launch_bounds__(kLuCThreads, 1)
+k_blu_cluster(const BLuDesc *__restrict__ desc, const int *__restrict__ Lcat, const int *__restrict__ Ucat,
+              const int *__restrict__ dcat, unsigned *__restrict__ pflag, unsigned *__restrict__ flags) {
+    namespace cg = cooperative_groups;
+    cg::cluster_group cl = cg::this_cluster();
+    const BLuDesc d = desc[blockIdx.x / kLuCtas];
+    const int q = (int)cl.block_rank();
+    const int n = d.n, npan = (n + 31) / 32;
+    const int nown = q < npan ? (npan - q + kLuCtas - 1) / kLuCtas : 0;  // panels q, q + C, ...
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    int *xs = (int *)smem_raw;                                                   // n * R solved values
+    long long *t = (long long *)(smem_raw + (((size_t)n * R * sizeof(int) + 15) & ~(size_t)15));  // own rows
+    const int *L = Lcat + d.mat_off, *U = Ucat + d.mat_off, *dinv = dcat + d.d_off;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    unsigned ovf = 0;
+    // own row lr (local) <-> global row (q + (lr / 32) * C) * 32 + lr % 32
+    auto grow = [&](int lr) { return (q + (lr >> 5) * kLuCtas) * 32 + (lr & 31); };
+    for (int i = tid; i < nown * 32 * R; i += kLuCThreads) {
+        const int lr = i / R, r = i % R, g = grow(lr);
+        t[i] = g < n ? wshl((long long)d.in[(size_t)g * R + r], d.bitL) : 0;
+    }
+    __syncthreads();
+    // ---------------- forward: unit lower
+    for (int p = 0; p < npan; p++) {
+        const int k0 = p * 32, kb = min(32, n - k0);
+        if (p % kLuCtas == q && warp == 0) {
+            const int lp = p / kLuCtas;
+            int dblk[32];
+            const int *row = L + (size_t)(k0 + lane) * n + k0;
+#pragma unroll
+            for (int c = 0; c < 32; c++) dblk[c] = (lane < kb && c < lane) ? __ldg(row + c) : 0;
+            long long tr[R];
+#pragma unroll
+            for (int r = 0; r < R; r++) tr[r] = lane < kb ? t[(lp * 32 + lane) * R + r] : 0;
+            int xv[R];
+#pragma unroll
+            for (int r = 0; r < R; r++) xv[r] = 0;
+#pragma unroll
+            for (int c = 0; c < 32; c++) {
+                if (c < kb) {
+#pragma unroll
+                    for (int r = 0; r < R; r++) {
+                        const long long sv = tr[r] >> d.bitL;
+                        if (lane == c && !fits32(sv)) ovf |= 1u << r;
+                        const int xc = __shfl_sync(0xffffffffu, lo32(sv), c);
+                        if (lane > c) tr[r] = wsub(tr[r], (long long)dblk[c] * xc);
+                        if (lane == c) xv[r] = xc;
+                    }
+                }
+            }
+            if (lane < kb)
+                for (int dst = 0; dst < kLuCtas; dst++) {
+                    int *rx = cl.map_shared_rank(xs, dst);
+#pragma unroll
+                    for (int r = 0; r < R; r++) rx[(k0 + lane) * R + r] = xv[r];
+                }
+        }
+        cl.sync();
+        // own rows of later panels: t_i -= L[i][k0 .. k0+kb) x
+        const int lp_first = p < q ? 0 : (p - q) / kLuCtas + 1;
+        for (int lr = lp_first * 32 + tid; lr < nown * 32; lr += kLuCThreads) {
+            const int g = grow(lr);
+            if (g >= n) continue;
+            const int *row = L + (size_t)g * n + k0;
+            long long acc[R];
+#pragma unroll
+            for (int r = 0; r < R; r++) acc[r] = 0;
+#pragma unroll 8
+            for (int c = 0; c < kb; c++) {
+                const long long v = __ldg(row + c);
+#pragma unroll
+                for (int r = 0; r < R; r++) acc[r] = wsub(acc[r], v * (long long)xs[(k0 + c) * R + r]);
+            }
+#pragma unroll
+            for (int r = 0; r < R; r++) t[lr * R + r] = wadd(t[lr * R + r], acc[r]);
+        }
+        __syncthreads();
+    }
+    // ---------------- backward: D^-1 U, last panel first
+    for (int i = tid; i < nown * 32 * R; i += kLuCThreads) {
+        const int lr = i / R, r = i % R, g = grow(lr);
+        t[i] = g < n ? wshl((long long)xs[(size_t)g * R + r], d.bitU) : 0;
+    }
+    cl.sync();  // every CTA has read its x before the backward values overwrite them
+    for (int p = npan - 1; p >= 0; p--) {
+        const int k0 = p * 32, kb = min(32, n - k0);
+        if (p % kLuCtas == q && warp == 0) {
+            const int lp = p / kLuCtas;
+            int dblk[32];
+            const int *row = U + (size_t)(k0 + lane) * n + k0;
+#pragma unroll
+            for (int c = 0; c < 32; c++) dblk[c] = (lane < kb && c > lane && c < kb) ? __ldg(row + c) : 0;
+            long long tr[R];
+#pragma unroll
+            for (int r = 0; r < R; r++) tr[r] = lane < kb ? t[(lp * 32 + lane) * R + r] : 0;
+            const long long dv = lane < kb ? (long long)__ldg(dinv + k0 + lane) : 0;
+            int xv[R];
+#pragma unroll
+            for (int r = 0; r < R; r++) xv[r] = 0;
+#pragma unroll
+            for (int c = 31; c >= 0; c--) {
+                if (c < kb) {
+#pragma unroll
+                    for (int r = 0; r < R; r++) {
+                        int xc = 0;
+                        if (lane == c) {
+                            const long long sv = wmul(tr[r] >> d.bitU, dv) >> d.dbitU;
+                            if (!fits32(sv)) ovf |= 1u << r;
+                            xc = lo32(sv);
+                        }
+                        xc = __shfl_sync(0xffffffffu, xc, c);
+                        if (lane < c) tr[r] = wsub(tr[r], (long long)dblk[c] * xc);
+                        if (lane == c) xv[r] = xc;
+                    }
+                }
+            }
+            if (lane < kb)
+                for (int dst = 0; dst < kLuCtas; dst++) {
+                    int *rx = cl.map_shared_rank(xs, dst);
+#pragma unroll
+                    for (int r = 0; r < R; r++) rx[(k0 + lane) * R + r] = xv[r];
+                }
+        }
+        cl.sync();
+        // own rows of earlier panels: t_i -= U[i][k0 .. k0+kb) x
+        const int lp_last = p > q ? (p - q - 1) / kLuCtas + 1 : 0;  // own panels strictly before p
+        for (int lr = tid; lr < lp_last * 32; lr += kLuCThreads) {
+            const int g = grow(lr);
+            const int *row = U + (size_t)g * n + k0;
+            long long acc[R];
+#pragma unroll
+            for (int r = 0; r < R; r++) acc[r] = 0;
+#pragma unroll 8
+            for (int c = 0; c < kb; c++) {
+                const long long v = __ldg(row + c);
+#pragma unroll
+                for (int r = 0; r < R; r++) acc[r] = wsub(acc[r], v * (long long)xs[(k0 + c) * R + r]);
+            }
+#pragma unroll
+            for (int r = 0; r < R; r++) t[lr * R + r] = wadd(t[lr * R + r], acc[r]);
+        }
+        __syncthreads();
+    }
+    // every CTA holds all values: CTA q writes its own panels
+    for (int i = tid; i < nown * 32 * R; i += kLuCThreads) {
+        const int lr = i / R, r = i % R, g = grow(lr);
+        if (g < n) d.out[(size_t)g * R + r] = xs[(size_t)g * R + r];
+    }
     if (ovf) {
         for (int r = 0; r < R; r++)
             if (ovf & (1u << r)) atomicOr(pflag + (size_t)d.sys * R + r, ST_OVERFLOW);
@@ -911,6 +1082,8 @@ struct BatchEngine::Impl {
     BLuDesc *d_lu = nullptr;
     int nlu = 0;
     size_t lu_smem = 0;
+    size_t lu_csmem = 0;   // the cluster form's shared memory
+    int lu_cluster = 0;    // 1: coarse LU through k_blu_cluster
     int *Lcat = nullptr, *Ucat = nullptr, *dcat = nullptr;
     DevCsr Af;
     std::vector<BTile> tiles_h;
@@ -999,6 +1172,12 @@ struct BatchEngine::Impl {
         nlu = (int)desc.size();
         lu_smem = (sizeof(long long) + sizeof(int)) * maxn * Rn;
         if (lu_smem > 227 * 1024) throw CudaError{"a coarsest level is too large for the batched LU kernel"};
+        {
+            const size_t np = (maxn + 31) / 32, own = (np + kLuCtas - 1) / kLuCtas;
+            lu_csmem = ((sizeof(int) * maxn * Rn + 15) & ~(size_t)15) + sizeof(long long) * own * 32 * Rn;
+        }
+        // one cluster per system: worth it when the systems leave SMs idle
+        lu_cluster = nlu > 0 && nlu * kLuCtas <= c.num_sms;
         Lcat = dupload(Lh);
         Ucat = dupload(Uh);
         dcat = dupload(dh);
@@ -1040,6 +1219,9 @@ struct BatchEngine::Impl {
             SAGB_CUDA(cudaFuncSetAttribute(k_blu<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
             SAGB_CUDA(cudaFuncSetAttribute(k_blu<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
             SAGB_CUDA(cudaFuncSetAttribute(k_blu<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
+            SAGB_CUDA(cudaFuncSetAttribute(k_blu_cluster<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
+            SAGB_CUDA(cudaFuncSetAttribute(k_blu_cluster<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
+            SAGB_CUDA(cudaFuncSetAttribute(k_blu_cluster<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
             attr = true;
         }
     }
@@ -1242,6 +1424,33 @@ struct BatchEngine::Impl {
         }
     }
 
+    // LUflex::Solve of every system (one CTA each, or one cluster each)
+    void lu(unsigned *pf) {
+        if (!nlu) return;
+        by_r([&](auto RR) {
+            constexpr int R = decltype(RR)::value;
+            if (lu_cluster) {
+                cudaLaunchConfig_t cfg = {};
+                cfg.gridDim = dim3(nlu * kLuCtas);
+                cfg.blockDim = dim3(kLuCThreads);
+                cfg.dynamicSmemBytes = lu_csmem;
+                cfg.stream = c.stream;
+                cudaLaunchAttribute at[1];
+                at[0].id = cudaLaunchAttributeClusterDimension;
+                at[0].val.clusterDim.x = kLuCtas;
+                at[0].val.clusterDim.y = 1;
+                at[0].val.clusterDim.z = 1;
+                cfg.attrs = at;
+                cfg.numAttrs = 1;
+                SAGB_CUDA(cudaLaunchKernelEx(&cfg, k_blu_cluster<R>, (const BLuDesc *)d_lu, (const int *)Lcat,
+                                             (const int *)Ucat, (const int *)dcat, pf, c.d_flags));
+            } else {
+                k_blu<R><<<nlu, kBLuThreads, lu_smem, c.stream>>>(d_lu, Lcat, Ucat, dcat, pf, c.d_flags);
+            }
+        });
+        c.launches++;
+    }
+
     // intAMGflex::Precondition (INTAMG.hpp:269-293) for the whole batch; int32
     // wraps inside it go to the preconditioner's status arrays (FGMRES is
     // flexible, so they cost convergence speed, not correctness)
@@ -1260,13 +1469,7 @@ struct BatchEngine::Impl {
             bspmv(lv[l].A, x_l, rr[l], SPMV_RESID, e_l, lv[l].row_sys);
             bspmv(lv[l].R, rr[l], ee[l + 1], SPMV_SET, nullptr, lv[l].row_sys_next);
         }
-        if (nlu) {
-            by_r([&](auto RR) {
-                constexpr int R = decltype(RR)::value;
-                k_blu<R><<<nlu, kBLuThreads, lu_smem, c.stream>>>(d_lu, Lcat, Ucat, dcat, cur_pflag, c.d_flags);
-            });
-            c.launches++;
-        }
+        lu(cur_pflag);
         for (int l = Dmax - 1; l >= 0; l--) {
             const int *e_l = l == 0 ? in : ee[l];
             int *x_l = l == 0 ? out : xx[l];
@@ -1532,12 +1735,7 @@ void BatchEngine::level_op(int level, int op, const int *in, int *out) {
 
 void BatchEngine::coarse_solve() {
     Impl &I = *impl_;
-    if (!I.nlu) return;
-    I.by_r([&](auto RR) {
-        constexpr int R = decltype(RR)::value;
-        k_blu<R><<<I.nlu, kBLuThreads, I.lu_smem, I.c.stream>>>(I.d_lu, I.Lcat, I.Ucat, I.dcat, I.pflag, I.c.d_flags);
-    });
-    I.c.launches++;
+    I.lu(I.pflag);
 }
 
 void BatchEngine::level_info(int level, int op, int *n, int *m, int64_t *nnz, int *ncolours) const {
@@ -1563,6 +1761,20 @@ void BatchEngine::autotune(int reps) {
     int *xa = (int *)dmalloc(sizeof(int) * I.N0 * I.Rn), *xb = (int *)dmalloc(sizeof(int) * I.N0 * I.Rn);
     SAGB_CUDA(cudaMemset(xa, 0, sizeof(int) * I.N0 * I.Rn));
     SAGB_CUDA(cudaMemset(xb, 0, sizeof(int) * I.N0 * I.Rn));
+    if (I.nlu) {
+        // the coarse LU: one CTA per system or one cluster per system
+        float bt[2] = {0, 0};
+        for (int uc = 0; uc < 2; uc++) {
+            I.lu_cluster = uc;
+            I.lu(I.pflag);
+            SAGB_CUDA(cudaEventRecord(e0, c.stream));
+            for (int k = 0; k < reps; k++) I.lu(I.pflag);
+            SAGB_CUDA(cudaEventRecord(e1, c.stream));
+            SAGB_CUDA(cudaEventSynchronize(e1));
+            SAGB_CUDA(cudaEventElapsedTime(&bt[uc], e0, e1));
+        }
+        I.lu_cluster = bt[1] < bt[0];
+    }
     const int cand[] = {0, 1, 2, 4, 8, 16, 32};  // 0: tile-staged stream (not for the colour sweep)
     for (int l = 0; l < I.Dmax; l++) {
         DevBLevel &L = I.lv[l];
