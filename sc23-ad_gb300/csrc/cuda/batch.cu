@@ -518,11 +518,20 @@ k_blu_cluster(const BLuDesc *__restrict__ desc, const int *__restrict__ Lcat, co
             long long acc[R];
 #pragma unroll
             for (int r = 0; r < R; r++) acc[r] = 0;
-#pragma unroll 8
-            for (int c = 0; c < kb; c++) {
-                const long long v = __ldg(row + c);
+            if (kb == 32) {
+                int v[32];  // the row's 32 entries in flight together
 #pragma unroll
-                for (int r = 0; r < R; r++) acc[r] = wsub(acc[r], v * (long long)xs[(k0 + c) * R + r]);
+                for (int c = 0; c < 32; c++) v[c] = __ldg(row + c);
+#pragma unroll
+                for (int c = 0; c < 32; c++)
+#pragma unroll
+                    for (int r = 0; r < R; r++) acc[r] = wsub(acc[r], (long long)v[c] * xs[(k0 + c) * R + r]);
+            } else {
+                for (int c = 0; c < kb; c++) {
+                    const long long v = __ldg(row + c);
+#pragma unroll
+                    for (int r = 0; r < R; r++) acc[r] = wsub(acc[r], v * (long long)xs[(k0 + c) * R + r]);
+                }
             }
 #pragma unroll
             for (int r = 0; r < R; r++) t[lr * R + r] = wadd(t[lr * R + r], acc[r]);
@@ -583,11 +592,20 @@ k_blu_cluster(const BLuDesc *__restrict__ desc, const int *__restrict__ Lcat, co
             long long acc[R];
 #pragma unroll
             for (int r = 0; r < R; r++) acc[r] = 0;
-#pragma unroll 8
-            for (int c = 0; c < kb; c++) {
-                const long long v = __ldg(row + c);
+            if (kb == 32) {
+                int v[32];  // the row's 32 entries in flight together
 #pragma unroll
-                for (int r = 0; r < R; r++) acc[r] = wsub(acc[r], v * (long long)xs[(k0 + c) * R + r]);
+                for (int c = 0; c < 32; c++) v[c] = __ldg(row + c);
+#pragma unroll
+                for (int c = 0; c < 32; c++)
+#pragma unroll
+                    for (int r = 0; r < R; r++) acc[r] = wsub(acc[r], (long long)v[c] * xs[(k0 + c) * R + r]);
+            } else {
+                for (int c = 0; c < kb; c++) {
+                    const long long v = __ldg(row + c);
+#pragma unroll
+                    for (int r = 0; r < R; r++) acc[r] = wsub(acc[r], v * (long long)xs[(k0 + c) * R + r]);
+                }
             }
 #pragma unroll
             for (int r = 0; r < R; r++) t[lr * R + r] = wadd(t[lr * R + r], acc[r]);
