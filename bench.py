@@ -358,7 +358,7 @@ def batch_rooflines(ctx, B, a):
             else:
                 # entries, row pointers, the shift, x once, y once (and z for the residuals)
                 by = 8 * nnz + 4 * (n + 1) + n + 4 * R * m + 4 * R * n
-                calls = 2 if op in (0, 2) else 1
+                calls = 1  # A (residual), U (post-smoothing residual), P and R once per V-cycle
             per.append({"level": l, "op": name, "n": n, "nnz": nnz, "colours": ncol if op == 1 else None,
                         "ms": t, "bytes": by, "per_vcycle": calls})
             key = "sweep" if op == 1 else "spmv"
