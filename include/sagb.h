@@ -97,6 +97,8 @@ typedef struct {
                             colouring helper/helper_graph.hpp:191-219); 0: natural order (default) */
     int max_colours;     /* multicolour: cap on the colours per level, rows beyond it join their least
                             conflicting colour (Jacobi-like inside it); 0: no cap (default) */
+    int coarse_size;     /* coarsen while the coarsest level has more rows than this; 0: the
+                            reference's 2000 (INTAMG.hpp:38-51) */
 } sa_amg_params;
 
 typedef struct {

@@ -476,11 +476,14 @@ extern "C" void sa_amg_params_default(sa_amg_params *p) {
     p->smooth_iter = 1;
     p->multicolor = 0;
     p->max_colours = 0;
+    p->coarse_size = 0;
 }
 
 static void build_setup(sa_hierarchy &s, const CsrD &A) {
     if (s.p.theta <= 0 || s.p.theta > 1) throw SetupError{"Theta must be in 0 < theta <= 1"};
-    if (!s.chain) s.chain = std::make_shared<RsChain>(rs_chain(A, s.p.theta, s.p.max_levels));
+    if (!s.chain)
+        s.chain = std::make_shared<RsChain>(
+            rs_chain(A, s.p.theta, s.p.max_levels, s.p.coarse_size > 0 ? s.p.coarse_size : 2000));
     const RsChain &chain = *s.chain;
     SmootherSpec sm;
     sm.block = s.p.smoother_blocks;
@@ -504,7 +507,7 @@ extern "C" int sa_setup_create(int precision, const sa_amg_params *p, int n, con
     else sa_amg_params_default(&s->p);
     if (s->p.smooth_iter < 1 || s->p.max_levels < 1 || s->p.smoother_blocks < 0 ||
         s->p.multicolor < 0 || s->p.multicolor > 1 || (s->p.multicolor && s->p.smoother_blocks) ||
-        s->p.max_colours < 0) {
+        s->p.max_colours < 0 || s->p.coarse_size < 0) {
         delete s;
         return fail(SA_ERR_ARG, "invalid AMG parameters");
     }
@@ -1080,7 +1083,8 @@ extern "C" int sa_batch_create(sa_ctx ctx, int nsys, const int *n, const int32_t
     sa_amg_params q;
     if (p) q = *p;
     else sa_amg_params_default(&q);
-    if (q.smooth_iter < 1 || q.max_levels < 1 || q.smoother_blocks != 0 || q.theta <= 0 || q.theta > 1)
+    if (q.smooth_iter < 1 || q.max_levels < 1 || q.smoother_blocks != 0 || q.theta <= 0 || q.theta > 1 ||
+        q.max_colours < 0 || q.coarse_size < 0)
         return fail(SA_ERR_ARG, "invalid AMG parameters (the batch uses the multicolour SOR smoother)");
     q.multicolor = 1;
     SA_GUARD_BEGIN
@@ -1109,7 +1113,8 @@ extern "C" int sa_batch_create(sa_ctx ctx, int nsys, const int *n, const int32_t
     B->p = q;
     try {
         B->h = std::make_shared<BatchHierarchy>(
-            build_batch(sys, q.theta, q.max_levels, q.omega, q.smooth_iter, threads, src, q.max_colours));
+            build_batch(sys, q.theta, q.max_levels, q.omega, q.smooth_iter, threads, src, q.max_colours,
+                        q.coarse_size > 0 ? q.coarse_size : 2000));
         SAGB_CUDA(cudaSetDevice(ctx->c.device));
         B->eng = std::make_unique<BatchEngine>(ctx->c, B->h, nrhs);
         SAGB_CUDA(cudaDeviceSynchronize());

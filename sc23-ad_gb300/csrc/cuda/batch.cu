@@ -440,43 +440,15 @@ k_blu(const BLuDesc *__restrict__ desc, const int *__restrict__ Lcat, const int 
 // The same LU solves spread over a thread-block cluster (kLuCtas CTAs, one
 // system per cluster).  Panel p of 32 rows belongs to CTA p % kLuCtas, which
 // keeps the int64 accumulators of its rows in its own shared memory; every CTA
-// keeps a full copy of the solved values.  Step p: with the values of panel p
-// in every copy (distributed shared memory), each CTA subtracts panel p's
-// columns from its own later rows, one thread per row; the owner of the next
-// panel first updates that panel's 32 rows (warp 0), solves its 32x32 diagonal
-// block from registers and writes the 32 values into every CTA's copy, while
-// its other warps and the other CTAs do the rest; one cluster barrier ends the
-// step.  Each CTA reads only its own rows of L and U, so the factors stream
-// through kLuCtas SMs, and the serial diagonal solves overlap the bulk
-// updates.  Integer sums wrap, so the results are those of k_blu.
+// keeps a full copy of the solved values.  Per panel: the owner solves the
+// 32x32 diagonal block (warp 0, block in registers) and writes the 32 values
+// into every CTA's copy (distributed shared memory); one cluster barrier; then
+// each CTA subtracts the panel's columns from its own later rows (one thread
+// per row).  Each CTA thus reads only its own rows of L and U, so the factors
+// stream through kLuCtas SMs instead of one.  Integer sums wrap, so the
+// results are those of k_blu.
 constexpr int kLuCtas = 8;
 constexpr int kLuCThreads = 256;
-
-// t_row -= M[g][k0 .. k0+kb) . x[k0 .. k0+kb) for one row (R right-hand sides)
-template <int R>
-__device__ __forceinline__ void lu_row_update(const int *__restrict__ row, int k0, int kb, const int *xs,
-                                              long long *t) {
-    long long acc[R];
-#pragma unroll
-    for (int r = 0; r < R; r++) acc[r] = 0;
-    if (kb == 32) {
-        int v[32];  // the row's 32 entries in flight together
-#pragma unroll
-        for (int c = 0; c < 32; c++) v[c] = __ldg(row + c);
-#pragma unroll
-        for (int c = 0; c < 32; c++)
-#pragma unroll
-            for (int r = 0; r < R; r++) acc[r] = wsub(acc[r], (long long)v[c] * xs[(k0 + c) * R + r]);
-    } else {
-        for (int c = 0; c < kb; c++) {
-            const long long v = __ldg(row + c);
-#pragma unroll
-            for (int r = 0; r < R; r++) acc[r] = wsub(acc[r], v * (long long)xs[(k0 + c) * R + r]);
-        }
-    }
-#pragma unroll
-    for (int r = 0; r < R; r++) t[r] = wadd(t[r], acc[r]);
-}
 
 template <int R>
 __global__ void __launch_bounds__(kLuCThreads, 1)
@@ -496,23 +468,26 @@ k_blu_cluster(const BLuDesc *__restrict__ desc, const int *__restrict__ Lcat, co
     unsigned ovf = 0;
     // own row lr (local) <-> global row (q + (lr / 32) * C) * 32 + lr % 32
     auto grow = [&](int lr) { return (q + (lr >> 5) * kLuCtas) * 32 + (lr & 31); };
-    // warp 0 of the owner: solve the diagonal block of panel p (forward or
-    // backward) from its updated rows and write the values into every copy
-    auto diag = [&](int p, bool fwd) {
-        const int k0 = p * 32, kb = min(32, n - k0), lp = p / kLuCtas;
-        const int *row = (fwd ? L : U) + (size_t)(k0 + lane) * n + k0;
-        int dblk[32];
+    for (int i = tid; i < nown * 32 * R; i += kLuCThreads) {
+        const int lr = i / R, r = i % R, g = grow(lr);
+        t[i] = g < n ? wshl((long long)d.in[(size_t)g * R + r], d.bitL) : 0;
+    }
+    __syncthreads();
+    // ---------------- forward: unit lower
+    for (int p = 0; p < npan; p++) {
+        const int k0 = p * 32, kb = min(32, n - k0);
+        if (p % kLuCtas == q && warp == 0) {
+            const int lp = p / kLuCtas;
+            int dblk[32];
+            const int *row = L + (size_t)(k0 + lane) * n + k0;
 #pragma unroll
-        for (int c = 0; c < 32; c++)
-            dblk[c] = (lane < kb && c < kb && (fwd ? c < lane : c > lane)) ? __ldg(row + c) : 0;
-        const long long dv = (!fwd && lane < kb) ? (long long)__ldg(dinv + k0 + lane) : 0;
-        long long tr[R];
+            for (int c = 0; c < 32; c++) dblk[c] = (lane < kb && c < lane) ? __ldg(row + c) : 0;
+            long long tr[R];
 #pragma unroll
-        for (int r = 0; r < R; r++) tr[r] = lane < kb ? t[(lp * 32 + lane) * R + r] : 0;
-        int xv[R];
+            for (int r = 0; r < R; r++) tr[r] = lane < kb ? t[(lp * 32 + lane) * R + r] : 0;
+            int xv[R];
 #pragma unroll
-        for (int r = 0; r < R; r++) xv[r] = 0;
-        if (fwd) {
+            for (int r = 0; r < R; r++) xv[r] = 0;
 #pragma unroll
             for (int c = 0; c < 32; c++) {
                 if (c < kb) {
@@ -526,7 +501,64 @@ k_blu_cluster(const BLuDesc *__restrict__ desc, const int *__restrict__ Lcat, co
                     }
                 }
             }
-        } else {
+            if (lane < kb)
+                for (int dst = 0; dst < kLuCtas; dst++) {
+                    int *rx = cl.map_shared_rank(xs, dst);
+#pragma unroll
+                    for (int r = 0; r < R; r++) rx[(k0 + lane) * R + r] = xv[r];
+                }
+        }
+        cl.sync();
+        // own rows of later panels: t_i -= L[i][k0 .. k0+kb) x
+        const int lp_first = p < q ? 0 : (p - q) / kLuCtas + 1;
+        for (int lr = lp_first * 32 + tid; lr < nown * 32; lr += kLuCThreads) {
+            const int g = grow(lr);
+            if (g >= n) continue;
+            const int *row = L + (size_t)g * n + k0;
+            long long acc[R];
+#pragma unroll
+            for (int r = 0; r < R; r++) acc[r] = 0;
+            if (kb == 32) {
+                int v[32];  // the row's 32 entries in flight together
+#pragma unroll
+                for (int c = 0; c < 32; c++) v[c] = __ldg(row + c);
+#pragma unroll
+                for (int c = 0; c < 32; c++)
+#pragma unroll
+                    for (int r = 0; r < R; r++) acc[r] = wsub(acc[r], (long long)v[c] * xs[(k0 + c) * R + r]);
+            } else {
+                for (int c = 0; c < kb; c++) {
+                    const long long v = __ldg(row + c);
+#pragma unroll
+                    for (int r = 0; r < R; r++) acc[r] = wsub(acc[r], v * (long long)xs[(k0 + c) * R + r]);
+                }
+            }
+#pragma unroll
+            for (int r = 0; r < R; r++) t[lr * R + r] = wadd(t[lr * R + r], acc[r]);
+        }
+        __syncthreads();
+    }
+    // ---------------- backward: D^-1 U, last panel first
+    for (int i = tid; i < nown * 32 * R; i += kLuCThreads) {
+        const int lr = i / R, r = i % R, g = grow(lr);
+        t[i] = g < n ? wshl((long long)xs[(size_t)g * R + r], d.bitU) : 0;
+    }
+    cl.sync();  // every CTA has read its x before the backward values overwrite them
+    for (int p = npan - 1; p >= 0; p--) {
+        const int k0 = p * 32, kb = min(32, n - k0);
+        if (p % kLuCtas == q && warp == 0) {
+            const int lp = p / kLuCtas;
+            int dblk[32];
+            const int *row = U + (size_t)(k0 + lane) * n + k0;
+#pragma unroll
+            for (int c = 0; c < 32; c++) dblk[c] = (lane < kb && c > lane && c < kb) ? __ldg(row + c) : 0;
+            long long tr[R];
+#pragma unroll
+            for (int r = 0; r < R; r++) tr[r] = lane < kb ? t[(lp * 32 + lane) * R + r] : 0;
+            const long long dv = lane < kb ? (long long)__ldg(dinv + k0 + lane) : 0;
+            int xv[R];
+#pragma unroll
+            for (int r = 0; r < R; r++) xv[r] = 0;
 #pragma unroll
             for (int c = 31; c >= 0; c--) {
                 if (c < kb) {
@@ -544,70 +576,41 @@ k_blu_cluster(const BLuDesc *__restrict__ desc, const int *__restrict__ Lcat, co
                     }
                 }
             }
-        }
-        if (lane < kb)
-            for (int dst = 0; dst < kLuCtas; dst++) {
-                int *rx = cl.map_shared_rank(xs, dst);
+            if (lane < kb)
+                for (int dst = 0; dst < kLuCtas; dst++) {
+                    int *rx = cl.map_shared_rank(xs, dst);
 #pragma unroll
-                for (int r = 0; r < R; r++) rx[(k0 + lane) * R + r] = xv[r];
-            }
-    };
-    for (int i = tid; i < nown * 32 * R; i += kLuCThreads) {
-        const int lr = i / R, r = i % R, g = grow(lr);
-        t[i] = g < n ? wshl((long long)d.in[(size_t)g * R + r], d.bitL) : 0;
-    }
-    __syncthreads();
-    // ---------------- forward: unit lower
-    if (q == 0 && warp == 0) diag(0, true);
-    cl.sync();
-    for (int p = 0; p < npan; p++) {
-        const int k0 = p * 32, kb = min(32, n - k0);
-        const int nxt = p + 1;
-        const bool look = nxt < npan && nxt % kLuCtas == q;  // this CTA owns the next panel
-        const int lp_nxt = nxt / kLuCtas;
-        if (look && warp == 0) {
-            lu_row_update<R>(L + (size_t)(nxt * 32 + lane) * n + k0, k0, kb, xs, t + (lp_nxt * 32 + lane) * R);
-            __syncwarp();
-            diag(nxt, true);
+                    for (int r = 0; r < R; r++) rx[(k0 + lane) * R + r] = xv[r];
+                }
         }
-        // own rows of panels after p (the next panel's rows are done above)
-        const int lp_first = p < q ? 0 : (p - q) / kLuCtas + 1;
-        const int t0 = look ? tid - 32 : tid, nt = look ? kLuCThreads - 32 : kLuCThreads;
-        if (t0 >= 0)
-            for (int lr = lp_first * 32 + t0; lr < nown * 32; lr += nt) {
-                if (look && (lr >> 5) == lp_nxt) continue;
-                const int g = grow(lr);
-                if (g < n) lu_row_update<R>(L + (size_t)g * n + k0, k0, kb, xs, t + lr * R);
-            }
         cl.sync();
-    }
-    // ---------------- backward: D^-1 U, last panel first
-    for (int i = tid; i < nown * 32 * R; i += kLuCThreads) {
-        const int lr = i / R, r = i % R, g = grow(lr);
-        t[i] = g < n ? wshl((long long)xs[(size_t)g * R + r], d.bitU) : 0;
-    }
-    cl.sync();  // every CTA has read its x before the backward values overwrite them
-    if ((npan - 1) % kLuCtas == q && warp == 0) diag(npan - 1, false);
-    cl.sync();
-    for (int p = npan - 1; p >= 0; p--) {
-        const int k0 = p * 32, kb = min(32, n - k0);
-        const int nxt = p - 1;
-        const bool look = nxt >= 0 && nxt % kLuCtas == q;
-        const int lp_nxt = look ? nxt / kLuCtas : -1;
-        if (look && warp == 0) {
-            lu_row_update<R>(U + (size_t)(nxt * 32 + lane) * n + k0, k0, kb, xs, t + (lp_nxt * 32 + lane) * R);
-            __syncwarp();
-            diag(nxt, false);
+        // own rows of earlier panels: t_i -= U[i][k0 .. k0+kb) x
+        const int lp_last = p > q ? (p - q - 1) / kLuCtas + 1 : 0;  // own panels strictly before p
+        for (int lr = tid; lr < lp_last * 32; lr += kLuCThreads) {
+            const int g = grow(lr);
+            const int *row = U + (size_t)g * n + k0;
+            long long acc[R];
+#pragma unroll
+            for (int r = 0; r < R; r++) acc[r] = 0;
+            if (kb == 32) {
+                int v[32];  // the row's 32 entries in flight together
+#pragma unroll
+                for (int c = 0; c < 32; c++) v[c] = __ldg(row + c);
+#pragma unroll
+                for (int c = 0; c < 32; c++)
+#pragma unroll
+                    for (int r = 0; r < R; r++) acc[r] = wsub(acc[r], (long long)v[c] * xs[(k0 + c) * R + r]);
+            } else {
+                for (int c = 0; c < kb; c++) {
+                    const long long v = __ldg(row + c);
+#pragma unroll
+                    for (int r = 0; r < R; r++) acc[r] = wsub(acc[r], v * (long long)xs[(k0 + c) * R + r]);
+                }
+            }
+#pragma unroll
+            for (int r = 0; r < R; r++) t[lr * R + r] = wadd(t[lr * R + r], acc[r]);
         }
-        // own rows of panels before p
-        const int lp_last = p > q ? (p - q - 1) / kLuCtas + 1 : 0;
-        const int t0 = look ? tid - 32 : tid, nt = look ? kLuCThreads - 32 : kLuCThreads;
-        if (t0 >= 0)
-            for (int lr = t0; lr < lp_last * 32; lr += nt) {
-                if (look && (lr >> 5) == lp_nxt) continue;
-                lu_row_update<R>(U + (size_t)grow(lr) * n + k0, k0, kb, xs, t + lr * R);
-            }
-        cl.sync();
+        __syncthreads();
     }
     // every CTA holds all values: CTA q writes its own panels
     for (int i = tid; i < nown * 32 * R; i += kLuCThreads) {

@@ -417,14 +417,17 @@ void rs_level(const CsrD &A, double theta, CsrD &CA, CsrD &P, CsrD &R) {
     CA = galerkin(A, P, R);
 }
 
-RsChain rs_chain(const CsrD &A, double theta, int max_levels) {
+RsChain rs_chain(const CsrD &A, double theta, int max_levels, int coarse_size) {
     RsChain ch;
     ch.CA.emplace_back();
     ch.P.emplace_back();
     ch.R.emplace_back();
     rs_level(A, theta, ch.CA[0], ch.P[0], ch.R[0]);
     int depth = 1;
-    while (max_levels > depth && ch.CA[depth - 1].n > 2000) {
+    while (max_levels > depth && ch.CA[depth - 1].n > coarse_size) {
+        // a coarsening step that barely shrinks the operator ends the chain
+        // (only outside the reference's rule, coarse_size 2000)
+        if (coarse_size != 2000 && depth >= 2 && ch.CA[depth - 1].n * 10 > ch.CA[depth - 2].n * 9) break;
         depth++;
         CsrD ca, p, r;
         rs_level(ch.CA[depth - 2], theta, ca, p, r);

@@ -37,12 +37,15 @@ void lmax1_scaling(CsrD &A, double *b);
 void rs_level(const CsrD &A, double theta, CsrD &CA, CsrD &P, CsrD &R);
 
 // The level loop shared by dfAMG and intAMGflex (INTAMG.hpp:38-51, 162-195):
-// levels are added while max_levels > depth and the last coarse size > 2000.
+// levels are added while max_levels > depth and the last coarse size >
+// coarse_size (the reference's 2000 by default).  With another coarse_size
+// (not the reference's rule) the chain also ends when a step keeps more than
+// 90 % of the rows.
 struct RsChain {
     std::vector<CsrD> CA, P, R;  // unscaled, CA[i] = R[i] * A_i * P[i]
     int depth() const { return (int)CA.size(); }
 };
-RsChain rs_chain(const CsrD &A, double theta, int max_levels);
+RsChain rs_chain(const CsrD &A, double theta, int max_levels, int coarse_size = 2000);
 
 // ---------------------------------------------------------------- smoother splits
 // SOR ctor (smoother/stationary.hpp:195-231): LD = strict lower + diag/omega

@@ -29,7 +29,8 @@ static void start(BatchCsr &B, int m) {
 static int level_size(const IntHierarchy &h, int l) { return l == 0 ? h.A0.n : h.R[l - 1].n; }
 
 BatchHierarchy build_batch(const std::vector<CsrD> &systems, double theta, int max_levels, double omega,
-                           int smooth_iter, int threads, const std::vector<int> &src_in, int max_colours) {
+                           int smooth_iter, int threads, const std::vector<int> &src_in, int max_colours,
+                           int coarse_size) {
     BatchHierarchy B;
     const int S = (int)systems.size();
     if (S == 0) throw SetupError{"empty batch"};
@@ -61,7 +62,7 @@ BatchHierarchy build_batch(const std::vector<CsrD> &systems, double theta, int m
             if (src[s] != s) continue;  // a copy: shares the hierarchy below
             try {
                 B.A_sys[s] = std::make_shared<CsrD>(systems[s]);
-                B.chain[s] = std::make_shared<RsChain>(rs_chain(systems[s], theta, max_levels));
+                B.chain[s] = std::make_shared<RsChain>(rs_chain(systems[s], theta, max_levels, coarse_size));
                 B.hi[s] = std::make_shared<IntHierarchy>(build_int_hierarchy(systems[s], *B.chain[s], sm));
             } catch (const SetupError &e) {
                 errs[s] = e.msg;

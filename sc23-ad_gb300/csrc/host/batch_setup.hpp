@@ -67,6 +67,7 @@ struct BatchHierarchy {
 // so copies of one matrix, e.g. solved with different fractional bits, share
 // one setup.
 BatchHierarchy build_batch(const std::vector<CsrD> &systems, double theta, int max_levels, double omega,
-                           int smooth_iter, int threads, const std::vector<int> &src = {}, int max_colours = 0);
+                           int smooth_iter, int threads, const std::vector<int> &src = {}, int max_colours = 0,
+                           int coarse_size = 2000);
 
 }  // namespace sagb

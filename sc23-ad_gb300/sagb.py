@@ -35,7 +35,7 @@ class CsrView(C.Structure):
 class AmgParams(C.Structure):
     _fields_ = [("max_levels", C.c_int), ("theta", C.c_double), ("smoother_blocks", C.c_int),
                 ("omega", C.c_double), ("smooth_iter", C.c_int), ("multicolor", C.c_int),
-                ("max_colours", C.c_int)]
+                ("max_colours", C.c_int), ("coarse_size", C.c_int)]
 
 
 class SolverParams(C.Structure):
@@ -245,8 +245,9 @@ class HostCsr:
     __del__ = close
 
 
-def amg_params(max_levels=20, theta=0.8, smoother_blocks=0, omega=1.0, smooth_iter=1, multicolor=0, max_colours=0):
-    return AmgParams(max_levels, theta, smoother_blocks, omega, smooth_iter, multicolor, max_colours)
+def amg_params(max_levels=20, theta=0.8, smoother_blocks=0, omega=1.0, smooth_iter=1, multicolor=0, max_colours=0,
+               coarse_size=0):
+    return AmgParams(max_levels, theta, smoother_blocks, omega, smooth_iter, multicolor, max_colours, coarse_size)
 
 
 class Setup:
