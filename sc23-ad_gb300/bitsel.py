@@ -34,31 +34,36 @@ def rule_of(ratio):
     return 29 if ratio < 1 else 31 - (int(np.ceil(np.log2(int(ratio) + 1))) + 1)
 
 
-def training_specs(count, seed, side=(24, 48)):
-    """(kind, nx, param, seed) of `count` matrices from the training mixture."""
+def training_specs(count, seed, side=(16, 64)):
+    """(kind, nx, param, seed, rhs) of `count` matrices from the training
+    mixture; rhs 0: b = A x* with x* ~ U[-1, 1], rhs 1: b ~ U[-1, 1]."""
     rng = np.random.default_rng(seed)
     specs = []
     for k in range(count):
         fam = int(rng.integers(0, 5))
         s3 = int(rng.integers(side[0], side[1] + 1))
+        rhs = int(rng.integers(0, 2))
         if fam == 0:    # 5-point 2D, anisotropy 1e-4..1 (side^1.5 rows ~ a 3D cube's)
             n2 = int(round(s3 ** 1.5))
-            specs.append((sagb.GEN_ANISO2D, n2, float(10 ** rng.uniform(-4, 0)), k + 1))
+            specs.append((sagb.GEN_ANISO2D, n2, float(10 ** rng.uniform(-4, 0)), k + 1, rhs))
         elif fam == 1:  # 7-point 3D Poisson
-            specs.append((sagb.GEN_POISSON3D, s3, 0.0, k + 1))
+            specs.append((sagb.GEN_POISSON3D, s3, 0.0, k + 1, rhs))
         elif fam == 2:  # 27-point
-            specs.append((sagb.GEN_STENCIL27, s3, 0.0, k + 1))
+            specs.append((sagb.GEN_STENCIL27, s3, 0.0, k + 1, rhs))
         elif fam == 3:  # lognormal coefficients
-            specs.append((sagb.GEN_VARCOEF3D, s3, float(rng.uniform(0, 3)), k + 1))
+            specs.append((sagb.GEN_VARCOEF3D, s3, float(rng.uniform(0, 3)), k + 1, rhs))
         else:           # upwinded convection-diffusion
-            specs.append((sagb.GEN_CONVDIFF3D, s3, float(rng.uniform(0, 100)), k + 1))
+            specs.append((sagb.GEN_CONVDIFF3D, s3, float(rng.uniform(0, 100)), k + 1, rhs))
     return specs
 
 
 def make_system(spec):
-    kind, nx, prm, sd = spec
+    kind, nx, prm, sd = spec[:4]
+    rhs = spec[4] if len(spec) > 4 else 0
     A = sagb.HostCsr.generate(kind, nx, prm, seed=sd)
     xs, b = A.rhs(sd)
+    if rhs == 1:
+        b = np.random.default_rng(sd).uniform(-1.0, 1.0, size=len(b))
     A.lmax1_scaling(b)
     r, c, v = A.arrays()
     return r, c, v, b
@@ -177,7 +182,8 @@ def build_dataset(ctx, specs, chunk=16, m=30, max_outer=4, log=None):
                 out.append({"bit": f, "iters": int(it[s]), "converged": int(cv[s] and res <= 1e-10), "res": res})
             X.append(feats[i])
             T.append(targets(out))
-            meta.append({"spec": [int(part[i][0]), int(part[i][1]), float(part[i][2]), int(part[i][3])],
+            meta.append({"spec": [int(part[i][0]), int(part[i][1]), float(part[i][2]), int(part[i][3]),
+                                  int(part[i][4]) if len(part[i]) > 4 else 0],
                          "rule": rules[i], "ratio": ratios[i], "rows": len(r) - 1, "sweep": out})
             if log:
                 best = min(out, key=lambda q: (not q["converged"], q["iters"]))

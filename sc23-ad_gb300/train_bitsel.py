@@ -1,6 +1,6 @@
 """Build the bit-sweep dataset on the GPU and train the selector's MLP.
 
-    python sc23-ad_gb300/train_bitsel.py [--count 300] [--side 24 48] [--seed 7]
+    python sc23-ad_gb300/train_bitsel.py [--count 600] [--side 16 64] [--seed 7]
                                          [--epochs 400] [--train-only]
 
 Writes data/bitsel_dataset.npz (features, targets and every sweep point) and
@@ -48,8 +48,8 @@ def evaluate(net, f_lo, X, meta, fail_cost=120):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--count", type=int, default=300)
-    ap.add_argument("--side", type=int, nargs=2, default=[24, 48])
+    ap.add_argument("--count", type=int, default=600)
+    ap.add_argument("--side", type=int, nargs=2, default=[16, 64])
     ap.add_argument("--seed", type=int, default=7)
     ap.add_argument("--epochs", type=int, default=400)
     ap.add_argument("--train-only", action="store_true", help="reuse the dataset file")
