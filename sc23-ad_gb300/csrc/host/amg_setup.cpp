@@ -7,6 +7,7 @@
 #include "sort.hpp"
 
 #include <algorithm>
+#include <thread>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -351,16 +352,13 @@ static CsrD transpose(const CsrD &P) {
 // zero is removed (and restarts from alpha*x if hit again, which is the same as
 // adding to 0.0).  A dense accumulator gives the same values; the touched rows
 // are emitted in increasing order, as the merge-based original does.
-static void csc_product(const std::vector<int> &lp, const std::vector<int> &li, const std::vector<double> &lv,
+static void csc_columns(const std::vector<int> &lp, const std::vector<int> &li, const std::vector<double> &lv,
                         int L, const std::vector<int> &rp, const std::vector<int> &ri, const std::vector<double> &rv,
-                        int R, std::vector<int> &op, std::vector<int> &oi, std::vector<double> &ov) {
+                        int c0, int c1, std::vector<int> &cnt, std::vector<int> &oi, std::vector<double> &ov) {
     std::vector<double> acc(L, 0.0);
     std::vector<int> stamp(L, -1);
     std::vector<int> touched;
-    op.assign(R + 1, 0);
-    oi.clear();
-    ov.clear();
-    for (int c = 0; c < R; c++) {
+    for (int c = c0; c < c1; c++) {
         touched.clear();
         for (int k = rp[c]; k < rp[c + 1]; k++) {
             const int src = ri[k];
@@ -376,12 +374,46 @@ static void csc_product(const std::vector<int> &lp, const std::vector<int> &li, 
             }
         }
         std::sort(touched.begin(), touched.end());
+        int k = 0;
         for (int row : touched) {
             if (std::fabs(acc[row]) == 0.0) continue;
             oi.push_back(row);
             ov.push_back(acc[row]);
+            k++;
         }
-        op[c + 1] = (int)oi.size();
+        cnt[c] = k;
+    }
+}
+
+// Columns are independent: blocks of columns run on host threads, each with
+// its own accumulator, and are concatenated in order (the values and their
+// order do not depend on the number of threads).
+static void csc_product(const std::vector<int> &lp, const std::vector<int> &li, const std::vector<double> &lv,
+                        int L, const std::vector<int> &rp, const std::vector<int> &ri, const std::vector<double> &rv,
+                        int R, std::vector<int> &op, std::vector<int> &oi, std::vector<double> &ov) {
+    const int hw = (int)std::max(1u, std::thread::hardware_concurrency());
+    const int T = R < 20000 ? 1 : std::min(hw, 16);
+    std::vector<int> cnt(R, 0);
+    std::vector<std::vector<int>> pi(T);
+    std::vector<std::vector<double>> pv(T);
+    std::vector<std::thread> pool;
+    for (int t = 0; t < T; t++) {
+        const int c0 = (int)((long long)R * t / T), c1 = (int)((long long)R * (t + 1) / T);
+        if (t + 1 < T)
+            pool.emplace_back([&, t, c0, c1] { csc_columns(lp, li, lv, L, rp, ri, rv, c0, c1, cnt, pi[t], pv[t]); });
+        else
+            csc_columns(lp, li, lv, L, rp, ri, rv, c0, c1, cnt, pi[t], pv[t]);
+    }
+    for (auto &th : pool) th.join();
+    op.assign(R + 1, 0);
+    for (int c = 0; c < R; c++) op[c + 1] = op[c] + cnt[c];
+    oi.clear();
+    ov.clear();
+    oi.reserve(op[R]);
+    ov.reserve(op[R]);
+    for (int t = 0; t < T; t++) {
+        oi.insert(oi.end(), pi[t].begin(), pi[t].end());
+        ov.insert(ov.end(), pv[t].begin(), pv[t].end());
     }
 }
 
