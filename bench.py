@@ -330,7 +330,8 @@ def plain_row(ctx, a, r, c, v, b, nrm_b):
 
 
 def batch_rooflines(ctx, B, a):
-    """Average launch time (CUDA events on the library stream) and algorithmic
+    """Average time per call (CUDA events on the library stream around a CUDA
+    graph of repeated calls, as the solver's graphs run them) and algorithmic
     bytes of every batched level operator, and the V-cycle they make up."""
     import sagb
     R = B.nrhs
@@ -338,18 +339,7 @@ def batch_rooflines(ctx, B, a):
     big = B.rows * R
     xin = sagb.DeviceArray.from_host(ctx, rng.integers(-(1 << 28), 1 << 28, size=big).astype(np.int32))
     xout = sagb.DeviceArray(ctx, big, np.int32)
-    e0, e1 = sagb.Event(), sagb.Event()
     reps = 10
-
-    def timed(fn):
-        fn()
-        ctx.sync()
-        e0.record(ctx)
-        for _ in range(reps):
-            fn()
-        e1.record(ctx)
-        return e0.elapsed_ms(e1) / reps
-
     fam = {"spmv": [0.0, 0], "sweep": [0.0, 0]}
     per = []
     for l in range(B.depth):
@@ -357,7 +347,7 @@ def batch_rooflines(ctx, B, a):
             n, m, nnz, ncol = B.level_info(l, op)
             if n == 0:
                 continue
-            t = timed(lambda: sagb.check(sagb.lib().sa_batch_level_op(ctx.h, B.h, l, op, xin.ptr, xout.ptr)))
+            t = B.time_op(l, op, xin, xout, reps)
             if op == 1:
                 # LD entries, row pointers, two shifts, the colour row list, in once, out written once
                 by = 8 * nnz + 4 * (n + 1) + 2 * n + 4 * n + 8 * R * n
@@ -371,9 +361,9 @@ def batch_rooflines(ctx, B, a):
             key = "sweep" if op == 1 else "spmv"
             fam[key][0] += calls * t
             fam[key][1] += calls * by
-    t_lu = timed(lambda: B.coarse_solve())
+    t_lu = B.time_op(0, B.OP_LU, reps=reps)
     vin = sagb.DeviceArray.from_host(ctx, rng.integers(-(1 << 28), 1 << 28, size=big).astype(np.int32))
-    t_v = timed(lambda: B.precondition(vin, xout))
+    t_v = B.time_op(0, B.OP_VCYCLE, vin, xout, reps)
     for o in (xin, xout, vin):
         o.close()
     return {"per_op": per, "families": fam, "coarse_lu_ms": t_lu, "vcycle_ms": t_v}

@@ -121,6 +121,8 @@ int sa_ctx_create(int device, sa_ctx *out);
 int sa_ctx_destroy(sa_ctx ctx);
 #define SA_OPT_FP_EXACT 0 /* FP kernels in the reference's sequential order, no FMA (bit-exact) */
 #define SA_OPT_GRAPHS 1   /* capture Arnoldi steps into CUDA graphs (default on)              */
+#define SA_OPT_PDL 2      /* batched engine: start each V-cycle kernel while the one before it
+                           * drains (programmatic dependent launch; default on)               */
 int sa_ctx_set_option(sa_ctx ctx, int option, int value);
 int sa_ctx_flags(sa_ctx ctx, unsigned *flags, int clear);
 int sa_ctx_launches(sa_ctx ctx, long long *count);
@@ -299,6 +301,14 @@ int sa_batch_precondition(sa_ctx ctx, sa_batch B, const int32_t *in, int32_t *ou
 int sa_batch_autotune(sa_ctx ctx, sa_batch B, int reps);
 /* the chosen lanes per row of one operator (op: 0 A, 1 LD sweep, 2 U, 3 P, 4 R) */
 int sa_batch_group(sa_batch B, int level, int op, int *group);
+/* sets the lanes per row of one operator (1, 2, 4, 8, 16, 32; 0 = tile-staged
+ * stream, not for op 1); results do not depend on it */
+int sa_batch_set_group(sa_batch B, int level, int op, int group);
+/* the colour sweep's launch form at one level: 0 one launch per colour, 1 one
+ * thread-block-cluster launch, 2 the same over a packed copy of LD; set >= 0
+ * chooses it (SA_ERR_ARG / an error if the level lacks that form), -1 reads
+ * it; results do not depend on it */
+int sa_batch_sweep_form(sa_batch B, int level, int set, int *form);
 /* Work/main.cpp:153-161 per system and right-hand side: max|M_f64 b| / ||b|| */
 int sa_batch_rule_ratios(sa_ctx ctx, sa_batch B, const double *b, const double *nrm_b, double *ratio);
 /* one operator of one batch level on interleaved vectors: op 0 A, 2 U, 3 P,
@@ -307,6 +317,11 @@ int sa_batch_rule_ratios(sa_ctx ctx, sa_batch B, const double *b, const double *
 int sa_batch_level_op(sa_ctx ctx, sa_batch B, int level, int op, const int32_t *in, int32_t *out);
 /* the batched coarsest LU solve on the batch's own level vectors (for timing) */
 int sa_batch_coarse_solve(sa_ctx ctx, sa_batch B);
+/* milliseconds per call of one operator as the solver runs it (max(reps, 5)
+ * calls captured in one CUDA graph when graphs are on, else reps calls on the
+ * stream): op 0..4 as sa_batch_level_op, 5 the coarsest LU (in/out unused), 6
+ * the whole V-cycle (level unused); the autotuner times its candidates so */
+int sa_batch_time_op(sa_ctx ctx, sa_batch B, int level, int op, const int32_t *in, int32_t *out, int reps, float *ms);
 /* rows, columns, entries and colour count of one batch level operator */
 int sa_batch_level_info(sa_batch B, int level, int op, int *n, int *m, int64_t *nnz, int *ncolours);
 /* Restarted(FGMRESflex) per pair; bits: F_G per system; nrm_b per pair;

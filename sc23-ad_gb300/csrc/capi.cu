@@ -178,6 +178,7 @@ extern "C" int sa_ctx_set_option(sa_ctx ctx, int option, int value) {
     if (!ctx) return fail(SA_ERR_ARG, "null context");
     if (option == SA_OPT_FP_EXACT) ctx->c.fp_exact = value != 0;
     else if (option == SA_OPT_GRAPHS) ctx->c.use_graphs = value != 0;
+    else if (option == SA_OPT_PDL) ctx->c.use_pdl = value != 0;
     else return fail(SA_ERR_ARG, "unknown option");
     return SA_OK;
 }
@@ -1183,6 +1184,25 @@ extern "C" int sa_batch_autotune(sa_ctx ctx, sa_batch B, int reps) {
     SA_GUARD_END
 }
 
+extern "C" int sa_batch_set_group(sa_batch B, int level, int op, int group) {
+    if (!B || level < 0 || level >= B->h->Dmax || op < 0 || op > 4 ||
+        !(group == 1 || group == 2 || group == 4 || group == 8 || group == 16 || group == 32 || (group == 0 && op != 1)))
+        return fail(SA_ERR_ARG, "invalid argument");
+    SA_GUARD_BEGIN
+    B->eng->set_groups(level, op, group);
+    return SA_OK;
+    SA_GUARD_END
+}
+
+extern "C" int sa_batch_sweep_form(sa_batch B, int level, int set, int *form) {
+    if (!B || !form || level < 0 || level >= B->h->Dmax || set < -1 || set > 2)
+        return fail(SA_ERR_ARG, "invalid argument");
+    SA_GUARD_BEGIN
+    *form = B->eng->sweep_form(level, set);
+    return SA_OK;
+    SA_GUARD_END
+}
+
 extern "C" int sa_batch_group(sa_batch B, int level, int op, int *group) {
     if (!B || !group || level < 0 || level >= B->h->Dmax || op < 0 || op > 4) return fail(SA_ERR_ARG, "invalid argument");
     *group = B->eng->group(level, op);
@@ -1300,6 +1320,17 @@ extern "C" int sa_batch_level_op(sa_ctx ctx, sa_batch B, int level, int op, cons
     Staged so(c, out, sizeof(int32_t) * std::max<size_t>(rows_out, 1) * R, op == 1, true);
     B->eng->level_op(level, op, (const int *)si.get(), (int *)so.get());
     so.finish();
+    return SA_OK;
+    SA_GUARD_END
+}
+
+extern "C" int sa_batch_time_op(sa_ctx ctx, sa_batch B, int level, int op, const int32_t *in, int32_t *out, int reps,
+                                float *ms) {
+    if (!ctx || !B || !ms || reps < 1 || op < 0 || op > 6 || (op <= 4 && (level < 0 || level >= B->h->Dmax)) ||
+        (op != 5 && (!in || !out)))
+        return fail(SA_ERR_ARG, "invalid argument");
+    SA_GUARD_BEGIN
+    *ms = B->eng->time_op(level, op, in, out, reps);
     return SA_OK;
     SA_GUARD_END
 }

@@ -41,6 +41,17 @@ constexpr int kBThreads = 256;
 constexpr int kTileRows = 2048;
 constexpr int kBLuThreads = 512;  // 16 warps: room for 128 registers a thread
 
+// Programmatic dependent launch.  The V-cycle's kernels are launched with the
+// programmatic-serialization attribute: a kernel may start while the one
+// before it drains, reads what does not change during the V-cycle (row
+// pointers, row lists), then waits at pdl_wait() until the previous grid has
+// completed and its writes are visible; nothing it reads or writes that the
+// previous kernels produce or read is touched before that wait.  Each kernel
+// lets its successor start as soon as all of its own CTAs are running.
+// Launched without the attribute, both instructions have no effect.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 struct DBCsr {
     int n;
     const int *rptr, *cind, *val;
@@ -172,13 +183,15 @@ template <int R, int G, int MODE>
 __global__ void __launch_bounds__(kBThreads)
 k_bspmv(DBCsr A, const int *__restrict__ x, int *__restrict__ y, const int *__restrict__ z,
         const int *__restrict__ row_sys, unsigned *__restrict__ pflag, unsigned *__restrict__ flags) {
+    pdl_trigger();
     const long long tid = (long long)blockIdx.x * kBThreads + threadIdx.x;
     const int row = (int)(tid / G), lane = (int)(tid % G);
     long long acc[R];
 #pragma unroll
     for (int r = 0; r < R; r++) acc[r] = 0;
-    if (row < A.n) row_accumulate<R, G, false, false>(A.cind, A.val, __ldg(A.rptr + row), __ldg(A.rptr + row + 1),
-                                                      lane, x, acc);
+    const int e0 = row < A.n ? __ldg(A.rptr + row) : 0, e1 = row < A.n ? __ldg(A.rptr + row + 1) : 0;
+    pdl_wait();
+    if (row < A.n) row_accumulate<R, G, false, false>(A.cind, A.val, e0, e1, lane, x, acc);
 #pragma unroll
     for (int r = 0; r < R; r++)
 #pragma unroll
@@ -191,6 +204,8 @@ template <int R, int MODE>
 __global__ void __launch_bounds__(kStreamThreads)
 k_bspmv_stream(DBCsr A, const int *__restrict__ x, int *__restrict__ y, const int *__restrict__ z,
                const int *__restrict__ row_sys, unsigned *__restrict__ pflag, unsigned *__restrict__ flags) {
+    pdl_trigger();
+    pdl_wait();
     long long acc[R];
 #pragma unroll
     for (int r = 0; r < R; r++) acc[r] = 0;
@@ -207,17 +222,20 @@ template <int R, int G>
 __global__ void __launch_bounds__(kBThreads)
 k_bcolour(int cnt, const int *__restrict__ rows, DBCsr LD, const int *__restrict__ in, int *out,
           const int *__restrict__ row_sys, unsigned *__restrict__ pflag, unsigned *__restrict__ flags) {
+    pdl_trigger();
     const long long tid = (long long)blockIdx.x * kBThreads + threadIdx.x;
     const int k = (int)(tid / G), lane = (int)(tid % G);
     long long acc[R];
 #pragma unroll
     for (int r = 0; r < R; r++) acc[r] = 0;
-    int row = -1, dpos = 0;
+    int row = -1, dpos = 0, e0 = 0;
     if (k < cnt) {
         row = __ldg(rows + k);
+        e0 = __ldg(LD.rptr + row);
         dpos = __ldg(LD.rptr + row + 1) - 1;
-        row_accumulate<R, G, true, false>(LD.cind, LD.val, __ldg(LD.rptr + row), dpos, lane, out, acc);
     }
+    pdl_wait();
+    if (k < cnt) row_accumulate<R, G, true, false>(LD.cind, LD.val, e0, dpos, lane, out, acc);
 #pragma unroll
     for (int r = 0; r < R; r++)
 #pragma unroll
@@ -262,6 +280,8 @@ __global__ void __launch_bounds__(kBThreads)
 k_bsweep_cluster(const int *__restrict__ gc_ptr, const int *__restrict__ cbound, const int *__restrict__ grows,
                  DBCsr LD, const int *__restrict__ in, int *out, const int *__restrict__ row_sys,
                  unsigned *__restrict__ pflag, unsigned *__restrict__ flags) {
+    pdl_trigger();
+    pdl_wait();
     const int g = blockIdx.x / kClusterCtas, rank = blockIdx.x % kClusterCtas;
     const int t = rank * kBThreads + threadIdx.x;  // thread index inside the cluster
     const int lane = t % G, slot = t / G;
@@ -308,6 +328,153 @@ k_bsweep_cluster(const int *__restrict__ gc_ptr, const int *__restrict__ cbound,
     }
 }
 
+// ------------------------------------ packed cluster sweep (coarse levels)
+// The cluster sweep above spends most of a pass waiting on a chain of
+// dependent loads (row list -> row pointers -> entries -> vector -> shifts)
+// although only the vector values change during the sweep.  This form reads
+// a copy of the level's LD packed at setup in the order the cluster consumes
+// it: colour k's rows are dealt to the cluster's CTAs in turn (row i of the
+// colour to CTA i % kClusterCtas), each (colour, CTA) run of rows is one
+// contiguous range of items, and each item carries everything static about
+// its row:
+//   item = {row, first entry, inverse diagonal, meta}, meta = len | bit << 20 | dbit << 26
+//   entry = {column, value} of the strictly lower part (the diagonal is the item's dinv)
+// A CTA fetches the items, up to kPkU entries a lane and the input values of
+// its next pass before it works on (and waits at the barrier after) the
+// current one, so a pass costs one round trip for the vector values it reads
+// plus the barrier.  Results are those of k_bcolour / k_bsweep_cluster.
+constexpr int kPkU = 4;          // entries per lane fetched ahead; longer rows finish in a loop
+// a CTA per SM with many loads in flight (four right-hand sides need the registers of 512)
+template <int R>
+constexpr int pk_threads() { return R == 4 ? 512 : 1024; }
+
+template <int R>
+struct PkPass {
+    int4 hd;
+    int2 e[kPkU];
+    int iv[R];
+    bool ok;
+};
+
+template <int R, int G, bool IN = true>
+__device__ __forceinline__ void pk_fetch(const int4 *__restrict__ items, const int2 *__restrict__ ents,
+                                         const int *__restrict__ in, int it, int ie, int lane, PkPass<R> &p) {
+    p.ok = it < ie;
+    p.hd = p.ok ? __ldg(items + it) : make_int4(0, 0, 0, 0);
+    const int len = p.hd.w & 0xFFFFF;
+#pragma unroll
+    for (int u = 0; u < kPkU; u++) {
+        const int j = lane + u * G;
+        p.e[u] = j < len ? __ldg(ents + p.hd.y + j) : make_int2(0, 0);
+    }
+    if (IN && p.ok) load_r<R>(in, p.hd.x, p.iv);
+}
+
+template <int R, int G>
+__global__ void __launch_bounds__(pk_threads<R>())
+k_bsweep_packed(const int *__restrict__ gc_ptr, const int *__restrict__ sw_ptr, const int4 *__restrict__ items,
+                const int2 *__restrict__ ents, const int *__restrict__ in, int *out, const int *__restrict__ row_sys,
+                unsigned *__restrict__ pflag, unsigned *__restrict__ flags) {
+    pdl_trigger();
+    const int g = blockIdx.x / kClusterCtas, q = blockIdx.x % kClusterCtas;
+    const int lane = threadIdx.x % G, ls = threadIdx.x / G;
+    constexpr int kS = pk_threads<R>() / G;  // rows of one pass of this CTA
+    const int k1 = gc_ptr[g + 1] - 1;  // colours k of the group: gc_ptr[g] <= k < k1
+    int k = gc_ptr[g];
+    if (k >= k1) {  // a group without colours (no barrier is reached by any CTA of it)
+        pdl_wait();
+        return;
+    }
+    int ie = __ldg(sw_ptr + k * kClusterCtas + q + 1);
+    int base = __ldg(sw_ptr + k * kClusterCtas + q);
+    PkPass<R> cur, nxt;
+    pk_fetch<R, G, false>(items, ents, in, base + ls, ie, lane, cur);  // the packed LD does not change
+    pdl_wait();
+    if (cur.ok) load_r<R>(in, cur.hd.x, cur.iv);
+    while (k < k1) {
+        // the next pass: more rows of this colour, or the next colour's first
+        int nk = k, nbase = base + kS, nie = ie;
+        const bool colour_end = nbase >= ie;
+        if (colour_end) {
+            nk = k + 1;
+            if (nk < k1) {
+                nbase = __ldg(sw_ptr + nk * kClusterCtas + q);
+                nie = __ldg(sw_ptr + nk * kClusterCtas + q + 1);
+            }
+        }
+        if (nk < k1) pk_fetch<R, G>(items, ents, in, nbase + ls, nie, lane, nxt);
+        else nxt.ok = false;
+
+        long long acc[R];
+#pragma unroll
+        for (int r = 0; r < R; r++) acc[r] = 0;
+        const int len = cur.hd.w & 0xFFFFF;
+        {
+            int xv[kPkU][R];
+#pragma unroll
+            for (int u = 0; u < kPkU; u++) {
+                if (lane + u * G < len) load_cg_r<R>(out, cur.e[u].x, xv[u]);
+                else
+#pragma unroll
+                    for (int r = 0; r < R; r++) xv[u][r] = 0;
+            }
+#pragma unroll
+            for (int u = 0; u < kPkU; u++)
+#pragma unroll
+                for (int r = 0; r < R; r++) acc[r] = wsub(acc[r], (long long)cur.e[u].y * (long long)xv[u][r]);
+        }
+        // rows longer than kPkU * G entries: four entries a lane in flight
+        int j = lane + kPkU * G;
+        for (; j + 3 * G < len; j += 4 * G) {
+            int2 ev[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) ev[u] = __ldg(ents + cur.hd.y + j + u * G);
+            int xv[4][R];
+#pragma unroll
+            for (int u = 0; u < 4; u++) load_cg_r<R>(out, ev[u].x, xv[u]);
+#pragma unroll
+            for (int u = 0; u < 4; u++)
+#pragma unroll
+                for (int r = 0; r < R; r++) acc[r] = wsub(acc[r], (long long)ev[u].y * (long long)xv[u][r]);
+        }
+        for (; j < len; j += G) {
+            const int2 ev = __ldg(ents + cur.hd.y + j);
+            int xv[R];
+            load_cg_r<R>(out, ev.x, xv);
+#pragma unroll
+            for (int r = 0; r < R; r++) acc[r] = wsub(acc[r], (long long)ev.y * (long long)xv[r]);
+        }
+#pragma unroll
+        for (int r = 0; r < R; r++)
+#pragma unroll
+            for (int o = G / 2; o > 0; o >>= 1) acc[r] = wadd(acc[r], shfl_xor(acc[r], o));
+        if (lane == 0 && cur.ok) {
+            const int row = cur.hd.x;
+            const int bit = (cur.hd.w >> 20) & 63, dbit = (int)((unsigned)cur.hd.w >> 26);
+            const long long dinv = cur.hd.z;
+            int res[R];
+            bool any = false;
+#pragma unroll
+            for (int r = 0; r < R; r++) {
+                const long long tt = wadd(wshl((long long)cur.iv[r], bit), acc[r]);
+                const long long sv = wmul(tt >> bit, dinv) >> dbit;
+                res[r] = lo32(sv);
+                if (!fits32(sv)) {
+                    atomicOr(pflag + (size_t)row_sys[row] * R + r, ST_OVERFLOW);
+                    any = true;
+                }
+            }
+            store_r<R>(out, row, res);
+            if (any) atomicOr(flags, ST_OVERFLOW);
+        }
+        if (colour_end) cluster_barrier();
+        cur = nxt;
+        k = nk;
+        base = nbase;
+        ie = nie;
+    }
+}
+
 // ------------------------------------------------------------ coarse LU
 struct BLuDesc {
     int n, sys;
@@ -325,6 +492,8 @@ template <int R>
 __global__ void __launch_bounds__(kBLuThreads, 1)
 k_blu(const BLuDesc *__restrict__ desc, const int *__restrict__ Lcat, const int *__restrict__ Ucat,
       const int *__restrict__ dcat, unsigned *__restrict__ pflag, unsigned *__restrict__ flags) {
+    pdl_trigger();
+    pdl_wait();
     const BLuDesc d = desc[blockIdx.x];
     const int n = d.n;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -454,6 +623,8 @@ template <int R>
 __global__ void __launch_bounds__(kLuCThreads, 1)
 k_blu_cluster(const BLuDesc *__restrict__ desc, const int *__restrict__ Lcat, const int *__restrict__ Ucat,
               const int *__restrict__ dcat, unsigned *__restrict__ pflag, unsigned *__restrict__ flags) {
+    pdl_trigger();
+    pdl_wait();
     namespace cg = cooperative_groups;
     cg::cluster_group cl = cg::this_cluster();
     const BLuDesc d = desc[blockIdx.x / kLuCtas];
@@ -1085,8 +1256,12 @@ struct DevBLevel {
     int *row_sys = nullptr;       // system of each row of this level
     int *row_sys_next = nullptr;  // ... and of level l+1 (rows of R)
     // cluster sweep: groups of systems, each walking its own colours
+    // (use_cluster 0: one launch per colour, 1: k_bsweep_cluster, 2: k_bsweep_packed)
     int use_cluster = 0, ngroups = 0;
     int *gc_ptr = nullptr, *cbound = nullptr, *grows = nullptr;
+    int *sw_ptr = nullptr;          // packed form: items of (colour, CTA) run k * kClusterCtas + q
+    int4 *pk_items = nullptr;
+    int2 *pk_ents = nullptr;
 };
 
 struct BatchEngine::Impl {
@@ -1121,6 +1296,12 @@ struct BatchEngine::Impl {
     BPair *pairs = nullptr;
     BInfo *info_d = nullptr, *info_h = nullptr;
     std::vector<cudaGraphExec_t> graphs;
+    bool graph_pdl = true;  // the PDL setting the graphs were captured with
+    // the stand-alone V-cycle (precondition) replayed from a graph captured for one in/out pair
+    cudaGraphExec_t vc_graph = nullptr;
+    const int *vc_in = nullptr;
+    int *vc_out = nullptr;
+    long long vc_launches = 0;
     std::vector<long long> graph_launches;
     size_t N0 = 0;  // level-0 rows
 
@@ -1292,6 +1473,44 @@ struct BatchEngine::Impl {
         d.grows = dupload(rows);
         const int ncol = (int)L.colour_ptr.size() - 1;
         d.use_cluster = ncol > 0 && (double)L.n_smooth / ncol < 16384.0;
+        if (ncol > 0 && (double)L.n_smooth / ncol < 65536.0) build_packed(l, gc, cb, rows);
+    }
+
+    // the packed copy of LD read by k_bsweep_packed (rows of each colour dealt
+    // to the cluster's CTAs in turn); left out when a row does not fit the
+    // item format, and the level then keeps the other two forms
+    void build_packed(int l, const std::vector<int> &gc, const std::vector<int> &cb, const std::vector<int> &rows) {
+        const BatchCsr &LD = h->lv[l].LD;
+        DevBLevel &d = lv[l];
+        const size_t K = cb.size();
+        std::vector<char> is_end(K, 0);  // cb entries that close a group (no rows of their own)
+        for (size_t g = 0; g + 1 < gc.size(); g++) is_end[gc[g + 1] - 1] = 1;
+        std::vector<int> sw(K * kClusterCtas + 1, 0);
+        std::vector<int4> items;
+        std::vector<int2> ents;
+        items.reserve(rows.size());
+        for (size_t kk = 0; kk < K; kk++)
+            for (int q = 0; q < kClusterCtas; q++) {
+                sw[kk * kClusterCtas + q] = (int)items.size();
+                if (is_end[kk]) continue;
+                for (int i = cb[kk] + q; i < cb[kk + 1]; i += kClusterCtas) {
+                    const int row = rows[i];
+                    const int e0 = LD.rptr[row], dp = LD.rptr[row + 1] - 1;
+                    const int len = dp - e0, bit = LD.bit[row], dbit = LD.dbit[row];
+                    if (len < 0 || len >= (1 << 20) || bit < 0 || bit > 63 || dbit < 0 || dbit > 63 ||
+                        ents.size() + (size_t)len >= (size_t)1 << 31)
+                        return;
+                    const unsigned meta = (unsigned)len | (unsigned)bit << 20 | (unsigned)dbit << 26;
+                    items.push_back(make_int4(row, (int)ents.size(), LD.val[dp], (int)meta));
+                    for (int e = e0; e < dp; e++) ents.push_back(make_int2(LD.cind[e], LD.val[e]));
+                }
+            }
+        sw[K * kClusterCtas] = (int)items.size();
+        if (items.empty()) return;
+        d.sw_ptr = dupload(sw);
+        d.pk_items = dupload(items);
+        d.pk_ents = ents.empty() ? (int2 *)dmalloc(sizeof(int2)) : dupload(ents);
+        if (d.use_cluster) d.use_cluster = 2;
     }
 
     void free_krylov() {
@@ -1308,6 +1527,88 @@ struct BatchEngine::Impl {
             if (g) cudaGraphExecDestroy(g);
         graphs.clear();
         graph_launches.clear();
+        if (vc_graph) cudaGraphExecDestroy(vc_graph);
+        vc_graph = nullptr;
+    }
+
+    // Milliseconds per call of fn the way the solver runs it: max(reps, 5)
+    // calls captured in one CUDA graph (launch gaps and programmatic overlap
+    // as in the Arnoldi-step graphs), timed on its second launch; or reps
+    // calls on the stream after one warm-up call when graphs are off.
+    template <typename F>
+    float timed(F &&fn, int reps, cudaEvent_t e0, cudaEvent_t e1) {
+        const long long before = c.launches;
+        float ms = 0;
+        int n = reps;
+        if (c.use_graphs) {
+            n = std::max(reps, 5);
+            cudaGraph_t g = nullptr;
+            cudaGraphExec_t ge;
+            SAGB_CUDA(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
+            try {
+                for (int k = 0; k < n; k++) fn();
+            } catch (...) {
+                cudaStreamEndCapture(c.stream, &g);
+                if (g) cudaGraphDestroy(g);
+                c.launches = before;
+                throw;
+            }
+            SAGB_CUDA(cudaStreamEndCapture(c.stream, &g));
+            SAGB_CUDA(cudaGraphInstantiate(&ge, g, 0));
+            cudaGraphDestroy(g);
+            SAGB_CUDA(cudaGraphLaunch(ge, c.stream));
+            SAGB_CUDA(cudaEventRecord(e0, c.stream));
+            SAGB_CUDA(cudaGraphLaunch(ge, c.stream));
+            SAGB_CUDA(cudaEventRecord(e1, c.stream));
+            SAGB_CUDA(cudaEventSynchronize(e1));
+            SAGB_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+            cudaGraphExecDestroy(ge);
+        } else {
+            fn();
+            SAGB_CUDA(cudaEventRecord(e0, c.stream));
+            for (int k = 0; k < n; k++) fn();
+            SAGB_CUDA(cudaEventRecord(e1, c.stream));
+            SAGB_CUDA(cudaEventSynchronize(e1));
+            SAGB_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        }
+        c.launches = before;
+        return ms / n;
+    }
+
+    // precondition(): the V-cycle from a captured graph (re-captured when the
+    // vectors, the launch shapes or the PDL setting change)
+    void vcycle_graph(const int *in, int *out) {
+        if (!c.use_graphs) return vcycle(in, out);
+        if (graph_pdl != c.use_pdl) {
+            clear_graphs();
+            graph_pdl = c.use_pdl;
+        }
+        if (vc_graph && (vc_in != in || vc_out != out)) {
+            cudaGraphExecDestroy(vc_graph);
+            vc_graph = nullptr;
+        }
+        if (!vc_graph) {
+            cudaGraph_t g = nullptr;
+            const long long before = c.launches;
+            SAGB_CUDA(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
+            try {
+                vcycle(in, out);
+            } catch (...) {
+                cudaStreamEndCapture(c.stream, &g);
+                if (g) cudaGraphDestroy(g);
+                c.launches = before;
+                throw;
+            }
+            SAGB_CUDA(cudaStreamEndCapture(c.stream, &g));
+            SAGB_CUDA(cudaGraphInstantiate(&vc_graph, g, 0));
+            cudaGraphDestroy(g);
+            vc_launches = c.launches - before;
+            c.launches = before;
+            vc_in = in;
+            vc_out = out;
+        }
+        SAGB_CUDA(cudaGraphLaunch(vc_graph, c.stream));
+        c.launches += vc_launches;
     }
 
     ~Impl() {
@@ -1318,6 +1619,9 @@ struct BatchEngine::Impl {
             dfree(d.gc_ptr);
             dfree(d.cbound);
             dfree(d.grows);
+            dfree(d.sw_ptr);
+            dfree(d.pk_items);
+            dfree(d.pk_ents);
         }
         for (auto p : row_sys) dfree(p);
         for (auto p : ee) dfree(p);
@@ -1350,23 +1654,45 @@ struct BatchEngine::Impl {
         }
     }
 
+    // one kernel of the V-cycle on the library stream: programmatic dependent
+    // launch when enabled, a thread-block cluster when cluster > 1
+    template <typename... KArgs, typename... Args>
+    void launch(void (*k)(KArgs...), int grid, int block, size_t smem, int cluster, Args... args) {
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(grid);
+        cfg.blockDim = dim3(block);
+        cfg.dynamicSmemBytes = smem;
+        cfg.stream = c.stream;
+        cudaLaunchAttribute at[2];
+        int na = 0;
+        if (c.use_pdl) {
+            at[na].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+            at[na].val.programmaticStreamSerializationAllowed = 1;
+            na++;
+        }
+        if (cluster > 1) {
+            at[na].id = cudaLaunchAttributeClusterDimension;
+            at[na].val.clusterDim.x = cluster;
+            at[na].val.clusterDim.y = 1;
+            at[na].val.clusterDim.z = 1;
+            na++;
+        }
+        cfg.attrs = at;
+        cfg.numAttrs = na;
+        SAGB_CUDA(cudaLaunchKernelEx(&cfg, k, args...));
+        c.launches++;
+    }
+
     void bspmv(const DevBMat &M, const int *x, int *y, int mode, const int *z, const int *row_sys) {
         if (M.d.n == 0) return;
         if (M.group == 0) {
             const int blocks = (M.d.n + kStreamThreads - 1) / kStreamThreads;
             by_r([&](auto RR) {
                 constexpr int R = decltype(RR)::value;
-                if (mode == SPMV_SET)
-                    k_bspmv_stream<R, SPMV_SET><<<blocks, kStreamThreads, 0, c.stream>>>(M.d, x, y, z, row_sys, cur_pflag,
-                                                                                     c.d_flags);
-                else if (mode == SPMV_RESID)
-                    k_bspmv_stream<R, SPMV_RESID><<<blocks, kStreamThreads, 0, c.stream>>>(M.d, x, y, z, row_sys,
-                                                                                       cur_pflag, c.d_flags);
-                else
-                    k_bspmv_stream<R, SPMV_ADD><<<blocks, kStreamThreads, 0, c.stream>>>(M.d, x, y, z, row_sys, cur_pflag,
-                                                                                     c.d_flags);
+                auto k = mode == SPMV_SET ? k_bspmv_stream<R, SPMV_SET>
+                         : mode == SPMV_RESID ? k_bspmv_stream<R, SPMV_RESID> : k_bspmv_stream<R, SPMV_ADD>;
+                launch(k, blocks, kStreamThreads, 0, 1, M.d, x, y, z, row_sys, cur_pflag, c.d_flags);
             });
-            c.launches++;
             return;
         }
         const long long threads = (long long)M.d.n * M.group;
@@ -1375,41 +1701,37 @@ struct BatchEngine::Impl {
             constexpr int R = decltype(RR)::value;
             by_g(M.group, [&](auto GG) {
                 constexpr int G = decltype(GG)::value;
-                if (mode == SPMV_SET)
-                    k_bspmv<R, G, SPMV_SET><<<blocks, kBThreads, 0, c.stream>>>(M.d, x, y, z, row_sys, cur_pflag, c.d_flags);
-                else if (mode == SPMV_RESID)
-                    k_bspmv<R, G, SPMV_RESID><<<blocks, kBThreads, 0, c.stream>>>(M.d, x, y, z, row_sys, cur_pflag, c.d_flags);
-                else
-                    k_bspmv<R, G, SPMV_ADD><<<blocks, kBThreads, 0, c.stream>>>(M.d, x, y, z, row_sys, cur_pflag, c.d_flags);
+                auto k = mode == SPMV_SET ? k_bspmv<R, G, SPMV_SET>
+                         : mode == SPMV_RESID ? k_bspmv<R, G, SPMV_RESID> : k_bspmv<R, G, SPMV_ADD>;
+                launch(k, blocks, kBThreads, 0, 1, M.d, x, y, z, row_sys, cur_pflag, c.d_flags);
             });
         });
-        c.launches++;
     }
 
     void sweep(int l, const int *in, int *out) {
         const DevBLevel &L = lv[l];
-        if (L.use_cluster && L.ngroups > 0) {
-            cudaLaunchConfig_t cfg = {};
-            cfg.gridDim = dim3(L.ngroups * kClusterCtas);
-            cfg.blockDim = dim3(kBThreads);
-            cfg.stream = c.stream;
-            cudaLaunchAttribute at[1];
-            at[0].id = cudaLaunchAttributeClusterDimension;
-            at[0].val.clusterDim.x = kClusterCtas;
-            at[0].val.clusterDim.y = 1;
-            at[0].val.clusterDim.z = 1;
-            cfg.attrs = at;
-            cfg.numAttrs = 1;
+        if (L.use_cluster == 2 && L.pk_items && L.ngroups > 0) {
             by_r([&](auto RR) {
                 constexpr int R = decltype(RR)::value;
                 by_g(L.LD.group, [&](auto GG) {
                     constexpr int G = decltype(GG)::value;
-                    SAGB_CUDA(cudaLaunchKernelEx(&cfg, k_bsweep_cluster<R, G>, (const int *)L.gc_ptr,
-                                                 (const int *)L.cbound, (const int *)L.grows, L.LD.d, in, out,
-                                                 (const int *)L.row_sys, cur_pflag, c.d_flags));
+                    launch(k_bsweep_packed<R, G>, L.ngroups * kClusterCtas, pk_threads<R>(), 0, kClusterCtas,
+                           (const int *)L.gc_ptr, (const int *)L.sw_ptr, (const int4 *)L.pk_items,
+                           (const int2 *)L.pk_ents, in, out, (const int *)L.row_sys, cur_pflag, c.d_flags);
                 });
             });
-            c.launches++;
+            return;
+        }
+        if (L.use_cluster && L.ngroups > 0) {
+            by_r([&](auto RR) {
+                constexpr int R = decltype(RR)::value;
+                by_g(L.LD.group, [&](auto GG) {
+                    constexpr int G = decltype(GG)::value;
+                    launch(k_bsweep_cluster<R, G>, L.ngroups * kClusterCtas, kBThreads, 0, kClusterCtas,
+                           (const int *)L.gc_ptr, (const int *)L.cbound, (const int *)L.grows, L.LD.d, in, out,
+                           (const int *)L.row_sys, cur_pflag, c.d_flags);
+                });
+            });
             return;
         }
         const int nc = (int)L.colour_ptr.size() - 1;
@@ -1422,11 +1744,10 @@ struct BatchEngine::Impl {
                 constexpr int R = decltype(RR)::value;
                 by_g(L.LD.group, [&](auto GG) {
                     constexpr int G = decltype(GG)::value;
-                    k_bcolour<R, G><<<blocks, kBThreads, 0, c.stream>>>(cnt, L.colour_rows + a, L.LD.d, in, out,
-                                                                       L.row_sys, cur_pflag, c.d_flags);
+                    launch(k_bcolour<R, G>, blocks, kBThreads, 0, 1, cnt, (const int *)(L.colour_rows + a), L.LD.d, in,
+                           out, (const int *)L.row_sys, cur_pflag, c.d_flags);
                 });
             });
-            c.launches++;
         }
     }
 
@@ -1447,26 +1768,13 @@ struct BatchEngine::Impl {
         if (!nlu) return;
         by_r([&](auto RR) {
             constexpr int R = decltype(RR)::value;
-            if (lu_cluster) {
-                cudaLaunchConfig_t cfg = {};
-                cfg.gridDim = dim3(nlu * kLuCtas);
-                cfg.blockDim = dim3(kLuCThreads);
-                cfg.dynamicSmemBytes = lu_csmem;
-                cfg.stream = c.stream;
-                cudaLaunchAttribute at[1];
-                at[0].id = cudaLaunchAttributeClusterDimension;
-                at[0].val.clusterDim.x = kLuCtas;
-                at[0].val.clusterDim.y = 1;
-                at[0].val.clusterDim.z = 1;
-                cfg.attrs = at;
-                cfg.numAttrs = 1;
-                SAGB_CUDA(cudaLaunchKernelEx(&cfg, k_blu_cluster<R>, (const BLuDesc *)d_lu, (const int *)Lcat,
-                                             (const int *)Ucat, (const int *)dcat, pf, c.d_flags));
-            } else {
-                k_blu<R><<<nlu, kBLuThreads, lu_smem, c.stream>>>(d_lu, Lcat, Ucat, dcat, pf, c.d_flags);
-            }
+            if (lu_cluster)
+                launch(k_blu_cluster<R>, nlu * kLuCtas, kLuCThreads, lu_csmem, kLuCtas, (const BLuDesc *)d_lu,
+                       (const int *)Lcat, (const int *)Ucat, (const int *)dcat, pf, c.d_flags);
+            else
+                launch(k_blu<R>, nlu, kBLuThreads, lu_smem, 1, (const BLuDesc *)d_lu, (const int *)Lcat,
+                       (const int *)Ucat, (const int *)dcat, pf, c.d_flags);
         });
-        c.launches++;
     }
 
     // intAMGflex::Precondition (INTAMG.hpp:269-293) for the whole batch; int32
@@ -1561,6 +1869,10 @@ struct BatchEngine::Impl {
     }
 
     void step(int j) {
+        if (graph_pdl != c.use_pdl) {
+            clear_graphs();
+            graph_pdl = c.use_pdl;
+        }
         if (!c.use_graphs) {
             arnoldi_step(j);
         } else {
@@ -1569,7 +1881,7 @@ struct BatchEngine::Impl {
                 graph_launches.resize(j + 1, 0);
             }
             if (!graphs[j]) {
-                cudaGraph_t g;
+                cudaGraph_t g = nullptr;
                 const long long before = c.launches;
                 SAGB_CUDA(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
                 try {
@@ -1718,7 +2030,7 @@ BatchEngine::BatchEngine(Ctx &c, std::shared_ptr<BatchHierarchy> h, int nrhs)
 BatchEngine::~BatchEngine() { delete impl_; }
 int BatchEngine::nrhs() const { return impl_->Rn; }
 size_t BatchEngine::rows() const { return impl_->N0; }
-void BatchEngine::precondition(const int *in, int *out) { impl_->vcycle(in, out); }
+void BatchEngine::precondition(const int *in, int *out) { impl_->vcycle_graph(in, out); }
 void BatchEngine::pair_norms(const double *v, double *out_dev) {
     impl_->pair_norms(v);
     SAGB_CUDA(cudaMemcpyAsync(out_dev, impl_->nrm, sizeof(double) * (size_t)impl_->S * impl_->Rn,
@@ -1735,6 +2047,17 @@ void BatchEngine::set_groups(int level, int op, int group) {
     M->group = group;
     impl_->clear_graphs();
 }
+int BatchEngine::sweep_form(int level, int set) {
+    if (level < 0 || level >= impl_->Dmax) throw CudaError{"no such level"};
+    DevBLevel &L = impl_->lv[level];
+    if (set >= 0) {
+        if (set > 2 || (set >= 1 && L.ngroups == 0) || (set == 2 && !L.pk_items))
+            throw CudaError{"sweep form not available at this level"};
+        L.use_cluster = set;
+        impl_->clear_graphs();
+    }
+    return L.use_cluster;
+}
 int BatchEngine::group(int level, int op) const {
     const DevBLevel &L = impl_->lv[level];
     const DevBMat *M = op == 0 ? &L.A : op == 1 ? &L.LD : op == 2 ? &L.U : op == 3 ? &L.P : &L.R;
@@ -1749,6 +2072,28 @@ void BatchEngine::level_op(int level, int op, const int *in, int *out) {
     if (op == 1) return I.sweep(level, in, out);
     const DevBMat &M = op == 0 ? L.A : op == 2 ? L.U : op == 3 ? L.P : L.R;
     I.bspmv(M, in, out, SPMV_SET, nullptr, op == 4 ? L.row_sys_next : L.row_sys);
+}
+
+float BatchEngine::time_op(int level, int op, const int *in, int *out, int reps) {
+    Impl &I = *impl_;
+    if (reps < 1 || op < 0 || op > 6 || (op <= 4 && (level < 0 || level >= I.Dmax)))
+        throw CudaError{"no such operator"};
+    cudaEvent_t e0, e1;
+    SAGB_CUDA(cudaEventCreate(&e0));
+    SAGB_CUDA(cudaEventCreate(&e1));
+    float ms = 0;
+    try {
+        if (op == 5) ms = I.timed([&] { I.lu(I.pflag); }, reps, e0, e1);
+        else if (op == 6) ms = I.timed([&] { I.vcycle(in, out); }, reps, e0, e1);
+        else ms = I.timed([&] { level_op(level, op, in, out); }, reps, e0, e1);
+    } catch (...) {
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        throw;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return ms;
 }
 
 void BatchEngine::coarse_solve() {
@@ -1779,17 +2124,13 @@ void BatchEngine::autotune(int reps) {
     int *xa = (int *)dmalloc(sizeof(int) * I.N0 * I.Rn), *xb = (int *)dmalloc(sizeof(int) * I.N0 * I.Rn);
     SAGB_CUDA(cudaMemset(xa, 0, sizeof(int) * I.N0 * I.Rn));
     SAGB_CUDA(cudaMemset(xb, 0, sizeof(int) * I.N0 * I.Rn));
+    auto timeit = [&](auto &&fn) { return I.timed(fn, reps, e0, e1); };
     if (I.nlu) {
         // the coarse LU: one CTA per system or one cluster per system
         float bt[2] = {0, 0};
         for (int uc = 0; uc < 2; uc++) {
             I.lu_cluster = uc;
-            I.lu(I.pflag);
-            SAGB_CUDA(cudaEventRecord(e0, c.stream));
-            for (int k = 0; k < reps; k++) I.lu(I.pflag);
-            SAGB_CUDA(cudaEventRecord(e1, c.stream));
-            SAGB_CUDA(cudaEventSynchronize(e1));
-            SAGB_CUDA(cudaEventElapsedTime(&bt[uc], e0, e1));
+            bt[uc] = timeit([&] { I.lu(I.pflag); });
         }
         I.lu_cluster = bt[1] < bt[0];
     }
@@ -1799,36 +2140,36 @@ void BatchEngine::autotune(int reps) {
         for (int op = 0; op < 5; op++) {
             DevBMat *M = op == 0 ? &L.A : op == 1 ? &L.LD : op == 2 ? &L.U : op == 3 ? &L.P : &L.R;
             if (M->d.n == 0) continue;
+            if (op == 1) {
+                // the sweep form first: one launch per colour, or one cluster
+                // launch per level (plain or packed); each form at its best group
+                float bt[3] = {1e30f, 1e30f, 1e30f};
+                int bg[3] = {M->group, M->group, M->group};
+                const int nform = L.ngroups == 0 ? 1 : L.pk_items ? 3 : 2;
+                for (int uc = 0; uc < nform; uc++) {
+                    L.use_cluster = uc;
+                    for (int g : cand) {
+                        if (g == 0) continue;
+                        M->group = g;
+                        const float ms = timeit([&] { I.sweep(l, xa, xb); });
+                        if (ms < bt[uc]) {
+                            bt[uc] = ms;
+                            bg[uc] = g;
+                        }
+                    }
+                }
+                int best_form = 0;
+                for (int uc = 1; uc < nform; uc++)
+                    if (bt[uc] < bt[best_form]) best_form = uc;
+                L.use_cluster = best_form;
+                M->group = bg[best_form];
+                continue;
+            }
             float best = 1e30f;
             int bestg = M->group;
-            if (op == 1) {
-                // the sweep form first: one cluster launch per level or one launch per colour
-                float bt[2] = {0, 0};
-                for (int uc = 0; uc < 2; uc++) {
-                    L.use_cluster = uc;
-                    I.sweep(l, xa, xb);
-                    SAGB_CUDA(cudaEventRecord(e0, c.stream));
-                    for (int k = 0; k < reps; k++) I.sweep(l, xa, xb);
-                    SAGB_CUDA(cudaEventRecord(e1, c.stream));
-                    SAGB_CUDA(cudaEventSynchronize(e1));
-                    SAGB_CUDA(cudaEventElapsedTime(&bt[uc], e0, e1));
-                }
-                L.use_cluster = bt[1] < bt[0];
-            }
             for (int g : cand) {
-                if (g == 0 && op == 1) continue;
                 M->group = g;
-                auto run = [&] {
-                    if (op == 1) I.sweep(l, xa, xb);
-                    else I.bspmv(*M, xa, xb, SPMV_SET, nullptr, L.row_sys);
-                };
-                run();
-                SAGB_CUDA(cudaEventRecord(e0, c.stream));
-                for (int k = 0; k < reps; k++) run();
-                SAGB_CUDA(cudaEventRecord(e1, c.stream));
-                SAGB_CUDA(cudaEventSynchronize(e1));
-                float ms = 0;
-                SAGB_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+                const float ms = timeit([&] { I.bspmv(*M, xa, xb, SPMV_SET, nullptr, L.row_sys); });
                 if (ms < best) {
                     best = ms;
                     bestg = g;

@@ -35,6 +35,7 @@ struct Ctx {
     unsigned *h_flags = nullptr;     // pinned mirror
     bool fp_exact = false;           // FP kernels in sequential order without FMA
     bool use_graphs = true;
+    bool use_pdl = true;             // batched V-cycle kernels chained by programmatic dependent launch
     long long launches = 0;          // kernels launched by this context (for reporting)
     std::string err;
 };
@@ -237,9 +238,15 @@ class BatchEngine {
     void autotune(int reps);
     void set_groups(int level, int op, int group);  // op: 0 A, 1 LD, 2 U, 3 P, 4 R
     int group(int level, int op) const;
+    // the colour sweep's form at one level (0: a launch per colour, 1: cluster
+    // launch, 2: packed cluster launch); set >= 0 chooses it, -1 only reads
+    int sweep_form(int level, int set);
     // one operator of one level on caller vectors (op 1: the colour sweep LD^-1 in)
     void level_op(int level, int op, const int *in, int *out);
     void coarse_solve();  // the batched LU on the engine's own level vectors
+    // milliseconds per call as the solver runs it (inside a CUDA graph when
+    // graphs are on): op 0..4 as level_op, 5 the coarsest LU, 6 the V-cycle
+    float time_op(int level, int op, const int *in, int *out, int reps);
     void level_info(int level, int op, int *n, int *m, int64_t *nnz, int *ncolours) const;
 
   private:

@@ -19,7 +19,7 @@ INT, F64, F32 = 0, 1, 2
 MAT_FIXED, MAT_FLEX, MAT_F64, MAT_F32 = 0, 1, 2, 3
 OP_A0, OP_CA, OP_P, OP_R, OP_LD, OP_U, OP_LUL, OP_LUU, OP_BJ, OP_COLOR = range(10)
 GEN_POISSON2D, GEN_POISSON3D, GEN_ANISO2D, GEN_STENCIL27, GEN_CONVDIFF3D, GEN_VARCOEF3D = range(6)
-OPT_FP_EXACT, OPT_GRAPHS = 0, 1
+OPT_FP_EXACT, OPT_GRAPHS, OPT_PDL = 0, 1, 2
 
 VP = C.c_void_p
 I32P = C.POINTER(C.c_int32)
@@ -128,6 +128,9 @@ SIGNATURES = {
     "sa_batch_precondition": (C.c_int, [VP, VP, VP, VP]),
     "sa_batch_autotune": (C.c_int, [VP, VP, C.c_int]),
     "sa_batch_group": (C.c_int, [VP, C.c_int, C.c_int, C.POINTER(C.c_int)]),
+    "sa_batch_set_group": (C.c_int, [VP, C.c_int, C.c_int, C.c_int]),
+    "sa_batch_sweep_form": (C.c_int, [VP, C.c_int, C.c_int, C.POINTER(C.c_int)]),
+    "sa_batch_time_op": (C.c_int, [VP, VP, C.c_int, C.c_int, VP, VP, C.c_int, C.POINTER(C.c_float)]),
     "sa_batch_rule_ratios": (C.c_int, [VP, VP, VP, VP, F64P]),
     "sa_batch_solve": (C.c_int, [VP, VP, C.POINTER(SolverParams), I32P, VP, VP, VP, I32P, I32P, I32P]),
     "sa_profiler_range": (C.c_int, [C.c_int]),
@@ -689,6 +692,17 @@ class Batch:
     def coarse_solve(self):
         check(lib().sa_batch_coarse_solve(self.ctx.h, self.h))
 
+    OP_LU, OP_VCYCLE = 5, 6
+
+    def time_op(self, level, op, x=None, out=None, reps=10):
+        """Milliseconds per call of one level operator (0 A, 1 LD sweep, 2 U,
+        3 P, 4 R), the coarsest LU (5) or the V-cycle (6), timed as the solver
+        runs it; x and out are DeviceArrays."""
+        ms = C.c_float()
+        check(lib().sa_batch_time_op(self.ctx.h, self.h, level, op, None if x is None else x.ptr,
+                                     None if out is None else out.ptr, reps, C.byref(ms)))
+        return ms.value
+
     def autotune(self, reps=3):
         check(lib().sa_batch_autotune(self.ctx.h, self.h, reps))
 
@@ -696,6 +710,19 @@ class Batch:
         g = C.c_int()
         check(lib().sa_batch_group(self.h, level, op, C.byref(g)))
         return g.value
+
+    def set_group(self, level, op, group):
+        check(lib().sa_batch_set_group(self.h, level, op, group))
+
+    SWEEP_PER_COLOUR, SWEEP_CLUSTER, SWEEP_PACKED = 0, 1, 2
+
+    def sweep_form(self, level, set=-1):
+        """The colour sweep's launch form at one level (0 a launch per colour,
+        1 a cluster launch, 2 a cluster launch over the packed LD); set >= 0
+        chooses it."""
+        f = C.c_int()
+        check(lib().sa_batch_sweep_form(self.h, level, set, C.byref(f)))
+        return f.value
 
     def rule_ratios(self, b, nrm_b):
         q = np.zeros(self.nsys * self.nrhs)

@@ -82,6 +82,41 @@ def test_batched_vcycle_bit_exact(ctx, nrhs):
     # the autotuner changes launch shapes only, never results
     B.autotune(2)
     np.testing.assert_array_equal(B.precondition(vin).reshape(B.rows, nrhs), out)
+    # nor does the sweep's launch form (per colour, cluster, packed cluster) or its lanes per row
+    for form in (0, 1, 2):
+        for g in (1, 4, 32):
+            for lv in range(B.depth):
+                try:
+                    B.sweep_form(lv, form)
+                except sagb.SagbError:
+                    continue
+                B.set_group(lv, 1, g)
+            np.testing.assert_array_equal(B.precondition(vin).reshape(B.rows, nrhs), out, err_msg=f"form {form} G {g}")
+    B.close()
+
+
+def test_packed_sweep_many_groups_and_long_rows(ctx):
+    """The packed cluster sweep on a batch of many systems (one cluster per
+    group of systems) whose coarse rows are longer than the entries a lane
+    fetches ahead, compared with the one-launch-per-colour form."""
+    specs = [(sagb.GEN_STENCIL27, 9 + (k % 5), 0.0) for k in range(40)]
+    systems, _ = _systems(specs, 2)
+    B = sagb.Batch(ctx, systems, 2)
+    rng = np.random.default_rng(5)
+    vin = rng.integers(-(1 << 28), 1 << 28, size=B.rows * 2).astype(np.int32)
+    for lv in range(B.depth):
+        B.sweep_form(lv, 0)
+    ref = B.precondition(vin)
+    packed = 0
+    for lv in range(B.depth):
+        try:
+            B.sweep_form(lv, 2)
+            packed += 1
+        except sagb.SagbError:
+            pass
+        B.set_group(lv, 1, 1)  # one lane a row: rows longer than 4 entries take the tail loop
+    assert packed >= 1
+    np.testing.assert_array_equal(B.precondition(vin), ref)
     B.close()
 
 
@@ -159,4 +194,45 @@ def test_copies_share_one_setup(ctx):
         it1, cv1 = S1.solve(np.ascontiguousarray(bs[0][:, 0]), float(nrm), x1)
         assert cv[k] == cv1 and abs(int(it[k]) - it1) <= 2, (f, it[k], it1)
         S1.close()
+    B.close()
+
+
+def test_launch_options_do_not_change_results(ctx):
+    """Graph replay of the V-cycle, programmatic dependent launch and the
+    graph-timed operator clock change launch mechanics only: V-cycles and
+    whole solves are identical bit for bit with each of them off."""
+    nrhs = 2
+    systems, bs = _systems(SYSTEMS, nrhs)
+    B = sagb.Batch(ctx, systems, nrhs)
+    rng = np.random.default_rng(9)
+    vin = rng.integers(-(1 << 28), 1 << 28, size=B.rows * nrhs).astype(np.int32)
+    b = _interleave(B, bs)
+    nrm_b = np.array([np.linalg.norm(bs[s][:, r]) for s in range(B.nsys) for r in range(nrhs)])
+    params = sagb.solver_params(m=20, explicit_stop=1)
+    bits = [28] * B.nsys
+
+    def run():
+        out = B.precondition(vin)
+        x = np.zeros(B.rows * nrhs)
+        it, cv, fb = B.solve(params, bits, b, nrm_b, x)
+        return out, x, it
+
+    ref = run()
+    try:
+        for opt in (sagb.OPT_PDL, sagb.OPT_GRAPHS):
+            ctx.set_option(opt, 0)
+            got = run()
+            np.testing.assert_array_equal(got[0], ref[0])
+            np.testing.assert_array_equal(got[1], ref[1])
+            np.testing.assert_array_equal(got[2], ref[2])
+    finally:
+        ctx.set_option(sagb.OPT_PDL, 1)
+        ctx.set_option(sagb.OPT_GRAPHS, 1)
+    x = sagb.DeviceArray.from_host(ctx, vin)
+    y = sagb.DeviceArray(ctx, B.rows * nrhs, np.int32)
+    for op in range(5):
+        assert B.time_op(0, op, x, y, 3) > 0
+    assert B.time_op(0, B.OP_LU, reps=3) > 0
+    assert B.time_op(0, B.OP_VCYCLE, x, y, 3) > 0
+    x.close(); y.close()
     B.close()
