@@ -171,6 +171,12 @@ void sa_amg_params_default(sa_amg_params *p);
  *                                   Library/preconditioner/INTAMG.hpp:25-84, 149-245 */
 int sa_setup_create(int precision, const sa_amg_params *p, int n, const int32_t *rptr, const int32_t *cind,
                     const double *val, sa_setup *out);
+/* the same hierarchy, bit for bit, with the Ruge-Stueben levels' strength
+ * split, transposes, interpolation and Galerkin products on the context's GPU
+ * (the C/F splitting, smoother splits and quantisation stay on the host)
+ *                                   Library/helper/helper_multigrid.hpp:34-586 */
+int sa_setup_create_gpu(sa_ctx ctx, int precision, const sa_amg_params *p, int n, const int32_t *rptr,
+                        const int32_t *cind, const double *val, sa_setup *out);
 /* the hierarchy of another precision over the same coarsening (the Ruge-Stueben
  * chain does not depend on the precision; dfAMG and intAMGflex both build it from
  * the unscaled operators, Library/preconditioner/INTAMG.hpp:38-51, 162-173) */

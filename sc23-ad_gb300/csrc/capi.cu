@@ -480,11 +480,12 @@ extern "C" void sa_amg_params_default(sa_amg_params *p) {
     p->coarse_size = 0;
 }
 
-static void build_setup(sa_hierarchy &s, const CsrD &A) {
+static void build_setup(sa_hierarchy &s, const CsrD &A, Ctx *gpu = nullptr) {
     if (s.p.theta <= 0 || s.p.theta > 1) throw SetupError{"Theta must be in 0 < theta <= 1"};
+    const int cs = s.p.coarse_size > 0 ? s.p.coarse_size : 2000;
     if (!s.chain)
-        s.chain = std::make_shared<RsChain>(
-            rs_chain(A, s.p.theta, s.p.max_levels, s.p.coarse_size > 0 ? s.p.coarse_size : 2000));
+        s.chain = std::make_shared<RsChain>(gpu ? rs_chain_gpu(*gpu, A, s.p.theta, s.p.max_levels, cs)
+                                                : rs_chain(A, s.p.theta, s.p.max_levels, cs));
     const RsChain &chain = *s.chain;
     SmootherSpec sm;
     sm.block = s.p.smoother_blocks;
@@ -497,8 +498,8 @@ static void build_setup(sa_hierarchy &s, const CsrD &A) {
     else s.hf = std::make_shared<FpHierarchy<float>>(build_f32_hierarchy(A, chain, sm));
 }
 
-extern "C" int sa_setup_create(int precision, const sa_amg_params *p, int n, const int32_t *rptr,
-                               const int32_t *cind, const double *val, sa_setup *out) {
+static int setup_create(Ctx *gpu, int precision, const sa_amg_params *p, int n, const int32_t *rptr,
+                        const int32_t *cind, const double *val, sa_setup *out) {
     if (!out || precision < SA_INT || precision > SA_F32) return fail(SA_ERR_ARG, "invalid argument");
     if (int e = check_csr(n, n, rptr, cind)) return e;
     SA_GUARD_BEGIN
@@ -519,7 +520,7 @@ extern "C" int sa_setup_create(int precision, const sa_amg_params *p, int n, con
     A->val.assign(val, val + rptr[n]);
     s->A = A;
     try {
-        build_setup(*s, *A);
+        build_setup(*s, *A, gpu);
     } catch (...) {
         delete s;
         throw;
@@ -527,6 +528,17 @@ extern "C" int sa_setup_create(int precision, const sa_amg_params *p, int n, con
     *out = s;
     return SA_OK;
     SA_GUARD_END
+}
+
+extern "C" int sa_setup_create(int precision, const sa_amg_params *p, int n, const int32_t *rptr,
+                               const int32_t *cind, const double *val, sa_setup *out) {
+    return setup_create(nullptr, precision, p, n, rptr, cind, val, out);
+}
+
+extern "C" int sa_setup_create_gpu(sa_ctx ctx, int precision, const sa_amg_params *p, int n, const int32_t *rptr,
+                                   const int32_t *cind, const double *val, sa_setup *out) {
+    if (!ctx) return fail(SA_ERR_ARG, "null context");
+    return setup_create(&ctx->c, precision, p, n, rptr, cind, val, out);
 }
 
 extern "C" int sa_setup_derive(sa_setup s, int precision, sa_setup *out) {

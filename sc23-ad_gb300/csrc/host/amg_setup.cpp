@@ -64,11 +64,6 @@ void lmax1_scaling(CsrD &A, double *b) {
 
 // ======================================================= Ruge-Stueben coarsening
 
-struct Pattern {  // CSR without values
-    int n = 0;
-    std::vector<int> rptr, cind;
-};
-
 // get_strong_weak_set (helper_multigrid.hpp:67-108): off-diagonal a_ij is strong
 // when |a_ij| >= theta * max_k!=i |a_ik|; everything else (diagonal included)
 // goes to the weak set.
@@ -115,7 +110,7 @@ static Pattern transpose_pattern(const CsrD &S) {
 // first_pass (helper_multigrid.hpp:138-266): greedy C/F selection by the number
 // of points a candidate strongly influences, kept in buckets that are updated
 // in place as points are classified.
-static void first_pass(const CsrD &S, const Pattern &St, std::vector<int> &is_coarse) {
+void rs_first_pass(const CsrD &S, const Pattern &St, std::vector<int> &is_coarse) {
     const int N = S.n;
     is_coarse.assign(N, 0);
     std::vector<int> visited(N, 0), card(N), scard(N), infl(N, 0), index(N), where(N, 0);
@@ -219,7 +214,7 @@ static void first_pass(const CsrD &S, const Pattern &St, std::vector<int> &is_co
 
 // second_pass (helper_multigrid.hpp:378-417): a fine point with a strong fine
 // neighbour that shares no strong coarse point with it becomes coarse.
-static void second_pass(const CsrD &S, std::vector<int> &is_coarse) {
+void rs_second_pass(const CsrD &S, std::vector<int> &is_coarse) {
     const int N = S.n;
     for (int i = 0; i < N; i++) {
         if (is_coarse[i] == -38) {
@@ -352,7 +347,7 @@ static CsrD transpose(const CsrD &P) {
 // zero is removed (and restarts from alpha*x if hit again, which is the same as
 // adding to 0.0).  A dense accumulator gives the same values; the touched rows
 // are emitted in increasing order, as the merge-based original does.
-static void csc_columns(const std::vector<int> &lp, const std::vector<int> &li, const std::vector<double> &lv,
+void csc_columns(const std::vector<int> &lp, const std::vector<int> &li, const std::vector<double> &lv,
                         int L, const std::vector<int> &rp, const std::vector<int> &ri, const std::vector<double> &rv,
                         int c0, int c1, std::vector<int> &cnt, std::vector<int> &oi, std::vector<double> &ov) {
     std::vector<double> acc(L, 0.0);
@@ -442,8 +437,8 @@ void rs_level(const CsrD &A, double theta, CsrD &CA, CsrD &P, CsrD &R) {
     strong_weak(A, theta, S, W);
     Pattern St = transpose_pattern(S);
     std::vector<int> is_coarse;
-    first_pass(S, St, is_coarse);
-    second_pass(S, is_coarse);
+    rs_first_pass(S, St, is_coarse);
+    rs_second_pass(S, is_coarse);
     P = interpolation(A, S, W, is_coarse);
     R = transpose(P);
     CA = galerkin(A, P, R);

@@ -32,6 +32,22 @@ int rule_frac_bits(double c_max, double nrm_b);
 void lmax1_scaling(CsrD &A, double *b);
 
 // ------------------------------------------------------------ one coarsening level
+// The two sequential steps of the C/F splitting, also used by the GPU setup
+// (which runs the rest of a level on the device):
+//   first_pass (helper_multigrid.hpp:138-266), second_pass (378-417).
+struct Pattern {  // CSR without values
+    int n = 0;
+    std::vector<int> rptr, cind;
+};
+void rs_first_pass(const CsrD &S, const Pattern &St, std::vector<int> &is_coarse);
+void rs_second_pass(const CsrD &S, std::vector<int> &is_coarse);
+// Columns c0..c1-1 of helper::sparse::cscSpMM (helper_sparse.hpp:257-285) with
+// both operands as compressed columns (left: lp/li/lv with L rows; right:
+// rp/ri/rv): cnt[c] entries of column c are appended to oi/ov in row order.
+void csc_columns(const std::vector<int> &lp, const std::vector<int> &li, const std::vector<double> &lv, int L,
+                 const std::vector<int> &rp, const std::vector<int> &ri, const std::vector<double> &rv, int c0, int c1,
+                 std::vector<int> &cnt, std::vector<int> &oi, std::vector<double> &ov);
+
 // helper::multigrid::get_amg_set (helper/helper_multigrid.hpp:34-63):
 // from A build the coarse operator CA = P^T A P, P (Intrpl) and R = P^T (Intrpl_t).
 void rs_level(const CsrD &A, double theta, CsrD &CA, CsrD &P, CsrD &R);

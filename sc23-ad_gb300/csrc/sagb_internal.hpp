@@ -46,6 +46,13 @@ struct Ctx {
 // exact, so the solvers report such overflow (SA_FLAG_PRECOND_OVERFLOW) and
 // keep going, while overflow in A Z_j, the Gram-Schmidt sums or the Givens step
 // discards the cycle.
+// The Ruge-Stueben chain (host rs_chain) with the strength split, transposes,
+// interpolation and Galerkin products on the context's GPU and the C/F
+// splitting on the host; bit for bit the host chain (cuda/rs_setup.cu).
+struct RsChain;
+struct CsrD;
+RsChain rs_chain_gpu(Ctx &c, const CsrD &A, double theta, int max_levels, int coarse_size);
+
 struct PrecFlags {
     Ctx &c;
     unsigned *saved;

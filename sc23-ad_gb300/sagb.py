@@ -78,6 +78,7 @@ SIGNATURES = {
     "sa_spmv": (C.c_int, [VP, VP, VP, VP]),
     "sa_amg_params_default": (None, [C.POINTER(AmgParams)]),
     "sa_setup_create": (C.c_int, [C.c_int, C.POINTER(AmgParams), C.c_int, I32P, I32P, F64P, C.POINTER(VP)]),
+    "sa_setup_create_gpu": (C.c_int, [VP, C.c_int, C.POINTER(AmgParams), C.c_int, I32P, I32P, F64P, C.POINTER(VP)]),
     "sa_setup_derive": (C.c_int, [VP, C.c_int, C.POINTER(VP)]),
     "sa_setup_destroy": (C.c_int, [VP]),
     "sa_setup_depth": (C.c_int, [VP]),
@@ -254,9 +255,11 @@ def amg_params(max_levels=20, theta=0.8, smoother_blocks=0, omega=1.0, smooth_it
 
 
 class Setup:
-    """Host hierarchy (no GPU)."""
+    """The AMG hierarchy (host arrays).  With a Context the Ruge-Stueben
+    levels' strength split, transposes, interpolation and Galerkin products
+    run on its GPU; the hierarchy is the same bit for bit."""
 
-    def __init__(self, precision, rptr=None, cind=None, val=None, params=None, _handle=None):
+    def __init__(self, precision, rptr=None, cind=None, val=None, params=None, _handle=None, ctx=None):
         if _handle is not None:
             self.precision, self.h = precision, _handle
             return
@@ -266,8 +269,12 @@ class Setup:
         p = params or amg_params()
         self.precision = precision
         self.h = VP()
-        check(lib().sa_setup_create(precision, C.byref(p), len(rptr) - 1, _ptr(rptr, I32P), _ptr(cind, I32P),
-                                    _ptr(val, F64P), C.byref(self.h)))
+        if ctx is None:
+            check(lib().sa_setup_create(precision, C.byref(p), len(rptr) - 1, _ptr(rptr, I32P), _ptr(cind, I32P),
+                                        _ptr(val, F64P), C.byref(self.h)))
+        else:
+            check(lib().sa_setup_create_gpu(ctx.h, precision, C.byref(p), len(rptr) - 1, _ptr(rptr, I32P),
+                                            _ptr(cind, I32P), _ptr(val, F64P), C.byref(self.h)))
 
     def derive(self, precision):
         """The same coarsening in another precision."""
