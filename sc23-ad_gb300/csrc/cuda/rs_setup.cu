@@ -19,8 +19,8 @@
 //                   hash table keyed by row accumulates y + alpha * x in k
 //                   order (the rows of one left column are distinct, so no two
 //                   lanes of a step touch one entry), then the nonzero entries
-//                   are ranked by row; columns too long for shared memory run
-//                   through the host's own loop
+//                   are ranked by row; the longest columns keep their table
+//                   in global memory (one table per CTA)
 #include <algorithm>
 #include <climits>
 #include <cstdio>
@@ -364,6 +364,73 @@ k_sp_cols(int ncols, const int *__restrict__ cols, const int *__restrict__ lp, c
     }
 }
 
+// The same for columns whose table does not fit in shared memory: one CTA a
+// column, its table (2^log2cap slots) in global memory, one table per CTA.
+__global__ void __launch_bounds__(512)
+k_sp_cols_global(int ncols, const int *__restrict__ cols, const int *__restrict__ lp, const int *__restrict__ li,
+                 const double *__restrict__ lv, const int *__restrict__ rp, const int *__restrict__ ri,
+                 const double *__restrict__ rv, const long long *__restrict__ off, int *__restrict__ s1r,
+                 double *__restrict__ s1v, int *__restrict__ s2r, double *__restrict__ s2v, int *__restrict__ cnt,
+                 int log2cap, int *__restrict__ gkeys, double *__restrict__ gvals, unsigned *__restrict__ err) {
+    __shared__ int nlist;
+    const int cap = 1 << log2cap;
+    int *keys = gkeys + (size_t)blockIdx.x * cap;
+    double *vals = gvals + (size_t)blockIdx.x * cap;
+    const int tid = threadIdx.x, T = blockDim.x;
+    for (int w = blockIdx.x; w < ncols; w += gridDim.x) {
+        const int c = cols[w];
+        for (int s = tid; s < cap; s += T) {
+            keys[s] = -1;
+            vals[s] = 0.0;
+        }
+        if (tid == 0) nlist = 0;
+        __syncthreads();
+        for (int k = rp[c]; k < rp[c + 1]; k++) {
+            const int src = ri[k];
+            const double alpha = rv[k];
+            for (int t = lp[src] + tid; t < lp[src + 1]; t += T) {
+                const int row = li[t];
+                const double p = __dmul_rn(alpha, lv[t]);
+                int slot = (int)(((unsigned)row * 2654435761u) >> (32 - log2cap));
+                int probes = 0;
+                for (; probes < cap; probes++) {
+                    const int kk = keys[slot];
+                    if (kk == row) break;
+                    if (kk == -1) {
+                        const int prev = atomicCAS(keys + slot, -1, row);
+                        if (prev == -1 || prev == row) break;
+                    }
+                    slot = (slot + 1) & (cap - 1);
+                }
+                if (probes == cap) {
+                    atomicOr(err, 2u);
+                    continue;
+                }
+                vals[slot] = __dadd_rn(vals[slot], p);
+            }
+            __syncthreads();
+        }
+        const long long o = off[c];
+        for (int s = tid; s < cap; s += T)
+            if (keys[s] != -1 && vals[s] != 0.0) {
+                const int p = atomicAdd(&nlist, 1);
+                s1r[o + p] = keys[s];
+                s1v[o + p] = vals[s];
+            }
+        __syncthreads();
+        const int nl = nlist;
+        for (int e = tid; e < nl; e += T) {
+            const int key = s1r[o + e];
+            int rank = 0;
+            for (int j = 0; j < nl; j++) rank += s1r[o + j] < key;
+            s2r[o + rank] = key;
+            s2v[o + rank] = s1v[o + e];
+        }
+        if (tid == 0) cnt[c] = nl;
+        __syncthreads();
+    }
+}
+
 __global__ void k_sp_gather(int ncols, const int *__restrict__ cols, const long long *__restrict__ off,
                             const int *__restrict__ rptr, const int *__restrict__ s2r,
                             const double *__restrict__ s2v, int *__restrict__ oi, double *__restrict__ ov) {
@@ -402,8 +469,8 @@ void launch_cols(Ctx &c, const std::vector<int> &list, const int *lp, const int 
 // out[:, c] = sum_k right[k, c] * left[:, k] (cscSpMM, helper_sparse.hpp:257-285)
 // for c < R; left has L rows.  Returned as compressed columns in a DMat
 // (n = R columns, m = L).
-DMat product(Ctx &c, const int *lp, const int *li, const double *lv, int nl_cols, long long nl_nnz, int L,
-             const int *rp, const int *ri, const double *rv, int R, long long nr_nnz, unsigned *d_err) {
+DMat product(Ctx &c, const int *lp, const int *li, const double *lv, int L, const int *rp, const int *ri,
+             const double *rv, int R, unsigned *d_err) {
     DMat O;
     O.n = R;
     O.m = L;
@@ -413,21 +480,24 @@ DMat product(Ctx &c, const int *lp, const int *li, const double *lv, int nl_cols
     std::vector<long long> hb(R);
     down(c, hb.data(), bound, R);
     sync(c);
-    // classes by hash size: warps up to 2048 slots, whole CTAs up to 8192; longer columns on the host
-    std::vector<int> lists[8], host_cols;
+    // classes by table size (at least twice the column's products): warps up
+    // to 2^11 slots, CTAs up to 2^13 in shared memory, longer in global memory
+    std::vector<int> lists[8], glist;
+    int glog2 = 0;
     std::vector<long long> off(R + 1, 0);
     for (int col = 0; col < R; col++) {
         const long long b = hb[col];
-        off[col + 1] = off[col];
+        off[col + 1] = off[col] + b;
         if (b == 0) continue;
         int lg = 6;
-        while ((1LL << lg) < 2 * b && lg <= 13) lg++;
+        while ((1LL << lg) < 2 * b) lg++;
+        if (lg > 30) throw SetupError{"GPU setup: Galerkin column too long"};
         if (lg > 13) {
-            host_cols.push_back(col);
-            continue;
+            glist.push_back(col);
+            glog2 = std::max(glog2, lg);
+        } else {
+            lists[lg - 6].push_back(col);
         }
-        lists[lg - 6].push_back(col);
-        off[col + 1] += b;
     }
     const long long total = off[R];
     long long *doff = dnew<long long>(R + 1);
@@ -444,51 +514,39 @@ DMat product(Ctx &c, const int *lp, const int *li, const double *lv, int nl_cols
     launch_cols<11, 32>(c, lists[5], lp, li, lv, rp, ri, rv, doff, s1r, s1v, s2r, s2v, cnt, d_err);
     launch_cols<12, 256>(c, lists[6], lp, li, lv, rp, ri, rv, doff, s1r, s1v, s2r, s2v, cnt, d_err);
     launch_cols<13, 256>(c, lists[7], lp, li, lv, rp, ri, rv, doff, s1r, s1v, s2r, s2v, cnt, d_err);
-    // the long columns through the host's loop
-    std::vector<int> hcnt(R, 0), hoi;
-    std::vector<double> hov;
-    std::vector<int> hcol_start;
-    if (!host_cols.empty()) {
-        std::vector<int> hlp(nl_cols + 1), hli(nl_nnz), hrp(R + 1), hri(nr_nnz);
-        std::vector<double> hlv(nl_nnz), hrv(nr_nnz);
-        down(c, hlp.data(), lp, nl_cols + 1);
-        down(c, hli.data(), li, nl_nnz);
-        down(c, hlv.data(), lv, nl_nnz);
-        down(c, hrp.data(), rp, R + 1);
-        down(c, hri.data(), ri, nr_nnz);
-        down(c, hrv.data(), rv, nr_nnz);
+    if (!glist.empty()) {
+        // one table per CTA, at most ~2 GB of tables
+        const long long per = (1LL << glog2) * (long long)(sizeof(int) + sizeof(double));
+        const int grid = (int)std::max<long long>(
+            1, std::min<long long>({(long long)glist.size(), (long long)c.num_sms * 2, (2LL << 30) / per}));
+        int *gk = dnew<int>((size_t)grid << glog2);
+        double *gv = dnew<double>((size_t)grid << glog2);
+        int *dl = dnew<int>(glist.size());
+        up(c, dl, glist.data(), glist.size());
+        k_sp_cols_global<<<grid, 512, 0, c.stream>>>((int)glist.size(), dl, lp, li, lv, rp, ri, rv, doff, s1r, s1v,
+                                                     s2r, s2v, cnt, glog2, gk, gv, d_err);
+        SAGB_CUDA(cudaGetLastError());
         sync(c);
-        for (int col : host_cols) {
-            hcol_start.push_back((int)hoi.size());
-            csc_columns(hlp, hli, hlv, L, hrp, hri, hrv, col, col + 1, hcnt, hoi, hov);
-        }
-        std::vector<int> tmp(host_cols.size());
-        for (size_t k = 0; k < host_cols.size(); k++) tmp[k] = hcnt[host_cols[k]];
-        for (size_t k = 0; k < host_cols.size(); k++)
-            SAGB_CUDA(cudaMemcpyAsync(cnt + host_cols[k], &tmp[k], sizeof(int), cudaMemcpyHostToDevice, c.stream));
-        sync(c);
+        dfree(dl);
+        dfree(gk);
+        dfree(gv);
     }
     const std::vector<int> rptr = scan_counts(c, cnt, R, O.rptr);
     O.nnz = rptr[R];
     O.cind = dnew<int>(O.nnz);
     O.val = dnew<double>(O.nnz);
-    std::vector<int> gpu_cols;
-    for (int k = 0; k < 8; k++) gpu_cols.insert(gpu_cols.end(), lists[k].begin(), lists[k].end());
-    if (!gpu_cols.empty()) {
-        int *dl = dnew<int>(gpu_cols.size());
-        up(c, dl, gpu_cols.data(), gpu_cols.size());
-        k_sp_gather<<<blocks_for((long long)gpu_cols.size() * 32), kRsThreads, 0, c.stream>>>(
-            (int)gpu_cols.size(), dl, doff, O.rptr, s2r, s2v, O.cind, O.val);
+    std::vector<int> all;
+    for (int k = 0; k < 8; k++) all.insert(all.end(), lists[k].begin(), lists[k].end());
+    all.insert(all.end(), glist.begin(), glist.end());
+    if (!all.empty()) {
+        int *dl = dnew<int>(all.size());
+        up(c, dl, all.data(), all.size());
+        k_sp_gather<<<blocks_for((long long)all.size() * 32), kRsThreads, 0, c.stream>>>(
+            (int)all.size(), dl, doff, O.rptr, s2r, s2v, O.cind, O.val);
         SAGB_CUDA(cudaGetLastError());
         sync(c);
         dfree(dl);
     }
-    for (size_t k = 0; k < host_cols.size(); k++) {
-        const int col = host_cols[k], nn = hcnt[col];
-        up(c, O.cind + rptr[col], hoi.data() + hcol_start[k], nn);
-        up(c, O.val + rptr[col], hov.data() + hcol_start[k], nn);
-    }
-    sync(c);
     dfree(bound);
     dfree(doff);
     dfree(s1r);
@@ -608,8 +666,8 @@ void rs_level_gpu(Ctx &c, const DMat &A, double theta, DMat &CA, CsrD &P_h, CsrD
     // T = A^T P, then C = P^T T, read back as CSR
     DMat R = transpose(c, P, true);
     SAGB_CUDA(cudaMemsetAsync(d_err, 0, sizeof(unsigned), c.stream));
-    DMat T = product(c, A.rptr, A.cind, A.val, A.n, A.nnz, A.n, R.rptr, R.cind, R.val, P.m, R.nnz, d_err);
-    DMat C = product(c, P.rptr, P.cind, P.val, P.n, P.nnz, P.m, T.rptr, T.cind, T.val, P.m, T.nnz, d_err);
+    DMat T = product(c, A.rptr, A.cind, A.val, A.n, R.rptr, R.cind, R.val, P.m, d_err);
+    DMat C = product(c, P.rptr, P.cind, P.val, P.m, T.rptr, T.cind, T.val, P.m, d_err);
     down(c, &err, d_err, 1);
     sync(c);
     dfree(d_err);

@@ -7,6 +7,9 @@
 #include "sort.hpp"
 
 #include <algorithm>
+#include <atomic>
+#include <exception>
+#include <mutex>
 #include <thread>
 #include <cmath>
 #include <cstdio>
@@ -15,6 +18,11 @@
 #include <utility>
 
 namespace sagb {
+
+static thread_local int tl_serial = 0;
+HostSerial::HostSerial() { tl_serial++; }
+HostSerial::~HostSerial() { tl_serial--; }
+bool host_serial() { return tl_serial > 0; }
 
 // ============================================================ conversion rules
 
@@ -347,7 +355,7 @@ static CsrD transpose(const CsrD &P) {
 // zero is removed (and restarts from alpha*x if hit again, which is the same as
 // adding to 0.0).  A dense accumulator gives the same values; the touched rows
 // are emitted in increasing order, as the merge-based original does.
-void csc_columns(const std::vector<int> &lp, const std::vector<int> &li, const std::vector<double> &lv,
+static void csc_columns(const std::vector<int> &lp, const std::vector<int> &li, const std::vector<double> &lv,
                         int L, const std::vector<int> &rp, const std::vector<int> &ri, const std::vector<double> &rv,
                         int c0, int c1, std::vector<int> &cnt, std::vector<int> &oi, std::vector<double> &ov) {
     std::vector<double> acc(L, 0.0);
@@ -387,7 +395,7 @@ static void csc_product(const std::vector<int> &lp, const std::vector<int> &li, 
                         int L, const std::vector<int> &rp, const std::vector<int> &ri, const std::vector<double> &rv,
                         int R, std::vector<int> &op, std::vector<int> &oi, std::vector<double> &ov) {
     const int hw = (int)std::max(1u, std::thread::hardware_concurrency());
-    const int T = R < 20000 ? 1 : std::min(hw, 16);
+    const int T = R < 20000 || host_serial() ? 1 : std::min(hw, 16);
     std::vector<int> cnt(R, 0);
     std::vector<std::vector<int>> pi(T);
     std::vector<std::vector<double>> pv(T);
@@ -786,6 +794,35 @@ static CsrD invert_last(const CsrD &LD) {
     return B;
 }
 
+// f(0) .. f(n-1) on up to hardware_concurrency host threads; every task
+// writes its own pre-sized slot, so results do not depend on the thread count
+template <typename F>
+static void parallel_tasks(int n, F &&f) {
+    const int T = host_serial() ? 1 : std::min(n, (int)std::max(1u, std::thread::hardware_concurrency()));
+    if (T <= 1) {
+        for (int i = 0; i < n; i++) f(i);
+        return;
+    }
+    std::atomic<int> next(0);
+    std::exception_ptr first;
+    std::mutex mu;
+    std::vector<std::thread> pool;
+    for (int t = 0; t < T; t++)
+        pool.emplace_back([&] {
+            HostSerial inner;
+            for (int i; (i = next++) < n;) {
+                try {
+                    f(i);
+                } catch (...) {
+                    std::lock_guard<std::mutex> g(mu);
+                    if (!first) first = std::current_exception();
+                }
+            }
+        });
+    for (auto &th : pool) th.join();
+    if (first) std::rethrow_exception(first);
+}
+
 static void smoother_split(const CsrD &A, const SmootherSpec &sm, CsrD &LD, CsrD &U, std::vector<int> &bj,
                            std::vector<int> &colour) {
     colour.clear();
@@ -831,25 +868,33 @@ IntHierarchy build_int_hierarchy(const CsrD &A, const RsChain &chain, const Smoo
     // prev is still all zero, so the restriction becomes zero (INTAMG.hpp:197-211)
     scale_level(D - 1, true);
 
+    // the levels' smoother splits and conversions are independent: host threads
     h.LD.resize(D);
     h.U.resize(D);
     h.bj.resize(D);
     h.colour.resize(D);
-    for (int l = 0; l < D; l++) {
-        const CsrD &Al = l == 0 ? A : CA[l - 1];
-        CsrD LD, U;
-        smoother_split(Al, sm, LD, U, h.bj[l], h.colour[l]);
-        h.LD[l] = to_ldtri_flex(sm.multicolor ? invert_last(LD) : extract_ldinv(LD));
-        h.U[l] = to_flex(U);
-    }
-    for (int i = 0; i < D; i++) {
-        if (i < D - 1) h.CA.push_back(to_flex(CA[i]));
-        h.P.push_back(to_flex(chain.P[i]));
-        h.R.push_back(to_flex(It[i]));
-    }
-    CsrD F = ilu_full(CA[D - 1]);
-    h.LUL = to_ltri_flex(extract_l(F));
-    h.LUU = to_dutri_flex(extract_dinvu(F));
+    h.CA.resize(D - 1);
+    h.P.resize(D);
+    h.R.resize(D);
+    parallel_tasks(2 * D + 1, [&](int t) {
+        if (t < D) {
+            const int l = t;
+            const CsrD &Al = l == 0 ? A : CA[l - 1];
+            CsrD LD, U;
+            smoother_split(Al, sm, LD, U, h.bj[l], h.colour[l]);
+            h.LD[l] = to_ldtri_flex(sm.multicolor ? invert_last(LD) : extract_ldinv(LD));
+            h.U[l] = to_flex(U);
+        } else if (t < 2 * D) {
+            const int i = t - D;
+            if (i < D - 1) h.CA[i] = to_flex(CA[i]);
+            h.P[i] = to_flex(chain.P[i]);
+            h.R[i] = to_flex(It[i]);
+        } else {
+            CsrD F = ilu_full(CA[D - 1]);
+            h.LUL = to_ltri_flex(extract_l(F));
+            h.LUU = to_dutri_flex(extract_dinvu(F));
+        }
+    });
     return h;
 }
 
@@ -876,21 +921,28 @@ static FpHierarchy<T> build_fp(const CsrD &A, const RsChain &chain, const Smooth
     h.U.resize(D);
     h.bj.resize(D);
     h.colour.resize(D);
-    for (int l = 0; l < D; l++) {
-        const CsrD &Al = l == 0 ? A : chain.CA[l - 1];
-        CsrD LD, U;
-        smoother_split(Al, sm, LD, U, h.bj[l], h.colour[l]);
-        h.LD[l] = convert<T>(sm.multicolor ? invert_last(LD) : extract_ldinv(LD));
-        h.U[l] = convert<T>(U);
-    }
-    for (int i = 0; i < D; i++) {
-        if (i < D - 1) h.CA.push_back(convert<T>(chain.CA[i]));
-        h.P.push_back(convert<T>(chain.P[i]));
-        h.R.push_back(convert<T>(chain.R[i]));
-    }
-    CsrD F = ilu_full(chain.CA[D - 1]);
-    h.LUL = convert<T>(extract_l(F));
-    h.LUU = convert<T>(extract_dinvu(F));
+    h.CA.resize(D - 1);
+    h.P.resize(D);
+    h.R.resize(D);
+    parallel_tasks(2 * D + 1, [&](int t) {
+        if (t < D) {
+            const int l = t;
+            const CsrD &Al = l == 0 ? A : chain.CA[l - 1];
+            CsrD LD, U;
+            smoother_split(Al, sm, LD, U, h.bj[l], h.colour[l]);
+            h.LD[l] = convert<T>(sm.multicolor ? invert_last(LD) : extract_ldinv(LD));
+            h.U[l] = convert<T>(U);
+        } else if (t < 2 * D) {
+            const int i = t - D;
+            if (i < D - 1) h.CA[i] = convert<T>(chain.CA[i]);
+            h.P[i] = convert<T>(chain.P[i]);
+            h.R[i] = convert<T>(chain.R[i]);
+        } else {
+            CsrD F = ilu_full(chain.CA[D - 1]);
+            h.LUL = convert<T>(extract_l(F));
+            h.LUU = convert<T>(extract_dinvu(F));
+        }
+    });
     return h;
 }
 

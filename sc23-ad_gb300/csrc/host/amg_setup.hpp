@@ -15,6 +15,19 @@
 
 namespace sagb {
 
+// ------------------------------------------------------------ host threads
+// The setup spreads independent work (Galerkin columns, the levels' smoother
+// splits and conversions) over host threads.  A caller that already runs
+// setups on several threads holds a HostSerial in each worker, and the setup
+// then stays on that thread.
+struct HostSerial {
+    HostSerial();
+    ~HostSerial();
+    HostSerial(const HostSerial &) = delete;
+    HostSerial &operator=(const HostSerial &) = delete;
+};
+bool host_serial();
+
 // ------------------------------------------------------------ conversion rules
 int ceil_log2_int(int64_t k);
 // CSRflex / ldtri::CSRflex rule (matrix/spmat.hpp:108, ldtri.hpp:144-145)
@@ -41,12 +54,6 @@ struct Pattern {  // CSR without values
 };
 void rs_first_pass(const CsrD &S, const Pattern &St, std::vector<int> &is_coarse);
 void rs_second_pass(const CsrD &S, std::vector<int> &is_coarse);
-// Columns c0..c1-1 of helper::sparse::cscSpMM (helper_sparse.hpp:257-285) with
-// both operands as compressed columns (left: lp/li/lv with L rows; right:
-// rp/ri/rv): cnt[c] entries of column c are appended to oi/ov in row order.
-void csc_columns(const std::vector<int> &lp, const std::vector<int> &li, const std::vector<double> &lv, int L,
-                 const std::vector<int> &rp, const std::vector<int> &ri, const std::vector<double> &rv, int c0, int c1,
-                 std::vector<int> &cnt, std::vector<int> &oi, std::vector<double> &ov);
 
 // helper::multigrid::get_amg_set (helper/helper_multigrid.hpp:34-63):
 // from A build the coarse operator CA = P^T A P, P (Intrpl) and R = P^T (Intrpl_t).

@@ -2,6 +2,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <memory>
 #include <thread>
 
 namespace sagb {
@@ -55,7 +56,10 @@ BatchHierarchy build_batch(const std::vector<CsrD> &systems, double theta, int m
     sm.max_colours = max_colours;
     std::atomic<int> next{0};
     std::vector<std::string> errs(S);
+    const int T = std::max(1, std::min(threads, S));
     auto work = [&]() {
+        // several systems at once: each worker builds its systems alone
+        std::unique_ptr<HostSerial> serial(T > 1 ? new HostSerial() : nullptr);
         for (;;) {
             const int s = next.fetch_add(1);
             if (s >= S) return;
@@ -69,7 +73,6 @@ BatchHierarchy build_batch(const std::vector<CsrD> &systems, double theta, int m
             }
         }
     };
-    const int T = std::max(1, std::min(threads, S));
     std::vector<std::thread> pool;
     for (int t = 1; t < T; t++) pool.emplace_back(work);
     work();
