@@ -274,7 +274,30 @@ def run_ours(a, dist):
         out["multicolor"] = multicolor_row(ctx, a, r, c, v, b, nrm_b)
     if not a.no_batched:
         out["batched"] = batched_rows(ctx, a, r, c, v, b, nrm_b, dist, bits, rule)
+    out["setup"] = setup_row(ctx, r, c, v)
     return sec, out, ctx, out["plain"].pop("state")
+
+
+def setup_row(ctx, r, c, v):
+    """The AMG setup of the same system (the headline's parameters: multicolour
+    smoother, 8 colours, 400-row coarsest level) on the host and with the
+    Ruge-Stueben levels on the GPU; the two hierarchies are compared array by
+    array (they must be identical)."""
+    import sagb
+    params = sagb.amg_params(multicolor=1, max_colours=8, coarse_size=400)
+    t = time.perf_counter()
+    g = sagb.Setup(sagb.INT, r, c, v, params, ctx=ctx)
+    t_gpu = time.perf_counter() - t
+    t = time.perf_counter()
+    h = sagb.Setup(sagb.INT, r, c, v, params)
+    t_host = time.perf_counter() - t
+    same = g.depth == h.depth
+    for i in range(h.depth):
+        for op in (sagb.OP_P, sagb.OP_R, sagb.OP_LD, sagb.OP_U) + ((sagb.OP_CA,) if i < h.depth - 1 else ()):
+            x, y = g.view(op, i), h.view(op, i)
+            same = same and all(np.array_equal(p, q) for p, q in zip(x[:3], y[:3])) and x[3:] == y[3:]
+    return {"gpu_s": t_gpu, "host_s": t_host, "host_threads": os.cpu_count(), "levels": h.depth,
+            "identical": bool(same)}
 
 
 def plain_row(ctx, a, r, c, v, b, nrm_b):
@@ -595,7 +618,7 @@ def main_ours(a):
         # per level and operator: rows, colours (sweeps), ms per launch set, algorithmic GB/s
         line["ops"] = [(p["level"], p["op"], p["n"], p["colours"], round(p["ms"], 4),
                         round(p["bytes"] / (p["ms"] * 1e-3) / 1e9, 1)) for p in k["per_op"]]
-    for key in ("plain", "multicolor", "batched"):
+    for key in ("plain", "multicolor", "batched", "setup"):
         if key in out:
             line[key] = out[key]
     if "plain" in out:

@@ -123,6 +123,8 @@ int sa_ctx_destroy(sa_ctx ctx);
 #define SA_OPT_GRAPHS 1   /* capture Arnoldi steps into CUDA graphs (default on)              */
 #define SA_OPT_PDL 2      /* batched engine: start each V-cycle kernel while the one before it
                            * drains (programmatic dependent launch; default on)               */
+#define SA_OPT_GPU_SETUP 3 /* sa_batch_create: the Ruge-Stueben chain of each system of at least
+                            * 100000 rows on the GPU (same hierarchy bit for bit; default on) */
 int sa_ctx_set_option(sa_ctx ctx, int option, int value);
 int sa_ctx_flags(sa_ctx ctx, unsigned *flags, int clear);
 int sa_ctx_launches(sa_ctx ctx, long long *count);

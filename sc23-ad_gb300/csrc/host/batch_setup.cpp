@@ -31,7 +31,7 @@ static int level_size(const IntHierarchy &h, int l) { return l == 0 ? h.A0.n : h
 
 BatchHierarchy build_batch(const std::vector<CsrD> &systems, double theta, int max_levels, double omega,
                            int smooth_iter, int threads, const std::vector<int> &src_in, int max_colours,
-                           int coarse_size) {
+                           int coarse_size, const std::function<RsChain(const CsrD &)> &big_chain, int big_rows) {
     BatchHierarchy B;
     const int S = (int)systems.size();
     if (S == 0) throw SetupError{"empty batch"};
@@ -54,6 +54,10 @@ BatchHierarchy build_batch(const std::vector<CsrD> &systems, double theta, int m
     sm.iter = smooth_iter;
     sm.multicolor = 1;
     sm.max_colours = max_colours;
+    if (big_chain)
+        for (int s = 0; s < S; s++)
+            if (src[s] == s && systems[s].n >= big_rows)
+                B.chain[s] = std::make_shared<RsChain>(big_chain(systems[s]));
     std::atomic<int> next{0};
     std::vector<std::string> errs(S);
     const int T = std::max(1, std::min(threads, S));
@@ -66,7 +70,8 @@ BatchHierarchy build_batch(const std::vector<CsrD> &systems, double theta, int m
             if (src[s] != s) continue;  // a copy: shares the hierarchy below
             try {
                 B.A_sys[s] = std::make_shared<CsrD>(systems[s]);
-                B.chain[s] = std::make_shared<RsChain>(rs_chain(systems[s], theta, max_levels, coarse_size));
+                if (!B.chain[s])
+                    B.chain[s] = std::make_shared<RsChain>(rs_chain(systems[s], theta, max_levels, coarse_size));
                 B.hi[s] = std::make_shared<IntHierarchy>(build_int_hierarchy(systems[s], *B.chain[s], sm));
             } catch (const SetupError &e) {
                 errs[s] = e.msg;

@@ -12,6 +12,7 @@
 #pragma once
 #include <cstdint>
 #include <memory>
+#include <functional>
 #include <vector>
 
 #include "amg_setup.hpp"
@@ -66,8 +67,12 @@ struct BatchHierarchy {
 // names the system whose matrix and hierarchy system s repeats (src[s] <= s),
 // so copies of one matrix, e.g. solved with different fractional bits, share
 // one setup.
+// big_chain, when given, builds the Ruge-Stueben chain of every system with at
+// least big_rows rows (on the calling thread, before the others start), e.g.
+// on a GPU; it must return what rs_chain returns.
 BatchHierarchy build_batch(const std::vector<CsrD> &systems, double theta, int max_levels, double omega,
                            int smooth_iter, int threads, const std::vector<int> &src = {}, int max_colours = 0,
-                           int coarse_size = 2000);
+                           int coarse_size = 2000,
+                           const std::function<RsChain(const CsrD &)> &big_chain = nullptr, int big_rows = 0);
 
 }  // namespace sagb

@@ -19,7 +19,7 @@ INT, F64, F32 = 0, 1, 2
 MAT_FIXED, MAT_FLEX, MAT_F64, MAT_F32 = 0, 1, 2, 3
 OP_A0, OP_CA, OP_P, OP_R, OP_LD, OP_U, OP_LUL, OP_LUU, OP_BJ, OP_COLOR = range(10)
 GEN_POISSON2D, GEN_POISSON3D, GEN_ANISO2D, GEN_STENCIL27, GEN_CONVDIFF3D, GEN_VARCOEF3D = range(6)
-OPT_FP_EXACT, OPT_GRAPHS, OPT_PDL = 0, 1, 2
+OPT_FP_EXACT, OPT_GRAPHS, OPT_PDL, OPT_GPU_SETUP = 0, 1, 2, 3
 
 VP = C.c_void_p
 I32P = C.POINTER(C.c_int32)

@@ -92,3 +92,28 @@ def test_gpu_setup_matches_host(ctx, kind, n, prm, prec):
         host = sagb.Setup(prec, r, c, v, params)
         gpu = sagb.Setup(prec, r, c, v, params, ctx=ctx)
         _views_equal(host, gpu)
+
+
+def test_batch_gpu_chain_matches_host(ctx):
+    """sa_batch_create builds the chain of a system of 100000 rows or more on
+    the GPU (SA_OPT_GPU_SETUP, default on): the batch's hierarchy and its
+    V-cycle are those of the host-built batch."""
+    systems = []
+    for kind, n in ((sagb.GEN_POISSON3D, 48), (sagb.GEN_STENCIL27, 12)):
+        A = sagb.HostCsr.generate(kind, n, 0.0, seed=2)
+        xs, b = A.rhs(3)
+        A.lmax1_scaling(b)
+        systems.append(A.arrays())
+    assert len(systems[0][0]) - 1 >= 100000
+    Bg = sagb.Batch(ctx, systems, 1)
+    ctx.set_option(sagb.OPT_GPU_SETUP, 0)
+    try:
+        Bh = sagb.Batch(ctx, systems, 1)
+    finally:
+        ctx.set_option(sagb.OPT_GPU_SETUP, 1)
+    for s in range(2):
+        _views_equal(Bg.system_setup(s), Bh.system_setup(s))
+    vin = np.random.default_rng(1).integers(-(1 << 28), 1 << 28, size=Bg.rows).astype(np.int32)
+    np.testing.assert_array_equal(Bg.precondition(vin), Bh.precondition(vin))
+    Bg.close()
+    Bh.close()
