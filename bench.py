@@ -54,6 +54,9 @@ def parse():
     ap.add_argument("--no-multicolor", action="store_true", help="skip the multicolour-smoother row")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-engine rows")
     ap.add_argument("--profile", action="store_true", help="skip extras (for profilers)")
+    ap.add_argument("--tune-file", default=None,
+                    help="vcycle workload: launch shapes to apply (written by a run without it, so that a run under "
+                         "a profiler does not autotune under the profiler)")
     ap.add_argument("--workload", choices=["poisson128", "batch256", "convdiff128", "precision", "vcycle"],
                     default="poisson128",
                     help="poisson128: the headline; batch256: 256 27-point systems x 4 right-hand sides; "
@@ -893,7 +896,19 @@ def main_vcycle(a):
     ctx = sagb.Context(0)
     r, c, v, b = build_system(a.n, seed=1)
     B = sagb.Batch(ctx, [(r, c, v)], 1)
-    B.autotune(2)
+    if a.tune_file and os.path.exists(a.tune_file):
+        with open(a.tune_file) as f:
+            tune = json.load(f)
+        for l, (form, groups) in enumerate(zip(tune["forms"], tune["groups"])):
+            B.sweep_form(l, form)
+            for op, g in enumerate(groups):
+                B.set_group(l, op, g)
+    else:
+        B.autotune(2)
+        if a.tune_file:
+            with open(a.tune_file, "w") as f:
+                json.dump({"forms": [B.sweep_form(l) for l in range(B.depth)],
+                           "groups": [[B.group(l, op) for op in range(5)] for l in range(B.depth)]}, f)
     x = sagb.DeviceArray.from_host(ctx, np.random.default_rng(3).integers(-(1 << 28), 1 << 28, size=B.rows)
                                    .astype(np.int32))
     y = sagb.DeviceArray(ctx, B.rows, np.int32)
