@@ -313,9 +313,10 @@ int sa_batch_group(sa_batch B, int level, int op, int *group);
  * stream, not for op 1); results do not depend on it */
 int sa_batch_set_group(sa_batch B, int level, int op, int group);
 /* the colour sweep's launch form at one level: 0 one launch per colour, 1 one
- * thread-block-cluster launch, 2 the same over a packed copy of LD; set >= 0
- * chooses it (SA_ERR_ARG / an error if the level lacks that form), -1 reads
- * it; results do not depend on it */
+ * thread-block-cluster launch, 2 the same over a packed copy of LD, 3 one
+ * launch per colour over LD packed in colour order; set >= 0 chooses it
+ * (SA_ERR_ARG / an error if the level lacks that form), -1 reads it; results
+ * do not depend on it */
 int sa_batch_sweep_form(sa_batch B, int level, int set, int *form);
 /* Work/main.cpp:153-161 per system and right-hand side: max|M_f64 b| / ||b|| */
 int sa_batch_rule_ratios(sa_ctx ctx, sa_batch B, const double *b, const double *nrm_b, double *ratio);

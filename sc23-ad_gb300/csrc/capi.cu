@@ -1212,7 +1212,7 @@ extern "C" int sa_batch_set_group(sa_batch B, int level, int op, int group) {
 }
 
 extern "C" int sa_batch_sweep_form(sa_batch B, int level, int set, int *form) {
-    if (!B || !form || level < 0 || level >= B->h->Dmax || set < -1 || set > 2)
+    if (!B || !form || level < 0 || level >= B->h->Dmax || set < -1 || set > 3)
         return fail(SA_ERR_ARG, "invalid argument");
     SA_GUARD_BEGIN
     *form = B->eng->sweep_form(level, set);

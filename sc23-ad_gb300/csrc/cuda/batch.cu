@@ -370,6 +370,84 @@ __device__ __forceinline__ void pk_fetch(const int4 *__restrict__ items, const i
     if (IN && p.ok) load_r<R>(in, p.hd.x, p.iv);
 }
 
+// One row of a packed sweep: subtract the lower entries' products (the first
+// kPkU a lane already fetched in cur), then the SOR row update and the store
+// (the row rule of k_bcolour).  CG: the vector values come from other CTAs of
+// the same launch (read through L2).
+template <int R, bool CG>
+__device__ __forceinline__ void load_dep(const int *x, int row, int (&v)[R]) {
+    if constexpr (CG) load_cg_r<R>(x, row, v);
+    else load_rw<R>(x, row, v);
+}
+
+template <int R, int G, bool CG>
+__device__ __forceinline__ void pk_row(const PkPass<R> &cur, const int2 *__restrict__ ents, int *out, int lane,
+                                       const int *__restrict__ row_sys, unsigned *__restrict__ pflag,
+                                       unsigned *__restrict__ flags) {
+    long long acc[R];
+#pragma unroll
+    for (int r = 0; r < R; r++) acc[r] = 0;
+    const int len = cur.hd.w & 0xFFFFF;
+    {
+        int xv[kPkU][R];
+#pragma unroll
+        for (int u = 0; u < kPkU; u++) {
+            if (lane + u * G < len) load_dep<R, CG>(out, cur.e[u].x, xv[u]);
+            else
+#pragma unroll
+                for (int r = 0; r < R; r++) xv[u][r] = 0;
+        }
+#pragma unroll
+        for (int u = 0; u < kPkU; u++)
+#pragma unroll
+            for (int r = 0; r < R; r++) acc[r] = wsub(acc[r], (long long)cur.e[u].y * (long long)xv[u][r]);
+    }
+    // rows longer than kPkU * G entries: four entries a lane in flight
+    int j = lane + kPkU * G;
+    for (; j + 3 * G < len; j += 4 * G) {
+        int2 ev[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) ev[u] = __ldg(ents + cur.hd.y + j + u * G);
+        int xv[4][R];
+#pragma unroll
+        for (int u = 0; u < 4; u++) load_dep<R, CG>(out, ev[u].x, xv[u]);
+#pragma unroll
+        for (int u = 0; u < 4; u++)
+#pragma unroll
+            for (int r = 0; r < R; r++) acc[r] = wsub(acc[r], (long long)ev[u].y * (long long)xv[u][r]);
+    }
+    for (; j < len; j += G) {
+        const int2 ev = __ldg(ents + cur.hd.y + j);
+        int xv[R];
+        load_dep<R, CG>(out, ev.x, xv);
+#pragma unroll
+        for (int r = 0; r < R; r++) acc[r] = wsub(acc[r], (long long)ev.y * (long long)xv[r]);
+    }
+#pragma unroll
+    for (int r = 0; r < R; r++)
+#pragma unroll
+        for (int o = G / 2; o > 0; o >>= 1) acc[r] = wadd(acc[r], shfl_xor(acc[r], o));
+    if (lane == 0 && cur.ok) {
+        const int row = cur.hd.x;
+        const int bit = (cur.hd.w >> 20) & 63, dbit = (int)((unsigned)cur.hd.w >> 26);
+        const long long dinv = cur.hd.z;
+        int res[R];
+        bool any = false;
+#pragma unroll
+        for (int r = 0; r < R; r++) {
+            const long long tt = wadd(wshl((long long)cur.iv[r], bit), acc[r]);
+            const long long sv = wmul(tt >> bit, dinv) >> dbit;
+            res[r] = lo32(sv);
+            if (!fits32(sv)) {
+                atomicOr(pflag + (size_t)row_sys[row] * R + r, ST_OVERFLOW);
+                any = true;
+            }
+        }
+        store_r<R>(out, row, res);
+        if (any) atomicOr(flags, ST_OVERFLOW);
+    }
+}
+
 template <int R, int G>
 __global__ void __launch_bounds__(pk_threads<R>())
 k_bsweep_packed(const int *__restrict__ gc_ptr, const int *__restrict__ sw_ptr, const int4 *__restrict__ items,
@@ -405,74 +483,33 @@ k_bsweep_packed(const int *__restrict__ gc_ptr, const int *__restrict__ sw_ptr, 
         if (nk < k1) pk_fetch<R, G>(items, ents, in, nbase + ls, nie, lane, nxt);
         else nxt.ok = false;
 
-        long long acc[R];
-#pragma unroll
-        for (int r = 0; r < R; r++) acc[r] = 0;
-        const int len = cur.hd.w & 0xFFFFF;
-        {
-            int xv[kPkU][R];
-#pragma unroll
-            for (int u = 0; u < kPkU; u++) {
-                if (lane + u * G < len) load_cg_r<R>(out, cur.e[u].x, xv[u]);
-                else
-#pragma unroll
-                    for (int r = 0; r < R; r++) xv[u][r] = 0;
-            }
-#pragma unroll
-            for (int u = 0; u < kPkU; u++)
-#pragma unroll
-                for (int r = 0; r < R; r++) acc[r] = wsub(acc[r], (long long)cur.e[u].y * (long long)xv[u][r]);
-        }
-        // rows longer than kPkU * G entries: four entries a lane in flight
-        int j = lane + kPkU * G;
-        for (; j + 3 * G < len; j += 4 * G) {
-            int2 ev[4];
-#pragma unroll
-            for (int u = 0; u < 4; u++) ev[u] = __ldg(ents + cur.hd.y + j + u * G);
-            int xv[4][R];
-#pragma unroll
-            for (int u = 0; u < 4; u++) load_cg_r<R>(out, ev[u].x, xv[u]);
-#pragma unroll
-            for (int u = 0; u < 4; u++)
-#pragma unroll
-                for (int r = 0; r < R; r++) acc[r] = wsub(acc[r], (long long)ev[u].y * (long long)xv[u][r]);
-        }
-        for (; j < len; j += G) {
-            const int2 ev = __ldg(ents + cur.hd.y + j);
-            int xv[R];
-            load_cg_r<R>(out, ev.x, xv);
-#pragma unroll
-            for (int r = 0; r < R; r++) acc[r] = wsub(acc[r], (long long)ev.y * (long long)xv[r]);
-        }
-#pragma unroll
-        for (int r = 0; r < R; r++)
-#pragma unroll
-            for (int o = G / 2; o > 0; o >>= 1) acc[r] = wadd(acc[r], shfl_xor(acc[r], o));
-        if (lane == 0 && cur.ok) {
-            const int row = cur.hd.x;
-            const int bit = (cur.hd.w >> 20) & 63, dbit = (int)((unsigned)cur.hd.w >> 26);
-            const long long dinv = cur.hd.z;
-            int res[R];
-            bool any = false;
-#pragma unroll
-            for (int r = 0; r < R; r++) {
-                const long long tt = wadd(wshl((long long)cur.iv[r], bit), acc[r]);
-                const long long sv = wmul(tt >> bit, dinv) >> dbit;
-                res[r] = lo32(sv);
-                if (!fits32(sv)) {
-                    atomicOr(pflag + (size_t)row_sys[row] * R + r, ST_OVERFLOW);
-                    any = true;
-                }
-            }
-            store_r<R>(out, row, res);
-            if (any) atomicOr(flags, ST_OVERFLOW);
-        }
+        pk_row<R, G, true>(cur, ents, out, lane, row_sys, pflag, flags);
         if (colour_end) cluster_barrier();
         cur = nxt;
         k = nk;
         base = nbase;
         ie = nie;
     }
+}
+
+// One colour of the sweep over a packed copy of LD in colour order (the
+// items of colour k are ib..ie-1): the item, its first entries and (after the
+// wait for the previous kernel) its input value come in one round trip each,
+// the vector values of the earlier colours in one more.
+template <int R, int G>
+__global__ void __launch_bounds__(kBThreads)
+k_bcolour_packed(int ib, int ie, const int4 *__restrict__ items, const int2 *__restrict__ ents,
+                 const int *__restrict__ in, int *out, const int *__restrict__ row_sys, unsigned *__restrict__ pflag,
+                 unsigned *__restrict__ flags) {
+    pdl_trigger();
+    const long long tid = (long long)blockIdx.x * kBThreads + threadIdx.x;
+    const int lane = (int)(tid % G);
+    const long long it = ib + tid / G;
+    PkPass<R> cur;
+    pk_fetch<R, G, false>(items, ents, in, it < ie ? (int)it : ie, ie, lane, cur);
+    pdl_wait();
+    if (cur.ok) load_r<R>(in, cur.hd.x, cur.iv);
+    pk_row<R, G, false>(cur, ents, out, lane, row_sys, pflag, flags);
 }
 
 // ------------------------------------------------------------ coarse LU
@@ -1262,6 +1299,9 @@ struct DevBLevel {
     int *sw_ptr = nullptr;          // packed form: items of (colour, CTA) run k * kClusterCtas + q
     int4 *pk_items = nullptr;
     int2 *pk_ents = nullptr;
+    // use_cluster 3: k_bcolour_packed over LD packed in colour order (colour k: colour_ptr[k] ..)
+    int4 *cp_items = nullptr;
+    int2 *cp_ents = nullptr;
 };
 
 struct BatchEngine::Impl {
@@ -1329,6 +1369,7 @@ struct BatchEngine::Impl {
             d.colour_ptr = L.colour_ptr;
         }
         for (int l = 0; l < Dmax; l++) build_cluster_groups(l);
+        for (int l = 0; l < Dmax; l++) build_colour_pack(l);
         for (int l = 0; l <= Dmax; l++) row_sys.push_back(dupload(h->row_sys[l]));
         for (int l = 0; l < Dmax; l++) {
             lv[l].row_sys = row_sys[l];
@@ -1476,6 +1517,37 @@ struct BatchEngine::Impl {
         if (ncol > 0 && (double)L.n_smooth / ncol < 65536.0) build_packed(l, gc, cb, rows);
     }
 
+    // LD packed in the colour row order for k_bcolour_packed (levels of at most
+    // 2^21 smoothing rows; left out, like the cluster pack, when a row does not
+    // fit the item format)
+    static bool pack_rows(const BatchCsr &LD, const int *rows, size_t nrows, std::vector<int4> &items,
+                          std::vector<int2> &ents) {
+        for (size_t k = 0; k < nrows; k++) {
+            const int row = rows[k];
+            const int e0 = LD.rptr[row], dp = LD.rptr[row + 1] - 1;
+            const int len = dp - e0, bit = LD.bit[row], dbit = LD.dbit[row];
+            if (len < 0 || len >= (1 << 20) || bit < 0 || bit > 63 || dbit < 0 || dbit > 63 ||
+                ents.size() + (size_t)len >= (size_t)1 << 31)
+                return false;
+            const unsigned meta = (unsigned)len | (unsigned)bit << 20 | (unsigned)dbit << 26;
+            items.push_back(make_int4(row, (int)ents.size(), LD.val[dp], (int)meta));
+            for (int e = e0; e < dp; e++) ents.push_back(make_int2(LD.cind[e], LD.val[e]));
+        }
+        return true;
+    }
+
+    void build_colour_pack(int l) {
+        const BatchLevel &L = h->lv[l];
+        DevBLevel &d = lv[l];
+        if (L.colour_rows.empty() || L.n_smooth > (1 << 21)) return;
+        std::vector<int4> items;
+        std::vector<int2> ents;
+        items.reserve(L.colour_rows.size());
+        if (!pack_rows(L.LD, L.colour_rows.data(), L.colour_rows.size(), items, ents)) return;
+        d.cp_items = dupload(items);
+        d.cp_ents = ents.empty() ? (int2 *)dmalloc(sizeof(int2)) : dupload(ents);
+    }
+
     // the packed copy of LD read by k_bsweep_packed (rows of each colour dealt
     // to the cluster's CTAs in turn); left out when a row does not fit the
     // item format, and the level then keeps the other two forms
@@ -1493,17 +1565,8 @@ struct BatchEngine::Impl {
             for (int q = 0; q < kClusterCtas; q++) {
                 sw[kk * kClusterCtas + q] = (int)items.size();
                 if (is_end[kk]) continue;
-                for (int i = cb[kk] + q; i < cb[kk + 1]; i += kClusterCtas) {
-                    const int row = rows[i];
-                    const int e0 = LD.rptr[row], dp = LD.rptr[row + 1] - 1;
-                    const int len = dp - e0, bit = LD.bit[row], dbit = LD.dbit[row];
-                    if (len < 0 || len >= (1 << 20) || bit < 0 || bit > 63 || dbit < 0 || dbit > 63 ||
-                        ents.size() + (size_t)len >= (size_t)1 << 31)
-                        return;
-                    const unsigned meta = (unsigned)len | (unsigned)bit << 20 | (unsigned)dbit << 26;
-                    items.push_back(make_int4(row, (int)ents.size(), LD.val[dp], (int)meta));
-                    for (int e = e0; e < dp; e++) ents.push_back(make_int2(LD.cind[e], LD.val[e]));
-                }
+                for (int i = cb[kk] + q; i < cb[kk + 1]; i += kClusterCtas)
+                    if (!pack_rows(LD, &rows[i], 1, items, ents)) return;
             }
         sw[K * kClusterCtas] = (int)items.size();
         if (items.empty()) return;
@@ -1628,6 +1691,8 @@ struct BatchEngine::Impl {
             dfree(d.sw_ptr);
             dfree(d.pk_items);
             dfree(d.pk_ents);
+            dfree(d.cp_items);
+            dfree(d.cp_ents);
         }
         for (auto p : row_sys) dfree(p);
         for (auto p : ee) dfree(p);
@@ -1716,6 +1781,24 @@ struct BatchEngine::Impl {
 
     void sweep(int l, const int *in, int *out) {
         const DevBLevel &L = lv[l];
+        if (L.use_cluster == 3 && L.cp_items) {
+            const int nc = (int)L.colour_ptr.size() - 1;
+            for (int k = 0; k < nc; k++) {
+                const int a = L.colour_ptr[k], b = L.colour_ptr[k + 1];
+                if (b == a) continue;
+                const long long threads = (long long)(b - a) * L.LD.group;
+                const int blocks = (int)((threads + kBThreads - 1) / kBThreads);
+                by_r([&](auto RR) {
+                    constexpr int R = decltype(RR)::value;
+                    by_g(L.LD.group, [&](auto GG) {
+                        constexpr int G = decltype(GG)::value;
+                        launch(k_bcolour_packed<R, G>, blocks, kBThreads, 0, 1, a, b, (const int4 *)L.cp_items,
+                               (const int2 *)L.cp_ents, in, out, (const int *)L.row_sys, cur_pflag, c.d_flags);
+                    });
+                });
+            }
+            return;
+        }
         if (L.use_cluster == 2 && L.pk_items && L.ngroups > 0) {
             by_r([&](auto RR) {
                 constexpr int R = decltype(RR)::value;
@@ -2057,7 +2140,8 @@ int BatchEngine::sweep_form(int level, int set) {
     if (level < 0 || level >= impl_->Dmax) throw CudaError{"no such level"};
     DevBLevel &L = impl_->lv[level];
     if (set >= 0) {
-        if (set > 2 || (set >= 1 && L.ngroups == 0) || (set == 2 && !L.pk_items))
+        if (set > 3 || ((set == 1 || set == 2) && L.ngroups == 0) || (set == 2 && !L.pk_items) ||
+            (set == 3 && !L.cp_items))
             throw CudaError{"sweep form not available at this level"};
         L.use_cluster = set;
         impl_->clear_graphs();
@@ -2149,10 +2233,13 @@ void BatchEngine::autotune(int reps) {
             if (op == 1) {
                 // the sweep form first: one launch per colour, or one cluster
                 // launch per level (plain or packed); each form at its best group
-                float bt[3] = {1e30f, 1e30f, 1e30f};
-                int bg[3] = {M->group, M->group, M->group};
-                const int nform = L.ngroups == 0 ? 1 : L.pk_items ? 3 : 2;
+                float bt[4] = {1e30f, 1e30f, 1e30f, 1e30f};
+                int bg[4] = {M->group, M->group, M->group, M->group};
+                const bool avail[4] = {true, L.ngroups > 0, L.ngroups > 0 && L.pk_items != nullptr,
+                                       L.cp_items != nullptr};
+                const int nform = 4;
                 for (int uc = 0; uc < nform; uc++) {
+                    if (!avail[uc]) continue;
                     L.use_cluster = uc;
                     for (int g : cand) {
                         if (g == 0) continue;

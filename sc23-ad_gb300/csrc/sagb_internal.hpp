@@ -248,7 +248,8 @@ class BatchEngine {
     void set_groups(int level, int op, int group);  // op: 0 A, 1 LD, 2 U, 3 P, 4 R
     int group(int level, int op) const;
     // the colour sweep's form at one level (0: a launch per colour, 1: cluster
-    // launch, 2: packed cluster launch); set >= 0 chooses it, -1 only reads
+    // launch, 2: packed cluster launch, 3: a launch per colour over LD packed
+    // in colour order); set >= 0 chooses it, -1 only reads
     int sweep_form(int level, int set);
     // one operator of one level on caller vectors (op 1: the colour sweep LD^-1 in)
     void level_op(int level, int op, const int *in, int *out);

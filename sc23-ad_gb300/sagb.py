@@ -721,12 +721,12 @@ class Batch:
     def set_group(self, level, op, group):
         check(lib().sa_batch_set_group(self.h, level, op, group))
 
-    SWEEP_PER_COLOUR, SWEEP_CLUSTER, SWEEP_PACKED = 0, 1, 2
+    SWEEP_PER_COLOUR, SWEEP_CLUSTER, SWEEP_PACKED, SWEEP_PACKED_COLOUR = 0, 1, 2, 3
 
     def sweep_form(self, level, set=-1):
         """The colour sweep's launch form at one level (0 a launch per colour,
-        1 a cluster launch, 2 a cluster launch over the packed LD); set >= 0
-        chooses it."""
+        1 a cluster launch, 2 a cluster launch over the packed LD, 3 a launch
+        per colour over LD packed in colour order); set >= 0 chooses it."""
         f = C.c_int()
         check(lib().sa_batch_sweep_form(self.h, level, set, C.byref(f)))
         return f.value

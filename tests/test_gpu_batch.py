@@ -82,8 +82,9 @@ def test_batched_vcycle_bit_exact(ctx, nrhs):
     # the autotuner changes launch shapes only, never results
     B.autotune(2)
     np.testing.assert_array_equal(B.precondition(vin).reshape(B.rows, nrhs), out)
-    # nor does the sweep's launch form (per colour, cluster, packed cluster) or its lanes per row
-    for form in (0, 1, 2):
+    # nor does the sweep's launch form (per colour, cluster, packed cluster, packed per colour) or its
+    # lanes per row
+    for form in (0, 1, 2, 3):
         for g in (1, 4, 32):
             for lv in range(B.depth):
                 try:
@@ -107,16 +108,17 @@ def test_packed_sweep_many_groups_and_long_rows(ctx):
     for lv in range(B.depth):
         B.sweep_form(lv, 0)
     ref = B.precondition(vin)
-    packed = 0
-    for lv in range(B.depth):
-        try:
-            B.sweep_form(lv, 2)
-            packed += 1
-        except sagb.SagbError:
-            pass
-        B.set_group(lv, 1, 1)  # one lane a row: rows longer than 4 entries take the tail loop
-    assert packed >= 1
-    np.testing.assert_array_equal(B.precondition(vin), ref)
+    for form in (2, 3):
+        packed = 0
+        for lv in range(B.depth):
+            try:
+                B.sweep_form(lv, form)
+                packed += 1
+            except sagb.SagbError:
+                pass
+            B.set_group(lv, 1, 1)  # one lane a row: rows longer than 4 entries take the tail loop
+        assert packed >= 1
+        np.testing.assert_array_equal(B.precondition(vin), ref, err_msg=f"form {form}")
     B.close()
 
 
