@@ -41,16 +41,6 @@ constexpr int kBThreads = 256;
 constexpr int kTileRows = 2048;
 constexpr int kBLuThreads = 512;  // 16 warps: room for 128 registers a thread
 
-// Programmatic dependent launch.  The V-cycle's kernels are launched with the
-// programmatic-serialization attribute: a kernel may start while the one
-// before it drains, reads what does not change during the V-cycle (row
-// pointers, row lists), then waits at pdl_wait() until the previous grid has
-// completed and its writes are visible; nothing it reads or writes that the
-// previous kernels produce or read is touched before that wait.  Each kernel
-// lets its successor start as soon as all of its own CTAs are running.
-// Launched without the attribute, both instructions have no effect.
-__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
-__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 
 struct DBCsr {
     int n;
@@ -190,8 +180,30 @@ k_bspmv(DBCsr A, const int *__restrict__ x, int *__restrict__ y, const int *__re
 #pragma unroll
     for (int r = 0; r < R; r++) acc[r] = 0;
     const int e0 = row < A.n ? __ldg(A.rptr + row) : 0, e1 = row < A.n ? __ldg(A.rptr + row + 1) : 0;
+    // the first four entries of each lane are static: fetched before the wait
+    int cc[4], vv[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        const int j = e0 + lane + q * G;
+        cc[q] = j < e1 ? __ldg(A.cind + j) : -1;
+        vv[q] = j < e1 ? __ldg(A.val + j) : 0;
+    }
     pdl_wait();
-    if (row < A.n) row_accumulate<R, G, false, false>(A.cind, A.val, e0, e1, lane, x, acc);
+    {
+        int xv[4][R];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            if (cc[q] >= 0) load_r<R>(x, cc[q], xv[q]);
+            else
+#pragma unroll
+                for (int r = 0; r < R; r++) xv[q][r] = 0;
+        }
+#pragma unroll
+        for (int q = 0; q < 4; q++)
+#pragma unroll
+            for (int r = 0; r < R; r++) acc[r] = wadd(acc[r], (long long)vv[q] * (long long)xv[q][r]);
+    }
+    if (e1 - e0 > 4 * G) row_accumulate<R, G, false, false>(A.cind, A.val, e0 + 4 * G, e1, lane, x, acc);
 #pragma unroll
     for (int r = 0; r < R; r++)
 #pragma unroll
@@ -205,12 +217,11 @@ __global__ void __launch_bounds__(kStreamThreads)
 k_bspmv_stream(DBCsr A, const int *__restrict__ x, int *__restrict__ y, const int *__restrict__ z,
                const int *__restrict__ row_sys, unsigned *__restrict__ pflag, unsigned *__restrict__ flags) {
     pdl_trigger();
-    pdl_wait();
     long long acc[R];
 #pragma unroll
     for (int r = 0; r < R; r++) acc[r] = 0;
     const int r0 = blockIdx.x * kStreamThreads;
-    stream_rows<R>(r0, min(A.n, r0 + kStreamThreads), A.rptr, A.cind, A.val, x, acc);
+    stream_rows<R, true>(r0, min(A.n, r0 + kStreamThreads), A.rptr, A.cind, A.val, x, acc);  // waits inside
     const int row = r0 + threadIdx.x;
     if (row < A.n) bspmv_finish<R, MODE>(A, row, acc, y, z, row_sys, pflag, flags);
 }
@@ -935,6 +946,8 @@ __global__ void __launch_bounds__(kBThreads)
 k_bspmv_dot(const BTile *__restrict__ tiles, DBCsr A, const int *__restrict__ z, int *__restrict__ w,
             const int *__restrict__ v0, const BPair *__restrict__ pairs, unsigned long long *acc, int m,
             unsigned *__restrict__ pflag, unsigned *__restrict__ flags) {
+    pdl_trigger();
+    pdl_wait();
     __shared__ long long sh[kBThreads / 32][R];
     const BTile t = tiles[blockIdx.x];
     const int lane = threadIdx.x % G;
@@ -986,6 +999,8 @@ __global__ void __launch_bounds__(kStreamThreads)
 k_bspmv_dot_stream(const BTile *__restrict__ tiles, DBCsr A, const int *__restrict__ z, int *__restrict__ w,
                    const int *__restrict__ v0, unsigned long long *acc, int m, unsigned *__restrict__ pflag,
                    unsigned *__restrict__ flags) {
+    pdl_trigger();
+    pdl_wait();
     __shared__ long long sh[kStreamThreads / 32][R];
     const BTile t = tiles[blockIdx.x];
     long long a[R], dot[R];
@@ -1025,6 +1040,8 @@ template <int R, bool LAST>
 __global__ void __launch_bounds__(kBThreads)
 k_bmgs(const BTile *__restrict__ tiles, int k, int j, int m, size_t vstride, const int *__restrict__ V,
        int *__restrict__ w, const BPair *__restrict__ pairs, unsigned long long *acc, long long *H) {
+    pdl_trigger();
+    pdl_wait();
     __shared__ long long sh[kBThreads / 32][R];
     const BTile t = tiles[blockIdx.x];
     long long a[R];
@@ -1080,6 +1097,8 @@ __device__ long long bggen(long long a, long long b, long long *c, long long *s,
 // convergence test (gmres.hpp:240-262); converged pairs leave the cycle
 __global__ void k_bgivens(int P, int j, int m, BPair *pairs, long long *Hall, long long *call, long long *sall,
                           long long *eall, unsigned long long *acc, unsigned *pflag, BInfo *info) {
+    pdl_trigger();
+    pdl_wait();
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p < P && pairs[p].active) {
         BPair &q = pairs[p];
@@ -1128,6 +1147,8 @@ __global__ void k_bgivens(int P, int j, int m, BPair *pairs, long long *Hall, lo
 // V_{j+1} = (int)(hinv * w >> bit) for the pairs that took step j
 template <int R>
 __global__ void k_bscal(const BTile *__restrict__ tiles, int j, const BPair *__restrict__ pairs, int *__restrict__ w) {
+    pdl_trigger();
+    pdl_wait();
     const BTile t = tiles[blockIdx.x];
     long long a[R];
     int bit[R];
@@ -1150,6 +1171,8 @@ __global__ void k_bscal(const BTile *__restrict__ tiles, int j, const BPair *__r
 }
 
 __global__ void k_binfo_reset(BInfo *info) {
+    pdl_trigger();
+    pdl_wait();
     info->n_active = 0;
 }
 
@@ -1926,34 +1949,37 @@ struct BatchEngine::Impl {
         const int P = S * Rn;
         const size_t vs = N0 * Rn;
         int *Vj = V + (size_t)j * vs, *Zj = Z + (size_t)j * vs, *w = V + (size_t)(j + 1) * vs;
-        k_binfo_reset<<<1, 1, 0, c.stream>>>(info_d);
+        // the Arnoldi kernels wait for their predecessor at their first
+        // instruction: programmatic launch only hides the launch latency
+        launch(k_binfo_reset, 1, 1, 0, 1, info_d);
         vcycle(Vj, Zj);
         const DevBMat &A0 = lv[0].A;
         by_r([&](auto RR) {
             constexpr int R = decltype(RR)::value;
             if (A0.group == 0) {
-                k_bspmv_dot_stream<R><<<nstiles, kStreamThreads, 0, c.stream>>>(stiles, A0.d, Zj, w, V, acc, m, pflag,
-                                                                              c.d_flags);
+                launch(k_bspmv_dot_stream<R>, nstiles, kStreamThreads, 0, 1, (const BTile *)stiles, A0.d,
+                       (const int *)Zj, w, (const int *)V, acc, m, pflag, c.d_flags);
             } else {
                 by_g(A0.group, [&](auto GG) {
                     constexpr int G = decltype(GG)::value;
-                    k_bspmv_dot<R, G><<<ntiles, kBThreads, 0, c.stream>>>(tiles, A0.d, Zj, w, V, pairs, acc, m,
-                                                                         pflag, c.d_flags);
+                    launch(k_bspmv_dot<R, G>, ntiles, kBThreads, 0, 1, (const BTile *)tiles, A0.d, (const int *)Zj, w,
+                           (const int *)V, (const BPair *)pairs, acc, m, pflag, c.d_flags);
                 });
             }
             for (int k = 0; k <= j; k++) {
                 if (k < j)
-                    k_bmgs<R, false><<<ntiles, kBThreads, 0, c.stream>>>(tiles, k, j, m, vs, V, w, pairs, acc, H);
+                    launch(k_bmgs<R, false>, ntiles, kBThreads, 0, 1, (const BTile *)tiles, k, j, m, vs,
+                           (const int *)V, w, (const BPair *)pairs, acc, H);
                 else
-                    k_bmgs<R, true><<<ntiles, kBThreads, 0, c.stream>>>(tiles, k, j, m, vs, V, w, pairs, acc, H);
+                    launch(k_bmgs<R, true>, ntiles, kBThreads, 0, 1, (const BTile *)tiles, k, j, m, vs,
+                           (const int *)V, w, (const BPair *)pairs, acc, H);
             }
         });
-        k_bgivens<<<(P + 127) / 128, 128, 0, c.stream>>>(P, j, m, pairs, H, cs, sn, e, acc, pflag, info_d);
+        launch(k_bgivens, (P + 127) / 128, 128, 0, 1, P, j, m, pairs, H, cs, sn, e, acc, pflag, info_d);
         by_r([&](auto RR) {
             constexpr int R = decltype(RR)::value;
-            k_bscal<R><<<ntiles, kBThreads, 0, c.stream>>>(tiles, j, pairs, w);
+            launch(k_bscal<R>, ntiles, kBThreads, 0, 1, (const BTile *)tiles, j, (const BPair *)pairs, w);
         });
-        c.launches += j + 5;
         SAGB_CUDA(cudaMemcpyAsync(info_h, info_d, sizeof(BInfo), cudaMemcpyDeviceToHost, c.stream));
     }
 

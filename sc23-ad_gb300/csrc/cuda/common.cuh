@@ -123,4 +123,16 @@ __device__ __forceinline__ long long lsqrt_dev(long long x) {
     return t;
 }
 
+
+// Programmatic dependent launch.  The V-cycle's kernels are launched with the
+// programmatic-serialization attribute: a kernel may start while the one
+// before it drains, reads what does not change during the V-cycle (row
+// pointers, row lists), then waits at pdl_wait() until the previous grid has
+// completed and its writes are visible; nothing it reads or writes that the
+// previous kernels produce or read is touched before that wait.  Each kernel
+// lets its successor start as soon as all of its own CTAs are running.
+// Launched without the attribute, both instructions have no effect.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 }  // namespace sagb

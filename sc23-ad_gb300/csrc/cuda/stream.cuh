@@ -32,8 +32,9 @@ __device__ __forceinline__ void gather_r(const int *__restrict__ x, int col, int
 
 // Rows [r0, r1) with r1 - r0 <= blockDim.x: thread t adds the sum over row
 // r0 + t of val * x to acc[r].  Every thread of the CTA must call it (it
-// synchronises the CTA).
-template <int R>
+// synchronises the CTA).  PDL: the first chunk of the matrix is staged before
+// pdl_wait(), x is read after it.
+template <int R, bool PDL = false>
 __device__ __forceinline__ void stream_rows(int r0, int r1, const int *__restrict__ rptr,
                                             const int *__restrict__ cind, const int *__restrict__ val,
                                             const int *__restrict__ x, long long (&acc)[R]) {
@@ -42,6 +43,7 @@ __device__ __forceinline__ void stream_rows(int r0, int r1, const int *__restric
     const int row = r0 + tid;
     const int a = __ldg(rptr + r0), b = __ldg(rptr + r1);
     const int ra = row < r1 ? __ldg(rptr + row) : 0, rb = row < r1 ? __ldg(rptr + row + 1) : 0;
+    if (PDL && a >= b) pdl_wait();  // no entries: nothing staged
     for (int base = a; base < b; base += kStreamCap) {
         const int cnt = min(kStreamCap, b - base);
         const int head = min(cnt, (4 - (base & 3)) & 3);
@@ -63,6 +65,7 @@ __device__ __forceinline__ void stream_rows(int r0, int r1, const int *__restric
             s_col[i] = __ldg(cind + base + i);
         }
         __syncthreads();
+        if (PDL && base == a) pdl_wait();
         const int lo = max(ra, base), hi = min(rb, base + cnt);
         for (int j = lo; j < hi; j++) {
             const long long v = s_val[j - base];
