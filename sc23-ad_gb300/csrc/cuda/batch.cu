@@ -1540,9 +1540,9 @@ struct BatchEngine::Impl {
         if (ncol > 0 && (double)L.n_smooth / ncol < 65536.0) build_packed(l, gc, cb, rows);
     }
 
-    // LD packed in the colour row order for k_bcolour_packed (levels of at most
-    // 2^21 smoothing rows; left out, like the cluster pack, when a row does not
-    // fit the item format)
+    // LD packed in the colour row order for k_bcolour_packed (up to 2^30 entries
+    // of LD, 8 GB; left out, like the cluster pack, when a row does not fit the
+    // item format)
     static bool pack_rows(const BatchCsr &LD, const int *rows, size_t nrows, std::vector<int4> &items,
                           std::vector<int2> &ents) {
         for (size_t k = 0; k < nrows; k++) {
@@ -1562,7 +1562,7 @@ struct BatchEngine::Impl {
     void build_colour_pack(int l) {
         const BatchLevel &L = h->lv[l];
         DevBLevel &d = lv[l];
-        if (L.colour_rows.empty() || L.n_smooth > (1 << 21)) return;
+        if (L.colour_rows.empty() || L.LD.nnz() > (int64_t(1) << 30)) return;
         std::vector<int4> items;
         std::vector<int2> ents;
         items.reserve(L.colour_rows.size());
