@@ -145,6 +145,13 @@ int sa_event_destroy(sa_event ev);
 /* ------------------------------------------------- host CSR and generators */
 /* io::ReadMM(path, true, false)                      Library/io/mm.hpp:24-98 */
 int sa_hcsr_read_mm(const char *path, sa_hcsr *out);
+/* the same through a binary cache file: read when it records this very
+ * Matrix Market file (size and modification time), else written after the
+ * parse (an unwritable cache is skipped) */
+int sa_hcsr_read_mm_cached(const char *mm_path, const char *cache_path, sa_hcsr *out);
+/* a host CSR to / from the binary CSR file (header, rptr, cind, val) */
+int sa_hcsr_save(sa_hcsr A, const char *path);
+int sa_hcsr_load(const char *path, sa_hcsr *out);
 int sa_hcsr_create(int n, int m, const int32_t *rptr, const int32_t *cind, const double *val, sa_hcsr *out);
 int sa_hcsr_view(sa_hcsr A, sa_csr_view *out);
 /* CSRMat::LMax1Scaling(b)                            Library/matrix/csrmat.hpp:70-80 */

@@ -297,6 +297,42 @@ extern "C" int sa_hcsr_read_mm(const char *path, sa_hcsr *out) {
     SA_GUARD_END
 }
 
+extern "C" int sa_hcsr_read_mm_cached(const char *mm_path, const char *cache_path, sa_hcsr *out) {
+    if (!mm_path || !cache_path || !out) return fail(SA_ERR_ARG, "null argument");
+    SA_GUARD_BEGIN
+    auto *h = new sa_host_csr();
+    try {
+        h->A = read_matrix_market_cached(mm_path, cache_path);
+    } catch (...) {
+        delete h;
+        throw;
+    }
+    *out = h;
+    return SA_OK;
+    SA_GUARD_END
+}
+
+extern "C" int sa_hcsr_save(sa_hcsr A, const char *path) {
+    if (!A || !path) return fail(SA_ERR_ARG, "null argument");
+    SA_GUARD_BEGIN
+    write_csr_binary(A->A, path);
+    return SA_OK;
+    SA_GUARD_END
+}
+
+extern "C" int sa_hcsr_load(const char *path, sa_hcsr *out) {
+    if (!path || !out) return fail(SA_ERR_ARG, "null argument");
+    SA_GUARD_BEGIN
+    auto *h = new sa_host_csr();
+    if (!read_csr_binary(path, h->A, nullptr, nullptr)) {
+        delete h;
+        return fail(SA_ERR_ARG, std::string("not a valid CSR file: ") + path);
+    }
+    *out = h;
+    return SA_OK;
+    SA_GUARD_END
+}
+
 static int check_csr(int n, int m, const int32_t *rptr, const int32_t *cind) {
     if (n < 0 || m < 0 || !rptr || (!cind && n > 0 && rptr[n] > 0)) return fail(SA_ERR_ARG, "invalid CSR");
     if (rptr[0] != 0) return fail(SA_ERR_ARG, "rptr[0] must be 0");

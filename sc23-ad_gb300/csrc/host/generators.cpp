@@ -1,10 +1,18 @@
 #include "generators.hpp"
 
+#include <sys/stat.h>
+
+#include <algorithm>
+#include <cctype>
+#include <charconv>
 #include <cmath>
+#include <cstdint>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <system_error>
+#include <thread>
 
 #include "sort.hpp"
 
@@ -179,18 +187,108 @@ void gen_rhs(const CsrD &A, uint64_t seed, double *xstar, double *b) {
 
 // ------------------------------------------------------------ Matrix Market
 
-CsrD read_matrix_market(const char *path) {
+// ------------------------------------------------------- Matrix Market input
+static std::vector<char> read_file(const char *path) {
     FILE *f = fopen(path, "rb");
     if (!f) throw SetupError{std::string("cannot open ") + path};
-    std::string data;
-    {
+    std::vector<char> data;
+    struct stat st;
+    if (fstat(fileno(f), &st) == 0 && S_ISREG(st.st_mode) && st.st_size > 0) {
+        data.resize((size_t)st.st_size);
+        const size_t k = fread(data.data(), 1, data.size(), f);
+        data.resize(k);
+    } else {
         char buf[1 << 16];
         size_t k;
-        while ((k = fread(buf, 1, sizeof buf, f)) > 0) data.append(buf, k);
-        fclose(f);
+        while ((k = fread(buf, 1, sizeof buf, f)) > 0) data.insert(data.end(), buf, buf + k);
     }
-    if (data.empty()) throw SetupError{"empty Matrix Market file"};
-    const char *p = data.c_str();
+    fclose(f);
+    data.push_back('\0');
+    return data;
+}
+
+static bool token_end(char ch) { return ch == '\0' || isspace((unsigned char)ch); }
+
+// strtol / strtod on one token; the fast paths (plain decimal digits,
+// std::from_chars, which rounds correctly like strtod) are taken only when
+// they consume the whole whitespace-delimited token, otherwise the C library
+// call decides
+static long parse_long(const char *p, const char **end) {
+    while (isspace((unsigned char)*p)) p++;
+    const char *q = p;
+    bool neg = false;
+    if (*q == '-') {
+        neg = true;
+        q++;
+    }
+    if (*q >= '0' && *q <= '9') {
+        long v = 0;
+        int digits = 0;
+        while (*q >= '0' && *q <= '9' && digits < 18) {
+            v = v * 10 + (*q - '0');
+            q++;
+            digits++;
+        }
+        if (token_end(*q)) {
+            *end = q;
+            return neg ? -v : v;
+        }
+    }
+    char *e;
+    const long v = strtol(p, &e, 10);
+    *end = e;
+    return v;
+}
+
+static double parse_double(const char *p, const char *limit, const char **end) {
+    while (isspace((unsigned char)*p)) p++;
+    double v = 0;
+    const auto r = std::from_chars(p, limit, v, std::chars_format::general);
+    if (r.ec == std::errc() && r.ptr > p && token_end(*r.ptr)) {
+        *end = r.ptr;
+        return v;
+    }
+    char *e;
+    v = strtod(p, &e);
+    *end = e;
+    return v;
+}
+
+struct MmPart {
+    std::vector<int> row, col;
+    std::vector<double> val;
+    bool ok = true;
+};
+
+// the entries of [p, q), which starts and ends at line boundaries; a triple
+// that does not end inside the range (a file that breaks entries across
+// lines in a way the split does not see) marks the part as not ok
+static void parse_part(const char *p, const char *q, const char *limit, MmPart &out) {
+    while (true) {
+        while (p < q && isspace((unsigned char)*p)) p++;
+        if (p >= q) return;
+        const char *e;
+        const long r = parse_long(p, &e);
+        if (e == p) break;
+        const char *e2;
+        const long c = parse_long(e, &e2);
+        if (e2 == e) break;
+        const char *e3;
+        const double v = parse_double(e2, limit, &e3);
+        if (e3 == e2 || e3 > q) break;
+        out.row.push_back((int)r - 1);
+        out.col.push_back((int)c - 1);
+        out.val.push_back(v);
+        p = e3;
+    }
+    out.ok = false;
+}
+
+CsrD read_matrix_market(const char *path) {
+    const std::vector<char> buf = read_file(path);
+    if (buf.size() <= 1) throw SetupError{"empty Matrix Market file"};
+    const char *p = buf.data();
+    const char *limit = buf.data() + buf.size() - 1;  // the terminating NUL
     const char *hdr = "%%MatrixMarket matrix coordinate";
     if (strncmp(p, hdr, strlen(hdr)) != 0) throw SetupError{"invalid Matrix Market header"};
     p += strlen(hdr);
@@ -211,22 +309,57 @@ CsrD read_matrix_market(const char *path) {
     const long PE = strtol(end, &end, 10);
     p = end;
     if (N <= 0 || M <= 0 || PE < 0) throw SetupError{"invalid Matrix Market size line"};
+    // the entry lines in parts on host threads (line-aligned, kept in file order)
+    const size_t len = (size_t)(limit - p);
+    const int hw = (int)std::max(1u, std::thread::hardware_concurrency());
+    const int T = (int)std::max<size_t>(1, std::min<size_t>((size_t)std::min(hw, 32), len >> 16));
+    std::vector<const char *> cut(T + 1);
+    cut[0] = p;
+    cut[T] = limit;
+    for (int t = 1; t < T; t++) {
+        const char *c = std::max(cut[t - 1], p + len * t / T);
+        while (c < limit && *c != '\n') c++;
+        cut[t] = c < limit ? c + 1 : limit;
+    }
+    std::vector<MmPart> parts(T);
+    {
+        std::vector<std::thread> pool;
+        for (int t = 1; t < T; t++) pool.emplace_back([&, t] { parse_part(cut[t], cut[t + 1], limit, parts[t]); });
+        parse_part(cut[0], cut[1], limit, parts[0]);
+        for (auto &th : pool) th.join();
+    }
+    // the first PE entries in file order; a part that stopped early ends the
+    // entries there (what follows is not read, as in a sequential read)
     std::vector<int> row, col;
     std::vector<double> val;
+    auto gather = [&](const std::vector<MmPart> &ps) {
+        row.clear();
+        col.clear();
+        val.clear();
+        long taken = 0;
+        for (size_t t = 0; t < ps.size() && taken < PE; t++) {
+            const MmPart &q = ps[t];
+            for (size_t k = 0; k < q.row.size() && taken < PE; k++, taken++) {
+                if (q.val[k] == 0) continue;  // has_zeros == false
+                row.push_back(q.row[k]);
+                col.push_back(q.col[k]);
+                val.push_back(q.val[k]);
+            }
+            if (!q.ok) break;
+        }
+        return taken;
+    };
     row.reserve(PE);
     col.reserve(PE);
     val.reserve(PE);
-    for (long e = 0; e < PE; e++) {
-        const long r = strtol(p, &end, 10);
-        const long c = strtol(end, &end, 10);
-        const double v = strtod(end, &end);
-        if (end == p) throw SetupError{"truncated Matrix Market file"};
-        p = end;
-        if (v == 0) continue;  // has_zeros == false
-        row.push_back((int)r - 1);
-        col.push_back((int)c - 1);
-        val.push_back(v);
+    long taken = gather(parts);
+    if (taken < PE && T > 1) {
+        // an entry broken across a split point: read the whole body in one part
+        std::vector<MmPart> one(1);
+        parse_part(p, limit, limit, one[0]);
+        taken = gather(one);
     }
+    if (taken < PE) throw SetupError{"truncated Matrix Market file"};
     const int nnz = (int)row.size();
     if (nnz > 0) hoare_sort(0, nnz - 1, true, row.data(), col.data(), val.data());
     CsrD A;
@@ -240,8 +373,10 @@ CsrD read_matrix_market(const char *path) {
         A.rptr[i + 1] = A.rptr[i] + num;
         if (num > 1) hoare_sort(A.rptr[i], A.rptr[i + 1] - 1, true, col.data(), val.data());
     }
-    A.cind.assign(col.begin(), col.begin() + nnz);
-    A.val.assign(val.begin(), val.begin() + nnz);
+    col.resize(nnz);
+    val.resize(nnz);
+    A.cind = std::move(col);
+    A.val = std::move(val);
     if (sym) {
         // helper::matrix::expand(..., "L") (helper_matrix.hpp:730-766): the stored
         // lower triangle plus its transpose without the diagonal
@@ -263,6 +398,8 @@ CsrD read_matrix_market(const char *path) {
         E.n = A.n;
         E.m = A.m;
         E.rptr.assign(A.n + 1, 0);
+        E.cind.reserve(2 * (size_t)nnz);
+        E.val.reserve(2 * (size_t)nnz);
         for (int i = 0; i < A.n; i++) {
             for (int j = A.rptr[i]; j < A.rptr[i + 1]; j++) {
                 E.cind.push_back(A.cind[j]);
@@ -275,6 +412,95 @@ CsrD read_matrix_market(const char *path) {
             E.rptr[i + 1] = (int)E.cind.size();
         }
         return E;
+    }
+    return A;
+}
+
+// ------------------------------------------------------------ binary CSR cache
+// Our own format, in the host's byte order: the header, then rptr (int32,
+// n + 1), cind (int32, nnz), val (float64, nnz).
+namespace {
+struct CsrFileHeader {
+    char magic[8];
+    int64_t n, m, nnz;
+    int64_t src_size, src_mtime_ns;  // the Matrix Market file it came from (-1: none)
+};
+constexpr char kCsrMagic[8] = {'S', 'A', 'C', 'S', 'R', '0', '1', 0};
+
+bool file_stamp(const char *path, int64_t *size, int64_t *mtime_ns) {
+    struct stat st;
+    if (stat(path, &st) != 0) return false;
+    *size = (int64_t)st.st_size;
+    *mtime_ns = (int64_t)st.st_mtim.tv_sec * 1000000000LL + (int64_t)st.st_mtim.tv_nsec;
+    return true;
+}
+}  // namespace
+
+void write_csr_binary(const CsrD &A, const char *path, int64_t src_size, int64_t src_mtime_ns) {
+    const std::string tmp = std::string(path) + ".tmp";
+    FILE *f = fopen(tmp.c_str(), "wb");
+    if (!f) throw SetupError{std::string("cannot write ") + tmp};
+    CsrFileHeader h;
+    memcpy(h.magic, kCsrMagic, 8);
+    h.n = A.n;
+    h.m = A.m;
+    h.nnz = A.nnz();
+    h.src_size = src_size;
+    h.src_mtime_ns = src_mtime_ns;
+    bool ok = fwrite(&h, sizeof h, 1, f) == 1;
+    ok = ok && fwrite(A.rptr.data(), sizeof(int), A.n + 1, f) == (size_t)A.n + 1;
+    ok = ok && (h.nnz == 0 || fwrite(A.cind.data(), sizeof(int), h.nnz, f) == (size_t)h.nnz);
+    ok = ok && (h.nnz == 0 || fwrite(A.val.data(), sizeof(double), h.nnz, f) == (size_t)h.nnz);
+    ok = fclose(f) == 0 && ok;
+    if (!ok || rename(tmp.c_str(), path) != 0) {
+        remove(tmp.c_str());
+        throw SetupError{std::string("cannot write ") + path};
+    }
+}
+
+bool read_csr_binary(const char *path, CsrD &A, int64_t *src_size, int64_t *src_mtime_ns) {
+    FILE *f = fopen(path, "rb");
+    if (!f) return false;
+    CsrFileHeader h;
+    struct stat st;
+    bool ok = fread(&h, sizeof h, 1, f) == 1 && memcmp(h.magic, kCsrMagic, 8) == 0 && h.n >= 0 && h.m >= 0 &&
+              h.nnz >= 0 && h.n < INT32_MAX && h.m < INT32_MAX && h.nnz < INT32_MAX &&
+              fstat(fileno(f), &st) == 0 &&
+              (int64_t)st.st_size == (int64_t)sizeof h + 4 * (h.n + 1) + 12 * h.nnz;
+    CsrD B;
+    if (ok) {
+        B.n = (int)h.n;
+        B.m = (int)h.m;
+        B.rptr.resize(h.n + 1);
+        B.cind.resize(h.nnz);
+        B.val.resize(h.nnz);
+        ok = fread(B.rptr.data(), sizeof(int), h.n + 1, f) == (size_t)h.n + 1 &&
+             (h.nnz == 0 || fread(B.cind.data(), sizeof(int), h.nnz, f) == (size_t)h.nnz) &&
+             (h.nnz == 0 || fread(B.val.data(), sizeof(double), h.nnz, f) == (size_t)h.nnz);
+    }
+    fclose(f);
+    if (!ok || B.rptr[0] != 0 || B.rptr[B.n] != h.nnz) return false;
+    for (int i = 0; i < B.n; i++)
+        if (B.rptr[i + 1] < B.rptr[i]) return false;
+    for (int64_t j = 0; j < h.nnz; j++)
+        if (B.cind[j] < 0 || B.cind[j] >= B.m) return false;
+    A = std::move(B);
+    if (src_size) *src_size = h.src_size;
+    if (src_mtime_ns) *src_mtime_ns = h.src_mtime_ns;
+    return true;
+}
+
+CsrD read_matrix_market_cached(const char *mm_path, const char *cache_path) {
+    int64_t size = -1, mtime = -1;
+    if (!file_stamp(mm_path, &size, &mtime)) throw SetupError{std::string("cannot open ") + mm_path};
+    CsrD A;
+    int64_t cs = 0, cm = 0;
+    if (read_csr_binary(cache_path, A, &cs, &cm) && cs == size && cm == mtime) return A;
+    A = read_matrix_market(mm_path);
+    try {
+        write_csr_binary(A, cache_path, size, mtime);
+    } catch (const SetupError &) {
+        // an unwritable cache only costs the next read its parse
     }
     return A;
 }

@@ -64,6 +64,9 @@ SIGNATURES = {
     "sa_event_elapsed_ms": (C.c_int, [VP, VP, C.POINTER(C.c_float)]),
     "sa_event_destroy": (C.c_int, [VP]),
     "sa_hcsr_read_mm": (C.c_int, [C.c_char_p, C.POINTER(VP)]),
+    "sa_hcsr_read_mm_cached": (C.c_int, [C.c_char_p, C.c_char_p, C.POINTER(VP)]),
+    "sa_hcsr_save": (C.c_int, [VP, C.c_char_p]),
+    "sa_hcsr_load": (C.c_int, [C.c_char_p, C.POINTER(VP)]),
     "sa_hcsr_create": (C.c_int, [C.c_int, C.c_int, I32P, I32P, F64P, C.POINTER(VP)]),
     "sa_hcsr_view": (C.c_int, [VP, C.POINTER(CsrView)]),
     "sa_hcsr_lmax1_scaling": (C.c_int, [VP, F64P]),
@@ -216,9 +219,23 @@ class HostCsr:
         return HostCsr(h)
 
     @staticmethod
-    def read_mm(path):
+    def read_mm(path, cache=None):
+        """io::ReadMM; with cache, through a binary CSR file that is reused
+        while it records this very Matrix Market file."""
         h = VP()
-        check(lib().sa_hcsr_read_mm(path.encode(), C.byref(h)))
+        if cache is None:
+            check(lib().sa_hcsr_read_mm(path.encode(), C.byref(h)))
+        else:
+            check(lib().sa_hcsr_read_mm_cached(path.encode(), cache.encode(), C.byref(h)))
+        return HostCsr(h)
+
+    def save(self, path):
+        check(lib().sa_hcsr_save(self.h, path.encode()))
+
+    @staticmethod
+    def load(path):
+        h = VP()
+        check(lib().sa_hcsr_load(path.encode(), C.byref(h)))
         return HostCsr(h)
 
     def arrays(self):

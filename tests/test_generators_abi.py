@@ -100,3 +100,80 @@ def test_no_gpu_context_fails_cleanly():
         pytest.skip("a GPU is present")
     assert code == sagb.SA_ERR_CUDA
     assert sagb.lib().sa_last_error()
+
+
+def _mm_text(n, rows, cols, vals, shape="general", split=False, extra=""):
+    lines = [f"%%MatrixMarket matrix coordinate real {shape}", "% comment", f"{n} {n} {len(rows)}"]
+    for k, (a, b_, x) in enumerate(zip(rows, cols, vals)):
+        if split and k % 97 == 5:  # an entry broken over two lines (strtod skips the newline)
+            lines.append(f"{a + 1} {b_ + 1}")
+            lines.append(f"{float(x)!r}")
+        else:
+            lines.append(f"{a + 1} {b_ + 1} {float(x)!r}")
+    return "\n".join(lines) + "\n" + extra
+
+
+def test_mm_reader_parallel_parse_matches_reference_rules(tmp_path):
+    """The parallel reader gives what a sequential strtol/strtod read gives:
+    the same values (exact decimal round trip, signs, exponents, integers,
+    zeros dropped), entries split across lines, extra lines after the
+    declared count ignored, too few entries rejected."""
+    rng = np.random.default_rng(4)
+    n = 3000
+    rows = rng.integers(0, n, size=60000)
+    cols = rng.integers(0, n, size=60000)
+    key = np.unique(rows.astype(np.int64) * n + cols)
+    rows, cols = (key // n).astype(int), (key % n).astype(int)
+    vals = rng.standard_normal(len(rows)) * 10.0 ** rng.integers(-12, 12, size=len(rows))
+    vals[::50] = 0.0  # dropped on read
+    vals[1::50] = np.round(vals[1::50])  # integral values written as e.g. 3.0
+    keep = vals != 0
+    rptr = np.zeros(n + 1, np.int32)
+    np.add.at(rptr, rows[keep] + 1, 1)
+    rptr = np.cumsum(rptr).astype(np.int32)
+    order = np.lexsort((cols[keep], rows[keep]))
+    for split, extra in ((False, ""), (True, ""), (False, "1 1 5.0\n2 2 6.0\n")):
+        p = tmp_path / f"m{int(split)}{len(extra)}.mtx"
+        p.write_text(_mm_text(n, rows, cols, vals, split=split, extra=extra))
+        r, c, v = sagb.HostCsr.read_mm(str(p)).arrays()
+        np.testing.assert_array_equal(r, rptr)
+        np.testing.assert_array_equal(c, cols[keep][order])
+        np.testing.assert_array_equal(v, vals[keep][order])
+    p = tmp_path / "short.mtx"
+    txt = _mm_text(n, rows, cols, vals).splitlines()
+    p.write_text("\n".join(txt[:-10]) + "\n")
+    with pytest.raises(sagb.SagbError):
+        sagb.HostCsr.read_mm(str(p))
+
+
+def test_binary_csr_cache(tmp_path):
+    """The binary CSR file round-trips a matrix exactly; the cached reader
+    writes it on the first read, reuses it while the Matrix Market file is
+    unchanged, and re-reads the Matrix Market file once it changes."""
+    import os
+    rptr, cind, val = gm.poisson2d(40)
+    A = sagb.HostCsr.from_arrays(rptr, cind, val)
+    A.save(str(tmp_path / "a.csr"))
+    r, c, v = sagb.HostCsr.load(str(tmp_path / "a.csr")).arrays()
+    np.testing.assert_array_equal(r, rptr)
+    np.testing.assert_array_equal(c, cind)
+    np.testing.assert_array_equal(v, val)
+    (tmp_path / "bad.csr").write_bytes(b"SACSR01\x00" + b"\x00" * 10)
+    with pytest.raises(sagb.SagbError):
+        sagb.HostCsr.load(str(tmp_path / "bad.csr"))
+    mm, cache = tmp_path / "a.mtx", tmp_path / "a.mtx.csr"
+    gm.write_mtx(str(mm), rptr, cind, val)
+    r, c, v = sagb.HostCsr.read_mm(str(mm), cache=str(cache)).arrays()
+    np.testing.assert_array_equal(v, val)
+    assert cache.exists()
+    stamp = os.stat(cache).st_mtime_ns
+    r, c, v = sagb.HostCsr.read_mm(str(mm), cache=str(cache)).arrays()  # from the cache
+    np.testing.assert_array_equal(v, val)
+    assert os.stat(cache).st_mtime_ns == stamp
+    # a changed source: scale the values, rewrite the file with a new modification time
+    gm.write_mtx(str(mm), rptr, cind, 2 * val)
+    os.utime(mm, ns=(stamp + 10**9, stamp + 10**9))
+    r, c, v = sagb.HostCsr.read_mm(str(mm), cache=str(cache)).arrays()
+    np.testing.assert_array_equal(v, 2 * val)
+    r, c, v = sagb.HostCsr.load(str(cache)).arrays()
+    np.testing.assert_array_equal(v, 2 * val)
