@@ -379,8 +379,10 @@ def batch_rooflines(ctx, B, a):
                 by = 8 * nnz + 4 * (n + 1) + 2 * n + 4 * n + 8 * R * n
                 calls = 2  # pre- and post-smoothing
             else:
-                # entries, row pointers, the shift, x once, y once (and z for the residuals)
-                by = 8 * nnz + 4 * (n + 1) + n + 4 * R * m + 4 * R * n
+                # entries (32-bit values and 32-bit columns, or 16-bit column offsets when the
+                # autotuner chose the compressed storage), row pointers, the shift, x once, y once
+                colb = 2 if op in (0, 2) and B.compressed(l, op) else 4
+                by = (4 + colb) * nnz + 4 * (n + 1) + n + 4 * R * m + 4 * R * n
                 calls = 1  # A (residual), U (post-smoothing residual), P and R once per V-cycle
             per.append({"level": l, "op": name, "n": n, "nnz": nnz, "colours": ncol if op == 1 else None,
                         "ms": t, "bytes": by, "per_vcycle": calls})

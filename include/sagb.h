@@ -325,6 +325,11 @@ int sa_batch_set_group(sa_batch B, int level, int op, int group);
  * (SA_ERR_ARG / an error if the level lacks that form), -1 reads it; results
  * do not depend on it */
 int sa_batch_sweep_form(sa_batch B, int level, int set, int *form);
+/* compressed column storage of a level's A (op 0) or U (op 2): 16-bit offsets
+ * column - row, 6 bytes an entry instead of 8, kept when every offset fits;
+ * set 1 / 0 chooses it (SA_ERR_ARG / an error if the operator has none), -1
+ * reads it; results do not depend on it (the autotuner chooses per operator) */
+int sa_batch_compressed(sa_batch B, int level, int op, int set, int *on);
 /* Work/main.cpp:153-161 per system and right-hand side: max|M_f64 b| / ||b|| */
 int sa_batch_rule_ratios(sa_ctx ctx, sa_batch B, const double *b, const double *nrm_b, double *ratio);
 /* one operator of one batch level on interleaved vectors: op 0 A, 2 U, 3 P,

@@ -1247,6 +1247,15 @@ extern "C" int sa_batch_set_group(sa_batch B, int level, int op, int group) {
     SA_GUARD_END
 }
 
+extern "C" int sa_batch_compressed(sa_batch B, int level, int op, int set, int *on) {
+    if (!B || !on || level < 0 || level >= B->h->Dmax || (op != 0 && op != 2) || set < -1 || set > 1)
+        return fail(SA_ERR_ARG, "invalid argument");
+    SA_GUARD_BEGIN
+    *on = B->eng->compressed(level, op, set);
+    return SA_OK;
+    SA_GUARD_END
+}
+
 extern "C" int sa_batch_sweep_form(sa_batch B, int level, int set, int *form) {
     if (!B || !form || level < 0 || level >= B->h->Dmax || set < -1 || set > 3)
         return fail(SA_ERR_ARG, "invalid argument");

@@ -46,6 +46,7 @@ struct DBCsr {
     int n;
     const int *rptr, *cind, *val;
     const signed char *bit, *dbit;
+    const short *cd;  // compressed columns: cind[j] = row + cd[j] (square operators whose offsets fit 16 bits)
 };
 
 template <int R>
@@ -99,16 +100,18 @@ __device__ __forceinline__ void store_r(int *x, int row, const int (&v)[R]) {
 //   SUB = false: acc += a_ij x_j (x through the read-only cache)
 //   SUB = true:  acc -= a_ij x_j (x written by earlier launches or colours:
 //                plain loads, or L2 loads when CG)
-template <int R, int G, bool SUB, bool CG>
-__device__ __forceinline__ void row_accumulate(const int *__restrict__ cind, const int *__restrict__ val, int e0,
-                                               int e1, int lane, const int *x, long long (&acc)[R]) {
+//   D16:         columns from the 16-bit offsets cd (column = row + cd[j])
+template <int R, int G, bool SUB, bool CG, bool D16 = false>
+__device__ __forceinline__ void row_accumulate(const int *__restrict__ cind, const short *__restrict__ cd,
+                                               const int *__restrict__ val, int e0, int e1, int lane, int row,
+                                               const int *x, long long (&acc)[R]) {
     int j = e0 + lane;
     for (; j + 3 * G < e1; j += 4 * G) {
         int cc[4];
         long long vv[4];
 #pragma unroll
         for (int q = 0; q < 4; q++) {
-            cc[q] = __ldg(cind + j + q * G);
+            cc[q] = D16 ? row + (int)__ldg(cd + j + q * G) : __ldg(cind + j + q * G);
             vv[q] = __ldg(val + j + q * G);
         }
         int xv[4][R];
@@ -128,10 +131,11 @@ __device__ __forceinline__ void row_accumulate(const int *__restrict__ cind, con
     }
     for (; j < e1; j += G) {
         const long long v = __ldg(val + j);
+        const int col = D16 ? row + (int)__ldg(cd + j) : __ldg(cind + j);
         int xv[R];
-        if constexpr (!SUB) load_r<R>(x, __ldg(cind + j), xv);
-        else if constexpr (CG) load_cg_r<R>(x, __ldg(cind + j), xv);
-        else load_rw<R>(x, __ldg(cind + j), xv);
+        if constexpr (!SUB) load_r<R>(x, col, xv);
+        else if constexpr (CG) load_cg_r<R>(x, col, xv);
+        else load_rw<R>(x, col, xv);
 #pragma unroll
         for (int r = 0; r < R; r++) {
             if constexpr (SUB) acc[r] = wsub(acc[r], v * (long long)xv[r]);
@@ -169,7 +173,7 @@ __device__ __forceinline__ void bspmv_finish(const DBCsr &A, int row, const long
     if (any) atomicOr(flags, ST_OVERFLOW);
 }
 
-template <int R, int G, int MODE>
+template <int R, int G, int MODE, bool D16>
 __global__ void __launch_bounds__(kBThreads)
 k_bspmv(DBCsr A, const int *__restrict__ x, int *__restrict__ y, const int *__restrict__ z,
         const int *__restrict__ row_sys, unsigned *__restrict__ pflag, unsigned *__restrict__ flags) {
@@ -185,7 +189,7 @@ k_bspmv(DBCsr A, const int *__restrict__ x, int *__restrict__ y, const int *__re
 #pragma unroll
     for (int q = 0; q < 4; q++) {
         const int j = e0 + lane + q * G;
-        cc[q] = j < e1 ? __ldg(A.cind + j) : -1;
+        cc[q] = j < e1 ? (D16 ? row + (int)__ldg(A.cd + j) : __ldg(A.cind + j)) : -1;
         vv[q] = j < e1 ? __ldg(A.val + j) : 0;
     }
     pdl_wait();
@@ -203,7 +207,8 @@ k_bspmv(DBCsr A, const int *__restrict__ x, int *__restrict__ y, const int *__re
 #pragma unroll
             for (int r = 0; r < R; r++) acc[r] = wadd(acc[r], (long long)vv[q] * (long long)xv[q][r]);
     }
-    if (e1 - e0 > 4 * G) row_accumulate<R, G, false, false>(A.cind, A.val, e0 + 4 * G, e1, lane, x, acc);
+    if (e1 - e0 > 4 * G)
+        row_accumulate<R, G, false, false, D16>(A.cind, A.cd, A.val, e0 + 4 * G, e1, lane, row, x, acc);
 #pragma unroll
     for (int r = 0; r < R; r++)
 #pragma unroll
@@ -246,7 +251,7 @@ k_bcolour(int cnt, const int *__restrict__ rows, DBCsr LD, const int *__restrict
         dpos = __ldg(LD.rptr + row + 1) - 1;
     }
     pdl_wait();
-    if (k < cnt) row_accumulate<R, G, true, false>(LD.cind, LD.val, e0, dpos, lane, out, acc);
+    if (k < cnt) row_accumulate<R, G, true, false>(LD.cind, nullptr, LD.val, e0, dpos, lane, row, out, acc);
 #pragma unroll
     for (int r = 0; r < R; r++)
 #pragma unroll
@@ -309,7 +314,8 @@ k_bsweep_cluster(const int *__restrict__ gc_ptr, const int *__restrict__ cbound,
             if (idx < b) {
                 row = __ldg(grows + idx);
                 dpos = __ldg(LD.rptr + row + 1) - 1;
-                row_accumulate<R, G, true, true>(LD.cind, LD.val, __ldg(LD.rptr + row), dpos, lane, out, acc);
+                row_accumulate<R, G, true, true>(LD.cind, nullptr, LD.val, __ldg(LD.rptr + row), dpos, lane, row, out,
+                                                 acc);
             }
 #pragma unroll
             for (int r = 0; r < R; r++)
@@ -941,7 +947,7 @@ __global__ void k_bv0(const BTile *__restrict__ tiles, const double *__restrict_
 }
 
 // w = A z on the tile's rows and acc[p][0] += V0 . w
-template <int R, int G>
+template <int R, int G, bool D16>
 __global__ void __launch_bounds__(kBThreads)
 k_bspmv_dot(const BTile *__restrict__ tiles, DBCsr A, const int *__restrict__ z, int *__restrict__ w,
             const int *__restrict__ v0, const BPair *__restrict__ pairs, unsigned long long *acc, int m,
@@ -961,7 +967,8 @@ k_bspmv_dot(const BTile *__restrict__ tiles, DBCsr A, const int *__restrict__ z,
 #pragma unroll
         for (int r = 0; r < R; r++) a[r] = 0;
         if (row < t.row1)
-            row_accumulate<R, G, false, false>(A.cind, A.val, __ldg(A.rptr + row), __ldg(A.rptr + row + 1), lane, z, a);
+            row_accumulate<R, G, false, false, D16>(A.cind, A.cd, A.val, __ldg(A.rptr + row), __ldg(A.rptr + row + 1),
+                                                    lane, row, z, a);
 #pragma unroll
         for (int r = 0; r < R; r++)
 #pragma unroll
@@ -1296,15 +1303,28 @@ struct DevBMat {
     int group = 1;
     int *rp = nullptr, *ci = nullptr, *va = nullptr;
     signed char *bi = nullptr, *db = nullptr;
-    void up(const BatchCsr &M) {
+    short *cdv = nullptr;  // 16-bit column offsets (square operators whose offsets all fit)
+    bool d16 = false;      // the lane kernels read cdv instead of ci (6 bytes an entry instead of 8)
+    void up(const BatchCsr &M, bool square = false) {
         d = dview(M, rp, ci, va, bi, db);
         const double avg = M.n ? (double)M.nnz() / M.n : 1.0;
         group = avg <= 32.0 ? 0 : pick_group(avg);  // 0: tile-staged stream
+        if (!square || M.nnz() == 0) return;
+        std::vector<short> cd(M.nnz());
+        for (int i = 0; i < M.n; i++)
+            for (int j = M.rptr[i]; j < M.rptr[i + 1]; j++) {
+                const int off = M.cind[j] - i;
+                if (off < -32768 || off > 32767) return;
+                cd[j] = (short)off;
+            }
+        cdv = dupload(cd);
+        d.cd = cdv;
     }
     void release() {
-        dfree(rp); dfree(ci); dfree(va); dfree(bi); dfree(db);
+        dfree(rp); dfree(ci); dfree(va); dfree(bi); dfree(db); dfree(cdv);
         rp = ci = va = nullptr;
         bi = db = nullptr;
+        cdv = nullptr;
     }
 };
 
@@ -1360,6 +1380,10 @@ struct BatchEngine::Impl {
     BInfo *info_d = nullptr, *info_h = nullptr;
     std::vector<cudaGraphExec_t> graphs;
     bool graph_pdl = true;  // the PDL setting the graphs were captured with
+    // the Arnoldi step's A Z_j fused with its first dot (tuned apart from the
+    // V-cycle's A: its tiles and reductions favour other lanes per row)
+    int dot_group = -1;  // -1: the level-0 A's lanes per row
+    bool dot_d16 = false;
     // the stand-alone V-cycle (precondition) replayed from a graph captured for one in/out pair
     cudaGraphExec_t vc_graph = nullptr;
     const int *vc_in = nullptr;
@@ -1381,9 +1405,9 @@ struct BatchEngine::Impl {
             DevBLevel &d = lv[l];
             d.n_all = L.n_all;
             d.n_smooth = L.n_smooth;
-            d.A.up(L.A);
+            d.A.up(L.A, true);
             d.LD.up(L.LD);
-            d.U.up(L.U);
+            d.U.up(L.U, true);
             d.P.up(L.P);
             d.R.up(L.R);
             // the colour pass reads a row's LD entries minus the diagonal (no stream form)
@@ -1791,12 +1815,16 @@ struct BatchEngine::Impl {
         }
         const long long threads = (long long)M.d.n * M.group;
         const int blocks = (int)((threads + kBThreads - 1) / kBThreads);
+        const bool d16 = M.d16 && M.cdv;
         by_r([&](auto RR) {
             constexpr int R = decltype(RR)::value;
             by_g(M.group, [&](auto GG) {
                 constexpr int G = decltype(GG)::value;
-                auto k = mode == SPMV_SET ? k_bspmv<R, G, SPMV_SET>
-                         : mode == SPMV_RESID ? k_bspmv<R, G, SPMV_RESID> : k_bspmv<R, G, SPMV_ADD>;
+                auto k = d16 ? (mode == SPMV_SET ? k_bspmv<R, G, SPMV_SET, true>
+                                : mode == SPMV_RESID ? k_bspmv<R, G, SPMV_RESID, true> : k_bspmv<R, G, SPMV_ADD, true>)
+                             : (mode == SPMV_SET ? k_bspmv<R, G, SPMV_SET, false>
+                                : mode == SPMV_RESID ? k_bspmv<R, G, SPMV_RESID, false>
+                                                     : k_bspmv<R, G, SPMV_ADD, false>);
                 launch(k, blocks, kBThreads, 0, 1, M.d, x, y, z, row_sys, cur_pflag, c.d_flags);
             });
         });
@@ -1945,6 +1973,26 @@ struct BatchEngine::Impl {
         c.launches += 2;
     }
 
+    // w = A z with the first Gram-Schmidt dot (v0 . w) per pair into acc
+    void spmv_dot(const int *z, int *w, const int *v0, unsigned long long *accp, int mm) {
+        const DevBMat &A0 = lv[0].A;
+        const int g = dot_group >= 0 ? dot_group : A0.group;
+        const bool d16 = dot_d16 && A0.cdv && g > 0;
+        by_r([&](auto RR) {
+            constexpr int R = decltype(RR)::value;
+            if (g == 0) {
+                launch(k_bspmv_dot_stream<R>, nstiles, kStreamThreads, 0, 1, (const BTile *)stiles, A0.d, z, w, v0,
+                       accp, mm, pflag, c.d_flags);
+            } else {
+                by_g(g, [&](auto GG) {
+                    constexpr int G = decltype(GG)::value;
+                    launch(d16 ? k_bspmv_dot<R, G, true> : k_bspmv_dot<R, G, false>, ntiles, kBThreads, 0, 1,
+                           (const BTile *)tiles, A0.d, z, w, v0, (const BPair *)pairs, accp, mm, pflag, c.d_flags);
+                });
+            }
+        });
+    }
+
     void arnoldi_step(int j) {
         const int P = S * Rn;
         const size_t vs = N0 * Rn;
@@ -1953,19 +2001,9 @@ struct BatchEngine::Impl {
         // instruction: programmatic launch only hides the launch latency
         launch(k_binfo_reset, 1, 1, 0, 1, info_d);
         vcycle(Vj, Zj);
-        const DevBMat &A0 = lv[0].A;
+        spmv_dot(Zj, w, V, acc, m);
         by_r([&](auto RR) {
             constexpr int R = decltype(RR)::value;
-            if (A0.group == 0) {
-                launch(k_bspmv_dot_stream<R>, nstiles, kStreamThreads, 0, 1, (const BTile *)stiles, A0.d,
-                       (const int *)Zj, w, (const int *)V, acc, m, pflag, c.d_flags);
-            } else {
-                by_g(A0.group, [&](auto GG) {
-                    constexpr int G = decltype(GG)::value;
-                    launch(k_bspmv_dot<R, G>, ntiles, kBThreads, 0, 1, (const BTile *)tiles, A0.d, (const int *)Zj, w,
-                           (const int *)V, (const BPair *)pairs, acc, m, pflag, c.d_flags);
-                });
-            }
             for (int k = 0; k <= j; k++) {
                 if (k < j)
                     launch(k_bmgs<R, false>, ntiles, kBThreads, 0, 1, (const BTile *)tiles, k, j, m, vs,
@@ -2174,6 +2212,16 @@ int BatchEngine::sweep_form(int level, int set) {
     }
     return L.use_cluster;
 }
+int BatchEngine::compressed(int level, int op, int set) {
+    if (level < 0 || level >= impl_->Dmax || (op != 0 && op != 2)) throw CudaError{"no such operator"};
+    DevBMat &M = op == 0 ? impl_->lv[level].A : impl_->lv[level].U;
+    if (set >= 0) {
+        if (set > 0 && !M.cdv) throw CudaError{"this operator has no compressed columns"};
+        M.d16 = set > 0;
+        impl_->clear_graphs();
+    }
+    return M.d16 && M.cdv ? 1 : 0;
+}
 int BatchEngine::group(int level, int op) const {
     const DevBLevel &L = impl_->lv[level];
     const DevBMat *M = op == 0 ? &L.A : op == 1 ? &L.LD : op == 2 ? &L.U : op == 3 ? &L.P : &L.R;
@@ -2286,16 +2334,45 @@ void BatchEngine::autotune(int reps) {
             }
             float best = 1e30f;
             int bestg = M->group;
+            bool bestd = false;
+            for (int dd = 0; dd < (M->cdv ? 2 : 1); dd++)
+                for (int g : cand) {
+                    if (dd && g == 0) continue;  // the compressed columns are read by the lane kernels
+                    M->group = g;
+                    M->d16 = dd;
+                    const float ms = timeit([&] { I.bspmv(*M, xa, xb, SPMV_SET, nullptr, L.row_sys); });
+                    if (ms < best) {
+                        best = ms;
+                        bestg = g;
+                        bestd = dd;
+                    }
+                }
+            M->group = bestg;
+            M->d16 = bestd;
+        }
+    }
+    {
+        // the Arnoldi SpMV + first dot, on its own (acc for one column, m = 1)
+        unsigned long long *acct = (unsigned long long *)dmalloc(sizeof(unsigned long long) * (size_t)I.S * I.Rn * 3);
+        SAGB_CUDA(cudaMemset(acct, 0, sizeof(unsigned long long) * (size_t)I.S * I.Rn * 3));
+        float best = 1e30f;
+        int bestg = I.lv[0].A.group;
+        bool bestd = false;
+        for (int dd = 0; dd < (I.lv[0].A.cdv ? 2 : 1); dd++)
             for (int g : cand) {
-                M->group = g;
-                const float ms = timeit([&] { I.bspmv(*M, xa, xb, SPMV_SET, nullptr, L.row_sys); });
+                if (dd && g == 0) continue;
+                I.dot_group = g;
+                I.dot_d16 = dd;
+                const float ms = timeit([&] { I.spmv_dot(xa, xb, xa, acct, 1); });
                 if (ms < best) {
                     best = ms;
                     bestg = g;
+                    bestd = dd;
                 }
             }
-            M->group = bestg;
-        }
+        I.dot_group = bestg;
+        I.dot_d16 = bestd;
+        dfree(acct);
     }
     SAGB_CUDA(cudaMemsetAsync(I.pflag, 0, sizeof(unsigned) * (size_t)I.S * I.Rn * 2, c.stream));
     SAGB_CUDA(cudaMemsetAsync(c.d_flags, 0, sizeof(unsigned), c.stream));

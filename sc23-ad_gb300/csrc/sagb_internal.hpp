@@ -251,6 +251,9 @@ class BatchEngine {
     // launch, 2: packed cluster launch, 3: a launch per colour over LD packed
     // in colour order); set >= 0 chooses it, -1 only reads
     int sweep_form(int level, int set);
+    // 16-bit column offsets for A (op 0) or U (op 2) of one level: set 1 / 0
+    // chooses them (1 needs offsets that fit), -1 only reads
+    int compressed(int level, int op, int set);
     // one operator of one level on caller vectors (op 1: the colour sweep LD^-1 in)
     void level_op(int level, int op, const int *in, int *out);
     void coarse_solve();  // the batched LU on the engine's own level vectors

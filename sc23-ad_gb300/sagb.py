@@ -134,6 +134,7 @@ SIGNATURES = {
     "sa_batch_group": (C.c_int, [VP, C.c_int, C.c_int, C.POINTER(C.c_int)]),
     "sa_batch_set_group": (C.c_int, [VP, C.c_int, C.c_int, C.c_int]),
     "sa_batch_sweep_form": (C.c_int, [VP, C.c_int, C.c_int, C.POINTER(C.c_int)]),
+    "sa_batch_compressed": (C.c_int, [VP, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int)]),
     "sa_batch_time_op": (C.c_int, [VP, VP, C.c_int, C.c_int, VP, VP, C.c_int, C.POINTER(C.c_float)]),
     "sa_batch_rule_ratios": (C.c_int, [VP, VP, VP, VP, F64P]),
     "sa_batch_solve": (C.c_int, [VP, VP, C.POINTER(SolverParams), I32P, VP, VP, VP, I32P, I32P, I32P]),
@@ -739,6 +740,13 @@ class Batch:
         check(lib().sa_batch_set_group(self.h, level, op, group))
 
     SWEEP_PER_COLOUR, SWEEP_CLUSTER, SWEEP_PACKED, SWEEP_PACKED_COLOUR = 0, 1, 2, 3
+
+    def compressed(self, level, op, set=-1):
+        """16-bit column offsets for the level's A (op 0) or U (op 2); set 1 /
+        0 chooses them."""
+        f = C.c_int()
+        check(lib().sa_batch_compressed(self.h, level, op, set, C.byref(f)))
+        return f.value
 
     def sweep_form(self, level, set=-1):
         """The colour sweep's launch form at one level (0 a launch per colour,

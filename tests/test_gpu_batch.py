@@ -93,6 +93,19 @@ def test_batched_vcycle_bit_exact(ctx, nrhs):
                     continue
                 B.set_group(lv, 1, g)
             np.testing.assert_array_equal(B.precondition(vin).reshape(B.rows, nrhs), out, err_msg=f"form {form} G {g}")
+    # nor does the compressed column storage of A and U (16-bit offsets), on or off at every level
+    for on in (1, 0):
+        n_on = 0
+        for lv in range(B.depth):
+            for op in (0, 2):
+                try:
+                    B.compressed(lv, op, on)
+                    B.set_group(lv, op, 2)  # a lane kernel (the stream form reads 32-bit columns)
+                    n_on += on
+                except sagb.SagbError:
+                    pass
+        assert n_on > 0 or on == 0
+        np.testing.assert_array_equal(B.precondition(vin).reshape(B.rows, nrhs), out, err_msg=f"compressed {on}")
     B.close()
 
 
@@ -220,6 +233,17 @@ def test_launch_options_do_not_change_results(ctx):
         return out, x, it
 
     ref = run()
+    # the Arnoldi SpMV and the V-cycle with compressed columns wherever they fit
+    for lv in range(B.depth):
+        for op in (0, 2):
+            try:
+                B.compressed(lv, op, 1)
+                B.set_group(lv, op, 1)
+            except sagb.SagbError:
+                pass
+    got = run()
+    for k in range(3):
+        np.testing.assert_array_equal(got[k], ref[k])
     try:
         for opt in (sagb.OPT_PDL, sagb.OPT_GRAPHS):
             ctx.set_option(opt, 0)
