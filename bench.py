@@ -608,8 +608,8 @@ def main_ours(a):
         name = max(fam, key=lambda f: fam[f][0])
         ms, by = fam[name]
         ach = by / (ms * 1e-3) / 1e9
-        kern = "k_bcolour / k_bsweep_packed / k_bsweep_cluster (the autotuned multicolour Gauss-Seidel sweeps, " \
-            "all levels)" if name == "sweep" else \
+        kern = "k_bcolour_packed / k_bcolour / k_bsweep_packed / k_bsweep_cluster (the autotuned multicolour " \
+            "Gauss-Seidel sweeps, all levels)" if name == "sweep" else \
             "k_bspmv / k_bspmv_stream (level SpMVs, all levels)"
         line["roofline"] = {"kernel": kern, "bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
                             "frac": ach / peak, "peak_kind": peak_kind, "traffic": ncu_traffic(name + "_per_vcycle"),
