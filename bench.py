@@ -6,8 +6,9 @@ Workload: 3D 7-point Poisson 128^3 (2,097,152 rows, 14,581,760 nonzeros, 6/-1,
 Dirichlet), b = A x* with x* ~ U[-1, 1] (splitmix64 seed), LMax1 row scaling,
 x0 = 0, m = 30, eps = 1e-10 on the explicit residual, one right-hand side.  A
 step is one full solve (Restarted + FGMRESflex + V-cycles) by the batched
-engine: multicolour SOR (8 colours per level), a 400-row coarsest level,
-autotuned launch shapes, graph-captured Arnoldi steps, and the F chosen by the
+engine: multicolour SOR (8 colours on the finest level, 2 on the coarser
+ones), a 400-row coarsest level, autotuned launch shapes, graph-captured
+Arnoldi steps chained by programmatic dependent launch, and the F chosen by the
 trained selector with the reference's rule (Work/main.cpp:153-161) as default
 and fallback.  Beside it, on the same GPU: the plain drop-in (the reference's
 bit-exact SOR order and bit rule), FP64-AMG-FGMRES, the single-system
@@ -283,11 +284,14 @@ def run_ours(a, dist):
 
 def setup_row(ctx, r, c, v):
     """The AMG setup of the same system (the headline's parameters: multicolour
-    smoother, 8 colours, 400-row coarsest level) on the host and with the
+    smoother, 8 colours on the finest level and 2 below, 400-row coarsest
+    level) on the host and with the
     Ruge-Stueben levels on the GPU; the two hierarchies are compared array by
     array (they must be identical)."""
     import sagb
-    params = sagb.amg_params(multicolor=1, max_colours=8, coarse_size=400)
+    params = sagb.amg_params(multicolor=1, max_colours=sagb.Batch.DEFAULT_MAX_COLOURS,
+                             coarse_colours=sagb.Batch.DEFAULT_COARSE_COLOURS,
+                             coarse_size=sagb.Batch.DEFAULT_COARSE_SIZE)
     t = time.perf_counter()
     g = sagb.Setup(sagb.INT, r, c, v, params, ctx=ctx)
     t_gpu = time.perf_counter() - t

@@ -99,6 +99,7 @@ typedef struct {
                             conflicting colour (Jacobi-like inside it); 0: no cap (default) */
     int coarse_size;     /* coarsen while the coarsest level has more rows than this; 0: the
                             reference's 2000 (INTAMG.hpp:38-51) */
+    int coarse_colours;  /* multicolour: the cap on the levels below the finest (0: max_colours) */
 } sa_amg_params;
 
 typedef struct {

@@ -514,6 +514,7 @@ extern "C" void sa_amg_params_default(sa_amg_params *p) {
     p->smooth_iter = 1;
     p->multicolor = 0;
     p->max_colours = 0;
+    p->coarse_colours = 0;
     p->coarse_size = 0;
 }
 
@@ -530,6 +531,7 @@ static void build_setup(sa_hierarchy &s, const CsrD &A, Ctx *gpu = nullptr) {
     sm.iter = s.p.smooth_iter;
     sm.multicolor = s.p.multicolor;
     sm.max_colours = s.p.max_colours;
+    sm.coarse_colours = s.p.coarse_colours;
     if (s.precision == SA_INT) s.hi = std::make_shared<IntHierarchy>(build_int_hierarchy(A, chain, sm));
     else if (s.precision == SA_F64) s.hd = std::make_shared<FpHierarchy<double>>(build_f64_hierarchy(A, chain, sm));
     else s.hf = std::make_shared<FpHierarchy<float>>(build_f32_hierarchy(A, chain, sm));
@@ -546,7 +548,7 @@ static int setup_create(Ctx *gpu, int precision, const sa_amg_params *p, int n, 
     else sa_amg_params_default(&s->p);
     if (s->p.smooth_iter < 1 || s->p.max_levels < 1 || s->p.smoother_blocks < 0 ||
         s->p.multicolor < 0 || s->p.multicolor > 1 || (s->p.multicolor && s->p.smoother_blocks) ||
-        s->p.max_colours < 0 || s->p.coarse_size < 0) {
+        s->p.max_colours < 0 || s->p.coarse_size < 0 || s->p.coarse_colours < 0) {
         delete s;
         return fail(SA_ERR_ARG, "invalid AMG parameters");
     }
@@ -1134,7 +1136,7 @@ extern "C" int sa_batch_create(sa_ctx ctx, int nsys, const int *n, const int32_t
     if (p) q = *p;
     else sa_amg_params_default(&q);
     if (q.smooth_iter < 1 || q.max_levels < 1 || q.smoother_blocks != 0 || q.theta <= 0 || q.theta > 1 ||
-        q.max_colours < 0 || q.coarse_size < 0)
+        q.max_colours < 0 || q.coarse_size < 0 || q.coarse_colours < 0)
         return fail(SA_ERR_ARG, "invalid AMG parameters (the batch uses the multicolour SOR smoother)");
     q.multicolor = 1;
     SA_GUARD_BEGIN
@@ -1167,7 +1169,8 @@ extern "C" int sa_batch_create(sa_ctx ctx, int nsys, const int *n, const int32_t
         if (ctx->c.gpu_setup)
             gpu_chain = [&](const CsrD &A) { return rs_chain_gpu(ctx->c, A, q.theta, q.max_levels, cs); };
         B->h = std::make_shared<BatchHierarchy>(build_batch(sys, q.theta, q.max_levels, q.omega, q.smooth_iter,
-                                                            threads, src, q.max_colours, cs, gpu_chain,
+                                                            threads, src, q.max_colours, q.coarse_colours, cs,
+                                                            gpu_chain,
                                                             kGpuChainRows));
         SAGB_CUDA(cudaSetDevice(ctx->c.device));
         B->eng = std::make_unique<BatchEngine>(ctx->c, B->h, nrhs);
@@ -1285,6 +1288,7 @@ extern "C" int sa_batch_rule_ratios(sa_ctx ctx, sa_batch B, const double *b, con
     sm.iter = B->p.smooth_iter;
     sm.multicolor = 1;
     sm.max_colours = B->p.max_colours;
+    sm.coarse_colours = B->p.coarse_colours;
     // FP64 hierarchies of all systems on host threads (copies of one matrix share one)
     std::vector<std::shared_ptr<FpHierarchy<double>>> hds(S);
     {

@@ -823,13 +823,13 @@ static void parallel_tasks(int n, F &&f) {
     if (first) std::rethrow_exception(first);
 }
 
-static void smoother_split(const CsrD &A, const SmootherSpec &sm, CsrD &LD, CsrD &U, std::vector<int> &bj,
-                           std::vector<int> &colour) {
+static void smoother_split(const CsrD &A, const SmootherSpec &sm, int level, CsrD &LD, CsrD &U,
+                           std::vector<int> &bj, std::vector<int> &colour) {
     colour.clear();
     bj.clear();
     if (sm.multicolor) {
         int nc = 0;
-        colour = greedy_colouring(A, &nc, sm.max_colours);
+        colour = greedy_colouring(A, &nc, sm.cap(level));
         mc_sor_split(A, sm.omega, colour, LD, U);
     } else if (sm.block > 0) {
         block_sor_split(A, sm.omega, sm.block, LD, U, bj);
@@ -881,7 +881,7 @@ IntHierarchy build_int_hierarchy(const CsrD &A, const RsChain &chain, const Smoo
             const int l = t;
             const CsrD &Al = l == 0 ? A : CA[l - 1];
             CsrD LD, U;
-            smoother_split(Al, sm, LD, U, h.bj[l], h.colour[l]);
+            smoother_split(Al, sm, l, LD, U, h.bj[l], h.colour[l]);
             h.LD[l] = to_ldtri_flex(sm.multicolor ? invert_last(LD) : extract_ldinv(LD));
             h.U[l] = to_flex(U);
         } else if (t < 2 * D) {
@@ -929,7 +929,7 @@ static FpHierarchy<T> build_fp(const CsrD &A, const RsChain &chain, const Smooth
             const int l = t;
             const CsrD &Al = l == 0 ? A : chain.CA[l - 1];
             CsrD LD, U;
-            smoother_split(Al, sm, LD, U, h.bj[l], h.colour[l]);
+            smoother_split(Al, sm, l, LD, U, h.bj[l], h.colour[l]);
             h.LD[l] = convert<T>(sm.multicolor ? invert_last(LD) : extract_ldinv(LD));
             h.U[l] = convert<T>(U);
         } else if (t < 2 * D) {

@@ -100,6 +100,8 @@ struct SmootherSpec {
     int iter = 1;
     int multicolor = 0;  // 1: SOR in colour order (the multicolour variant)
     int max_colours = 0; // multicolour: at most this many colours (0: as many as a proper colouring needs)
+    int coarse_colours = 0;  // multicolour: the cap below the finest level (0: max_colours)
+    int cap(int level) const { return level > 0 && coarse_colours > 0 ? coarse_colours : max_colours; }
 };
 
 // Greedy colouring, colour by colour, on the symmetrised pattern (the

@@ -31,7 +31,7 @@ static int level_size(const IntHierarchy &h, int l) { return l == 0 ? h.A0.n : h
 
 BatchHierarchy build_batch(const std::vector<CsrD> &systems, double theta, int max_levels, double omega,
                            int smooth_iter, int threads, const std::vector<int> &src_in, int max_colours,
-                           int coarse_size, const std::function<RsChain(const CsrD &)> &big_chain, int big_rows) {
+                           int coarse_colours, int coarse_size, const std::function<RsChain(const CsrD &)> &big_chain, int big_rows) {
     BatchHierarchy B;
     const int S = (int)systems.size();
     if (S == 0) throw SetupError{"empty batch"};
@@ -54,6 +54,7 @@ BatchHierarchy build_batch(const std::vector<CsrD> &systems, double theta, int m
     sm.iter = smooth_iter;
     sm.multicolor = 1;
     sm.max_colours = max_colours;
+    sm.coarse_colours = coarse_colours;
     if (big_chain)
         for (int s = 0; s < S; s++)
             if (src[s] == s && systems[s].n >= big_rows)

@@ -72,7 +72,7 @@ struct BatchHierarchy {
 // on a GPU; it must return what rs_chain returns.
 BatchHierarchy build_batch(const std::vector<CsrD> &systems, double theta, int max_levels, double omega,
                            int smooth_iter, int threads, const std::vector<int> &src = {}, int max_colours = 0,
-                           int coarse_size = 2000,
+                           int coarse_colours = 0, int coarse_size = 2000,
                            const std::function<RsChain(const CsrD &)> &big_chain = nullptr, int big_rows = 0);
 
 }  // namespace sagb

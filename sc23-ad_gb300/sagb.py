@@ -35,7 +35,7 @@ class CsrView(C.Structure):
 class AmgParams(C.Structure):
     _fields_ = [("max_levels", C.c_int), ("theta", C.c_double), ("smoother_blocks", C.c_int),
                 ("omega", C.c_double), ("smooth_iter", C.c_int), ("multicolor", C.c_int),
-                ("max_colours", C.c_int), ("coarse_size", C.c_int)]
+                ("max_colours", C.c_int), ("coarse_size", C.c_int), ("coarse_colours", C.c_int)]
 
 
 class SolverParams(C.Structure):
@@ -268,8 +268,9 @@ class HostCsr:
 
 
 def amg_params(max_levels=20, theta=0.8, smoother_blocks=0, omega=1.0, smooth_iter=1, multicolor=0, max_colours=0,
-               coarse_size=0):
-    return AmgParams(max_levels, theta, smoother_blocks, omega, smooth_iter, multicolor, max_colours, coarse_size)
+               coarse_size=0, coarse_colours=0):
+    return AmgParams(max_levels, theta, smoother_blocks, omega, smooth_iter, multicolor, max_colours, coarse_size,
+                     coarse_colours)
 
 
 class Setup:
@@ -659,16 +660,20 @@ class Mlp:
 class Batch:
     """Many systems (already scaled), nrhs right-hand sides each, solved together.
 
-    The default parameters cap the colours of every level at 8: coarse
-    operators need up to ~150 colours for a proper colouring, and each colour
-    is one dependent step of the sweep, while the capped split (rows beyond
-    the cap act Jacobi-like within their colour) keeps the iteration count
-    within about one iteration on the synthetic test families.  They also
-    coarsen down to 400 rows instead of the reference's 2000, so the dense
-    coarsest LU is ~20x smaller (0.05 instead of 0.55 ms per V-cycle at 128^3)
-    for two or three more cheap levels, with the same iteration counts."""
+    The default parameters cap the colours of the finest level at 8 (a proper
+    colouring of 7- and 27-point stencils) and of every coarser level at 2:
+    coarse operators need up to ~150 colours for a proper colouring, each
+    colour is one dependent step of the sweep (~1.6 us), and the capped split
+    (rows beyond the cap act Jacobi-like within their colour) keeps the
+    iteration count within about one iteration on the synthetic test
+    families while the V-cycle has 6 colour steps per coarse level instead
+    of ~16.  They also coarsen down to 400 rows instead of the reference's
+    2000, so the dense coarsest LU is ~20x smaller (0.05 instead of 0.55 ms
+    per V-cycle at 128^3) for two or three more cheap levels, with the same
+    iteration counts."""
 
-    DEFAULT_MAX_COLOURS = 8
+    DEFAULT_MAX_COLOURS = 8     # the finest level: a proper colouring of 7- and 27-point stencils
+    DEFAULT_COARSE_COLOURS = 2  # the levels below: fewer dependent colour steps (see the batched engine's notes)
     DEFAULT_COARSE_SIZE = 400
 
     def __init__(self, ctx, systems, nrhs=1, params=None, threads=0):
@@ -680,7 +685,8 @@ class Batch:
         rp = (I32P * S)(*[_ptr(r, I32P) for r, _, _ in self._keep])
         cp = (I32P * S)(*[_ptr(c, I32P) for _, c, _ in self._keep])
         vp = (F64P * S)(*[_ptr(v, F64P) for _, _, v in self._keep])
-        p = params or amg_params(max_colours=self.DEFAULT_MAX_COLOURS, coarse_size=self.DEFAULT_COARSE_SIZE)
+        p = params or amg_params(max_colours=self.DEFAULT_MAX_COLOURS, coarse_size=self.DEFAULT_COARSE_SIZE,
+                                 coarse_colours=self.DEFAULT_COARSE_COLOURS)
         self.h = VP()
         check(lib().sa_batch_create(ctx.h, S, _ptr(n, I32P), rp, cp, vp, nrhs, C.byref(p), threads,
                                     C.byref(self.h)))
