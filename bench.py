@@ -389,7 +389,8 @@ def batch_rooflines(ctx, B, a):
                 by = (4 + colb) * nnz + 4 * (n + 1) + n + 4 * R * m + 4 * R * n
                 calls = 1  # A (residual), U (post-smoothing residual), P and R once per V-cycle
             per.append({"level": l, "op": name, "n": n, "nnz": nnz, "colours": ncol if op == 1 else None,
-                        "ms": t, "bytes": by, "per_vcycle": calls})
+                        "ms": t, "bytes": by, "per_vcycle": calls,
+                        "d16": bool(op in (0, 2) and B.compressed(l, op))})
             key = "sweep" if op == 1 else "spmv"
             fam[key][0] += calls * t
             fam[key][1] += calls * by
@@ -621,7 +622,9 @@ def main_ours(a):
         sp = next(p for p in k["per_op"] if p["level"] == 0 and p["op"] == "A")
         spa = sp["bytes"] / (sp["ms"] * 1e-3) / 1e9
         line["spmv_A0"] = {"kernel": "k_bspmv level 0 (the autotuned form)", "achieved": spa, "peak": peak, "unit": "GB/s",
-                           "frac": spa / peak, "ms": sp["ms"], "bytes": sp["bytes"], "traffic": ncu_traffic("spmv_A0")}
+                           "frac": spa / peak, "ms": sp["ms"], "bytes": sp["bytes"],
+                           "columns": "16-bit offsets" if sp["d16"] else "32-bit",
+                           "traffic": ncu_traffic("spmv_A0_d16" if sp["d16"] else "spmv_A0")}
         line["vcycle_ms"] = k["vcycle_ms"]
         line["coarse_lu_ms"] = k["coarse_lu_ms"]
         line["families_ms_per_vcycle"] = {f: fam[f][0] for f in fam}
@@ -909,12 +912,15 @@ def main_vcycle(a):
             B.sweep_form(l, form)
             for op, g in enumerate(groups):
                 B.set_group(l, op, g)
+            for op, on in zip((0, 2), tune.get("compressed", [[0, 0]] * B.depth)[l]):
+                B.compressed(l, op, on)
     else:
         B.autotune(2)
         if a.tune_file:
             with open(a.tune_file, "w") as f:
                 json.dump({"forms": [B.sweep_form(l) for l in range(B.depth)],
-                           "groups": [[B.group(l, op) for op in range(5)] for l in range(B.depth)]}, f)
+                           "groups": [[B.group(l, op) for op in range(5)] for l in range(B.depth)],
+                           "compressed": [[B.compressed(l, 0), B.compressed(l, 2)] for l in range(B.depth)]}, f)
     x = sagb.DeviceArray.from_host(ctx, np.random.default_rng(3).integers(-(1 << 28), 1 << 28, size=B.rows)
                                    .astype(np.int32))
     y = sagb.DeviceArray(ctx, B.rows, np.int32)
