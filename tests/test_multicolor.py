@@ -154,3 +154,31 @@ def test_oracle_multicolour_solves(mc_setups):
     # points are then one colour and the multicolour two-grid cycle is much
     # stronger than the natural-order one
     assert its["mc"] <= its["nat"] and its["mc_int"] <= its["nat_int"] + 3, its
+
+
+def test_colour_caps_per_level():
+    """max_colours caps the finest level's colours, coarse_colours the coarser
+    levels' (rows beyond a cap join their least conflicting colour); the split
+    still reconstructs each operator, and a negative cap is rejected."""
+    A = sagb.HostCsr.generate(sagb.GEN_STENCIL27, 14)
+    xs, b = A.rhs(1)
+    A.lmax1_scaling(b)
+    r, c, v = A.arrays()
+    s = sagb.Setup(sagb.F64, r, c, v, sagb.amg_params(multicolor=1, max_colours=8, coarse_colours=2, coarse_size=100))
+    full = sagb.Setup(sagb.F64, r, c, v, sagb.amg_params(multicolor=1, coarse_size=100))
+    assert s.depth >= 3
+    assert s.view(sagb.OP_COLOR, 0).max() + 1 <= 8
+    np.testing.assert_array_equal(s.view(sagb.OP_COLOR, 0), full.view(sagb.OP_COLOR, 0))  # 27-point: 8 suffice
+    for lv in range(1, s.depth):
+        col = s.view(sagb.OP_COLOR, lv)
+        assert col.max() + 1 <= 2
+        assert full.view(sagb.OP_COLOR, lv).max() + 1 > 2  # the cap binds below the finest level
+        ar, ac, av, *_ = s.view(sagb.OP_CA, lv - 1)
+        lr, lc, lvv, *_ = s.view(sagb.OP_LD, lv)
+        ur, uc, uv, *_ = s.view(sagb.OP_U, lv)
+        n = len(ar) - 1
+        Ad, Ld, Ud = _dense(ar, ac, av, n), _dense(lr, lc, lvv, n), _dense(ur, uc, uv, n)
+        Ld_off = Ld - np.diag(np.diag(Ld))
+        np.testing.assert_array_equal(Ld_off + Ud - np.diag(np.diag(Ud)), Ad - np.diag(np.diag(Ad)))
+    with pytest.raises(sagb.SagbError):
+        sagb.Setup(sagb.F64, r, c, v, sagb.amg_params(multicolor=1, coarse_colours=-1))
