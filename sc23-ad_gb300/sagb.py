@@ -667,14 +667,14 @@ class Batch:
     (rows beyond the cap act Jacobi-like within their colour) keeps the
     iteration count within about one iteration on the synthetic test
     families while the V-cycle has 6 colour steps per coarse level instead
-    of ~16.  They also coarsen down to 400 rows instead of the reference's
-    2000, so the dense coarsest LU is ~20x smaller (0.05 instead of 0.55 ms
-    per V-cycle at 128^3) for two or three more cheap levels, with the same
+    of ~16.  They also coarsen down to 100 rows instead of the reference's
+    2000, so the dense coarsest LU is ~25x faster (0.02 instead of 0.55 ms
+    per V-cycle at 128^3) for four more cheap levels, with the same
     iteration counts."""
 
     DEFAULT_MAX_COLOURS = 8     # the finest level: a proper colouring of 7- and 27-point stencils
     DEFAULT_COARSE_COLOURS = 2  # the levels below: fewer dependent colour steps (see the batched engine's notes)
-    DEFAULT_COARSE_SIZE = 400
+    DEFAULT_COARSE_SIZE = 100
 
     def __init__(self, ctx, systems, nrhs=1, params=None, threads=0):
         self.ctx = ctx

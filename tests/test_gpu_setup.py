@@ -88,7 +88,7 @@ def test_gpu_setup_matches_host(ctx, kind, n, prm, prec):
     xs, b = A.rhs(5)
     A.lmax1_scaling(b)
     r, c, v = A.arrays()
-    for params in (sagb.amg_params(), sagb.amg_params(multicolor=1, max_colours=8, coarse_size=400)):
+    for params in (sagb.amg_params(), sagb.amg_params(multicolor=1, max_colours=8, coarse_colours=2, coarse_size=100)):
         host = sagb.Setup(prec, r, c, v, params)
         gpu = sagb.Setup(prec, r, c, v, params, ctx=ctx)
         _views_equal(host, gpu)
