@@ -331,6 +331,11 @@ int sa_batch_sweep_form(sa_batch B, int level, int set, int *form);
  * set 1 / 0 chooses it (SA_ERR_ARG / an error if the operator has none), -1
  * reads it; results do not depend on it (the autotuner chooses per operator) */
 int sa_batch_compressed(sa_batch B, int level, int op, int set, int *on);
+/* the V-cycle's persistent coarse tail: set = t >= 1 runs levels t .. depth-1
+ * and the coarsest LU solves in one cooperative launch (a grid barrier between
+ * steps), 0 turns it off, -1 reads; *from = the tail's first level (0: none).
+ * The autotuner picks t by V-cycle time; results do not depend on it */
+int sa_batch_tail(sa_batch B, int set, int *from);
 /* Work/main.cpp:153-161 per system and right-hand side: max|M_f64 b| / ||b|| */
 int sa_batch_rule_ratios(sa_ctx ctx, sa_batch B, const double *b, const double *nrm_b, double *ratio);
 /* one operator of one batch level on interleaved vectors: op 0 A, 2 U, 3 P,

@@ -1259,6 +1259,14 @@ extern "C" int sa_batch_compressed(sa_batch B, int level, int op, int set, int *
     SA_GUARD_END
 }
 
+extern "C" int sa_batch_tail(sa_batch B, int set, int *from) {
+    if (!B || !from || set < -1 || set >= B->h->Dmax) return fail(SA_ERR_ARG, "invalid argument");
+    SA_GUARD_BEGIN
+    *from = B->eng->tail(set);
+    return SA_OK;
+    SA_GUARD_END
+}
+
 extern "C" int sa_batch_sweep_form(sa_batch B, int level, int set, int *form) {
     if (!B || !form || level < 0 || level >= B->h->Dmax || set < -1 || set > 3)
         return fail(SA_ERR_ARG, "invalid argument");

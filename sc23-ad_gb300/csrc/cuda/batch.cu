@@ -99,7 +99,8 @@ __device__ __forceinline__ void store_r(int *x, int row, const int (&v)[R]) {
 // sums wrap, so the grouping does not change any result.
 //   SUB = false: acc += a_ij x_j (x through the read-only cache)
 //   SUB = true:  acc -= a_ij x_j (x written by earlier launches or colours:
-//                plain loads, or L2 loads when CG)
+//                plain loads)
+//   CG:          x through L2 (written earlier in the same launch)
 //   D16:         columns from the 16-bit offsets cd (column = row + cd[j])
 template <int R, int G, bool SUB, bool CG, bool D16 = false>
 __device__ __forceinline__ void row_accumulate(const int *__restrict__ cind, const short *__restrict__ cd,
@@ -117,8 +118,8 @@ __device__ __forceinline__ void row_accumulate(const int *__restrict__ cind, con
         int xv[4][R];
 #pragma unroll
         for (int q = 0; q < 4; q++) {
-            if constexpr (!SUB) load_r<R>(x, cc[q], xv[q]);
-            else if constexpr (CG) load_cg_r<R>(x, cc[q], xv[q]);
+            if constexpr (CG) load_cg_r<R>(x, cc[q], xv[q]);
+            else if constexpr (!SUB) load_r<R>(x, cc[q], xv[q]);
             else load_rw<R>(x, cc[q], xv[q]);
         }
 #pragma unroll
@@ -133,8 +134,8 @@ __device__ __forceinline__ void row_accumulate(const int *__restrict__ cind, con
         const long long v = __ldg(val + j);
         const int col = D16 ? row + (int)__ldg(cd + j) : __ldg(cind + j);
         int xv[R];
-        if constexpr (!SUB) load_r<R>(x, col, xv);
-        else if constexpr (CG) load_cg_r<R>(x, col, xv);
+        if constexpr (CG) load_cg_r<R>(x, col, xv);
+        else if constexpr (!SUB) load_r<R>(x, col, xv);
         else load_rw<R>(x, col, xv);
 #pragma unroll
         for (int r = 0; r < R; r++) {
@@ -147,13 +148,19 @@ __device__ __forceinline__ void row_accumulate(const int *__restrict__ cind, con
 // ------------------------------------------------------------------ SpMV
 // y = A x (SET), y = z - A x (RESID) or y = A x + y (ADD), per row shift;
 // the same integer results as k_spmv_i32 for every right-hand side.
-template <int R, int MODE>
+template <int R, int MODE, bool CG = false>
 __device__ __forceinline__ void bspmv_finish(const DBCsr &A, int row, const long long (&acc)[R], int *y,
                                              const int *z, const int *row_sys, unsigned *pflag, unsigned *flags) {
     const int bit = A.bit[row];
     int out[R], zz[R], yy[R];
-    if (MODE == SPMV_RESID) load_r<R>(z, row, zz);
-    if (MODE == SPMV_ADD) load_rw<R>(y, row, yy);
+    if (MODE == SPMV_RESID) {
+        if constexpr (CG) load_cg_r<R>(z, row, zz);
+        else load_r<R>(z, row, zz);
+    }
+    if (MODE == SPMV_ADD) {
+        if constexpr (CG) load_cg_r<R>(y, row, yy);
+        else load_rw<R>(y, row, yy);
+    }
     bool any = false;
 #pragma unroll
     for (int r = 0; r < R; r++) {
@@ -373,7 +380,7 @@ struct PkPass {
     bool ok;
 };
 
-template <int R, int G, bool IN = true>
+template <int R, int G, bool IN = true, bool INCG = false>
 __device__ __forceinline__ void pk_fetch(const int4 *__restrict__ items, const int2 *__restrict__ ents,
                                          const int *__restrict__ in, int it, int ie, int lane, PkPass<R> &p) {
     p.ok = it < ie;
@@ -384,7 +391,10 @@ __device__ __forceinline__ void pk_fetch(const int4 *__restrict__ items, const i
         const int j = lane + u * G;
         p.e[u] = j < len ? __ldg(ents + p.hd.y + j) : make_int2(0, 0);
     }
-    if (IN && p.ok) load_r<R>(in, p.hd.x, p.iv);
+    if (IN && p.ok) {
+        if constexpr (INCG) load_cg_r<R>(in, p.hd.x, p.iv);
+        else load_r<R>(in, p.hd.x, p.iv);
+    }
 }
 
 // One row of a packed sweep: subtract the lower entries' products (the first
@@ -542,25 +552,23 @@ struct BLuDesc {
 // per system, R right-hand sides at once.  Same panel algorithm as the
 // single-system dense LU kernel: 32-row panels, warps reduce a panel row
 // against the solved part, warp 0 solves the diagonal block from registers.
-template <int R>
-__global__ void __launch_bounds__(kBLuThreads, 1)
-k_blu(const BLuDesc *__restrict__ desc, const int *__restrict__ Lcat, const int *__restrict__ Ucat,
-      const int *__restrict__ dcat, unsigned *__restrict__ pflag, unsigned *__restrict__ flags) {
-    pdl_trigger();
-    pdl_wait();
-    const BLuDesc d = desc[blockIdx.x];
+// The LU solves of one system by the NT threads of one CTA (the body of
+// k_blu; CG: the input was written earlier in the same launch).
+template <int R, int NT, bool CG>
+__device__ void blu_body(const BLuDesc &d, const int *__restrict__ Lcat, const int *__restrict__ Ucat,
+                         const int *__restrict__ dcat, unsigned *__restrict__ pflag, unsigned *__restrict__ flags,
+                         unsigned char *smem_raw) {
     const int n = d.n;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
     long long *t = (long long *)smem_raw;              // n * R accumulators
     int *x = (int *)(smem_raw + sizeof(long long) * (size_t)n * R);  // n * R values
     const int *L = Lcat + d.mat_off, *U = Ucat + d.mat_off, *dinv = dcat + d.d_off;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     unsigned ovf = 0;
-    for (int i = tid; i < n * R; i += kBLuThreads) t[i] = wshl((long long)d.in[i], d.bitL);
+    for (int i = tid; i < n * R; i += NT) t[i] = wshl((long long)(CG ? __ldcg(d.in + i) : d.in[i]), d.bitL);
     __syncthreads();
     for (int k0 = 0; k0 < n; k0 += 32) {
         const int kb = min(32, n - k0);
-        for (int pr = warp; k0 > 0 && pr < kb; pr += kBLuThreads / 32) {
+        for (int pr = warp; k0 > 0 && pr < kb; pr += NT / 32) {
             const int *row = L + (size_t)(k0 + pr) * n;
             long long acc[R];
 #pragma unroll
@@ -601,12 +609,12 @@ k_blu(const BLuDesc *__restrict__ desc, const int *__restrict__ Lcat, const int 
         }
         __syncthreads();
     }
-    for (int i = tid; i < n * R; i += kBLuThreads) t[i] = wshl((long long)x[i], d.bitU);
+    for (int i = tid; i < n * R; i += NT) t[i] = wshl((long long)x[i], d.bitU);
     __syncthreads();
     for (int k1 = n; k1 > 0; k1 -= 32) {
         const int kb = min(32, k1);
         const int k0 = k1 - kb;
-        for (int pr = warp; k1 < n && pr < kb; pr += kBLuThreads / 32) {
+        for (int pr = warp; k1 < n && pr < kb; pr += NT / 32) {
             const int *row = U + (size_t)(k0 + pr) * n;
             long long acc[R];
 #pragma unroll
@@ -652,13 +660,153 @@ k_blu(const BLuDesc *__restrict__ desc, const int *__restrict__ Lcat, const int 
         }
         __syncthreads();
     }
-    for (int i = tid; i < n * R; i += kBLuThreads) d.out[i] = x[i];
+    for (int i = tid; i < n * R; i += NT) d.out[i] = x[i];
     if (ovf) {
         for (int r = 0; r < R; r++)
             if (ovf & (1u << r)) atomicOr(pflag + (size_t)d.sys * R + r, ST_OVERFLOW);
         atomicOr(flags, ST_OVERFLOW);
     }
 }
+
+template <int R>
+__global__ void __launch_bounds__(kBLuThreads, 1)
+k_blu(const BLuDesc *__restrict__ desc, const int *__restrict__ Lcat, const int *__restrict__ Ucat,
+      const int *__restrict__ dcat, unsigned *__restrict__ pflag, unsigned *__restrict__ flags) {
+    pdl_trigger();
+    pdl_wait();
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    blu_body<R, kBLuThreads, false>(desc[blockIdx.x], Lcat, Ucat, dcat, pflag, flags, smem_raw);
+}
+
+// ------------------------------------------- persistent coarse tail of the V-cycle
+// The coarse levels t .. Dmax-1 and the coarsest LU in one cooperative launch:
+// every CTA is resident (one per SM), the steps (one colour of a sweep, one
+// SpMV, the LU solves) run one after the other over the whole grid with a
+// grid barrier between them, instead of one dependent launch each.  Each step
+// computes what its launch computes (the same row rules and overflow flags);
+// vectors written earlier in the launch are read through L2.  The barrier's
+// wait is bounded in time (ST_TIMEOUT in the main status word, then every CTA
+// returns).
+constexpr int kTailThreads = 512;
+enum TailKind : int { TK_COLOUR = 0, TK_RESID = 1, TK_SET = 2, TK_ADD = 3, TK_LU = 4 };
+struct TailStep {
+    int kind, G, ib, ie;  // colour: items ib..ie-1 of the packed LD; SpMV: all rows of M
+    DBCsr M;
+    const int4 *items;
+    const int2 *ents;
+    const int *x;  // SpMV input; colour: unused
+    int *y;        // SpMV output; colour: the vector being swept
+    const int *z;  // SpMV residual minuend; colour: the sweep's input
+    const int *row_sys;
+};
+
+template <int R, int G>
+__device__ __forceinline__ void tail_colour(const TailStep &st, unsigned *pflag, unsigned *flags) {
+    const long long tid = (long long)blockIdx.x * kTailThreads + threadIdx.x;
+    const long long slots = (long long)gridDim.x * kTailThreads / G;
+    const int lane = (int)(tid % G);
+    for (long long base = st.ib; base < st.ie; base += slots) {
+        const long long it = base + tid / G;
+        PkPass<R> cur;
+        pk_fetch<R, G, true, true>(st.items, st.ents, st.z, it < st.ie ? (int)it : st.ie, st.ie, lane, cur);
+        pk_row<R, G, true>(cur, st.ents, st.y, lane, st.row_sys, pflag, flags);
+    }
+}
+
+template <int R, int G, int MODE>
+__device__ __forceinline__ void tail_spmv(const TailStep &st, unsigned *pflag, unsigned *flags) {
+    const DBCsr &A = st.M;
+    const long long tid = (long long)blockIdx.x * kTailThreads + threadIdx.x;
+    const long long rows = (long long)gridDim.x * kTailThreads / G;
+    const int lane = (int)(tid % G);
+    for (long long base = 0; base < A.n; base += rows) {
+        const long long r = base + tid / G;
+        const int row = r < A.n ? (int)r : -1;
+        long long acc[R];
+#pragma unroll
+        for (int q = 0; q < R; q++) acc[q] = 0;
+        if (row >= 0)
+            row_accumulate<R, G, false, true>(A.cind, nullptr, A.val, __ldg(A.rptr + row), __ldg(A.rptr + row + 1),
+                                              lane, row, st.x, acc);
+#pragma unroll
+        for (int q = 0; q < R; q++)
+#pragma unroll
+            for (int o = G / 2; o > 0; o >>= 1) acc[q] = wadd(acc[q], shfl_xor(acc[q], o));
+        if (lane == 0 && row >= 0) bspmv_finish<R, MODE, true>(A, row, acc, st.y, st.z, st.row_sys, pflag, flags);
+    }
+}
+
+// all CTAs of the grid; false when the bounded wait ran out (or ran out before)
+__device__ __forceinline__ bool tail_barrier(unsigned *bar, unsigned *status) {
+    __shared__ int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned *gen = bar + 1;
+        const unsigned g = *gen;
+        __threadfence();
+        int ok = 1;
+        if (atomicAdd(bar, 1u) == gridDim.x - 1) {
+            atomicExch(bar, 0u);
+            __threadfence();
+            atomicAdd(bar + 1, 1u);
+        } else {
+            const unsigned long long t0 = globaltimer_ns();
+            while (*gen == g) {
+                if (*(volatile unsigned *)status & ST_TIMEOUT) {  // another CTA already gave up
+                    ok = 0;
+                    break;
+                }
+                if (globaltimer_ns() - t0 > kSpinLimitNs) {
+                    atomicOr(status, ST_TIMEOUT);
+                    ok = 0;
+                    break;
+                }
+            }
+        }
+        __threadfence();
+        if (*(volatile unsigned *)status & ST_TIMEOUT) ok = 0;
+        s_ok = ok;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+template <int R>
+__global__ void __launch_bounds__(kTailThreads, 1)
+k_btail(const TailStep *__restrict__ steps, int nsteps, const BLuDesc *__restrict__ lu, int nlu,
+        const int *__restrict__ Lcat, const int *__restrict__ Ucat, const int *__restrict__ dcat, unsigned *bar,
+        unsigned *__restrict__ pflag, unsigned *__restrict__ flags, unsigned *__restrict__ status) {
+    pdl_trigger();
+    pdl_wait();
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    for (int k = 0; k < nsteps; k++) {
+        const TailStep st = steps[k];
+        if (st.kind == TK_LU) {
+            for (int sys = blockIdx.x; sys < nlu; sys += gridDim.x)
+                blu_body<R, kTailThreads, true>(lu[sys], Lcat, Ucat, dcat, pflag, flags, smem_raw);
+        } else {
+            switch (st.G) {
+#define SAGB_TAIL_G(GV)                                                                      \
+    case GV:                                                                                 \
+        if (st.kind == TK_COLOUR) tail_colour<R, GV>(st, pflag, flags);                     \
+        else if (st.kind == TK_RESID) tail_spmv<R, GV, SPMV_RESID>(st, pflag, flags);       \
+        else if (st.kind == TK_SET) tail_spmv<R, GV, SPMV_SET>(st, pflag, flags);           \
+        else tail_spmv<R, GV, SPMV_ADD>(st, pflag, flags);                                  \
+        break;
+                SAGB_TAIL_G(1)
+                SAGB_TAIL_G(2)
+                SAGB_TAIL_G(4)
+                SAGB_TAIL_G(8)
+                SAGB_TAIL_G(16)
+                default:
+                SAGB_TAIL_G(32)
+#undef SAGB_TAIL_G
+            }
+        }
+        if (!tail_barrier(bar, status)) return;
+    }
+}
+
 
 // The same LU solves spread over a thread-block cluster (kLuCtas CTAs, one
 // system per cluster).  Panel p of 32 rows belongs to CTA p % kLuCtas, which
@@ -1384,6 +1532,13 @@ struct BatchEngine::Impl {
     // V-cycle's A: its tiles and reductions favour other lanes per row)
     int dot_group = -1;  // -1: the level-0 A's lanes per row
     bool dot_d16 = false;
+    // persistent coarse tail (k_btail): levels tail_from .. Dmax-1 and the LU in
+    // one cooperative launch (0: off)
+    int tail_from = 0;
+    TailStep *d_steps = nullptr;
+    int nsteps = 0;
+    unsigned *tail_bar = nullptr;  // grid barrier: arrivals, generation
+    int tail_grid = 0;
     // the stand-alone V-cycle (precondition) replayed from a graph captured for one in/out pair
     cudaGraphExec_t vc_graph = nullptr;
     const int *vc_in = nullptr;
@@ -1509,6 +1664,9 @@ struct BatchEngine::Impl {
             SAGB_CUDA(cudaFuncSetAttribute(k_blu_cluster<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
             SAGB_CUDA(cudaFuncSetAttribute(k_blu_cluster<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
             SAGB_CUDA(cudaFuncSetAttribute(k_blu_cluster<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
+            SAGB_CUDA(cudaFuncSetAttribute(k_btail<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
+            SAGB_CUDA(cudaFuncSetAttribute(k_btail<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
+            SAGB_CUDA(cudaFuncSetAttribute(k_btail<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
             attr = true;
         }
     }
@@ -1747,6 +1905,7 @@ struct BatchEngine::Impl {
         for (auto p : rr) dfree(p);
         for (auto p : tmp) dfree(p);
         dfree(d_lu); dfree(Lcat); dfree(Ucat); dfree(dcat);
+        dfree(d_steps); dfree(tail_bar);
         Af.release();
         dfree(tiles); dfree(stiles); dfree(tile_ptr); dfree(pflag); dfree(rvec); dfree(nrm); dfree(e0); dfree(npart);
         dfree(pairs); dfree(info_d);
@@ -1917,6 +2076,107 @@ struct BatchEngine::Impl {
         });
     }
 
+    // the steps of levels t .. Dmax-1 and the LU, in the order vcycle_body runs
+    // them; false when a level lacks the colour-ordered packed LD
+    bool build_tail(int t) {
+        if (t < 1 || t >= Dmax) return false;
+        for (int l = t; l < Dmax; l++)
+            if (!lv[l].cp_items) return false;
+        std::vector<TailStep> st;
+        auto colours = [&](int l, const int *in, int *out) {
+            const DevBLevel &L = lv[l];
+            for (size_t k = 0; k + 1 < L.colour_ptr.size(); k++) {
+                if (L.colour_ptr[k + 1] == L.colour_ptr[k]) continue;
+                TailStep q{};
+                q.kind = TK_COLOUR;
+                q.G = std::max(1, L.LD.group);
+                q.ib = L.colour_ptr[k];
+                q.ie = L.colour_ptr[k + 1];
+                q.items = L.cp_items;
+                q.ents = L.cp_ents;
+                q.z = in;
+                q.y = out;
+                q.row_sys = L.row_sys;
+                st.push_back(q);
+            }
+        };
+        auto spmv = [&](const DevBMat &M, const int *x, int *y, int kind, const int *z, const int *row_sys) {
+            if (M.d.n == 0) return;
+            TailStep q{};
+            q.kind = kind;
+            q.G = std::max(1, M.group);
+            q.M = M.d;
+            q.x = x;
+            q.y = y;
+            q.z = z;
+            q.row_sys = row_sys;
+            st.push_back(q);
+        };
+        for (int l = t; l < Dmax; l++) {
+            colours(l, ee[l], xx[l]);
+            for (int k = 1; k < smooth_iter; k++) {
+                spmv(lv[l].U, xx[l], tmp[l], TK_RESID, ee[l], lv[l].row_sys);
+                colours(l, tmp[l], xx[l]);
+            }
+            spmv(lv[l].A, xx[l], rr[l], TK_RESID, ee[l], lv[l].row_sys);
+            spmv(lv[l].R, rr[l], ee[l + 1], TK_SET, nullptr, lv[l].row_sys_next);
+        }
+        if (nlu) {
+            TailStep q{};
+            q.kind = TK_LU;
+            st.push_back(q);
+        }
+        for (int l = Dmax - 1; l >= t; l--) {
+            spmv(lv[l].P, xx[l + 1], xx[l], TK_ADD, nullptr, lv[l].row_sys);
+            for (int k = 0; k < smooth_iter; k++) {
+                spmv(lv[l].U, xx[l], tmp[l], TK_RESID, ee[l], lv[l].row_sys);
+                colours(l, tmp[l], xx[l]);
+            }
+        }
+        int per_sm = 0;
+        by_r([&](auto RR) {
+            constexpr int R = decltype(RR)::value;
+            SAGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_btail<R>, kTailThreads, lu_smem));
+        });
+        if (per_sm < 1) return false;
+        dfree(d_steps);
+        d_steps = dupload(st);
+        nsteps = (int)st.size();
+        tail_grid = c.num_sms;  // one CTA per SM, all resident (cooperative launch)
+        if (!tail_bar) {
+            tail_bar = (unsigned *)dmalloc(sizeof(unsigned) * 2);
+            SAGB_CUDA(cudaMemset(tail_bar, 0, sizeof(unsigned) * 2));
+        }
+        tail_from = t;
+        clear_graphs();
+        return true;
+    }
+
+    void drop_tail() {
+        tail_from = 0;
+        clear_graphs();
+    }
+
+    void launch_tail() {
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(tail_grid);
+        cfg.blockDim = dim3(kTailThreads);
+        cfg.dynamicSmemBytes = lu_smem;
+        cfg.stream = c.stream;
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeCooperative;
+        at[0].val.cooperative = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        by_r([&](auto RR) {
+            constexpr int R = decltype(RR)::value;
+            SAGB_CUDA(cudaLaunchKernelEx(&cfg, k_btail<R>, (const TailStep *)d_steps, nsteps, (const BLuDesc *)d_lu,
+                                         nlu, (const int *)Lcat, (const int *)Ucat, (const int *)dcat, tail_bar,
+                                         cur_pflag, c.d_flags, c.d_flags_main));
+        });
+        c.launches++;
+    }
+
     // intAMGflex::Precondition (INTAMG.hpp:269-293) for the whole batch; int32
     // wraps inside it go to the preconditioner's status arrays (FGMRES is
     // flexible, so they cost convergence speed, not correctness)
@@ -1928,15 +2188,17 @@ struct BatchEngine::Impl {
     }
 
     void vcycle_body(const int *in, int *out) {
-        for (int l = 0; l < Dmax; l++) {
+        const int t = tail_from > 0 && d_steps ? tail_from : Dmax;
+        for (int l = 0; l < t; l++) {
             const int *e_l = l == 0 ? in : ee[l];
             int *x_l = l == 0 ? out : xx[l];
             smooth(l, e_l, x_l, false);
             bspmv(lv[l].A, x_l, rr[l], SPMV_RESID, e_l, lv[l].row_sys);
             bspmv(lv[l].R, rr[l], ee[l + 1], SPMV_SET, nullptr, lv[l].row_sys_next);
         }
-        lu(cur_pflag);
-        for (int l = Dmax - 1; l >= 0; l--) {
+        if (t < Dmax) launch_tail();
+        else lu(cur_pflag);
+        for (int l = t - 1; l >= 0; l--) {
             const int *e_l = l == 0 ? in : ee[l];
             int *x_l = l == 0 ? out : xx[l];
             bspmv(lv[l].P, xx[l + 1], x_l, SPMV_ADD, nullptr, lv[l].row_sys);
@@ -2165,6 +2427,14 @@ struct BatchEngine::Impl {
             for (unsigned f : pp)
                 if (f & ST_OVERFLOW) st.flags |= ST_PREC_OVF;
         }
+        if (tail_from > 0) {
+            unsigned mainf = 0;
+            SAGB_CUDA(cudaMemcpy(&mainf, c.d_flags_main, sizeof(unsigned), cudaMemcpyDeviceToHost));
+            if (mainf & ST_TIMEOUT) {
+                SAGB_CUDA(cudaMemset(tail_bar, 0, sizeof(unsigned) * 2));
+                throw CudaError{"the V-cycle's persistent coarse tail timed out at a grid barrier"};
+            }
+        }
         // the last cycle's update has not been checked yet
         residual(b, x);
         SAGB_CUDA(cudaMemcpyAsync(hn.data(), nrm, sizeof(double) * P, cudaMemcpyDeviceToHost, c.stream));
@@ -2221,6 +2491,12 @@ int BatchEngine::compressed(int level, int op, int set) {
         impl_->clear_graphs();
     }
     return M.d16 && M.cdv ? 1 : 0;
+}
+int BatchEngine::tail(int set) {
+    Impl &I = *impl_;
+    if (set == 0) I.drop_tail();
+    else if (set > 0 && !I.build_tail(set)) throw CudaError{"no persistent tail from this level"};
+    return I.tail_from;
 }
 int BatchEngine::group(int level, int op) const {
     const DevBLevel &L = impl_->lv[level];
@@ -2350,6 +2626,27 @@ void BatchEngine::autotune(int reps) {
             M->group = bestg;
             M->d16 = bestd;
         }
+    }
+    {
+        // the persistent coarse tail: from which level on (or none), by V-cycle time
+        I.drop_tail();
+        float best = timeit([&] { I.vcycle(xa, xb); });
+        int bestt = 0;
+        try {
+            for (int t = I.Dmax - 1; t >= 1; t--) {
+                if (!I.build_tail(t)) break;
+                const float ms = timeit([&] { I.vcycle(xa, xb); });
+                if (ms < best) {
+                    best = ms;
+                    bestt = t;
+                }
+            }
+        } catch (const CudaError &) {
+            bestt = 0;  // the cooperative launch is not available here: no tail
+            cudaGetLastError();
+        }
+        if (bestt > 0) I.build_tail(bestt);
+        else I.drop_tail();
     }
     {
         // the Arnoldi SpMV + first dot, on its own (acc for one column, m = 1)

@@ -135,6 +135,7 @@ SIGNATURES = {
     "sa_batch_set_group": (C.c_int, [VP, C.c_int, C.c_int, C.c_int]),
     "sa_batch_sweep_form": (C.c_int, [VP, C.c_int, C.c_int, C.POINTER(C.c_int)]),
     "sa_batch_compressed": (C.c_int, [VP, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int)]),
+    "sa_batch_tail": (C.c_int, [VP, C.c_int, C.POINTER(C.c_int)]),
     "sa_batch_time_op": (C.c_int, [VP, VP, C.c_int, C.c_int, VP, VP, C.c_int, C.POINTER(C.c_float)]),
     "sa_batch_rule_ratios": (C.c_int, [VP, VP, VP, VP, F64P]),
     "sa_batch_solve": (C.c_int, [VP, VP, C.POINTER(SolverParams), I32P, VP, VP, VP, I32P, I32P, I32P]),
@@ -752,6 +753,14 @@ class Batch:
         0 chooses them."""
         f = C.c_int()
         check(lib().sa_batch_compressed(self.h, level, op, set, C.byref(f)))
+        return f.value
+
+    def tail(self, set=-1):
+        """The V-cycle's persistent coarse tail: set t >= 1 runs levels t ..
+        depth-1 and the coarsest LU in one cooperative launch, 0 turns it off;
+        returns the tail's first level (0: none)."""
+        f = C.c_int()
+        check(lib().sa_batch_tail(self.h, set, C.byref(f)))
         return f.value
 
     def sweep_form(self, level, set=-1):

@@ -93,6 +93,11 @@ def test_batched_vcycle_bit_exact(ctx, nrhs):
                     continue
                 B.set_group(lv, 1, g)
             np.testing.assert_array_equal(B.precondition(vin).reshape(B.rows, nrhs), out, err_msg=f"form {form} G {g}")
+    # nor does the persistent coarse tail (levels t .. depth-1 and the LU in one cooperative launch)
+    for t in range(1, B.depth):
+        assert B.tail(t) == t
+        np.testing.assert_array_equal(B.precondition(vin).reshape(B.rows, nrhs), out, err_msg=f"tail from {t}")
+    B.tail(0)
     # nor does the compressed column storage of A and U (16-bit offsets), on or off at every level
     for on in (1, 0):
         n_on = 0
@@ -233,6 +238,13 @@ def test_launch_options_do_not_change_results(ctx):
         return out, x, it
 
     ref = run()
+    # a solve whose V-cycles run their coarse levels in the persistent tail
+    for t in (1, B.depth - 1):
+        B.tail(t)
+        got = run()
+        for k in range(3):
+            np.testing.assert_array_equal(got[k], ref[k], err_msg=f"tail from {t}")
+    B.tail(0)
     # the Arnoldi SpMV and the V-cycle with compressed columns wherever they fit
     for lv in range(B.depth):
         for op in (0, 2):
