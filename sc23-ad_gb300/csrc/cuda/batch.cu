@@ -688,6 +688,7 @@ k_blu(const BLuDesc *__restrict__ desc, const int *__restrict__ Lcat, const int 
 // wait is bounded in time (ST_TIMEOUT in the main status word, then every CTA
 // returns).
 constexpr int kTailThreads = 512;
+constexpr int kTailSmem = 200 * 1024;  // the LU's shared memory; the kernel's own few bytes come on top
 enum TailKind : int { TK_COLOUR = 0, TK_RESID = 1, TK_SET = 2, TK_ADD = 3, TK_LU = 4 };
 struct TailStep {
     int kind, G, ib, ie;  // colour: items ib..ie-1 of the packed LD; SpMV: all rows of M
@@ -736,35 +737,30 @@ __device__ __forceinline__ void tail_spmv(const TailStep &st, unsigned *pflag, u
     }
 }
 
-// all CTAs of the grid; false when the bounded wait ran out (or ran out before)
-__device__ __forceinline__ bool tail_barrier(unsigned *bar, unsigned *status) {
+// Grid barrier k of a launch: every CTA adds one to the arrival counter (set
+// to 0 before the launch) and waits until it reaches (k + 1) * gridDim.x;
+// false when the bounded wait ran out (or another CTA's did)
+__device__ __forceinline__ bool tail_barrier(unsigned *bar, unsigned k, unsigned *status) {
     __shared__ int s_ok;
     __syncthreads();
     if (threadIdx.x == 0) {
-        volatile unsigned *gen = bar + 1;
-        const unsigned g = *gen;
         __threadfence();
+        atomicAdd(bar, 1u);
+        const unsigned target = (k + 1) * gridDim.x;
         int ok = 1;
-        if (atomicAdd(bar, 1u) == gridDim.x - 1) {
-            atomicExch(bar, 0u);
-            __threadfence();
-            atomicAdd(bar + 1, 1u);
-        } else {
-            const unsigned long long t0 = globaltimer_ns();
-            while (*gen == g) {
-                if (*(volatile unsigned *)status & ST_TIMEOUT) {  // another CTA already gave up
-                    ok = 0;
-                    break;
-                }
-                if (globaltimer_ns() - t0 > kSpinLimitNs) {
-                    atomicOr(status, ST_TIMEOUT);
-                    ok = 0;
-                    break;
-                }
+        const unsigned long long t0 = globaltimer_ns();
+        while (*(volatile unsigned *)bar < target) {
+            if (*(volatile unsigned *)status & ST_TIMEOUT) {
+                ok = 0;
+                break;
+            }
+            if (globaltimer_ns() - t0 > kSpinLimitNs) {
+                atomicOr(status, ST_TIMEOUT);
+                ok = 0;
+                break;
             }
         }
         __threadfence();
-        if (*(volatile unsigned *)status & ST_TIMEOUT) ok = 0;
         s_ok = ok;
     }
     __syncthreads();
@@ -803,7 +799,7 @@ k_btail(const TailStep *__restrict__ steps, int nsteps, const BLuDesc *__restric
 #undef SAGB_TAIL_G
             }
         }
-        if (!tail_barrier(bar, status)) return;
+        if (!tail_barrier(bar, (unsigned)k, status)) return;
     }
 }
 
@@ -1537,8 +1533,8 @@ struct BatchEngine::Impl {
     int tail_from = 0;
     TailStep *d_steps = nullptr;
     int nsteps = 0;
-    unsigned *tail_bar = nullptr;  // grid barrier: arrivals, generation
-    int tail_grid = 0;
+    unsigned *tail_bar = nullptr;  // grid barrier: arrivals (reset before each launch)
+    int tail_grid = 0;             // CTAs of the tail (at most one per SM)
     // the stand-alone V-cycle (precondition) replayed from a graph captured for one in/out pair
     cudaGraphExec_t vc_graph = nullptr;
     const int *vc_in = nullptr;
@@ -1664,9 +1660,9 @@ struct BatchEngine::Impl {
             SAGB_CUDA(cudaFuncSetAttribute(k_blu_cluster<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
             SAGB_CUDA(cudaFuncSetAttribute(k_blu_cluster<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
             SAGB_CUDA(cudaFuncSetAttribute(k_blu_cluster<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
-            SAGB_CUDA(cudaFuncSetAttribute(k_btail<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
-            SAGB_CUDA(cudaFuncSetAttribute(k_btail<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
-            SAGB_CUDA(cudaFuncSetAttribute(k_btail<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
+            SAGB_CUDA(cudaFuncSetAttribute(k_btail<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTailSmem));
+            SAGB_CUDA(cudaFuncSetAttribute(k_btail<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTailSmem));
+            SAGB_CUDA(cudaFuncSetAttribute(k_btail<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTailSmem));
             attr = true;
         }
     }
@@ -2078,8 +2074,8 @@ struct BatchEngine::Impl {
 
     // the steps of levels t .. Dmax-1 and the LU, in the order vcycle_body runs
     // them; false when a level lacks the colour-ordered packed LD
-    bool build_tail(int t) {
-        if (t < 1 || t >= Dmax) return false;
+    bool build_tail(int t, int grid = 0) {
+        if (t < 1 || t >= Dmax || lu_smem > (size_t)kTailSmem) return false;
         for (int l = t; l < Dmax; l++)
             if (!lv[l].cp_items) return false;
         std::vector<TailStep> st;
@@ -2142,11 +2138,10 @@ struct BatchEngine::Impl {
         dfree(d_steps);
         d_steps = dupload(st);
         nsteps = (int)st.size();
-        tail_grid = c.num_sms;  // one CTA per SM, all resident (cooperative launch)
-        if (!tail_bar) {
-            tail_bar = (unsigned *)dmalloc(sizeof(unsigned) * 2);
-            SAGB_CUDA(cudaMemset(tail_bar, 0, sizeof(unsigned) * 2));
-        }
+        // at most one CTA per SM, all resident (cooperative launch); fewer CTAs
+        // make the barrier cheaper where the coarse levels have little work
+        tail_grid = grid > 0 ? std::min(grid, c.num_sms) : c.num_sms;
+        if (!tail_bar) tail_bar = (unsigned *)dmalloc(sizeof(unsigned) * 2);
         tail_from = t;
         clear_graphs();
         return true;
@@ -2158,6 +2153,7 @@ struct BatchEngine::Impl {
     }
 
     void launch_tail() {
+        SAGB_CUDA(cudaMemsetAsync(tail_bar, 0, sizeof(unsigned), c.stream));
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3(tail_grid);
         cfg.blockDim = dim3(kTailThreads);
@@ -2430,10 +2426,7 @@ struct BatchEngine::Impl {
         if (tail_from > 0) {
             unsigned mainf = 0;
             SAGB_CUDA(cudaMemcpy(&mainf, c.d_flags_main, sizeof(unsigned), cudaMemcpyDeviceToHost));
-            if (mainf & ST_TIMEOUT) {
-                SAGB_CUDA(cudaMemset(tail_bar, 0, sizeof(unsigned) * 2));
-                throw CudaError{"the V-cycle's persistent coarse tail timed out at a grid barrier"};
-            }
+            if (mainf & ST_TIMEOUT) throw CudaError{"the V-cycle's persistent coarse tail timed out at a grid barrier"};
         }
         // the last cycle's update has not been checked yet
         residual(b, x);
@@ -2492,10 +2485,10 @@ int BatchEngine::compressed(int level, int op, int set) {
     }
     return M.d16 && M.cdv ? 1 : 0;
 }
-int BatchEngine::tail(int set) {
+int BatchEngine::tail(int set, int grid) {
     Impl &I = *impl_;
     if (set == 0) I.drop_tail();
-    else if (set > 0 && !I.build_tail(set)) throw CudaError{"no persistent tail from this level"};
+    else if (set > 0 && !I.build_tail(set, grid)) throw CudaError{"no persistent tail from this level"};
     return I.tail_from;
 }
 int BatchEngine::group(int level, int op) const {
@@ -2631,21 +2624,27 @@ void BatchEngine::autotune(int reps) {
         // the persistent coarse tail: from which level on (or none), by V-cycle time
         I.drop_tail();
         float best = timeit([&] { I.vcycle(xa, xb); });
-        int bestt = 0;
+        int bestt = 0, bestg = 0;
         try {
             for (int t = I.Dmax - 1; t >= 1; t--) {
-                if (!I.build_tail(t)) break;
-                const float ms = timeit([&] { I.vcycle(xa, xb); });
-                if (ms < best) {
-                    best = ms;
-                    bestt = t;
+                bool any = false;
+                for (int g : {16, 32, 64, 0}) {
+                    if (!I.build_tail(t, g)) break;
+                    any = true;
+                    const float ms = timeit([&] { I.vcycle(xa, xb); });
+                    if (ms < best) {
+                        best = ms;
+                        bestt = t;
+                        bestg = g;
+                    }
                 }
+                if (!any) break;
             }
         } catch (const CudaError &) {
             bestt = 0;  // the cooperative launch is not available here: no tail
             cudaGetLastError();
         }
-        if (bestt > 0) I.build_tail(bestt);
+        if (bestt > 0) I.build_tail(bestt, bestg);
         else I.drop_tail();
     }
     {

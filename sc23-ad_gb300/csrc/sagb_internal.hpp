@@ -256,8 +256,8 @@ class BatchEngine {
     int compressed(int level, int op, int set);
     // the V-cycle's persistent coarse tail: set t >= 1 runs levels t .. Dmax-1
     // and the coarsest LU in one cooperative launch, 0 turns it off, -1 reads;
-    // returns the first level of the tail (0: none)
-    int tail(int set);
+    // returns the first level of the tail (0: none); grid > 0: that many CTAs
+    int tail(int set, int grid = 0);
     // one operator of one level on caller vectors (op 1: the colour sweep LD^-1 in)
     void level_op(int level, int op, const int *in, int *out);
     void coarse_solve();  // the batched LU on the engine's own level vectors
