@@ -7,7 +7,7 @@ Dirichlet), b = A x* with x* ~ U[-1, 1] (splitmix64 seed), LMax1 row scaling,
 x0 = 0, m = 30, eps = 1e-10 on the explicit residual, one right-hand side.  A
 step is one full solve (Restarted + FGMRESflex + V-cycles) by the batched
 engine: multicolour SOR (8 colours on the finest level, 2 on the coarser
-ones), a 100-row coarsest level, autotuned launch shapes, graph-captured
+ones), a 400-row coarsest level, autotuned launch shapes, graph-captured
 Arnoldi steps chained by programmatic dependent launch, and the F chosen by the
 trained selector with the reference's rule (Work/main.cpp:153-161) as default
 and fallback.  Beside it, on the same GPU: the plain drop-in (the reference's
@@ -284,7 +284,7 @@ def run_ours(a, dist):
 
 def setup_row(ctx, r, c, v):
     """The AMG setup of the same system (the headline's parameters: multicolour
-    smoother, 8 colours on the finest level and 2 below, 100-row coarsest
+    smoother, 8 colours on the finest level and 2 below, 400-row coarsest
     level) on the host and with the
     Ruge-Stueben levels on the GPU; the two hierarchies are compared array by
     array (they must be identical)."""

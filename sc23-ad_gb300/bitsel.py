@@ -224,7 +224,7 @@ def load(ctx, path=WEIGHTS):
 # the selector leaves the rule's F only when the network predicts at least this
 # much (log2 iterations) fewer iterations: on the held-out sweeps this keeps the
 # rule where it is already near best and still removes its failures
-MARGIN = 0.5
+MARGIN = 1.0
 
 
 class Selector:

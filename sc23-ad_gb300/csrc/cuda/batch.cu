@@ -2626,19 +2626,25 @@ void BatchEngine::autotune(int reps) {
         float best = timeit([&] { I.vcycle(xa, xb); });
         int bestt = 0, bestg = 0;
         try {
+            // from the coarsest level up; stop once a start level is no better
+            // than the one below it (the tail only pays where levels are tiny)
+            float prev = best;
             for (int t = I.Dmax - 1; t >= 1; t--) {
                 bool any = false;
-                for (int g : {16, 32, 64, 0}) {
+                float here = 1e30f;
+                for (int g : {32, 0}) {
                     if (!I.build_tail(t, g)) break;
                     any = true;
                     const float ms = timeit([&] { I.vcycle(xa, xb); });
+                    here = std::min(here, ms);
                     if (ms < best) {
                         best = ms;
                         bestt = t;
                         bestg = g;
                     }
                 }
-                if (!any) break;
+                if (!any || here >= prev) break;
+                prev = here;
             }
         } catch (const CudaError &) {
             bestt = 0;  // the cooperative launch is not available here: no tail

@@ -668,14 +668,16 @@ class Batch:
     (rows beyond the cap act Jacobi-like within their colour) keeps the
     iteration count within about one iteration on the synthetic test
     families while the V-cycle has 6 colour steps per coarse level instead
-    of ~16.  They also coarsen down to 100 rows instead of the reference's
-    2000, so the dense coarsest LU is ~25x faster (0.02 instead of 0.55 ms
-    per V-cycle at 128^3) for four more cheap levels, with the same
-    iteration counts."""
+    of ~16.  They also coarsen down to 400 rows instead of the reference's
+    2000, so the dense coarsest LU is ~11x faster (0.05 instead of 0.55 ms
+    per V-cycle at 128^3) for two or three more cheap levels, with the same
+    iteration counts.  (100 rows is ~5 % faster still, but the bit
+    selector's features describe the hierarchy, and its network was trained
+    on 400-row hierarchies.)"""
 
     DEFAULT_MAX_COLOURS = 8     # the finest level: a proper colouring of 7- and 27-point stencils
     DEFAULT_COARSE_COLOURS = 2  # the levels below: fewer dependent colour steps (see the batched engine's notes)
-    DEFAULT_COARSE_SIZE = 100
+    DEFAULT_COARSE_SIZE = 400
 
     def __init__(self, ctx, systems, nrhs=1, params=None, threads=0):
         self.ctx = ctx

@@ -6,6 +6,7 @@ features are host computations over the integer setup."""
 import numpy as np
 import pytest
 
+import bitsel
 import mlp_oracle as mo
 import sagb
 
@@ -109,7 +110,7 @@ def test_trained_selector_gains_on_heldout_sweeps():
     for k, y in enumerate(Y):
         sw = {q["bit"]: q for q in meta[ntr + k]["sweep"]}
         f = f_lo + int(np.argmin(y))
-        if y[meta[ntr + k]["rule"] - f_lo] - y[f - f_lo] < 0.5:  # the selector's margin
+        if y[meta[ntr + k]["rule"] - f_lo] - y[f - f_lo] < bitsel.MARGIN:  # the selector's margin
             f = meta[ntr + k]["rule"]
         rule = sw[meta[ntr + k]["rule"]]
         r_it = rule["iters"] if rule["converged"] else 120
