@@ -336,6 +336,12 @@ int sa_batch_compressed(sa_batch B, int level, int op, int set, int *on);
  * steps), 0 turns it off, -1 reads; *from = the tail's first level (0: none).
  * The autotuner picks t by V-cycle time; results do not depend on it */
 int sa_batch_tail(sa_batch B, int set, int *from);
+/* failure detection of the tail's grid barrier: one tail launch from `level`
+ * whose first barrier waits for one CTA more than the grid has, so its wait
+ * (bounded by timeout_ms, at most 2000) runs out; *status = the bits raised
+ * (SA_FLAG_TIMEOUT expected).  The context stays usable; the batch's status
+ * words and tail setting are restored */
+int sa_batch_tail_selftest(sa_ctx ctx, sa_batch B, int level, double timeout_ms, unsigned *status);
 /* Work/main.cpp:153-161 per system and right-hand side: max|M_f64 b| / ||b|| */
 int sa_batch_rule_ratios(sa_ctx ctx, sa_batch B, const double *b, const double *nrm_b, double *ratio);
 /* one operator of one batch level on interleaved vectors: op 0 A, 2 U, 3 P,

@@ -1267,6 +1267,15 @@ extern "C" int sa_batch_tail(sa_batch B, int set, int *from) {
     SA_GUARD_END
 }
 
+extern "C" int sa_batch_tail_selftest(sa_ctx ctx, sa_batch B, int level, double timeout_ms, unsigned *status) {
+    if (!ctx || !B || !status || level < 1 || level >= B->h->Dmax || !(timeout_ms > 0) || timeout_ms > 2000)
+        return fail(SA_ERR_ARG, "invalid argument");
+    SA_GUARD_BEGIN
+    *status = B->eng->tail_selftest(level, timeout_ms);
+    return SA_OK;
+    SA_GUARD_END
+}
+
 extern "C" int sa_batch_sweep_form(sa_batch B, int level, int set, int *form) {
     if (!B || !form || level < 0 || level >= B->h->Dmax || set < -1 || set > 3)
         return fail(SA_ERR_ARG, "invalid argument");

@@ -737,24 +737,29 @@ __device__ __forceinline__ void tail_spmv(const TailStep &st, unsigned *pflag, u
     }
 }
 
-// Grid barrier k of a launch: every CTA adds one to the arrival counter (set
-// to 0 before the launch) and waits until it reaches (k + 1) * gridDim.x;
-// false when the bounded wait ran out (or another CTA's did)
-__device__ __forceinline__ bool tail_barrier(unsigned *bar, unsigned k, unsigned *status) {
+// Grid barrier k of a launch: every CTA adds one to the arrival counter
+// bar[0] and waits until it reaches (k + 1) * (gridDim.x + extra) (extra = 0;
+// the self-test's 1 makes the wait run out).  The wait is bounded by limit_ns;
+// when it runs out the CTA marks bar[1] (both words are zeroed before each
+// launch) and the caller's status word, and every CTA that sees bar[1] set
+// stops waiting.  Returns false then.
+__device__ __forceinline__ bool tail_barrier(unsigned *bar, unsigned k, unsigned *status, unsigned extra,
+                                             unsigned long long limit_ns) {
     __shared__ int s_ok;
     __syncthreads();
     if (threadIdx.x == 0) {
         __threadfence();
         atomicAdd(bar, 1u);
-        const unsigned target = (k + 1) * gridDim.x;
+        const unsigned target = (k + 1) * (gridDim.x + extra);
         int ok = 1;
         const unsigned long long t0 = globaltimer_ns();
         while (*(volatile unsigned *)bar < target) {
-            if (*(volatile unsigned *)status & ST_TIMEOUT) {
+            if (*(volatile unsigned *)(bar + 1) & ST_TIMEOUT) {
                 ok = 0;
                 break;
             }
-            if (globaltimer_ns() - t0 > kSpinLimitNs) {
+            if (globaltimer_ns() - t0 > limit_ns) {
+                atomicOr(bar + 1, ST_TIMEOUT);
                 atomicOr(status, ST_TIMEOUT);
                 ok = 0;
                 break;
@@ -771,7 +776,8 @@ template <int R>
 __global__ void __launch_bounds__(kTailThreads, 1)
 k_btail(const TailStep *__restrict__ steps, int nsteps, const BLuDesc *__restrict__ lu, int nlu,
         const int *__restrict__ Lcat, const int *__restrict__ Ucat, const int *__restrict__ dcat, unsigned *bar,
-        unsigned *__restrict__ pflag, unsigned *__restrict__ flags, unsigned *__restrict__ status) {
+        unsigned *__restrict__ pflag, unsigned *__restrict__ flags, unsigned *__restrict__ status, unsigned extra,
+        unsigned long long limit_ns) {
     pdl_trigger();
     pdl_wait();
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -799,7 +805,7 @@ k_btail(const TailStep *__restrict__ steps, int nsteps, const BLuDesc *__restric
 #undef SAGB_TAIL_G
             }
         }
-        if (!tail_barrier(bar, (unsigned)k, status)) return;
+        if (!tail_barrier(bar, (unsigned)k, status, extra, limit_ns)) return;
     }
 }
 
@@ -2152,8 +2158,8 @@ struct BatchEngine::Impl {
         clear_graphs();
     }
 
-    void launch_tail() {
-        SAGB_CUDA(cudaMemsetAsync(tail_bar, 0, sizeof(unsigned), c.stream));
+    void launch_tail(unsigned extra = 0, unsigned long long limit_ns = kSpinLimitNs) {
+        SAGB_CUDA(cudaMemsetAsync(tail_bar, 0, sizeof(unsigned) * 2, c.stream));
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3(tail_grid);
         cfg.blockDim = dim3(kTailThreads);
@@ -2168,7 +2174,7 @@ struct BatchEngine::Impl {
             constexpr int R = decltype(RR)::value;
             SAGB_CUDA(cudaLaunchKernelEx(&cfg, k_btail<R>, (const TailStep *)d_steps, nsteps, (const BLuDesc *)d_lu,
                                          nlu, (const int *)Lcat, (const int *)Ucat, (const int *)dcat, tail_bar,
-                                         cur_pflag, c.d_flags, c.d_flags_main));
+                                         cur_pflag, c.d_flags, c.d_flags_main, extra, limit_ns));
         });
         c.launches++;
     }
@@ -2485,6 +2491,32 @@ int BatchEngine::compressed(int level, int op, int set) {
     }
     return M.d16 && M.cdv ? 1 : 0;
 }
+unsigned BatchEngine::tail_selftest(int level, double timeout_ms) {
+    Impl &I = *impl_;
+    const int keep_from = I.tail_from, keep_grid = I.tail_grid;
+    if (!I.build_tail(level)) throw CudaError{"no persistent tail from this level"};
+    unsigned before = 0, after = 0;
+    SAGB_CUDA(cudaStreamSynchronize(I.c.stream));
+    SAGB_CUDA(cudaMemcpy(&before, I.c.d_flags_main, sizeof(unsigned), cudaMemcpyDeviceToHost));
+    // one launch whose first grid barrier expects one CTA more than the grid has
+    {
+        PrecFlags guard(I.c);
+        I.cur_pflag = I.pflag_prec;
+        I.launch_tail(1u, (unsigned long long)(timeout_ms * 1e6));
+        I.cur_pflag = I.pflag;
+    }
+    unsigned tail_status = 0;
+    SAGB_CUDA(cudaMemcpyAsync(&tail_status, I.tail_bar + 1, sizeof(unsigned), cudaMemcpyDeviceToHost, I.c.stream));
+    SAGB_CUDA(cudaStreamSynchronize(I.c.stream));
+    SAGB_CUDA(cudaMemcpy(&after, I.c.d_flags_main, sizeof(unsigned), cudaMemcpyDeviceToHost));
+    // the status word as it was, and the tail as it was
+    SAGB_CUDA(cudaMemcpy(I.c.d_flags_main, &before, sizeof(unsigned), cudaMemcpyHostToDevice));
+    SAGB_CUDA(cudaMemset(I.pflag, 0, sizeof(unsigned) * (size_t)I.S * I.Rn * 2));
+    if (keep_from > 0) I.build_tail(keep_from, keep_grid);
+    else I.drop_tail();
+    return (tail_status | after) & ST_TIMEOUT;
+}
+
 int BatchEngine::tail(int set, int grid) {
     Impl &I = *impl_;
     if (set == 0) I.drop_tail();

@@ -258,6 +258,11 @@ class BatchEngine {
     // and the coarsest LU in one cooperative launch, 0 turns it off, -1 reads;
     // returns the first level of the tail (0: none); grid > 0: that many CTAs
     int tail(int set, int grid = 0);
+    // failure detection of the tail's bounded grid barrier: one tail launch
+    // from `level` whose first barrier can never complete; returns the status
+    // bits it raised (ST_TIMEOUT when the wait ran out after timeout_ms and
+    // every CTA returned).  The engine's status words and tail are restored.
+    unsigned tail_selftest(int level, double timeout_ms);
     // one operator of one level on caller vectors (op 1: the colour sweep LD^-1 in)
     void level_op(int level, int op, const int *in, int *out);
     void coarse_solve();  // the batched LU on the engine's own level vectors

@@ -136,6 +136,7 @@ SIGNATURES = {
     "sa_batch_sweep_form": (C.c_int, [VP, C.c_int, C.c_int, C.POINTER(C.c_int)]),
     "sa_batch_compressed": (C.c_int, [VP, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int)]),
     "sa_batch_tail": (C.c_int, [VP, C.c_int, C.POINTER(C.c_int)]),
+    "sa_batch_tail_selftest": (C.c_int, [VP, VP, C.c_int, C.c_double, C.POINTER(C.c_uint)]),
     "sa_batch_time_op": (C.c_int, [VP, VP, C.c_int, C.c_int, VP, VP, C.c_int, C.POINTER(C.c_float)]),
     "sa_batch_rule_ratios": (C.c_int, [VP, VP, VP, VP, F64P]),
     "sa_batch_solve": (C.c_int, [VP, VP, C.POINTER(SolverParams), I32P, VP, VP, VP, I32P, I32P, I32P]),
@@ -764,6 +765,14 @@ class Batch:
         f = C.c_int()
         check(lib().sa_batch_tail(self.h, set, C.byref(f)))
         return f.value
+
+    def tail_selftest(self, level, timeout_ms=100.0):
+        """One persistent-tail launch whose first grid barrier cannot complete:
+        returns the status bits it raised (FLAG_TIMEOUT when the bounded wait
+        ran out and every CTA returned)."""
+        st = C.c_uint()
+        check(lib().sa_batch_tail_selftest(self.ctx.h, self.h, level, timeout_ms, C.byref(st)))
+        return st.value
 
     def sweep_form(self, level, set=-1):
         """The colour sweep's launch form at one level (0 a launch per colour,

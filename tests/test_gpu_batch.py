@@ -274,3 +274,22 @@ def test_launch_options_do_not_change_results(ctx):
     assert B.time_op(0, B.OP_VCYCLE, x, y, 3) > 0
     x.close(); y.close()
     B.close()
+
+
+def test_tail_barrier_timeout_is_detected(ctx):
+    """Failure detection of the persistent tail's grid barrier without a GPU
+    fault: a launch whose first barrier waits for one CTA more than the grid
+    has runs out its bounded wait (50 ms), every CTA returns and the status
+    reports the timeout; the context and the engine stay usable."""
+    systems, _ = _systems(SYSTEMS, 1)
+    B = sagb.Batch(ctx, systems, 1)
+    vin = np.random.default_rng(12).integers(-(1 << 28), 1 << 28, size=B.rows).astype(np.int32)
+    B.tail(0)
+    ref = B.precondition(vin)
+    st = B.tail_selftest(B.depth - 1, 50.0)
+    assert st & sagb.FLAG_TIMEOUT
+    assert B.tail() == 0  # the setting is restored
+    np.testing.assert_array_equal(B.precondition(vin), ref)
+    B.tail(1)
+    np.testing.assert_array_equal(B.precondition(vin), ref)
+    B.close()
