@@ -125,7 +125,9 @@ int sa_ctx_destroy(sa_ctx ctx);
 #define SA_OPT_PDL 2      /* batched engine: start each V-cycle kernel while the one before it
                            * drains (programmatic dependent launch; default on)               */
 #define SA_OPT_GPU_SETUP 3 /* sa_batch_create: the Ruge-Stueben chain of each system of at least
-                            * 100000 rows on the GPU (same hierarchy bit for bit; default on) */
+                            * this many rows on the GPU (same hierarchy bit for bit): 0 none, 1
+                            * the default 2^20 (smaller systems build faster side by side on the
+                            * host threads), >= 2 that many rows */
 int sa_ctx_set_option(sa_ctx ctx, int option, int value);
 int sa_ctx_flags(sa_ctx ctx, unsigned *flags, int clear);
 int sa_ctx_launches(sa_ctx ctx, long long *count);

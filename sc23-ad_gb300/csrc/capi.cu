@@ -179,7 +179,7 @@ extern "C" int sa_ctx_set_option(sa_ctx ctx, int option, int value) {
     if (option == SA_OPT_FP_EXACT) ctx->c.fp_exact = value != 0;
     else if (option == SA_OPT_GRAPHS) ctx->c.use_graphs = value != 0;
     else if (option == SA_OPT_PDL) ctx->c.use_pdl = value != 0;
-    else if (option == SA_OPT_GPU_SETUP) ctx->c.gpu_setup = value != 0;
+    else if (option == SA_OPT_GPU_SETUP) ctx->c.gpu_setup_rows = value == 1 ? 1 << 20 : value < 0 ? 0 : value;
     else return fail(SA_ERR_ARG, "unknown option");
     return SA_OK;
 }
@@ -1166,12 +1166,12 @@ extern "C" int sa_batch_create(sa_ctx ctx, int nsys, const int *n, const int32_t
     try {
         const int cs = q.coarse_size > 0 ? q.coarse_size : 2000;
         std::function<RsChain(const CsrD &)> gpu_chain;
-        if (ctx->c.gpu_setup)
+        if (ctx->c.gpu_setup_rows > 0)
             gpu_chain = [&](const CsrD &A) { return rs_chain_gpu(ctx->c, A, q.theta, q.max_levels, cs); };
         B->h = std::make_shared<BatchHierarchy>(build_batch(sys, q.theta, q.max_levels, q.omega, q.smooth_iter,
                                                             threads, src, q.max_colours, q.coarse_colours, cs,
                                                             gpu_chain,
-                                                            kGpuChainRows));
+                                                            ctx->c.gpu_setup_rows));
         SAGB_CUDA(cudaSetDevice(ctx->c.device));
         B->eng = std::make_unique<BatchEngine>(ctx->c, B->h, nrhs);
         SAGB_CUDA(cudaDeviceSynchronize());

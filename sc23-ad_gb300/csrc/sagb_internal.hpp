@@ -36,7 +36,8 @@ struct Ctx {
     bool fp_exact = false;           // FP kernels in sequential order without FMA
     bool use_graphs = true;
     bool use_pdl = true;             // batched V-cycle kernels chained by programmatic dependent launch
-    bool gpu_setup = true;           // batches: Ruge-Stueben chains of large systems on the GPU
+    int gpu_setup_rows = 1 << 20;    // batches: systems from this size on build their Ruge-Stueben chain
+                                     // on the GPU (0: none); smaller ones share the host threads
     long long launches = 0;          // kernels launched by this context (for reporting)
     std::string err;
 };
@@ -53,7 +54,6 @@ struct Ctx {
 struct RsChain;
 struct CsrD;
 RsChain rs_chain_gpu(Ctx &c, const CsrD &A, double theta, int max_levels, int coarse_size);
-constexpr int kGpuChainRows = 100000;  // batches: systems from this size on take the GPU chain
 
 struct PrecFlags {
     Ctx &c;

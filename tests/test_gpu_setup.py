@@ -95,9 +95,9 @@ def test_gpu_setup_matches_host(ctx, kind, n, prm, prec):
 
 
 def test_batch_gpu_chain_matches_host(ctx):
-    """sa_batch_create builds the chain of a system of 100000 rows or more on
-    the GPU (SA_OPT_GPU_SETUP, default on): the batch's hierarchy and its
-    V-cycle are those of the host-built batch."""
+    """sa_batch_create builds the chains of large systems on the GPU
+    (SA_OPT_GPU_SETUP: here systems of 100000 rows or more): the batch's
+    hierarchy and its V-cycle are those of the host-built batch."""
     systems = []
     for kind, n in ((sagb.GEN_POISSON3D, 48), (sagb.GEN_STENCIL27, 12)):
         A = sagb.HostCsr.generate(kind, n, 0.0, seed=2)
@@ -105,9 +105,10 @@ def test_batch_gpu_chain_matches_host(ctx):
         A.lmax1_scaling(b)
         systems.append(A.arrays())
     assert len(systems[0][0]) - 1 >= 100000
-    Bg = sagb.Batch(ctx, systems, 1)
-    ctx.set_option(sagb.OPT_GPU_SETUP, 0)
+    ctx.set_option(sagb.OPT_GPU_SETUP, 100000)
     try:
+        Bg = sagb.Batch(ctx, systems, 1)
+        ctx.set_option(sagb.OPT_GPU_SETUP, 0)
         Bh = sagb.Batch(ctx, systems, 1)
     finally:
         ctx.set_option(sagb.OPT_GPU_SETUP, 1)
