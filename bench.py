@@ -37,7 +37,8 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(ROOT, "sc23-ad_gb300"))
 
-WORKLOAD = ("3D 7-point Poisson 128^3, one right-hand side: batched int-AMG-FGMRES(30) with FP64 refinement, "
+def workload(n, m):
+    return (f"3D 7-point Poisson {n}^3, one right-hand side: batched int-AMG-FGMRES({m}) with FP64 refinement, "
             "multicolour SOR smoother, learned fractional bits (rule as fallback); the plain drop-in (rule bits, "
             "bit-exact level-scheduled SOR) and FP64-AMG-FGMRES on the same GPU reported beside it")
 
@@ -595,7 +596,7 @@ def main_ours(a):
         "value": sec, "unit": "s", "n_gpus": dist.world, "steps": a.steps, "warmup": a.warmup,
         "ms_per_step": sec * 1000.0, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
         "dtype": "int32", "data": "synthetic (b = A x*, x* ~ U[-1,1] seeded; SuiteSparse inputs not shipped)",
-        "config": {"workload": WORKLOAD, "rows": N, "m": a.m, "eps": 1e-10, "parallelism": f"replicas{dist.world}",
+        "config": {"workload": workload(a.n, a.m), "rows": N, "m": a.m, "eps": 1e-10, "parallelism": f"replicas{dist.world}",
                    "l2": "inputs larger than L2 (hierarchy ~1.5 GB, Krylov basis 0.5 GB per solve)"},
         "iters": out["iters"], "converged": out["converged"], "explicit_res": out["explicit_res"],
         "frac_bits": out["frac_bits"], "rule_bits": out["rule_bits"], "learned_bits": out["learned_bits"],
@@ -689,7 +690,7 @@ def main_reference(a):
         "value": val, "unit": "s", "n_gpus": dist.world, "steps": a.steps, "warmup": a.warmup,
         "ms_per_step": val * 1000, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
         "dtype": "int32", "data": "synthetic (b = A x*, x* ~ U[-1,1] seeded)",
-        "config": {"workload": WORKLOAD, "rows": len(b), "m": a.m, "eps": 1e-10, "parallelism": "host threads"},
+        "config": {"workload": workload(a.n, a.m), "rows": len(b), "m": a.m, "eps": 1e-10, "parallelism": "host threads"},
         "iters": it, "explicit_res": explicit_res(r, c, v, b, x), "frac_bits": bits,
         "cpu_baseline": {"value": val, "unit": "s", "cores": threads, "kind": "port",
                          "sample": f"full solves of the 128^3 system, oracle C restatement of the reference "
