@@ -693,7 +693,7 @@ def main_reference(a):
         "config": {"workload": workload(a.n, a.m), "rows": len(b), "m": a.m, "eps": 1e-10, "parallelism": "host threads"},
         "iters": it, "explicit_res": explicit_res(r, c, v, b, x), "frac_bits": bits,
         "cpu_baseline": {"value": val, "unit": "s", "cores": threads, "kind": "port",
-                         "sample": f"full solves of the 128^3 system, oracle C restatement of the reference "
+                         "sample": f"full solves of the {a.n}^3 system, oracle C restatement of the reference "
                                    f"solve phase, {threads} threads (SpMV/BLAS parallel, SOR sweeps sequential "
                                    f"as in the reference)"},
         "e2e": {"value": val, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
