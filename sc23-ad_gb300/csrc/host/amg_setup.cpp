@@ -24,6 +24,36 @@ HostSerial::HostSerial() { tl_serial++; }
 HostSerial::~HostSerial() { tl_serial--; }
 bool host_serial() { return tl_serial > 0; }
 
+// f(0) .. f(n-1) on up to hardware_concurrency host threads; every task
+// writes its own pre-sized slot, so results do not depend on the thread count
+template <typename F>
+static void parallel_tasks(int n, F &&f) {
+    const int T = host_serial() ? 1 : std::min(n, (int)std::max(1u, std::thread::hardware_concurrency()));
+    if (T <= 1) {
+        for (int i = 0; i < n; i++) f(i);
+        return;
+    }
+    std::atomic<int> next(0);
+    std::exception_ptr first;
+    std::mutex mu;
+    std::vector<std::thread> pool;
+    for (int t = 0; t < T; t++)
+        pool.emplace_back([&] {
+            HostSerial inner;
+            for (int i; (i = next++) < n;) {
+                try {
+                    f(i);
+                } catch (...) {
+                    std::lock_guard<std::mutex> g(mu);
+                    if (!first) first = std::current_exception();
+                }
+            }
+        });
+    for (auto &th : pool) th.join();
+    if (first) std::rethrow_exception(first);
+}
+
+
 // ============================================================ conversion rules
 
 int ceil_log2_int(int64_t k) {
@@ -72,32 +102,58 @@ void lmax1_scaling(CsrD &A, double *b) {
 
 // ======================================================= Ruge-Stueben coarsening
 
+// rows [0, n) in blocks of at least 16384 rows, one task per block
+template <typename F>
+static void row_blocks(int n, F &&f) {
+    const int nb = std::max(1, std::min(64, n / 16384));
+    parallel_tasks(nb, [&](int b) { f((int)((long long)n * b / nb), (int)((long long)n * (b + 1) / nb)); });
+}
+
 // get_strong_weak_set (helper_multigrid.hpp:67-108): off-diagonal a_ij is strong
 // when |a_ij| >= theta * max_k!=i |a_ik|; everything else (diagonal included)
-// goes to the weak set.
+// goes to the weak set.  Rows are independent: counts, prefix sums, then the
+// entries of each row in order (host threads over row blocks).
 static void strong_weak(const CsrD &A, double theta, CsrD &S, CsrD &W) {
     const int N = A.n;
     S.n = W.n = S.m = W.m = N;
     S.rptr.assign(N + 1, 0);
     W.rptr.assign(N + 1, 0);
-    S.cind.clear(); S.val.clear(); W.cind.clear(); W.val.clear();
-    S.cind.reserve(A.nnz()); S.val.reserve(A.nnz());
-    W.cind.reserve(A.nnz()); W.val.reserve(A.nnz());
+    std::vector<double> thr(N);
+    row_blocks(N, [&](int i0, int i1) {
+        for (int i = i0; i < i1; i++) {
+            double mx = 0;
+            for (int j = A.rptr[i]; j < A.rptr[i + 1]; j++)
+                if (A.cind[j] != i && std::fabs(A.val[j]) > mx) mx = std::fabs(A.val[j]);
+            thr[i] = theta * mx;
+            int ns = 0;
+            for (int j = A.rptr[i]; j < A.rptr[i + 1]; j++)
+                if (A.cind[j] != i && std::fabs(A.val[j]) >= thr[i]) ns++;
+            S.rptr[i + 1] = ns;
+            W.rptr[i + 1] = A.rptr[i + 1] - A.rptr[i] - ns;
+        }
+    });
     for (int i = 0; i < N; i++) {
-        double mx = 0;
-        for (int j = A.rptr[i]; j < A.rptr[i + 1]; j++)
-            if (A.cind[j] != i && std::fabs(A.val[j]) > mx) mx = std::fabs(A.val[j]);
-        const double thr = theta * mx;
-        for (int j = A.rptr[i]; j < A.rptr[i + 1]; j++) {
-            if (A.cind[j] != i && std::fabs(A.val[j]) >= thr) {
-                S.cind.push_back(A.cind[j]); S.val.push_back(A.val[j]);
-            } else {
-                W.cind.push_back(A.cind[j]); W.val.push_back(A.val[j]);
+        S.rptr[i + 1] += S.rptr[i];
+        W.rptr[i + 1] += W.rptr[i];
+    }
+    S.cind.resize(S.rptr[N]);
+    S.val.resize(S.rptr[N]);
+    W.cind.resize(W.rptr[N]);
+    W.val.resize(W.rptr[N]);
+    row_blocks(N, [&](int i0, int i1) {
+        for (int i = i0; i < i1; i++) {
+            int a = S.rptr[i], b = W.rptr[i];
+            for (int j = A.rptr[i]; j < A.rptr[i + 1]; j++) {
+                if (A.cind[j] != i && std::fabs(A.val[j]) >= thr[i]) {
+                    S.cind[a] = A.cind[j];
+                    S.val[a++] = A.val[j];
+                } else {
+                    W.cind[b] = A.cind[j];
+                    W.val[b++] = A.val[j];
+                }
             }
         }
-        S.rptr[i + 1] = (int)S.cind.size();
-        W.rptr[i + 1] = (int)W.cind.size();
-    }
+    });
 }
 
 // get_influence_set (helper_multigrid.hpp:110-136): transpose of the pattern.
@@ -266,64 +322,88 @@ static CsrD interpolation(const CsrD &A, const CsrD &S, const CsrD &W, const std
     P.n = N;
     P.m = nc;
     P.rptr.assign(N + 1, 0);
-    // strong connections split by the class of the column
-    std::vector<int> cs, cf;        // column lists of C_Stg row i / DS_Stg row i
-    std::vector<double> vs, vf;
-    std::vector<double> amk_m, amj;
+    // a coarse row has one entry, a fine row one per strong coarse neighbour
     for (int i = 0; i < N; i++) {
-        if (is_coarse[i]) {
-            P.cind.push_back(col[i]);
-            P.val.push_back(1);
-            P.rptr[i + 1] = (int)P.cind.size();
-            continue;
+        int cnt = 1;
+        if (!is_coarse[i]) {
+            cnt = 0;
+            for (int j = S.rptr[i]; j < S.rptr[i + 1]; j++) cnt += is_coarse[S.cind[j]] != 0;
         }
-        cs.clear(); vs.clear(); cf.clear(); vf.clear();
-        for (int j = S.rptr[i]; j < S.rptr[i + 1]; j++) {
-            if (is_coarse[S.cind[j]]) { cs.push_back(S.cind[j]); vs.push_back(S.val[j]); }
-            else { cf.push_back(S.cind[j]); vf.push_back(S.val[j]); }
-        }
-        double deno = 0;
-        for (int j = W.rptr[i]; j < W.rptr[i + 1]; j++) deno += W.val[j];
-        const int ncs = (int)cs.size(), ncf = (int)cf.size();
-        // sum_{k in C_i} a_mk for each strong fine m (merge in column order),
-        // and a_mj for each (m, j) pair
-        amk_m.assign(ncf, 0.0);
-        amj.assign((size_t)ncf * ncs, 0.0);
-        for (int q = 0; q < ncf && ncs > 0; q++) {
-            const int mrow = cf[q];
-            double amk = 0;
-            bool hit = false;
-            int a = A.rptr[mrow], k = 0;
-            while (a < A.rptr[mrow + 1] && k < ncs) {
-                if (A.cind[a] < cs[k]) {
-                    a++;
-                } else if (A.cind[a] == cs[k]) {
-                    amk += A.val[a];
-                    amj[(size_t)q * ncs + k] = A.val[a];
-                    hit = true;
-                    a++; k++;
-                } else {
-                    k++;
-                }
+        P.rptr[i + 1] = P.rptr[i] + cnt;
+    }
+    P.cind.resize(P.rptr[N]);
+    P.val.resize(P.rptr[N]);
+    // rows on host threads; the "1 amk = 0" lines are counted per row and the
+    // "2 amk = 0" stop recorded, then both reported in row order
+    std::vector<int> warn(N, 0);
+    std::vector<char> stop(N, 0);
+    row_blocks(N, [&](int i0, int i1) {
+        std::vector<int> cs, cf;  // column lists of C_Stg row i / DS_Stg row i
+        std::vector<double> vs, vf;
+        std::vector<double> amk_m, amj;
+        for (int i = i0; i < i1; i++) {
+            if (is_coarse[i]) {
+                P.cind[P.rptr[i]] = col[i];
+                P.val[P.rptr[i]] = 1;
+                continue;
             }
-            if (amk == 0) {
-                if (hit) {
-                    for (int k = 0; k < ncs; k++) printf("1 amk = 0\n");  // once per (j, m) pair
-                    amk = 0.00001;
-                } else {
-                    printf("2 amk = 0\n");
-                    exit(1);  // as the reference (helper_multigrid.hpp:518)
-                }
+            cs.clear(); vs.clear(); cf.clear(); vf.clear();
+            for (int j = S.rptr[i]; j < S.rptr[i + 1]; j++) {
+                if (is_coarse[S.cind[j]]) { cs.push_back(S.cind[j]); vs.push_back(S.val[j]); }
+                else { cf.push_back(S.cind[j]); vf.push_back(S.val[j]); }
             }
-            amk_m[q] = amk;
+            double deno = 0;
+            for (int j = W.rptr[i]; j < W.rptr[i + 1]; j++) deno += W.val[j];
+            const int ncs = (int)cs.size(), ncf = (int)cf.size();
+            // sum_{k in C_i} a_mk for each strong fine m (merge in column order),
+            // and a_mj for each (m, j) pair
+            amk_m.assign(ncf, 0.0);
+            amj.assign((size_t)ncf * ncs, 0.0);
+            bool stopped = false;
+            for (int q = 0; q < ncf && ncs > 0; q++) {
+                const int mrow = cf[q];
+                double amk = 0;
+                bool hit = false;
+                int a = A.rptr[mrow], k = 0;
+                while (a < A.rptr[mrow + 1] && k < ncs) {
+                    if (A.cind[a] < cs[k]) {
+                        a++;
+                    } else if (A.cind[a] == cs[k]) {
+                        amk += A.val[a];
+                        amj[(size_t)q * ncs + k] = A.val[a];
+                        hit = true;
+                        a++; k++;
+                    } else {
+                        k++;
+                    }
+                }
+                if (amk == 0) {
+                    if (hit) {
+                        warn[i] += ncs;  // "1 amk = 0" once per (j, m) pair
+                        amk = 0.00001;
+                    } else {
+                        stop[i] = 1;  // "2 amk = 0": the reference exits (helper_multigrid.hpp:518)
+                        stopped = true;
+                        break;
+                    }
+                }
+                amk_m[q] = amk;
+            }
+            if (stopped) continue;
+            for (int k = 0; k < ncs; k++) {
+                double aij = vs[k];
+                for (int q = 0; q < ncf; q++) aij += vf[q] * amj[(size_t)q * ncs + k] / amk_m[q];
+                P.cind[P.rptr[i] + k] = col[cs[k]];
+                P.val[P.rptr[i] + k] = -aij / deno;
+            }
         }
-        for (int k = 0; k < ncs; k++) {
-            double aij = vs[k];
-            for (int q = 0; q < ncf; q++) aij += vf[q] * amj[(size_t)q * ncs + k] / amk_m[q];
-            P.cind.push_back(col[cs[k]]);
-            P.val.push_back(-aij / deno);
+    });
+    for (int i = 0; i < N; i++) {
+        for (int k = 0; k < warn[i]; k++) printf("1 amk = 0\n");
+        if (stop[i]) {
+            printf("2 amk = 0\n");
+            exit(1);  // as the reference (helper_multigrid.hpp:518)
         }
-        P.rptr[i + 1] = (int)P.cind.size();
     }
     return P;
 }
@@ -792,35 +872,6 @@ static CsrD invert_last(const CsrD &LD) {
     for (int i = 0; i < B.n; i++)
         if (B.rptr[i + 1] > B.rptr[i]) B.val[B.rptr[i + 1] - 1] = 1 / B.val[B.rptr[i + 1] - 1];
     return B;
-}
-
-// f(0) .. f(n-1) on up to hardware_concurrency host threads; every task
-// writes its own pre-sized slot, so results do not depend on the thread count
-template <typename F>
-static void parallel_tasks(int n, F &&f) {
-    const int T = host_serial() ? 1 : std::min(n, (int)std::max(1u, std::thread::hardware_concurrency()));
-    if (T <= 1) {
-        for (int i = 0; i < n; i++) f(i);
-        return;
-    }
-    std::atomic<int> next(0);
-    std::exception_ptr first;
-    std::mutex mu;
-    std::vector<std::thread> pool;
-    for (int t = 0; t < T; t++)
-        pool.emplace_back([&] {
-            HostSerial inner;
-            for (int i; (i = next++) < n;) {
-                try {
-                    f(i);
-                } catch (...) {
-                    std::lock_guard<std::mutex> g(mu);
-                    if (!first) first = std::current_exception();
-                }
-            }
-        });
-    for (auto &th : pool) th.join();
-    if (first) std::rethrow_exception(first);
 }
 
 static void smoother_split(const CsrD &A, const SmootherSpec &sm, int level, CsrD &LD, CsrD &U,
