@@ -219,8 +219,8 @@ __global__ void k_rs_interp(int n, const int *__restrict__ Arp, const int *__res
                             const int *__restrict__ ncs_row, const int *__restrict__ part,
                             const long long *__restrict__ amj_off, double *__restrict__ amj_all,
                             double *__restrict__ amk_all, const int *__restrict__ Prp, int *__restrict__ Pci,
-                            double *__restrict__ Pv, unsigned long long *__restrict__ warn,
-                            unsigned *__restrict__ err) {
+                            double *__restrict__ Pv, unsigned *__restrict__ warn_row,
+                            int *__restrict__ first_stop) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     if (isc[i]) {
@@ -255,11 +255,11 @@ __global__ void k_rs_interp(int n, const int *__restrict__ Arp, const int *__res
         }
         if (amk == 0) {
             if (hit) {
-                atomicAdd(warn, (unsigned long long)ncs);  // "1 amk = 0" once per (j, m) pair
+                warn_row[i] += (unsigned)ncs;  // "1 amk = 0" once per (j, m) pair
                 amk = 0.00001;
             } else {
-                atomicOr(err, 1u);  // "2 amk = 0": the host exits
-                amk = 1.0;
+                atomicMin(first_stop, i);  // "2 amk = 0": the setup stops at the first such row
+                return;
             }
         }
         amk_m[q] = amk;
@@ -559,10 +559,7 @@ DMat product(Ctx &c, const int *lp, const int *li, const double *lv, int L, cons
 
 // one level: A (device) -> CA (device), P and R (host copies); the host's rs_level
 void rs_level_gpu(Ctx &c, const DMat &A, double theta, DMat &CA, CsrD &P_h, CsrD &R_h) {
-    if (theta <= 0 || 1 < theta) {
-        printf("Error: Theta must be in 0 < theta <= 1\n");
-        exit(EXIT_FAILURE);
-    }
+    if (theta <= 0 || 1 < theta) throw SetupError{"Theta must be in 0 < theta <= 1"};
     const int N = A.n;
     // strength split
     double *thr = dnew<double>(N);
@@ -633,10 +630,11 @@ void rs_level_gpu(Ctx &c, const DMat &A, double theta, DMat &CA, CsrD &P_h, CsrD
     int *d_isc = dnew<int>(N), *d_col = dnew<int>(N), *d_ncs = dnew<int>(N), *d_part = dnew<int>(S.nnz);
     long long *d_amj_off = dnew<long long>(N + 1);
     double *d_amj = dnew<double>(amj_off[N]), *d_amk = dnew<double>(S.nnz);
-    unsigned long long *d_warn = dnew<unsigned long long>(1);
+    unsigned *d_warn = dnew<unsigned>(N);
+    int *d_stop = dnew<int>(1);
     unsigned *d_err = dnew<unsigned>(1);
-    SAGB_CUDA(cudaMemsetAsync(d_warn, 0, sizeof(unsigned long long), c.stream));
-    SAGB_CUDA(cudaMemsetAsync(d_err, 0, sizeof(unsigned), c.stream));
+    SAGB_CUDA(cudaMemsetAsync(d_warn, 0, sizeof(unsigned) * N, c.stream));
+    up(c, d_stop, &N, 1);
     up(c, P.rptr, prp.data(), N + 1);
     up(c, d_isc, is_coarse.data(), N);
     up(c, d_col, colmap.data(), N);
@@ -645,21 +643,29 @@ void rs_level_gpu(Ctx &c, const DMat &A, double theta, DMat &CA, CsrD &P_h, CsrD
     up(c, d_amj_off, amj_off.data(), N + 1);
     k_rs_interp<<<blocks_for(N), kRsThreads, 0, c.stream>>>(N, A.rptr, A.cind, A.val, S.rptr, S.cind, S.val, W.rptr,
                                                             W.val, d_isc, d_col, d_ncs, d_part, d_amj_off, d_amj,
-                                                            d_amk, P.rptr, P.cind, P.val, d_warn, d_err);
+                                                            d_amk, P.rptr, P.cind, P.val, d_warn, d_stop);
     SAGB_CUDA(cudaGetLastError());
-    unsigned long long warn = 0;
+    // the host setup's messages in its order: the warnings of the rows up to
+    // the first stopping row (helper_multigrid.hpp:511-518)
+    std::vector<unsigned> warn(N);
+    int first_stop = N;
     unsigned err = 0;
-    down(c, &warn, d_warn, 1);
-    down(c, &err, d_err, 1);
+    down(c, warn.data(), d_warn, N);
+    down(c, &first_stop, d_stop, 1);
     sync(c);
-    for (unsigned long long k = 0; k < warn; k++) printf("1 amk = 0\n");
-    if (err & 1u) {
+    for (int i = 0; i < N && i <= first_stop; i++)
+        for (unsigned k = 0; k < warn[i]; k++) printf("1 amk = 0\n");
+    if (first_stop < N) {
         printf("2 amk = 0\n");
-        exit(1);  // as the host setup and the reference (helper_multigrid.hpp:518)
+        fflush(stdout);
+        dfree(d_warn); dfree(d_stop); dfree(d_err);
+        throw SetupError{"interpolation: fine row " + std::to_string(first_stop) +
+                         " has a strong fine neighbour with no coupling to its coarse points (2 amk = 0)"};
     }
     dfree(thr); dfree(scnt); dfree(wcnt);
     dfree(d_isc); dfree(d_col); dfree(d_ncs); dfree(d_part); dfree(d_amj_off); dfree(d_amj); dfree(d_amk);
     dfree(d_warn);
+    dfree(d_stop);
     S.release();
     W.release();
     // R = P^T and the Galerkin operator (get_coarse_matrix, helper_multigrid.hpp:564-586):

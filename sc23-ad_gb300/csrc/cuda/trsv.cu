@@ -554,9 +554,9 @@ void trsv(Ctx &c, const DevTri &T, const void *in, void *out) {
 // kNoAllocRows rows (2 MiB) and every GPU that loads the library holds it
 // until the process exits.  All calls share it and it keeps the last call's
 // contents, so before each call the words of this level's rows and the
-// ticket/done counters are cleared (a previous call may have left words of
-// another precision there); the epoch keeps counting across calls.  Calls that
-// overlap on the GPU race on this array.
+// ticket, done and epoch counters are cleared (a previous call may have left
+// words of another precision there): every call starts at epoch 1 against
+// zeroed words.  Calls that overlap on the GPU race on this array.
 constexpr int kNoAllocRows = 262144;
 static __device__ __align__(256) unsigned long long g_noalloc_scratch[kNoAllocRows + 2];
 
@@ -591,7 +591,7 @@ void trsv_noalloc(Ctx &c, const DevTri &T, const void *in, void *out) {
     U.flag = (unsigned *)s;
     U.sync = (TriSync *)(s + kNoAllocRows);
     SAGB_CUDA(cudaMemsetAsync(s, 0, sizeof(unsigned long long) * (size_t)T.n, c.stream));
-    SAGB_CUDA(cudaMemsetAsync(U.sync, 0, 2 * sizeof(unsigned), c.stream));  // ticket, done
+    SAGB_CUDA(cudaMemsetAsync(U.sync, 0, sizeof(TriSync), c.stream));  // ticket, done, epoch
     if (U.vt == VT_I32) return tri_by_group<VT_I32, false>(c, U, in, out);
     if (U.vt == VT_F64) {
         if (c.fp_exact) return tri_by_group<VT_F64, true>(c, U, in, out);

@@ -171,108 +171,119 @@ static Pattern transpose_pattern(const CsrD &S) {
     return T;
 }
 
-// first_pass (helper_multigrid.hpp:138-266): greedy C/F selection by the number
-// of points a candidate strongly influences, kept in buckets that are updated
-// in place as points are classified.
+// C/F state of a point that neither pass has classified yet
+constexpr int kUnclassified = -1;
+
+// Candidate coarse points of the first pass, ordered by weight: the number of
+// not yet classified points that a candidate strongly influences.  The points
+// sit in slots 0..N-1; all points of one weight fill one contiguous run of
+// slots, the runs in decreasing weight, and inside a run the slot order breaks
+// ties.  `head` is the slot of the candidate taken last: slots below it are
+// spent.  lim[w] is the first slot after the runs of weight >= w.  A weight
+// change moves a point across the boundary between two neighbouring runs by
+// one exchange of slots, which keeps the order of everything else.
+class CandidateRuns {
+  public:
+    // Ranks the points by weight (decreasing), then inside each weight by the
+    // secondary key `tie` (increasing), with the reference's quicksort on the
+    // same key arrays (helper_multigrid.hpp:138-175), so ties fall the same way.
+    CandidateRuns(std::vector<int> weight, std::vector<int> second, std::vector<int> tie) : n_((int)weight.size()) {
+        pt_.resize(n_);
+        for (int i = 0; i < n_; i++) pt_[i] = i;
+        wt_ = std::move(weight);
+        if (n_ > 0) hoare_sort(0, n_ - 1, false, wt_.data(), second.data(), tie.data(), pt_.data());
+        top_ = n_ > 0 ? wt_[0] : 0;
+        std::vector<int> count(top_ + 1, 0);
+        for (int w : wt_) count[w]++;
+        lim_.assign(top_ + 2, 0);
+        for (int w = top_; w >= 0; w--) lim_[w] = lim_[w + 1] + count[w];
+        for (int w = top_; w >= 0; w--)
+            if (lim_[w] - lim_[w + 1] > 1) hoare_sort(lim_[w + 1], lim_[w] - 1, true, tie.data(), pt_.data());
+        slot_.resize(n_);
+        for (int k = 0; k < n_; k++) slot_[pt_[k]] = k;
+    }
+
+    // the next candidate at or after `head` that `skip` does not reject; -1 at the end
+    template <typename Skip>
+    int take(Skip &&skip) {
+        while (head_ < n_ && skip(pt_[head_])) head_++;
+        return head_ < n_ ? pt_[head_] : -1;
+    }
+    void advance() { head_++; }
+
+    // weight + 1: the point moves to the front of its run and joins the run above
+    void raise(int point) {
+        const int k = slot_[point];
+        const int w = ++wt_[k];
+        const int first_live = head_ + 1;
+        int dest;
+        if (w > top_) {  // a new heaviest run, just after the head
+            top_ = w;
+            lim_.resize(w + 2);
+            lim_[w + 1] = first_live;
+            lim_[w] = first_live + 1;
+            dest = first_live;
+        } else if (lim_[w] > first_live) {  // run w has live slots: append to it
+            dest = lim_[w]++;
+        } else {  // run w is spent: it restarts after the head
+            dest = first_live;
+            lim_[w] = first_live + 1;
+        }
+        exchange(k, dest);
+    }
+
+    // weight - 1 (not below 0): the point moves to the back of its run and joins the run below
+    void lower(int point) {
+        const int k = slot_[point];
+        if (wt_[k] == 0) return;
+        const int w = wt_[k]--;
+        exchange(k, --lim_[w]);
+    }
+
+  private:
+    void exchange(int a, int b) {
+        std::swap(wt_[a], wt_[b]);
+        std::swap(pt_[a], pt_[b]);
+        slot_[pt_[a]] = a;
+        slot_[pt_[b]] = b;
+    }
+    int n_, top_ = 0, head_ = 0;
+    std::vector<int> pt_, wt_, slot_, lim_;
+};
+
+// first_pass (helper_multigrid.hpp:138-266): the candidate that influences the
+// most unclassified points becomes coarse, the points it influences become
+// fine, and the weights of the points around them are updated before the next
+// candidate is taken.
 void rs_first_pass(const CsrD &S, const Pattern &St, std::vector<int> &is_coarse) {
     const int N = S.n;
-    is_coarse.assign(N, 0);
-    std::vector<int> visited(N, 0), card(N), scard(N), infl(N, 0), index(N), where(N, 0);
+    is_coarse.assign(N, kUnclassified);
+    std::vector<char> done(N, 0);
+    std::vector<int> weight(N), depends(N), reach(N, 0);
     for (int i = 0; i < N; i++) {
-        card[i] = St.rptr[i + 1] - St.rptr[i];
-        scard[i] = S.rptr[i + 1] - S.rptr[i];
-        index[i] = i;
-        if (card[i] == 0 && scard[i] == 0) {
+        weight[i] = St.rptr[i + 1] - St.rptr[i];  // points that depend strongly on i
+        depends[i] = S.rptr[i + 1] - S.rptr[i];
+        if (weight[i] == 0 && depends[i] == 0) {  // isolated: fine from the start
             is_coarse[i] = 0;
-            visited[i] = 1;
-        } else {
-            is_coarse[i] = -38;  // unclassified marker checked by second_pass
+            done[i] = 1;
         }
-        for (int j = St.rptr[i]; j < St.rptr[i + 1]; j++) {
-            int k = St.cind[j];
-            infl[i] += S.rptr[k + 1] - S.rptr[k];
-        }
+        for (int j = St.rptr[i]; j < St.rptr[i + 1]; j++) reach[i] += S.rptr[St.cind[j] + 1] - S.rptr[St.cind[j]];
     }
-    if (N > 0) hoare_sort(0, N - 1, false, card.data(), scard.data(), infl.data(), index.data());
-
-    int maxc = N > 0 ? card[0] : 0;
-    // bptr[c] = number of entries whose count is >= c (entries are sorted by
-    // decreasing count, so bucket c occupies [bptr[c+1], bptr[c])).
-    std::vector<int> bptr(maxc + 2);
-    bptr[maxc + 1] = 0;
-    int start = 0;
-    for (int c = maxc; c >= 0; c--) {
-        int num = 0;
-        bool cut = false;
-        for (int j = start; j < N; j++) {
-            if (card[j] == c) {
-                num++;
-            } else {
-                bptr[c] = bptr[c + 1] + num;
-                start = j;
-                cut = true;
-                break;
-            }
-        }
-        if (cut) continue;
-        bptr[c] = bptr[c + 1] + num;
-    }
-    for (int c = maxc; c >= 0; c--)
-        if (bptr[c] - bptr[c + 1] > 1) hoare_sort(bptr[c + 1], bptr[c] - 1, true, infl.data(), index.data());
-
-    for (int i = 0; i < N; i++) where[index[i]] = i;
-    auto exchange = [&](int a, int b) {
-        std::swap(card[a], card[b]);
-        std::swap(index[a], index[b]);
-        std::swap(where[index[a]], where[index[b]]);
-    };
-    int pos = 0;
-    while (pos < N) {
-        while (pos < N && visited[index[pos]]) pos++;
-        if (pos >= N) break;
-        const int cpt = index[pos];
-        visited[cpt] = 1;
-        is_coarse[cpt] = 1;
-        for (int t = St.rptr[cpt]; t < St.rptr[cpt + 1]; t++) {
+    CandidateRuns runs(std::move(weight), std::move(depends), std::move(reach));
+    for (int c; (c = runs.take([&](int p) { return done[p] != 0; })) >= 0; runs.advance()) {
+        done[c] = 1;
+        is_coarse[c] = 1;
+        for (int t = St.rptr[c]; t < St.rptr[c + 1]; t++) {
             const int f = St.cind[t];
-            if (visited[f]) continue;
-            visited[f] = 1;
+            if (done[f]) continue;
+            done[f] = 1;
             is_coarse[f] = 0;
-            for (int u = S.rptr[f]; u < S.rptr[f + 1]; u++) {
-                const int k = S.cind[u];
-                if (visited[k]) continue;
-                const int idx = where[k];
-                if (idx <= pos) printf("Warning 1: %d %d\n", idx, pos);
-                card[idx]++;
-                const int v = card[idx];
-                int obj;
-                if (v > maxc) {
-                    maxc = v;
-                    if (bptr[v] > pos + 1) printf("Warning 2: %d %d\n", bptr[v], pos + 1);
-                    obj = pos + 1;
-                    bptr.push_back(pos + 1);
-                    bptr[maxc] = pos + 2;
-                } else if (bptr[v] > pos + 1) {
-                    obj = bptr[v];
-                    bptr[v] += 1;
-                } else {
-                    obj = pos + 1;
-                    bptr[v] = pos + 2;
-                }
-                exchange(idx, obj);
-            }
+            // every open point that f depends on now influences one more new fine point
+            for (int u = S.rptr[f]; u < S.rptr[f + 1]; u++)
+                if (!done[S.cind[u]]) runs.raise(S.cind[u]);
         }
-        for (int u = S.rptr[cpt]; u < S.rptr[cpt + 1]; u++) {
-            const int k = S.cind[u];
-            if (visited[k]) continue;
-            const int idx = where[k];
-            if (card[idx] == 0) continue;
-            card[idx]--;
-            const int obj = bptr[card[idx] + 1] - 1;
-            bptr[card[idx] + 1] -= 1;
-            exchange(idx, obj);
-        }
-        pos++;
+        for (int u = S.rptr[c]; u < S.rptr[c + 1]; u++)
+            if (!done[S.cind[u]]) runs.lower(S.cind[u]);
     }
 }
 
@@ -281,10 +292,8 @@ void rs_first_pass(const CsrD &S, const Pattern &St, std::vector<int> &is_coarse
 void rs_second_pass(const CsrD &S, std::vector<int> &is_coarse) {
     const int N = S.n;
     for (int i = 0; i < N; i++) {
-        if (is_coarse[i] == -38) {
-            fprintf(stderr, "sagb: unclassified point in the coarsening\n");
-            exit(1);  // the reference exits here as well (helper_multigrid.hpp:384)
-        }
+        if (is_coarse[i] == kUnclassified)  // the reference exits here (helper_multigrid.hpp:384)
+            throw SetupError{"coarsening left point " + std::to_string(i) + " unclassified"};
         if (is_coarse[i]) continue;
         for (int j = S.rptr[i]; j < S.rptr[i + 1]; j++) {
             const int f = S.cind[j];
@@ -400,9 +409,11 @@ static CsrD interpolation(const CsrD &A, const CsrD &S, const CsrD &W, const std
     });
     for (int i = 0; i < N; i++) {
         for (int k = 0; k < warn[i]; k++) printf("1 amk = 0\n");
-        if (stop[i]) {
+        if (stop[i]) {  // the reference prints this and exits (helper_multigrid.hpp:518)
             printf("2 amk = 0\n");
-            exit(1);  // as the reference (helper_multigrid.hpp:518)
+            fflush(stdout);
+            throw SetupError{"interpolation: fine row " + std::to_string(i) +
+                             " has a strong fine neighbour with no coupling to its coarse points (2 amk = 0)"};
         }
     }
     return P;
@@ -517,10 +528,7 @@ static CsrD galerkin(const CsrD &A, const CsrD &P, const CsrD &R) {
 }
 
 void rs_level(const CsrD &A, double theta, CsrD &CA, CsrD &P, CsrD &R) {
-    if (theta <= 0 || 1 < theta) {
-        printf("Error: Theta must be in 0 < theta <= 1\n");
-        exit(EXIT_FAILURE);
-    }
+    if (theta <= 0 || 1 < theta) throw SetupError{"Theta must be in 0 < theta <= 1"};
     CsrD S, W;
     strong_weak(A, theta, S, W);
     Pattern St = transpose_pattern(S);
