@@ -108,9 +108,47 @@ static RedBuf &red_buf(Ctx &c) {
     return rb;
 }
 
+// ------------------------------------------- sequential-order reductions
+//
+// The sequential-order mode (SA_OPT_FP_EXACT) follows the reference's FP loops
+// operation for operation: every product and sum rounded on its own (no fused
+// multiply-add, which the compiler would otherwise form from a * b + c), each
+// dot product and norm summed by one thread in index order as the reference's
+// single-threaded build does (blas1.hpp:74-88).  It is a parity mode: one
+// thread per reduction is slow at large sizes.
+
+template <typename T>
+__device__ __forceinline__ T rn_mul(T a, T b) {
+    if constexpr (sizeof(T) == 8) return __dmul_rn(a, b);
+    else return __fmul_rn(a, b);
+}
+template <typename T>
+__device__ __forceinline__ T rn_add(T a, T b) {
+    if constexpr (sizeof(T) == 8) return __dadd_rn(a, b);
+    else return __fadd_rn(a, b);
+}
+template <typename T>
+__device__ __forceinline__ T rn_sub(T a, T b) {
+    if constexpr (sizeof(T) == 8) return __dsub_rn(a, b);
+    else return __fsub_rn(a, b);
+}
+
+// blas1::Dot / Nrm2 (blas1.hpp:74-88) in index order
+template <typename T, bool NRM>
+__global__ void k_dot_seq(int n, const T *__restrict__ x, const T *__restrict__ y, T *out) {
+    if (threadIdx.x || blockIdx.x) return;
+    T acc = 0;
+    for (int i = 0; i < n; i++) acc = rn_add(acc, rn_mul(x[i], NRM ? x[i] : y[i]));
+    *out = NRM ? (T)sqrt(acc) : acc;
+}
+
 void nrm2_f64_dev(Ctx &c, const double *x, int n, double *d_out) {
-    RedBuf &rb = red_buf(c);
-    k_nrm2_f64<<<rb.grid, kRedThreads, 0, c.stream>>>(n, x, rb.partials, rb.counter, d_out);
+    if (c.fp_exact) {
+        k_dot_seq<double, true><<<1, 32, 0, c.stream>>>(n, x, x, d_out);
+    } else {
+        RedBuf &rb = red_buf(c);
+        k_nrm2_f64<<<rb.grid, kRedThreads, 0, c.stream>>>(n, x, rb.partials, rb.counter, d_out);
+    }
     c.launches++;
 }
 
@@ -391,19 +429,24 @@ k_mgs_fp(int n, int k, int j, int m, const T *__restrict__ V, T *__restrict__ w,
     }
 }
 
-template <typename T>
+template <typename T, bool EXACT = false>
 __global__ void k_givens_fp(int j, int m, T *H, T *c, T *s, T *e, FScal<T> *sc, StepInfo *info,
                             unsigned *flags) {
     T *Hj = H + (size_t)j * (m + 1);
     if (Hj[j + 1] == 0) atomicOr(flags, ST_DIVZERO);
     sc->a_scal = (T)1 / Hj[j + 1];
-    for (int k = 0; k < j; k++) {
+    for (int k = 0; k < j; k++) {  // Grot (blas1.hpp:302-307)
         const T t = Hj[k];
-        Hj[k] = c[k] * t - s[k] * Hj[k + 1];
-        Hj[k + 1] = s[k] * t + c[k] * Hj[k + 1];
+        if constexpr (EXACT) {
+            Hj[k] = rn_sub(rn_mul(c[k], t), rn_mul(s[k], Hj[k + 1]));
+            Hj[k + 1] = rn_add(rn_mul(s[k], t), rn_mul(c[k], Hj[k + 1]));
+        } else {
+            Hj[k] = c[k] * t - s[k] * Hj[k + 1];
+            Hj[k + 1] = s[k] * t + c[k] * Hj[k + 1];
+        }
     }
-    const T aa = Hj[j], bb = Hj[j + 1];
-    const T r = sqrt(aa * aa + bb * bb);
+    const T aa = Hj[j], bb = Hj[j + 1];  // Ggen (blas1.hpp:292-300)
+    const T r = EXACT ? (T)sqrt(rn_add(rn_mul(aa, aa), rn_mul(bb, bb))) : (T)sqrt(aa * aa + bb * bb);
     c[j] = aa / r;
     s[j] = -bb / r;
     Hj[j] = r;
@@ -426,26 +469,41 @@ __global__ void k_scal_fp(int n, const FScal<T> *__restrict__ sc, T *__restrict_
 }
 
 // blas2::Trsv (blas2.hpp:25-34)
-template <typename T>
+template <typename T, bool EXACT = false>
 __global__ void k_trsv_fp(int jn, int m, const T *H, const T *e, T *y) {
     for (int i = jn - 1; i >= 0; i--) {
         T t = e[i];
-        for (int q = jn - 1; q > i; q--) t -= H[(size_t)q * (m + 1) + i] * y[q];
+        for (int q = jn - 1; q > i; q--) {
+            if constexpr (EXACT) t = rn_sub(t, rn_mul(H[(size_t)q * (m + 1) + i], y[q]));
+            else t -= H[(size_t)q * (m + 1) + i] * y[q];
+        }
         y[i] = t / H[(size_t)i * (m + 1) + i];
     }
 }
 
 // x += y_k Z_k (Axpy<double>, or AxpyFD for float: (double)(y_k * z))
-template <typename T>
+template <typename T, bool EXACT = false>
 __global__ void k_xupd_fp(int n, int jn, const T *__restrict__ y, const T *__restrict__ Z, double *__restrict__ x) {
     __shared__ T sy[64];
     if (threadIdx.x < jn) sy[threadIdx.x] = y[threadIdx.x];
     __syncthreads();
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         double xi = x[i];
-        for (int k = 0; k < jn; k++) xi += (double)(sy[k] * Z[(size_t)k * n + i]);
+        for (int k = 0; k < jn; k++) {
+            if constexpr (EXACT) xi = __dadd_rn(xi, (double)rn_mul(sy[k], Z[(size_t)k * n + i]));
+            else xi += (double)(sy[k] * Z[(size_t)k * n + i]);
+        }
         x[i] = xi;
     }
+}
+
+// w += (-h) x with h read on the device (Axpy, blas1.hpp:50-54), each
+// product and sum rounded on its own
+template <typename T>
+__global__ void k_axpy_neg_rn(int n, const T *__restrict__ hp, const T *__restrict__ x, T *__restrict__ w) {
+    const T a = -*hp;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        w[i] = rn_add(w[i], rn_mul(a, x[i]));
 }
 
 // ================================================================ driver
@@ -773,6 +831,11 @@ class FpSolver : public SolverBase {
                   SolveStats &st) override {
         const int m = p_.m, N = N_;
         const int gb = grid_for(c_, N);
+        const bool exact = c_.fp_exact;
+        if (exact != graphs_exact_) {  // the step graphs hold one mode's kernels
+            graphs_.clear();
+            graphs_exact_ = exact;
+        }
         k_begin_fp<T><<<1, 1, 0, c_.stream>>>(e0d, nrm_b, p_.eps, sc_, e_, m);
         k_v0_fp<T><<<gb, kRedThreads, 0, c_.stream>>>(N, r, sc_, V_);
         c_.launches += 2;
@@ -782,18 +845,32 @@ class FpSolver : public SolverBase {
             T *Hj = H_ + (size_t)j * (m + 1);
             StepInfo inf = step(j, [&] {
                 vcycle(c_, *M_, vj, zj);
-                by_group(A_->group, [&](auto G) {
-                    const long long thr = (long long)N * G.value;
-                    const int blocks = (int)((thr + kRedThreads - 1) / kRedThreads);
-                    k_spmv_dot_fp<T, G.value><<<blocks, kRedThreads, 0, c_.stream>>>(
-                        N, A_->rptr, A_->cind, (const T *)A_->val, zj, w, V_, partials_, counter_, Hj);
-                });
-                for (int k = 0; k < j; k++)
-                    k_mgs_fp<T, false><<<gb, kRedThreads, 0, c_.stream>>>(N, k, j, m, V_, w, H_, partials_, counter_);
-                k_mgs_fp<T, true><<<gb, kRedThreads, 0, c_.stream>>>(N, j, j, m, V_, w, H_, partials_, counter_);
-                k_givens_fp<T><<<1, 1, 0, c_.stream>>>(j, m, H_, cs_, sn_, e_, sc_, info_d_, c_.d_flags);
+                if (exact) {
+                    // the reference's order: SpMV, then per k Dot and Axpy, Nrm2
+                    spmv(c_, *A_, zj, w);
+                    for (int k = 0; k <= j; k++) {
+                        k_dot_seq<T, false><<<1, 32, 0, c_.stream>>>(N, V_ + (size_t)k * N, w, Hj + k);
+                        k_axpy_neg_rn<T><<<gb, kRedThreads, 0, c_.stream>>>(N, Hj + k, V_ + (size_t)k * N, w);
+                    }
+                    k_dot_seq<T, true><<<1, 32, 0, c_.stream>>>(N, w, w, Hj + j + 1);
+                    k_givens_fp<T, true><<<1, 1, 0, c_.stream>>>(j, m, H_, cs_, sn_, e_, sc_, info_d_, c_.d_flags);
+                    c_.launches += 2 * j + 4;
+                } else {
+                    by_group(A_->group, [&](auto G) {
+                        const long long thr = (long long)N * G.value;
+                        const int blocks = (int)((thr + kRedThreads - 1) / kRedThreads);
+                        k_spmv_dot_fp<T, G.value><<<blocks, kRedThreads, 0, c_.stream>>>(
+                            N, A_->rptr, A_->cind, (const T *)A_->val, zj, w, V_, partials_, counter_, Hj);
+                    });
+                    for (int k = 0; k < j; k++)
+                        k_mgs_fp<T, false><<<gb, kRedThreads, 0, c_.stream>>>(N, k, j, m, V_, w, H_, partials_,
+                                                                             counter_);
+                    k_mgs_fp<T, true><<<gb, kRedThreads, 0, c_.stream>>>(N, j, j, m, V_, w, H_, partials_, counter_);
+                    k_givens_fp<T><<<1, 1, 0, c_.stream>>>(j, m, H_, cs_, sn_, e_, sc_, info_d_, c_.d_flags);
+                    c_.launches += j + 3;
+                }
                 k_scal_fp<T><<<gb, kRedThreads, 0, c_.stream>>>(N, sc_, w);
-                c_.launches += j + 4;
+                c_.launches++;
             });
             st.flags |= inf.flags;
             st.history.push_back(inf.relres);
@@ -809,8 +886,13 @@ class FpSolver : public SolverBase {
                 break;
             }
         }
-        k_trsv_fp<T><<<1, 1, 0, c_.stream>>>(j, m, H_, e_, y_);
-        k_xupd_fp<T><<<gb, kRedThreads, 0, c_.stream>>>(N, j, y_, Z_, x);
+        if (exact) {
+            k_trsv_fp<T, true><<<1, 1, 0, c_.stream>>>(j, m, H_, e_, y_);
+            k_xupd_fp<T, true><<<gb, kRedThreads, 0, c_.stream>>>(N, j, y_, Z_, x);
+        } else {
+            k_trsv_fp<T><<<1, 1, 0, c_.stream>>>(j, m, H_, e_, y_);
+            k_xupd_fp<T><<<gb, kRedThreads, 0, c_.stream>>>(N, j, y_, Z_, x);
+        }
         c_.launches += 2;
         SAGB_CUDA(cudaStreamSynchronize(c_.stream));
         (void)dumps;
@@ -825,6 +907,7 @@ class FpSolver : public SolverBase {
     FScal<T> *sc_ = nullptr;
     T *partials_ = nullptr;
     unsigned *counter_ = nullptr;
+    bool graphs_exact_ = false;
 };
 
 std::unique_ptr<Solver> make_solver(Ctx &c, int vt, const DevCsr *dA, const DevCsr *A, DevAmg *M,

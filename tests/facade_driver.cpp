@@ -1,7 +1,9 @@
 // A driver written against the senk facade (include/senk): reads a Matrix
-// Market file, scales it, builds the FP64 and integer AMG preconditioners,
-// picks F by the reference's rule and solves with Restarted(FGMRESflex) or
-// Restarted(FGMRES<double>).  Arguments: <matrix.mtx> <0: FP64, 2: int> <m>.
+// Market file, scales it, builds the FP64, FP32 or integer AMG preconditioner,
+// picks F by the reference's rule and solves with Restarted(FGMRES<double>),
+// Restarted(FGMRES<float>) or Restarted(FGMRESflex), as Work/main.cpp does.
+// Arguments: <matrix.mtx> <0: FP64, 1: FP32-mixed, 2: int> <m> [b.f64], where
+// the optional file holds the unscaled right-hand side as raw FP64 values.
 // Prints "[Iter] : n" and "# [Res] : r" like the reference's driver.
 #include <cmath>
 #include <cstdio>
@@ -17,12 +19,18 @@
 using namespace senk;
 
 int main(int argc, char **argv) {
-    if (argc != 4) return 1;
+    if (argc != 4 && argc != 5) return 1;
     CSRMat *A = io::ReadMM(argv[1], true, false);
     const int kind = std::atoi(argv[2]), m = std::atoi(argv[3]);
     const int N = A->N;
     double *b = utils::SafeMalloc<double>(N);
-    for (int i = 0; i < N; i++) b[i] = 1.0 + 0.5 * std::sin(0.1 * i);
+    if (argc == 5) {
+        FILE *f = std::fopen(argv[4], "rb");
+        if (!f || std::fread(b, sizeof(double), N, f) != (size_t)N) return 2;
+        std::fclose(f);
+    } else {
+        for (int i = 0; i < N; i++) b[i] = 1.0 + 0.5 * std::sin(0.1 * i);
+    }
     A->LMax1Scaling(b);
     const double nrm_b = blas1::Nrm2<double>(b, N);
     auto *dA = new CSR<double>(A);
@@ -41,6 +49,17 @@ int main(int argc, char **argv) {
         timer->Elapsed();
         delete S;
         delete M;
+    } else if (kind == 1) {
+        auto *fA = new CSR<float>(A);
+        auto *M = new dfAMG<CSR<float>, SOR<ldtri::CSR<float>, CSR<float>>, float>(A, fA, param);
+        auto *inner = new FGMRES<float>(fA, m, 1e-10, M);
+        auto *S = new Restarted(dA, inner, 1000 / m, 1e-10);
+        timer->Restart();
+        cv = S->Solve(b, nrm_b, x);
+        timer->Elapsed();
+        delete S;
+        delete M;
+        delete fA;
     } else {
         auto *iA = new CSR<Fixed<30>>(A);
         auto *M = new dfAMG<CSR<double>, SOR<ldtri::CSR<double>, CSR<double>>, double>(A, dA, param);

@@ -211,3 +211,85 @@ def test_int_vcycle_vs_oracle_3d(ctx, n):
     of.lib().or_vcycle_i32(C.byref(h), of.ptr(vin, of.i32p), of.ptr(ref, of.i32p))
     np.testing.assert_array_equal(M.precondition(vin), ref)
     M.close()
+
+
+FP32_CASES = ["p2d64", "p3d16", "cd3d16", "vc3d16", "an2d64", "s27n14"]
+
+
+@pytest.mark.parametrize("case", FP32_CASES)
+def test_fp32_vcycle(ctx, case):
+    """dfAMG<CSR<float>, SOR<ldtri::CSR<float>, ...>, float>::Precondition
+    (INTAMG.hpp:13-134 with T = float) on the reference's own float hierarchy
+    input: bit for bit in the sequential-order mode, within float rounding
+    otherwise."""
+    g = of.load_golden(case)
+    ctx.set_option(sagb.OPT_FP_EXACT, 1)
+    try:
+        M = _amg(ctx, g, case, sagb.F32)
+        np.testing.assert_array_equal(M.precondition(g["f_t_V_in"]), g["f_t_V_out"])
+        if "f_t_S0_LD_out" in g:
+            np.testing.assert_array_equal(M.sweep(0, g["f_t_V_in"]), g["f_t_S0_LD_out"])
+        if "f_t_LU_in" in g:
+            np.testing.assert_array_equal(M.coarse_solve(g["f_t_LU_in"]), g["f_t_LU_out"])
+        M.close()
+    finally:
+        ctx.set_option(sagb.OPT_FP_EXACT, 0)
+    M = _amg(ctx, g, case, sagb.F32)
+    out = M.precondition(g["f_t_V_in"]).astype(np.float64)
+    ref = g["f_t_V_out"].astype(np.float64)
+    assert np.linalg.norm(out - ref) <= 1e-5 * np.linalg.norm(ref)
+    M.close()
+
+
+RULE_CASES = ["p2d64", "p3d16", "cd3d16", "vc3d16", "an2d64", "s27n14", "p3d16bj"]
+
+
+@pytest.mark.parametrize("case", RULE_CASES)
+def test_rule_bits(ctx, case):
+    """The reference's bit rule (Work/main.cpp:153-161): one FP64 V-cycle of
+    the scaled right-hand side, F from max|c| / ||b||.  The V-cycle output c is
+    the reference's bit for bit in the sequential-order mode and within 1e-12
+    otherwise; the ratio and the bit are the reference's."""
+    g = of.load_golden(case)
+    b, nrm_b = g["b_scaled"], float(g["nrm_b"][0])
+    ref_c = g["c_bitrule"]
+    ref_q = np.abs(ref_c).max() / nrm_b
+    for exact in (1, 0):
+        ctx.set_option(sagb.OPT_FP_EXACT, exact)
+        try:
+            M = _amg(ctx, g, case, sagb.F64)
+            c_gpu = M.precondition(b)
+            if exact:
+                np.testing.assert_array_equal(c_gpu, ref_c)
+            else:
+                assert np.linalg.norm(c_gpu - ref_c) <= FP_TOL * np.linalg.norm(ref_c)
+            q = sagb.rule_ratio(ctx, M, b, nrm_b)
+            assert abs(q - ref_q) <= 1e-12 * ref_q
+            assert sagb.rule_bits(ctx, M, b, nrm_b) == int(g["bit"][0])
+            M.close()
+        finally:
+            ctx.set_option(sagb.OPT_FP_EXACT, 0)
+
+
+@pytest.mark.parametrize("case,prec", [("p2d64", sagb.F64), ("p3d16", sagb.F64), ("cd3d16", sagb.F64),
+                                       ("vc3d16", sagb.F64), ("s27n14", sagb.F64), ("p3d16", sagb.F32),
+                                       ("cd3d16", sagb.F32)])
+def test_fp_full_solve_sequential_order(ctx, case, prec):
+    """Restarted(FGMRES<double|float>) with dfAMG in the sequential-order mode
+    (every reduction in the reference's index order, no fused multiply-add):
+    the iteration count and the solution are the reference's, within 1e-12
+    relative (FP64) or float rounding carried through FP64 refinement (FP32)."""
+    g = of.load_golden(case)
+    key = "fp64" if prec == sagb.F64 else "fp32"
+    ctx.set_option(sagb.OPT_FP_EXACT, 1)
+    try:
+        S, keep = _solver(ctx, g, case, prec)
+        x = np.zeros(len(g["b_scaled"]))
+        it, conv = S.solve(g["b_scaled"], float(g["nrm_b"][0]), x)
+        S.close()
+    finally:
+        ctx.set_option(sagb.OPT_FP_EXACT, 0)
+    assert conv == 1 and it == int(g[key + "_iter"][0]), (it, int(g[key + "_iter"][0]))
+    ref = g[key + "_x"]
+    err = np.linalg.norm(x - ref) / np.linalg.norm(ref)
+    assert err <= (FP_TOL if prec == sagb.F64 else 1e-6), err
