@@ -364,6 +364,33 @@ int sa_batch_level_info(sa_batch B, int level, int op, int *n, int *m, int64_t *
 int sa_batch_solve(sa_ctx ctx, sa_batch B, const sa_solver_params *p, const int *bits, const double *b,
                    const double *nrm_b, double *x, int *iters, int *converged, int *final_bits);
 
+/* ---------------------------------- floating-point siblings of a batch
+ * FP64-AMG-FGMRES and FP32-mixed AMG-FGMRES of the same systems, set up from an
+ * integer batch's coarsening and smoother parameters and run by the same
+ * batched GPU design (one launch per operation over all systems, CUDA-graph
+ * Arnoldi steps, programmatic dependent launch, autotuned lanes per row), so
+ * that the integer solver can be compared with an FP64 solver on equal terms.
+ * Per system: dfAMG<CSR<T>, SOR<ldtri::CSR<T>, CSR<T>>, T> in the multicolour
+ * order of the integer batch's colouring (Library/preconditioner/INTAMG.hpp:13-134),
+ * FGMRES<double> (Library/solver/gmres.hpp:19-98) or FGMRES<float>
+ * (gmres.hpp:101-180), Restarted (Library/solver/irsolver.hpp:27-43).
+ * Vectors are laid out as the integer batch's; precondition in/out are
+ * double (SA_F64) or float (SA_F32); b and x are double. */
+typedef struct sa_batch_fp_set *sa_batch_fp;
+/* precision: SA_F64 or SA_F32; threads: host threads for the per-system
+ * dfAMG setups (0: all).  The integer batch must outlive the handle. */
+int sa_batch_fp_create(sa_ctx ctx, sa_batch B, int precision, int threads, sa_batch_fp *out);
+int sa_batch_fp_destroy(sa_batch_fp F);
+/* dfAMG::Precondition (INTAMG.hpp:86-134) of every system and right-hand side */
+int sa_batch_fp_precondition(sa_ctx ctx, sa_batch_fp F, const void *in, void *out);
+/* lanes per row of each operator and the sweep form of each level, timed */
+int sa_batch_fp_autotune(sa_ctx ctx, sa_batch_fp F, int reps);
+/* milliseconds per V-cycle as the solver runs it */
+int sa_batch_fp_time_vcycle(sa_ctx ctx, sa_batch_fp F, int reps, float *ms);
+/* Restarted(FGMRES<T>) per pair; nrm_b per pair; iters / converged per pair (optional) */
+int sa_batch_fp_solve(sa_ctx ctx, sa_batch_fp F, const sa_solver_params *p, const double *b, const double *nrm_b,
+                      double *x, int *iters, int *converged);
+
 /* start (on = 1) or stop (0) the profiler's collection range: a profiler
  * started with collection off records only the launches in between */
 int sa_profiler_range(int on);

@@ -19,7 +19,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 HOST_SRC = ["host/amg_setup.cpp", "host/schedule.cpp", "host/generators.cpp", "host/features.cpp",
             "host/batch_setup.cpp"]
-CUDA_SRC = ["cuda/spmv.cu", "cuda/trsv.cu", "cuda/amg.cu", "cuda/krylov.cu", "cuda/mlp.cu", "cuda/batch.cu",
+CUDA_SRC = ["cuda/spmv.cu", "cuda/trsv.cu", "cuda/amg.cu", "cuda/krylov.cu", "cuda/mlp.cu", "cuda/batch.cu", "cuda/batch_fp.cu",
             "cuda/rs_setup.cu", "capi.cu"]
 
 

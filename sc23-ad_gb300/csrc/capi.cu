@@ -88,6 +88,11 @@ struct sa_batch_set {
     std::shared_ptr<BatchHierarchy> h;
     std::unique_ptr<BatchEngine> eng;
 };
+struct sa_batch_fp_set {
+    std::shared_ptr<BatchHierarchy> h;
+    int nrhs = 1;
+    std::unique_ptr<BatchFpEngine> eng;
+};
 
 // ------------------------------------------------------------------ helpers
 
@@ -1439,6 +1444,84 @@ extern "C" int sa_batch_level_info(sa_batch B, int level, int op, int *n, int *m
 extern "C" int sa_profiler_range(int on) {
     SA_GUARD_BEGIN
     SAGB_CUDA(on ? cudaProfilerStart() : cudaProfilerStop());
+    return SA_OK;
+    SA_GUARD_END
+}
+
+// --------------------------------------- floating-point siblings of a batch
+
+extern "C" int sa_batch_fp_create(sa_ctx ctx, sa_batch B, int precision, int threads, sa_batch_fp *out) {
+    if (!ctx || !B || !out) return fail(SA_ERR_ARG, "null argument");
+    if (precision != SA_F64 && precision != SA_F32) return fail(SA_ERR_ARG, "precision must be SA_F64 or SA_F32");
+    SA_GUARD_BEGIN
+    SAGB_CUDA(cudaSetDevice(ctx->c.device));
+    auto F = std::make_unique<sa_batch_fp_set>();
+    F->h = B->h;
+    F->nrhs = B->eng->nrhs();
+    F->eng = std::make_unique<BatchFpEngine>(ctx->c, B->h, precision == SA_F64 ? VT_F64 : VT_F32, F->nrhs,
+                                             threads);
+    SAGB_CUDA(cudaDeviceSynchronize());
+    *out = F.release();
+    return SA_OK;
+    SA_GUARD_END
+}
+
+extern "C" int sa_batch_fp_destroy(sa_batch_fp F) {
+    delete F;
+    return SA_OK;
+}
+
+extern "C" int sa_batch_fp_precondition(sa_ctx ctx, sa_batch_fp F, const void *in, void *out) {
+    if (!ctx || !F || !in || !out) return fail(SA_ERR_ARG, "null argument");
+    SA_GUARD_BEGIN
+    Ctx &c = ctx->c;
+    const size_t bytes = vt_size(F->eng->precision()) * F->eng->rows() * F->nrhs;
+    Staged si(c, in, bytes, true, false);
+    Staged so(c, out, bytes, false, true);
+    F->eng->precondition(si.get(), so.get());
+    so.finish();
+    return SA_OK;
+    SA_GUARD_END
+}
+
+extern "C" int sa_batch_fp_autotune(sa_ctx ctx, sa_batch_fp F, int reps) {
+    if (!ctx || !F || reps < 1) return fail(SA_ERR_ARG, "invalid argument");
+    SA_GUARD_BEGIN
+    F->eng->autotune(reps);
+    return SA_OK;
+    SA_GUARD_END
+}
+
+extern "C" int sa_batch_fp_time_vcycle(sa_ctx ctx, sa_batch_fp F, int reps, float *ms) {
+    if (!ctx || !F || !ms || reps < 1) return fail(SA_ERR_ARG, "invalid argument");
+    SA_GUARD_BEGIN
+    *ms = F->eng->time_vcycle(reps);
+    return SA_OK;
+    SA_GUARD_END
+}
+
+extern "C" int sa_batch_fp_solve(sa_ctx ctx, sa_batch_fp F, const sa_solver_params *p, const double *b,
+                                 const double *nrm_b, double *x, int *iters, int *converged) {
+    if (!ctx || !F || !p || !b || !nrm_b || !x) return fail(SA_ERR_ARG, "null argument");
+    if (p->m < 1 || p->m > 64 || p->max_outer < 1 || !(p->eps > 0)) return fail(SA_ERR_ARG, "invalid solver parameters");
+    SA_GUARD_BEGIN
+    Ctx &c = ctx->c;
+    KrylovParams kp;
+    kp.m = p->m;
+    kp.eps = p->eps;
+    kp.max_outer = p->max_outer;
+    kp.explicit_check = p->explicit_stop;
+    const size_t bytes = sizeof(double) * F->eng->rows() * F->nrhs;
+    Staged sb(c, b, bytes, true, false);
+    Staged sx(c, x, bytes, true, true);
+    BatchStats st;
+    F->eng->solve(kp, (const double *)sb.get(), nrm_b, (double *)sx.get(), st);
+    sx.finish();
+    const int P = F->h->S * F->nrhs;
+    for (int q = 0; q < P; q++) {
+        if (iters) iters[q] = st.iters[q];
+        if (converged) converged[q] = st.converged[q];
+    }
     return SA_OK;
     SA_GUARD_END
 }

@@ -55,6 +55,7 @@ BatchHierarchy build_batch(const std::vector<CsrD> &systems, double theta, int m
     sm.multicolor = 1;
     sm.max_colours = max_colours;
     sm.coarse_colours = coarse_colours;
+    B.sm = sm;
     if (big_chain)
         for (int s = 0; s < S; s++)
             if (src[s] == s && systems[s].n >= big_rows)
@@ -208,5 +209,146 @@ BatchHierarchy build_batch(const std::vector<CsrD> &systems, double theta, int m
     }
     return B;
 }
+
+// ------------------------------------------------ floating-point sibling
+
+template <typename T>
+static void start_t(BatchCsrT<T> &B, int m) {
+    B = BatchCsrT<T>();
+    B.m = m;
+    B.rptr.push_back(0);
+}
+
+template <typename T>
+static void append_t(BatchCsrT<T> &B, const CsrT<T> &M, int col_off) {
+    for (int i = 0; i < M.n; i++) {
+        for (int j = M.rptr[i]; j < M.rptr[i + 1]; j++) {
+            B.cind.push_back(M.cind[j] + col_off);
+            B.val.push_back(M.val[j]);
+        }
+        B.rptr.push_back((int)B.cind.size());
+    }
+    B.n += M.n;
+}
+
+template <typename T>
+static FpHierarchy<T> fp_hierarchy(const CsrD &A, const RsChain &chain, const SmootherSpec &sm);
+template <>
+FpHierarchy<double> fp_hierarchy<double>(const CsrD &A, const RsChain &chain, const SmootherSpec &sm) {
+    return build_f64_hierarchy(A, chain, sm);
+}
+template <>
+FpHierarchy<float> fp_hierarchy<float>(const CsrD &A, const RsChain &chain, const SmootherSpec &sm) {
+    return build_f32_hierarchy(A, chain, sm);
+}
+
+template <typename T>
+BatchFp<T> build_batch_fp(const BatchHierarchy &B, int threads) {
+    const int S = B.S, Dmax = B.Dmax;
+    // per-system hierarchies; systems that repeat another share its hierarchy
+    std::vector<std::shared_ptr<FpHierarchy<T>>> hs(S);
+    std::vector<int> src(S);
+    for (int s = 0; s < S; s++) {
+        src[s] = s;
+        for (int t = 0; t < s; t++)
+            if (B.hi[t] == B.hi[s]) {
+                src[s] = t;
+                break;
+            }
+    }
+    std::atomic<int> next{0};
+    std::vector<std::string> errs(S);
+    const int T_ = std::max(1, std::min(threads > 0 ? threads : (int)std::thread::hardware_concurrency(), S));
+    auto work = [&]() {
+        std::unique_ptr<HostSerial> serial(T_ > 1 ? new HostSerial() : nullptr);
+        for (;;) {
+            const int s = next.fetch_add(1);
+            if (s >= S) return;
+            if (src[s] != s) continue;
+            try {
+                hs[s] = std::make_shared<FpHierarchy<T>>(fp_hierarchy<T>(*B.A_sys[s], *B.chain[s], B.sm));
+            } catch (const SetupError &e) {
+                errs[s] = e.msg;
+            }
+        }
+    };
+    std::vector<std::thread> pool;
+    for (int t = 1; t < T_; t++) pool.emplace_back(work);
+    work();
+    for (auto &t : pool) t.join();
+    for (int s = 0; s < S; s++)
+        if (!errs[s].empty()) throw SetupError{"system " + std::to_string(s) + ": " + errs[s]};
+    for (int s = 0; s < S; s++) hs[s] = hs[src[s]];
+    // the integer batch's level order: smoothing systems first, then LU systems
+    std::vector<std::vector<int>> order(Dmax + 1);
+    for (int l = 0; l <= Dmax; l++) {
+        for (int s = 0; s < S; s++)
+            if (B.depth[s] > l) order[l].push_back(s);
+        for (int s = 0; s < S; s++)
+            if (B.depth[s] == l) order[l].push_back(s);
+    }
+    BatchFp<T> F;
+    F.lv.resize(Dmax);
+    for (int l = 0; l < Dmax; l++) {
+        BatchLevelT<T> &L = F.lv[l];
+        const int n_smooth = B.lv[l].n_smooth;
+        start_t(L.A, n_smooth);
+        start_t(L.LD, n_smooth);
+        start_t(L.U, n_smooth);
+        start_t(L.P, B.n_level[l + 1]);
+        std::vector<int> ncol;
+        for (int s : order[l]) {
+            const FpHierarchy<T> &h = *hs[s];
+            if (h.depth != B.depth[s]) throw SetupError{"FP hierarchy depth differs from the integer batch's"};
+            if (h.depth <= l) continue;
+            const int off = B.offset[l][s];
+            append_t(L.A, l == 0 ? h.A0 : h.CA[l - 1], off);
+            append_t(L.LD, h.LD[l], off);
+            append_t(L.U, h.U[l], off);
+            append_t(L.P, h.P[l], B.offset[l + 1][s]);
+            int nc = 0;
+            for (int c : h.colour[l]) nc = std::max(nc, c + 1);
+            if ((int)ncol.size() < nc) ncol.resize(nc, 0);
+            for (int c : h.colour[l]) ncol[c]++;
+        }
+        start_t(L.R, n_smooth);
+        for (int s : order[l + 1]) append_t(L.R, hs[s]->R[l], B.offset[l][s]);
+        L.colour_ptr.assign(ncol.size() + 1, 0);
+        for (size_t c = 0; c < ncol.size(); c++) L.colour_ptr[c + 1] = L.colour_ptr[c] + ncol[c];
+        L.colour_rows.assign(n_smooth, 0);
+        std::vector<int> fill(L.colour_ptr.begin(), L.colour_ptr.end() - 1);
+        for (int s : order[l]) {
+            const FpHierarchy<T> &h = *hs[s];
+            if (h.depth <= l) continue;
+            const int off = B.offset[l][s];
+            for (int i = 0; i < (int)h.colour[l].size(); i++) L.colour_rows[fill[h.colour[l][i]]++] = off + i;
+        }
+        for (size_t c = 0; c < ncol.size(); c++)
+            std::sort(L.colour_rows.begin() + L.colour_ptr[c], L.colour_rows.begin() + L.colour_ptr[c + 1]);
+    }
+    for (int s = 0; s < S; s++) {
+        const FpHierarchy<T> &h = *hs[s];
+        BatchLUT<T> lu;
+        lu.sys = s;
+        lu.level = h.depth;
+        lu.n = h.LUL.n;
+        lu.offset = B.offset[h.depth][s];
+        const int n = lu.n;
+        lu.L.assign((size_t)n * n, T(0));
+        lu.U.assign((size_t)n * n, T(0));
+        lu.dinv.assign(n, T(0));
+        for (int i = 0; i < n; i++) {
+            for (int j = h.LUL.rptr[i]; j < h.LUL.rptr[i + 1]; j++) lu.L[(size_t)i * n + h.LUL.cind[j]] = h.LUL.val[j];
+            if (h.LUU.rptr[i + 1] > h.LUU.rptr[i]) lu.dinv[i] = h.LUU.val[h.LUU.rptr[i]];
+            for (int j = h.LUU.rptr[i] + 1; j < h.LUU.rptr[i + 1]; j++)
+                lu.U[(size_t)i * n + h.LUU.cind[j]] = h.LUU.val[j];
+        }
+        F.lu.push_back(std::move(lu));
+    }
+    return F;
+}
+
+template BatchFp<double> build_batch_fp<double>(const BatchHierarchy &, int);
+template BatchFp<float> build_batch_fp<float>(const BatchHierarchy &, int);
 
 }  // namespace sagb

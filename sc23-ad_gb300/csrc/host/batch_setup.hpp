@@ -60,7 +60,49 @@ struct BatchHierarchy {
     std::vector<std::shared_ptr<RsChain>> chain;    // per system (for the FP64 rule V-cycle)
     std::vector<std::shared_ptr<CsrD>> A_sys;       // per system scaled fine matrix
     std::vector<std::shared_ptr<IntHierarchy>> hi;  // per system
+    SmootherSpec sm;                                // the smoother every system was built with
 };
+
+// The FP64 / FP32 sibling of a batch (dfAMG, INTAMG.hpp:13-134, per system):
+// the same systems, coarsening chains, level order and row offsets as the
+// integer batch it derives from, with the floating-point level operators
+// (no row scaling, no quantisation), the multicolour SOR split of each level
+// in the colours of that level's greedy colouring (the same cap), and dense
+// coarsest LU factors.  LD rows hold the couplings to earlier colours, then
+// the inverse diagonal last; the dense U holds the strict upper part and
+// dinv the inverse diagonal (ltri / dutri::CSR<T>, ltri.hpp:19-54,
+// dutri.hpp:19-55).
+template <typename T>
+struct BatchCsrT {
+    int n = 0, m = 0;
+    std::vector<int> rptr, cind;
+    std::vector<T> val;
+    int64_t nnz() const { return rptr.empty() ? 0 : rptr[n]; }
+};
+
+template <typename T>
+struct BatchLevelT {
+    BatchCsrT<T> A, LD, U, P, R;   // as BatchLevel
+    std::vector<int> colour_rows;  // smoothing rows grouped by colour (rows ascending in a colour)
+    std::vector<int> colour_ptr;
+};
+
+template <typename T>
+struct BatchLUT {
+    int sys = 0, level = 0, n = 0, offset = 0;
+    std::vector<T> L, U, dinv;  // dense row-major strict parts, inverse diagonal
+};
+
+template <typename T>
+struct BatchFp {
+    std::vector<BatchLevelT<T>> lv;  // l = 0 .. Dmax-1 of the integer batch
+    std::vector<BatchLUT<T>> lu;     // one per system
+};
+
+// Builds every system's dfAMG hierarchy on host threads from the batch's
+// chains and scaled matrices, then assembles the block-diagonal levels.
+template <typename T>
+BatchFp<T> build_batch_fp(const BatchHierarchy &B, int threads);
 
 // Build the hierarchies of all systems (threads over systems) and assemble the
 // batch.  The systems must already be scaled (LMax1Scaling).  src[s] (optional)

@@ -230,6 +230,27 @@ struct BatchStats {
     unsigned flags = 0;
 };
 
+// The FP64 / FP32-mixed sibling of an integer batch (cuda/batch_fp.cu): the
+// same systems, coarsening, level order and colour caps; vectors of T.
+class BatchFpEngine {
+  public:
+    BatchFpEngine(Ctx &c, std::shared_ptr<BatchHierarchy> h, int vt, int nrhs, int threads = 0);
+    ~BatchFpEngine();
+    int precision() const { return vt_; }
+    size_t rows() const;
+    int depth() const;
+    void precondition(const void *in, void *out);  // device pointers of the engine's type
+    // b, x: device (double); nrm_b: per pair (host or device)
+    void solve(const KrylovParams &kp, const double *b, const double *nrm_b, double *x, BatchStats &st);
+    void autotune(int reps);
+    float time_vcycle(int reps);
+    class Base;
+
+  private:
+    int vt_;
+    std::unique_ptr<Base> impl_;
+};
+
 // Many systems, nrhs right-hand sides each, solved together (cuda/batch.cu).
 // Vectors are level-0 rows with the right-hand sides interleaved.
 class BatchEngine {

@@ -141,6 +141,12 @@ SIGNATURES = {
     "sa_batch_rule_ratios": (C.c_int, [VP, VP, VP, VP, F64P]),
     "sa_batch_solve": (C.c_int, [VP, VP, C.POINTER(SolverParams), I32P, VP, VP, VP, I32P, I32P, I32P]),
     "sa_profiler_range": (C.c_int, [C.c_int]),
+    "sa_batch_fp_create": (C.c_int, [VP, VP, C.c_int, C.c_int, C.POINTER(VP)]),
+    "sa_batch_fp_destroy": (C.c_int, [VP]),
+    "sa_batch_fp_precondition": (C.c_int, [VP, VP, VP, VP]),
+    "sa_batch_fp_autotune": (C.c_int, [VP, VP, C.c_int]),
+    "sa_batch_fp_time_vcycle": (C.c_int, [VP, VP, C.c_int, C.POINTER(C.c_float)]),
+    "sa_batch_fp_solve": (C.c_int, [VP, VP, C.POINTER(SolverParams), VP, VP, VP, I32P, I32P]),
     "sa_batch_level_op": (C.c_int, [VP, VP, C.c_int, C.c_int, VP, VP]),
     "sa_batch_coarse_solve": (C.c_int, [VP, VP]),
     "sa_batch_level_info": (C.c_int, [VP, C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
@@ -800,6 +806,49 @@ class Batch:
     def close(self):
         if self.h:
             lib().sa_batch_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+
+class BatchFp:
+    """FP64-AMG-FGMRES (F64) or FP32-mixed AMG-FGMRES (F32) of an integer
+    batch's systems, on its coarsening, level order and colour caps, run by
+    the same batched GPU design (one launch per operation over all systems,
+    graph-captured Arnoldi steps)."""
+
+    def __init__(self, ctx, batch, precision=F64, threads=0):
+        self.ctx = ctx
+        self.batch = batch  # the integer batch must outlive this handle
+        self.precision = precision
+        self.rows, self.nrhs, self.nsys, self.offsets = batch.rows, batch.nrhs, batch.nsys, batch.offsets
+        self.h = VP()
+        check(lib().sa_batch_fp_create(ctx.h, batch.h, precision, threads, C.byref(self.h)))
+
+    def precondition(self, x, out=None):
+        out = np.zeros(self.rows * self.nrhs, ctype_of(self.precision)) if out is None else out
+        check(lib().sa_batch_fp_precondition(self.ctx.h, self.h, _arg(x), _arg(out)))
+        return out
+
+    def autotune(self, reps=3):
+        check(lib().sa_batch_fp_autotune(self.ctx.h, self.h, reps))
+
+    def time_vcycle(self, reps=10):
+        ms = C.c_float()
+        check(lib().sa_batch_fp_time_vcycle(self.ctx.h, self.h, reps, C.byref(ms)))
+        return ms.value
+
+    def solve(self, params, b, nrm_b, x):
+        P = self.nsys * self.nrhs
+        it, cv = np.zeros(P, np.int32), np.zeros(P, np.int32)
+        check(lib().sa_batch_fp_solve(self.ctx.h, self.h, C.byref(params), _arg(b),
+                                      _arg(np.ascontiguousarray(nrm_b, np.float64)), _arg(x), _ptr(it, I32P),
+                                      _ptr(cv, I32P)))
+        return it, cv
+
+    def close(self):
+        if self.h:
+            lib().sa_batch_fp_destroy(self.h)
             self.h = None
 
     __del__ = close
