@@ -588,7 +588,8 @@ def kernel_rooflines(ctx, M, A0, N, a):
 
 def cpu_baseline(state, threads, m):
     """The oracle (C restatement of the reference) on the host cores: one full
-    solve of the same system with the same hierarchy."""
+    solve of the same system with the same hierarchy, to explicit residual
+    1e-10 as the GPU arm."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle_ffi as of
     s_int, r, c, v, b, bits = state
@@ -598,9 +599,10 @@ def cpu_baseline(state, threads, m):
     L = of.lib()
     L.or_set_threads(threads)
     x = np.zeros(len(b))
+    res = C.c_double()
     t = time.perf_counter()
-    it = L.or_ir_solve_i32(C.byref(dA), C.byref(h.A0), C.byref(h), m, 1e-10, bits, of.ptr(b, of.f64p),
-                           float(np.linalg.norm(b)), of.ptr(x, of.f64p), 1000 // m, 0)
+    it = L.or_ir_solve_i32x(C.byref(dA), C.byref(h.A0), C.byref(h), m, 1e-10, bits, of.ptr(b, of.f64p),
+                            float(np.linalg.norm(b)), of.ptr(x, of.f64p), 1000 // m, 1, C.byref(res))
     return time.perf_counter() - t, it, explicit_res(r, c, v, b, x)
 
 
@@ -629,6 +631,13 @@ def oracle_hierarchy(of, keep, setup):
 METRIC = "time to 1e-10 rel. residual: batched+learned-bits vs plain int-AMG-FGMRES on GB300"
 
 
+def bench_config(a, world):
+    """The workload of both arms (the same dict in each line)."""
+    return {"workload": workload(a.n, a.m), "rows": a.n ** 3, "m": a.m, "eps": 1e-10,
+            "stop": "explicit relative residual", "parallelism": f"replicas{world}",
+            "l2": "inputs larger than L2 (hierarchy ~1.5 GB, Krylov basis 0.5 GB per solve)"}
+
+
 def main_ours(a):
     dist = Dist(a.gpus)
     sec, out, ctx, state = run_ours(a, dist)
@@ -642,8 +651,7 @@ def main_ours(a):
         "value": sec, "unit": "s", "n_gpus": dist.world, "steps": a.steps, "warmup": a.warmup,
         "ms_per_step": sec * 1000.0, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
         "dtype": "int32", "data": "synthetic (b = A x*, x* ~ U[-1,1] seeded; SuiteSparse inputs not shipped)",
-        "config": {"workload": workload(a.n, a.m), "rows": N, "m": a.m, "eps": 1e-10, "parallelism": f"replicas{dist.world}",
-                   "l2": "inputs larger than L2 (hierarchy ~1.5 GB, Krylov basis 0.5 GB per solve)"},
+        "config": bench_config(a, dist.world),
         "iters": out["iters"], "converged": out["converged"], "explicit_res": out["explicit_res"],
         "frac_bits": out["frac_bits"], "rule_bits": out["rule_bits"], "learned_bits": out["learned_bits"],
         "final_bits": out["final_bits"], "selector_fallbacks": out["selector_fallbacks"],
@@ -704,35 +712,47 @@ def main_ours(a):
 # ------------------------------------------------------------- reference arm
 
 def main_reference(a):
+    """The reference's solve phase on the host cores, without this repository's
+    library: the system from the numpy generators (tests/golden/gen_matrices.py,
+    the same arrays as the library's generators), LMax1 scaling, the hierarchy
+    from the oracle's own C restatement of the reference's AMG setup
+    (oracle/oracle_setup.c, pinned to the reference's hierarchies), the rule's
+    F from the oracle's FP64 V-cycle, and Restarted(FGMRESflex) from the
+    oracle's C restatement (pinned to the reference bit for bit), run until the
+    explicit residual reaches 1e-10 as the GPU arm is."""
     dist = Dist(a.gpus)
     if dist.rank != 0:
         dist.close()
         return
-    import sagb
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
+    import gen_matrices as gm
     import oracle_ffi as of
-    r, c, v, b = build_system(a.n, seed=1)
-    s_int = sagb.Setup(sagb.INT, r, c, v)
-    # the bit rule needs one FP64 V-cycle; the oracle runs it on the host
-    s_f64 = s_int.derive(sagb.F64)
-    keep = of.Keep()
-    hd = fp64_oracle_hierarchy(of, keep, s_f64, r, c, v)
+    r, c, v = gm.poisson3d(a.n)
+    _, b = gm.rhs(r, c, v, 1)
+    rmax = np.maximum.reduceat(np.abs(v), r[:-1])  # CSRMat::LMax1Scaling (csrmat.hpp:70-80)
+    v = v / np.repeat(rmax, np.diff(r))
+    b = b / rmax
+    t0 = time.time()
+    S = of.OracleSetup(r, c, v)
+    t_setup = time.time() - t0
     L = of.lib()
     threads = os.cpu_count() or 1
     L.or_set_threads(threads)
-    cvec = np.zeros(len(b))
-    L.or_vcycle_f64(C.byref(hd), of.ptr(b, of.f64p), of.ptr(cvec, of.f64p))
     nrm_b = float(np.linalg.norm(b))
+    cvec = np.zeros(len(b))
+    L.or_vcycle_f64(C.byref(S.h_f64), of.ptr(b, of.f64p), of.ptr(cvec, of.f64p))  # Work/main.cpp:153-161
     q = np.abs(cvec).max() / nrm_b
     bits = 29 if q < 1 else 31 - (int(np.ceil(np.log2(int(q) + 1))) + 1)
-    h = oracle_hierarchy(of, keep, s_int)
+    keep = of.Keep()
     dA = of.csr_f(keep, r, c, v, np.float64)
     ts, it, x = [], 0, np.zeros(len(b))
+    res = C.c_double()
     for k in range(a.warmup + a.steps):
         x[:] = 0
         t = time.perf_counter()
-        it = L.or_ir_solve_i32(C.byref(dA), C.byref(h.A0), C.byref(h), a.m, 1e-10, bits, of.ptr(b, of.f64p),
-                               nrm_b, of.ptr(x, of.f64p), 1000 // a.m, 0)
+        it = L.or_ir_solve_i32x(C.byref(dA), C.byref(S.h_i32.A0), C.byref(S.h_i32), a.m, 1e-10, bits,
+                                of.ptr(b, of.f64p), nrm_b, of.ptr(x, of.f64p), 1000 // a.m, 1, C.byref(res))
         if k >= a.warmup:
             ts.append(time.perf_counter() - t)
     val = float(np.mean(ts))
@@ -741,15 +761,16 @@ def main_reference(a):
         "metric": METRIC,
         "value": val, "unit": "s", "n_gpus": dist.world, "steps": a.steps, "warmup": a.warmup,
         "ms_per_step": val * 1000, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
-        "dtype": "int32", "data": "synthetic (b = A x*, x* ~ U[-1,1] seeded)",
-        "config": {"workload": workload(a.n, a.m), "rows": len(b), "m": a.m, "eps": 1e-10, "parallelism": "host threads"},
-        "iters": it, "explicit_res": explicit_res(r, c, v, b, x), "frac_bits": bits,
+        "dtype": "int32", "data": "synthetic (b = A x*, x* ~ U[-1,1] seeded; SuiteSparse inputs not shipped)",
+        "config": bench_config(a, dist.world),
+        "iters": it, "explicit_res": explicit_res(r, c, v, b, x), "frac_bits": bits, "setup_s": t_setup,
         "cpu_baseline": {"value": val, "unit": "s", "cores": threads, "kind": "port",
-                         "sample": f"full solves of the {a.n}^3 system, oracle C restatement of the reference "
-                                   f"solve phase, {threads} threads (SpMV/BLAS parallel, SOR sweeps sequential "
-                                   f"as in the reference)"},
+                         "sample": f"full solves of the {a.n}^3 system to explicit residual 1e-10, the oracle's C "
+                                   f"restatement of the reference's setup and solve phase, {threads} threads (SpMV "
+                                   f"and integer BLAS parallel, SOR sweeps sequential as in the reference)"},
         "e2e": {"value": val, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
+    S.close()
     print(json.dumps(line), flush=True)
     dist.close()
 

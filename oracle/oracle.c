@@ -361,6 +361,48 @@ int or_ir_solve_i32(const or_csr_f64 *dA, const or_csr_i32 *A, const or_amg_i32 
     return result;
 }
 
+int or_ir_solve_i32x(const or_csr_f64 *dA, const or_csr_i32 *A, const or_amg_i32 *M, int m, double eps,
+                     int bit, const double *b, double nrm_b, double *x, int max_outer, int explicit_stop,
+                     double *res_out) {
+    const int N = A->n;
+    const size_t NN = (size_t)N;
+    double *r = (double *)malloc(sizeof(double) * NN);
+    int32_t *V = (int32_t *)malloc(sizeof(int32_t) * NN * (size_t)(m + 1));
+    int32_t *Z = (int32_t *)malloc(sizeof(int32_t) * NN * (size_t)(m + 1));
+    int64_t *H = (int64_t *)calloc((size_t)(m + 1) * (size_t)m, sizeof(int64_t));
+    int64_t *c = (int64_t *)calloc((size_t)m, sizeof(int64_t));
+    int64_t *s = (int64_t *)calloc((size_t)m, sizeof(int64_t));
+    int64_t *e = (int64_t *)calloc((size_t)m + 1, sizeof(int64_t));
+    double *y = (double *)calloc((size_t)m, sizeof(double));
+    double prev = 0, nrm_r = 0;
+    int iter = 0, result = 0, done = 0;
+    for (int i = 0; i < max_outer && !done; i++) {
+        or_spmv_f64(dA, x, r); /* irsolver.hpp:66-68 */
+        axpby_sub_f64(b, r, N);
+        nrm_r = or_nrm2_f64(r, N);
+        if (explicit_stop && i > 0 && nrm_r <= eps * nrm_b) {
+            result = iter;
+            done = 1;
+            break;
+        }
+        if (fabs(nrm_r - prev) / nrm_r < 1.0e-8) break;
+        prev = nrm_r;
+        int conv = 0;
+        iter += or_fgmres_i32_cycle(A, M, m, eps, bit, r, nrm_b, x, V, Z, H, c, s, e, y, NULL, &conv, 0);
+        if (conv && !explicit_stop) {
+            result = iter;
+            done = 1;
+        }
+    }
+    or_spmv_f64(dA, x, r);
+    axpby_sub_f64(b, r, N);
+    nrm_r = or_nrm2_f64(r, N);
+    if (explicit_stop && !done && nrm_r <= eps * nrm_b) result = iter;
+    if (res_out) *res_out = nrm_r / nrm_b;
+    free(r); free(V); free(Z); free(H); free(c); free(s); free(e); free(y);
+    return result;
+}
+
 /* ====================================================== FP64 / FP32 siblings
  * One body per precision, instantiated by macro.  T is the vector type. */
 

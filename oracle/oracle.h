@@ -127,6 +127,35 @@ int or_ir_solve_f32(const or_csr_f64 *dA, const or_csr_f32 *fA, const or_amg_f32
 
 double or_nrm2_f64(const double *x, int n);
 
+/* Restarted(FGMRESflex) as or_ir_solve_i32 with a choice of stop: the
+ * reference's (the inner solver's estimate, irsolver.hpp:38-40) or, with
+ * explicit_stop, the explicit FP64 residual ||b - A x|| <= eps ||b|| checked
+ * before every refinement step after the first.  *res_out (optional) = the
+ * explicit relative residual at return.  Returns the iterations if converged,
+ * else 0. */
+int or_ir_solve_i32x(const or_csr_f64 *dA, const or_csr_i32 *A, const or_amg_i32 *M, int m, double eps,
+                     int bit, const double *b, double nrm_b, double *x, int max_outer, int explicit_stop,
+                     double *res_out);
+
+/* --- the AMG setup (oracle_setup.c) ---
+ * helper::multigrid::get_amg_set (helper_multigrid.hpp:34-63) in the level
+ * loop of the AMG constructors (INTAMG.hpp:38-51, 162-195: a level is added
+ * while max_levels > depth and the last coarse operator has more than
+ * coarse_limit rows; the reference uses 2000), with the data both
+ * constructors prepare: intAMGflex (coarse rows scaled by their maxima, SOR
+ * split, exact LU, fixed-point conversions) and dfAMG (FP64).  The input is the
+ * LMax1-scaled fine matrix (copied).  *status: 0, -1 where the reference exits
+ * (an unclassified point, or "2 amk = 0"), -2 for invalid arguments. */
+typedef struct or_setup or_setup;
+or_setup *or_setup_create(int n, const int32_t *rptr, const int32_t *cind, const double *val, double theta,
+                          int max_levels, int coarse_limit, double omega, int *status);
+void or_setup_destroy(or_setup *s);
+int or_setup_depth(const or_setup *s);
+long or_setup_warnings(const or_setup *s); /* the reference's "1 amk = 0" messages */
+/* hierarchy structs viewing the setup's arrays (valid while it lives) */
+void or_setup_amg_i32(const or_setup *s, or_amg_i32 *h);
+void or_setup_amg_f64(const or_setup *s, or_amg_f64 *h);
+
 #ifdef __cplusplus
 }
 #endif

@@ -97,6 +97,15 @@ def lib():
             "or_ir_solve_f32": (C.c_int, [cf, cs, as_, C.c_int, C.c_double, f64p, C.c_double, f64p, C.c_int,
                                           C.c_int]),
             "or_nrm2_f64": (C.c_double, [f64p, C.c_int]),
+            "or_ir_solve_i32x": (C.c_int, [cf, ci, ai, C.c_int, C.c_double, C.c_int, f64p, C.c_double, f64p,
+                                           C.c_int, C.c_int, f64p]),
+            "or_setup_create": (C.c_void_p, [C.c_int, i32p, i32p, f64p, C.c_double, C.c_int, C.c_int,
+                                             C.c_double, C.POINTER(C.c_int)]),
+            "or_setup_destroy": (None, [C.c_void_p]),
+            "or_setup_depth": (C.c_int, [C.c_void_p]),
+            "or_setup_warnings": (C.c_long, [C.c_void_p]),
+            "or_setup_amg_i32": (None, [C.c_void_p, ai]),
+            "or_setup_amg_f64": (None, [C.c_void_p, af]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -207,3 +216,43 @@ def golden_amg_f(keep, g, pfx, dtype):
     h.LUL = g_csr_f(keep, g, pfx + "LU_L", dtype)
     h.LUU = g_csr_f(keep, g, pfx + "LU_U", dtype)
     return h
+
+
+class OracleSetup:
+    """The oracle's own AMG setup (oracle_setup.c) of an LMax1-scaled matrix:
+    .h_i32 / .h_f64 are the intAMGflex / dfAMG hierarchy structs."""
+
+    def __init__(self, rptr, cind, val, theta=0.8, max_levels=20, coarse_limit=2000, omega=1.0):
+        self._keep = Keep()
+        r = self._keep.arr(rptr, np.int32)
+        c = self._keep.arr(cind, np.int32)
+        v = self._keep.arr(val, np.float64)
+        st = C.c_int()
+        self.h = lib().or_setup_create(len(r) - 1, ptr(r, i32p), ptr(c, i32p), ptr(v, f64p), theta, max_levels,
+                                       coarse_limit, omega, C.byref(st))
+        if not self.h:
+            raise RuntimeError(f"oracle setup failed (status {st.value})")
+        self.depth = lib().or_setup_depth(self.h)
+        self.h_i32 = AmgI32()
+        lib().or_setup_amg_i32(self.h, C.byref(self.h_i32))
+        self.h_f64 = AmgF64()
+        lib().or_setup_amg_f64(self.h, C.byref(self.h_f64))
+
+    def close(self):
+        if self.h:
+            lib().or_setup_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+
+def csr_arrays(c):
+    """(rptr, cind, val) numpy copies of an oracle CSR view."""
+    n = c.n
+    rptr = np.ctypeslib.as_array(c.rptr, shape=(n + 1,)).copy()
+    nnz = int(rptr[-1])
+    if nnz == 0:
+        return rptr, np.zeros(0, np.int32), np.zeros(0)
+    cind = np.ctypeslib.as_array(c.cind, shape=(nnz,)).copy()
+    val = np.ctypeslib.as_array(c.val, shape=(nnz,)).copy()
+    return rptr, cind, val

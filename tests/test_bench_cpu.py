@@ -1,8 +1,8 @@
 """bench.py's reference arm on the CPU: one JSON line with the contract's keys.
 
 The reference arm times the oracle (the C restatement of the reference's
-integer solve) on the host cores; here on a 16^3 system so that it finishes
-in a second."""
+setup and integer solve) on the host cores, without loading this repository's
+library; here on a 16^3 system so that it finishes in a second."""
 import json
 import os
 import subprocess
@@ -27,3 +27,15 @@ def test_reference_arm_prints_the_contract_line():
     assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["value"] == d["value"]
     assert d["explicit_res"] <= 1e-10
     assert "16^3" in d["config"]["workload"]
+    assert d["config"]["stop"] == "explicit relative residual"
+
+
+def test_reference_arm_does_not_load_the_library():
+    """The reference arm's process maps the oracle, never libsagb.so."""
+    code = ("import runpy, sys; sys.argv = ['bench.py', '--impl', 'reference', '--n', '12', '--steps', '1', "
+            "'--warmup', '0']; runpy.run_path('bench.py', run_name='__main__'); "
+            "maps = open('/proc/self/maps').read(); "
+            "print('MAPS', 'liboracle' in maps, 'libsagb' in maps)")
+    out = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=600, cwd=ROOT)
+    assert out.returncode == 0, out.stderr
+    assert "MAPS True False" in out.stdout, out.stdout[-500:]
