@@ -128,6 +128,10 @@ int sa_ctx_destroy(sa_ctx ctx);
                             * this many rows on the GPU (same hierarchy bit for bit): 0 none, 1
                             * the default 2^20 (smaller systems build faster side by side on the
                             * host threads), >= 2 that many rows */
+#define SA_OPT_CYCLE_GRAPH 4 /* batched engines: each restart cycle as one CUDA graph whose steps after
+                              * the first run only while a pair is still active (the convergence test
+                              * of gmres.hpp:257 on the device, no host round trip per step); off:
+                              * one graph per step and a status read after each (default on) */
 int sa_ctx_set_option(sa_ctx ctx, int option, int value);
 int sa_ctx_flags(sa_ctx ctx, unsigned *flags, int clear);
 int sa_ctx_launches(sa_ctx ctx, long long *count);
@@ -390,6 +394,10 @@ int sa_batch_fp_time_vcycle(sa_ctx ctx, sa_batch_fp F, int reps, float *ms);
 /* Restarted(FGMRES<T>) per pair; nrm_b per pair; iters / converged per pair (optional) */
 int sa_batch_fp_solve(sa_ctx ctx, sa_batch_fp F, const sa_solver_params *p, const double *b, const double *nrm_b,
                       double *x, int *iters, int *converged);
+/* restart cycles of the last sa_batch_solve (F null) or sa_batch_fp_solve (B
+ * null) that ran as one graph each (SA_OPT_CYCLE_GRAPH; 0 when the engine fell
+ * back to one graph per step, e.g. where the driver refuses conditional nodes) */
+int sa_batch_cycle_graphs(sa_batch B, sa_batch_fp F, int *cycles);
 
 /* start (on = 1) or stop (0) the profiler's collection range: a profiler
  * started with collection off records only the launches in between */

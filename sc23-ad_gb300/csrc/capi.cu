@@ -184,6 +184,7 @@ extern "C" int sa_ctx_set_option(sa_ctx ctx, int option, int value) {
     if (option == SA_OPT_FP_EXACT) ctx->c.fp_exact = value != 0;
     else if (option == SA_OPT_GRAPHS) ctx->c.use_graphs = value != 0;
     else if (option == SA_OPT_PDL) ctx->c.use_pdl = value != 0;
+    else if (option == SA_OPT_CYCLE_GRAPH) ctx->c.cycle_graph = value != 0;
     else if (option == SA_OPT_GPU_SETUP) ctx->c.gpu_setup_rows = value == 1 ? 1 << 20 : value < 0 ? 0 : value;
     else return fail(SA_ERR_ARG, "unknown option");
     return SA_OK;
@@ -1524,4 +1525,10 @@ extern "C" int sa_batch_fp_solve(sa_ctx ctx, sa_batch_fp F, const sa_solver_para
     }
     return SA_OK;
     SA_GUARD_END
+}
+
+extern "C" int sa_batch_cycle_graphs(sa_batch B, sa_batch_fp F, int *cycles) {
+    if ((!B) == (!F) || !cycles) return fail(SA_ERR_ARG, "pass one of the two batches and an output");
+    *cycles = B ? B->eng->last_cycle_graphs() : F->eng->last_cycle_graphs();
+    return SA_OK;
 }

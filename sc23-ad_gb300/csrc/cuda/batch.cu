@@ -33,6 +33,7 @@
 
 #include "../sagb_internal.hpp"
 #include "common.cuh"
+#include "cycle_graph.cuh"
 #include "stream.cuh"
 
 namespace sagb {
@@ -1529,6 +1530,7 @@ struct BatchEngine::Impl {
     BPair *pairs = nullptr;
     BInfo *info_d = nullptr, *info_h = nullptr;
     std::vector<cudaGraphExec_t> graphs;
+    CycleGraph cyc;         // a whole restart cycle, steps gated on the device
     bool graph_pdl = true;  // the PDL setting the graphs were captured with
     // the Arnoldi step's A Z_j fused with its first dot (tuned apart from the
     // V-cycle's A: its tiles and reductions favour other lanes per row)
@@ -1793,6 +1795,7 @@ struct BatchEngine::Impl {
     }
 
     void clear_graphs() {
+        cyc.clear();
         for (auto g : graphs)
             if (g) cudaGraphExecDestroy(g);
         graphs.clear();
@@ -2257,7 +2260,9 @@ struct BatchEngine::Impl {
         });
     }
 
-    void arnoldi_step(int j) {
+    // d2h: read the step status back (per-step mode); has_next: end with the
+    // kernel that opens step j+1 of the cycle graph when a pair is still active
+    void arnoldi_step(int j, bool d2h = true, cudaGraphConditionalHandle next = 0, bool has_next = false) {
         const int P = S * Rn;
         const size_t vs = N0 * Rn;
         int *Vj = V + (size_t)j * vs, *Zj = Z + (size_t)j * vs, *w = V + (size_t)(j + 1) * vs;
@@ -2282,7 +2287,34 @@ struct BatchEngine::Impl {
             constexpr int R = decltype(RR)::value;
             launch(k_bscal<R>, ntiles, kBThreads, 0, 1, (const BTile *)tiles, j, (const BPair *)pairs, w);
         });
-        SAGB_CUDA(cudaMemcpyAsync(info_h, info_d, sizeof(BInfo), cudaMemcpyDeviceToHost, c.stream));
+        if (has_next) launch(k_cycle_next, 1, 32, 0, 1, (const int *)&info_d->n_active, next);
+        if (d2h) SAGB_CUDA(cudaMemcpyAsync(info_h, info_d, sizeof(BInfo), cudaMemcpyDeviceToHost, c.stream));
+    }
+
+    // the Arnoldi steps of one restart cycle: one graph launch whose steps
+    // after the first run only while a pair is active (no host round trip),
+    // or step by step with a status read after each; returns true when the
+    // cycle graph ran (its launches are counted once the pairs are read back)
+    bool cycle_steps() {
+        if (c.use_graphs && c.cycle_graph && !cyc.refused) {
+            if (graph_pdl != c.use_pdl) {
+                clear_graphs();
+                graph_pdl = c.use_pdl;
+            }
+            if (!cyc.exec || cyc.m != m)
+                build_cycle_graph(c, m, cyc, [&](int j, cudaGraphConditionalHandle nx, bool has) {
+                    arnoldi_step(j, false, nx, has);
+                });
+            if (cyc.exec) {
+                SAGB_CUDA(cudaGraphLaunch(cyc.exec, c.stream));
+                return true;
+            }
+        }
+        for (int j = 0; j < m; j++) {
+            step(j);
+            if (info_h->n_active == 0) break;
+        }
+        return false;
     }
 
     void step(int j) {
@@ -2389,10 +2421,8 @@ struct BatchEngine::Impl {
                 k_bv0<R><<<ntiles, kBThreads, 0, c.stream>>>(tiles, rvec, pairs, V);
             });
             c.launches += 2;
-            for (int j = 0; j < m; j++) {
-                step(j);
-                if (info_h->n_active == 0) break;
-            }
+            const bool in_graph = cycle_steps();
+            st.cycle_graphs += in_graph;
             k_btrsv<<<(P + 127) / 128, 128, 0, c.stream>>>(P, m, pairs, H, e, y);
             by_r([&](auto RR) {
                 constexpr int R = decltype(RR)::value;
@@ -2401,6 +2431,11 @@ struct BatchEngine::Impl {
             c.launches += 2;
             SAGB_CUDA(cudaMemcpyAsync(hp.data(), pairs, sizeof(BPair) * P, cudaMemcpyDeviceToHost, c.stream));
             SAGB_CUDA(cudaStreamSynchronize(c.stream));
+            if (in_graph) {  // the steps that ran: as many as the longest pair took
+                int steps = 0;
+                for (int p = 0; p < P; p++) steps = std::max(steps, hp[p].jn);
+                for (int j = 0; j < steps && j < (int)cyc.step_launches.size(); j++) c.launches += cyc.step_launches[j];
+            }
             for (int p = 0; p < P; p++) {
                 if (done[p] || !(hp[p].jn > 0)) continue;
                 if (hp[p].bad) {
@@ -2461,6 +2496,7 @@ void BatchEngine::pair_norms(const double *v, double *out_dev) {
 void BatchEngine::solve(const KrylovParams &kp, const int *bits_sys, const double *b, const double *nrm_b, double *x,
                         BatchStats &st) {
     impl_->solve(kp, bits_sys, b, nrm_b, x, st);
+    last_cycle_graphs_ = st.cycle_graphs;
 }
 void BatchEngine::set_groups(int level, int op, int group) {
     if (level < 0 || level >= impl_->Dmax) throw CudaError{"no such level"};

@@ -28,6 +28,7 @@
 
 #include "../sagb_internal.hpp"
 #include "common.cuh"
+#include "cycle_graph.cuh"
 
 namespace sagb {
 namespace {
@@ -820,6 +821,7 @@ class FpImpl : public BatchFpEngine::Base {
     FInfo *info_d = nullptr, *info_h = nullptr;
     std::vector<cudaGraphExec_t> graphs;
     std::vector<long long> graph_launches;
+    CycleGraph cyc;
     bool graph_pdl = true;
     cudaGraphExec_t vc_graph = nullptr;
     const T *vc_in = nullptr;
@@ -947,6 +949,7 @@ class FpImpl : public BatchFpEngine::Base {
         clear_graphs();
     }
     void clear_graphs() {
+        cyc.clear();
         for (auto &g : graphs)
             if (g) cudaGraphExecDestroy(g);
         graphs.clear();
@@ -1181,7 +1184,7 @@ class FpImpl : public BatchFpEngine::Base {
         });
     }
 
-    void arnoldi_step(int j) {
+    void arnoldi_step(int j, bool d2h = true, cudaGraphConditionalHandle next = 0, bool has_next = false) {
         const int P = S * Rn;
         const size_t vs = N0 * Rn;
         T *Vj = V + (size_t)j * vs, *Zj = Z + (size_t)j * vs, *w = V + (size_t)(j + 1) * vs;
@@ -1206,7 +1209,32 @@ class FpImpl : public BatchFpEngine::Base {
             launch(k_fscal<T, R>, ntiles, kFThreads, 0, (const FTile *)tiles, j, (const FPair *)pairs,
                    (const T *)ascal, w);
         });
-        SAGB_CUDA(cudaMemcpyAsync(info_h, info_d, sizeof(FInfo), cudaMemcpyDeviceToHost, c.stream));
+        if (has_next) launch(k_cycle_next, 1, 32, 0, (const int *)&info_d->n_active, next);
+        if (d2h) SAGB_CUDA(cudaMemcpyAsync(info_h, info_d, sizeof(FInfo), cudaMemcpyDeviceToHost, c.stream));
+    }
+
+    // the steps of one restart cycle as one graph gated on the device (see
+    // cycle_graph.cuh), or step by step; true when the graph ran
+    bool cycle_steps() {
+        if (c.use_graphs && c.cycle_graph && !cyc.refused) {
+            if (graph_pdl != c.use_pdl) {
+                clear_graphs();
+                graph_pdl = c.use_pdl;
+            }
+            if (!cyc.exec || cyc.m != m)
+                build_cycle_graph(c, m, cyc, [&](int j, cudaGraphConditionalHandle nx, bool has) {
+                    arnoldi_step(j, false, nx, has);
+                });
+            if (cyc.exec) {
+                SAGB_CUDA(cudaGraphLaunch(cyc.exec, c.stream));
+                return true;
+            }
+        }
+        for (int j = 0; j < m; j++) {
+            step(j);
+            if (info_h->n_active == 0) break;
+        }
+        return false;
     }
 
     void step(int j) {
@@ -1277,10 +1305,8 @@ class FpImpl : public BatchFpEngine::Base {
                 k_fv0<T, R><<<ntiles, kFThreads, 0, c.stream>>>(tiles, rvec, pairs, V);
             });
             c.launches += 2;
-            for (int j = 0; j < m; j++) {
-                step(j);
-                if (info_h->n_active == 0) break;
-            }
+            const bool in_graph = cycle_steps();
+            st.cycle_graphs += in_graph;
             k_ftrsv<T><<<(P + 127) / 128, 128, 0, c.stream>>>(P, m, pairs, H, e, y);
             by_r([&](auto RR) {
                 constexpr int R = decltype(RR)::value;
@@ -1289,6 +1315,11 @@ class FpImpl : public BatchFpEngine::Base {
             c.launches += 2;
             SAGB_CUDA(cudaMemcpyAsync(hp.data(), pairs, sizeof(FPair) * P, cudaMemcpyDeviceToHost, c.stream));
             SAGB_CUDA(cudaStreamSynchronize(c.stream));
+            if (in_graph) {
+                int steps = 0;
+                for (int p = 0; p < P; p++) steps = std::max(steps, hp[p].jn);
+                for (int j = 0; j < steps && j < (int)cyc.step_launches.size(); j++) c.launches += cyc.step_launches[j];
+            }
             for (int p = 0; p < P; p++) {
                 if (done[p] || !(hp[p].jn > 0)) continue;
                 if (hp[p].bad) {
@@ -1434,6 +1465,7 @@ BatchFpEngine::~BatchFpEngine() = default;
 void BatchFpEngine::precondition(const void *in, void *out) { impl_->precondition(in, out); }
 void BatchFpEngine::solve(const KrylovParams &kp, const double *b, const double *nrm_b, double *x, BatchStats &st) {
     impl_->solve(kp, b, nrm_b, x, st);
+    last_cycle_graphs_ = st.cycle_graphs;
 }
 void BatchFpEngine::autotune(int reps) { impl_->autotune(reps); }
 float BatchFpEngine::time_vcycle(int reps) { return impl_->time_vcycle(reps); }

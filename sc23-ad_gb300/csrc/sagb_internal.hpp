@@ -36,6 +36,7 @@ struct Ctx {
     bool fp_exact = false;           // FP kernels in sequential order without FMA
     bool use_graphs = true;
     bool use_pdl = true;             // batched V-cycle kernels chained by programmatic dependent launch
+    bool cycle_graph = true;         // batched engines: a restart cycle as one graph, steps gated on the device
     int gpu_setup_rows = 1 << 20;    // batches: systems from this size on build their Ruge-Stueben chain
                                      // on the GPU (0: none); smaller ones share the host threads
     long long launches = 0;          // kernels launched by this context (for reporting)
@@ -228,6 +229,7 @@ struct BatchStats {
     std::vector<double> explicit_res;
     int restarts = 0;
     unsigned flags = 0;
+    int cycle_graphs = 0;  // restart cycles that ran as one graph (no host round trip per step)
 };
 
 // The FP64 / FP32-mixed sibling of an integer batch (cuda/batch_fp.cu): the
@@ -244,10 +246,12 @@ class BatchFpEngine {
     void solve(const KrylovParams &kp, const double *b, const double *nrm_b, double *x, BatchStats &st);
     void autotune(int reps);
     float time_vcycle(int reps);
+    int last_cycle_graphs() const { return last_cycle_graphs_; }
     class Base;
 
   private:
     int vt_;
+    int last_cycle_graphs_ = 0;
     std::unique_ptr<Base> impl_;
 };
 
@@ -265,6 +269,7 @@ class BatchEngine {
     // b, x: device; nrm_b: per pair (host or device); bits_sys: host, per system
     void solve(const KrylovParams &kp, const int *bits_sys, const double *b, const double *nrm_b, double *x,
                BatchStats &st);
+    int last_cycle_graphs() const { return last_cycle_graphs_; }  // of the last solve
     void autotune(int reps);
     void set_groups(int level, int op, int group);  // op: 0 A, 1 LD, 2 U, 3 P, 4 R
     int group(int level, int op) const;
@@ -295,6 +300,7 @@ class BatchEngine {
   private:
     struct Impl;
     Impl *impl_;
+    int last_cycle_graphs_ = 0;
 };
 
 // ------------------------------------------------------ learned bit selector

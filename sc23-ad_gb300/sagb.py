@@ -19,7 +19,7 @@ INT, F64, F32 = 0, 1, 2
 MAT_FIXED, MAT_FLEX, MAT_F64, MAT_F32 = 0, 1, 2, 3
 OP_A0, OP_CA, OP_P, OP_R, OP_LD, OP_U, OP_LUL, OP_LUU, OP_BJ, OP_COLOR = range(10)
 GEN_POISSON2D, GEN_POISSON3D, GEN_ANISO2D, GEN_STENCIL27, GEN_CONVDIFF3D, GEN_VARCOEF3D = range(6)
-OPT_FP_EXACT, OPT_GRAPHS, OPT_PDL, OPT_GPU_SETUP = 0, 1, 2, 3
+OPT_FP_EXACT, OPT_GRAPHS, OPT_PDL, OPT_GPU_SETUP, OPT_CYCLE_GRAPH = 0, 1, 2, 3, 4
 
 VP = C.c_void_p
 I32P = C.POINTER(C.c_int32)
@@ -147,6 +147,7 @@ SIGNATURES = {
     "sa_batch_fp_autotune": (C.c_int, [VP, VP, C.c_int]),
     "sa_batch_fp_time_vcycle": (C.c_int, [VP, VP, C.c_int, C.POINTER(C.c_float)]),
     "sa_batch_fp_solve": (C.c_int, [VP, VP, C.POINTER(SolverParams), VP, VP, VP, I32P, I32P]),
+    "sa_batch_cycle_graphs": (C.c_int, [VP, VP, C.POINTER(C.c_int)]),
     "sa_batch_level_op": (C.c_int, [VP, VP, C.c_int, C.c_int, VP, VP]),
     "sa_batch_coarse_solve": (C.c_int, [VP, VP]),
     "sa_batch_level_info": (C.c_int, [VP, C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
@@ -788,6 +789,12 @@ class Batch:
         check(lib().sa_batch_sweep_form(self.h, level, set, C.byref(f)))
         return f.value
 
+    def cycle_graphs(self):
+        """Restart cycles of the last solve that ran as one graph each."""
+        n = C.c_int()
+        check(lib().sa_batch_cycle_graphs(self.h, None, C.byref(n)))
+        return n.value
+
     def rule_ratios(self, b, nrm_b):
         q = np.zeros(self.nsys * self.nrhs)
         check(lib().sa_batch_rule_ratios(self.ctx.h, self.h, _arg(b), _arg(np.ascontiguousarray(nrm_b, np.float64)),
@@ -837,6 +844,12 @@ class BatchFp:
         ms = C.c_float()
         check(lib().sa_batch_fp_time_vcycle(self.ctx.h, self.h, reps, C.byref(ms)))
         return ms.value
+
+    def cycle_graphs(self):
+        """Restart cycles of the last solve that ran as one graph each."""
+        n = C.c_int()
+        check(lib().sa_batch_cycle_graphs(None, self.h, C.byref(n)))
+        return n.value
 
     def solve(self, params, b, nrm_b, x):
         P = self.nsys * self.nrhs

@@ -218,9 +218,10 @@ def test_copies_share_one_setup(ctx):
 
 
 def test_launch_options_do_not_change_results(ctx):
-    """Graph replay of the V-cycle, programmatic dependent launch and the
-    graph-timed operator clock change launch mechanics only: V-cycles and
-    whole solves are identical bit for bit with each of them off."""
+    """Graph replay of the V-cycle, programmatic dependent launch, the
+    restart cycle as one graph gated on the device and the graph-timed
+    operator clock change launch mechanics only: V-cycles and whole solves are
+    identical bit for bit with each of them off."""
     nrhs = 2
     systems, bs = _systems(SYSTEMS, nrhs)
     B = sagb.Batch(ctx, systems, nrhs)
@@ -238,6 +239,17 @@ def test_launch_options_do_not_change_results(ctx):
         return out, x, it
 
     ref = run()
+    # each restart cycle ran as one graph with its steps gated on the device;
+    # the same solve step by step (a status read after every step) is identical
+    assert B.cycle_graphs() > 0
+    ctx.set_option(sagb.OPT_CYCLE_GRAPH, 0)
+    try:
+        got = run()
+        assert B.cycle_graphs() == 0
+        for k in range(3):
+            np.testing.assert_array_equal(got[k], ref[k], err_msg="step by step")
+    finally:
+        ctx.set_option(sagb.OPT_CYCLE_GRAPH, 1)
     # a solve whose V-cycles run their coarse levels in the persistent tail
     for t in (1, B.depth - 1):
         B.tail(t)

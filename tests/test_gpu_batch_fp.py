@@ -152,3 +152,29 @@ def test_batched_fp_solve(ctx, prec):
             assert abs(int(it[s * nrhs + q]) - it_o) <= (1 if prec == sagb.F64 else 3), (s, q, it[s * nrhs + q], it_o)
     F.close()
     B.close()
+
+
+@pytest.mark.parametrize("prec", [sagb.F64, sagb.F32])
+def test_batched_fp_cycle_graph(ctx, prec):
+    """A restart cycle as one graph gated on the device gives the solve of
+    the step-by-step form bit for bit (the same kernels in the same order)."""
+    systems, bs = _systems(SYSTEMS[:3])
+    B = sagb.Batch(ctx, systems, 1)
+    F = sagb.BatchFp(ctx, B, prec)
+    bb = np.concatenate(bs)
+    nb = np.array([np.linalg.norm(b) for b in bs])
+    p = sagb.solver_params(m=20, explicit_stop=1)
+    x1 = np.zeros(B.rows)
+    it1, cv1 = F.solve(p, bb, nb, x1)
+    assert cv1.all() and F.cycle_graphs() > 0
+    ctx.set_option(sagb.OPT_CYCLE_GRAPH, 0)
+    try:
+        x2 = np.zeros(B.rows)
+        it2, cv2 = F.solve(p, bb, nb, x2)
+        assert F.cycle_graphs() == 0
+    finally:
+        ctx.set_option(sagb.OPT_CYCLE_GRAPH, 1)
+    np.testing.assert_array_equal(it1, it2)
+    np.testing.assert_array_equal(x1, x2)
+    F.close()
+    B.close()
