@@ -111,6 +111,12 @@ typedef struct {
     int overflow_fallback; /* int only: on an overflow flag, redo the cycle with F-1 (0: reference behaviour) */
     int explicit_stop;     /* 1: stop only when ||b - A x|| / ||b|| <= eps in FP64 (the reference stops on
                               the inner solver's implicit estimate, which can leave it above eps)      */
+    int cycle_bits;        /* batched integer solver only (no counterpart in the reference): a pair's
+                              restart cycle also ends, unconverged, once its estimate |e_{j+1}| has
+                              fallen 2^cycle_bits below the cycle's start e_0 = 2^F; the FP64
+                              refinement then restarts from the true residual.  An F-bit basis stops
+                              gaining about 2^20 below its start, so the rest of a long cycle is
+                              wasted.  0: the full m steps, as FGMRESflex (gmres.hpp:237-262)      */
 } sa_solver_params;
 
 /* ------------------------------------------------------------- library */

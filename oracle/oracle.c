@@ -282,6 +282,11 @@ double or_nrm2_f64(const double *x, int n) { /* blas1::Nrm2<double> (blas1.hpp:6
 }
 
 /* FGMRESflex::Solve (solver/gmres.hpp:307-353). */
+/* early restart of the batched engine (0: off, the reference's FGMRESflex) */
+static int g_cycle_bits = 0;
+void or_set_cycle_bits(int bits) { g_cycle_bits = bits; }
+static int64_t cycle_target(int bit) { return bit > g_cycle_bits ? (int64_t)1 << (bit - g_cycle_bits) : 1; }
+
 int or_fgmres_i32_cycle(const or_csr_i32 *A, const or_amg_i32 *M, int m, double eps, int bit,
                         const double *r, double nrm_b, double *x,
                         int32_t *V, int32_t *Z, int64_t *H, int64_t *c, int64_t *s, int64_t *e,
@@ -319,6 +324,16 @@ int or_fgmres_i32_cycle(const or_csr_i32 *A, const or_amg_i32 *M, int m, double 
             j++;
             flag = 1;
             break;
+        }
+        /* the batched engine's early restart (no counterpart in the
+         * reference): the cycle ends once the estimate has fallen 2^K below
+         * its start e[0] = 2^bit, where the fixed-point basis stops gaining */
+        if (g_cycle_bits > 0 && (e[j + 1] < 0 ? -e[j + 1] : e[j + 1]) <= cycle_target(bit)) {
+            j++;
+            *converged = 0;
+            or_trsv_i32(H, e0, e, y, m + 1, j, bit);
+            for (int k = 0; k < j; k++) or_axpy_d(y[k], Z + (size_t)k * NN, x, N, bit);
+            return j;
         }
     }
     or_trsv_i32(H, e0, e, y, m + 1, j, bit);

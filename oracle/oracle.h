@@ -137,6 +137,12 @@ int or_ir_solve_i32x(const or_csr_f64 *dA, const or_csr_i32 *A, const or_amg_i32
                      int bit, const double *b, double nrm_b, double *x, int max_outer, int explicit_stop,
                      double *res_out);
 
+/* The batched engine's early restart, which the reference lacks: with bits
+ * = K > 0 a cycle of or_fgmres_i32_cycle also ends (not converged) once
+ * |e_{j+1}| <= 2^(F-K), i.e. the estimate has fallen 2^K below its start
+ * e_0 = 2^F.  0 (the default) is the reference's FGMRESflex. */
+void or_set_cycle_bits(int bits);
+
 /* --- the AMG setup (oracle_setup.c) ---
  * helper::multigrid::get_amg_set (helper_multigrid.hpp:34-63) in the level
  * loop of the AMG constructors (INTAMG.hpp:38-51, 162-195: a level is added

@@ -97,6 +97,7 @@ def lib():
             "or_ir_solve_f32": (C.c_int, [cf, cs, as_, C.c_int, C.c_double, f64p, C.c_double, f64p, C.c_int,
                                           C.c_int]),
             "or_nrm2_f64": (C.c_double, [f64p, C.c_int]),
+            "or_set_cycle_bits": (None, [C.c_int]),
             "or_ir_solve_i32x": (C.c_int, [cf, ci, ai, C.c_int, C.c_double, C.c_int, f64p, C.c_double, f64p,
                                            C.c_int, C.c_int, f64p]),
             "or_setup_create": (C.c_void_p, [C.c_int, i32p, i32p, f64p, C.c_double, C.c_int, C.c_int,

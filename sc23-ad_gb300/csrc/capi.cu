@@ -860,6 +860,7 @@ extern "C" void sa_solver_params_default(sa_solver_params *p) {
     p->verbose = 0;
     p->overflow_fallback = 1;
     p->explicit_stop = 0;
+    p->cycle_bits = 0;
 }
 
 extern "C" int sa_solver_create(sa_ctx ctx, int precision, sa_mat dA, sa_mat A, sa_amg M, const sa_solver_params *p,
@@ -1381,6 +1382,8 @@ extern "C" int sa_batch_solve(sa_ctx ctx, sa_batch B, const sa_solver_params *p,
     kp.max_outer = p->max_outer;
     kp.fallback = p->overflow_fallback;
     kp.explicit_check = p->explicit_stop;
+    kp.cycle_bits = p->cycle_bits;
+    if (p->cycle_bits < 0 || p->cycle_bits > 30) return fail(SA_ERR_ARG, "cycle_bits out of range (0..30)");
     const size_t bytes = sizeof(double) * B->eng->rows() * R;
     Staged sb(c, b, bytes, true, false);
     Staged sx(c, x, bytes, true, true);

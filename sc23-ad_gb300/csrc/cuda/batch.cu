@@ -1009,6 +1009,7 @@ struct BTile {
 struct BPair {
     double e0, e_inv, nrm_b, relres;
     long long criteria, hinv;
+    long long cycle_target;  // the cycle ends once |e_{j+1}| <= this (-1: never)
     int bit, active, jn, conv;
     unsigned bad;  // status bits seen while the pair was active (the cycle is discarded)
     int pad;
@@ -1066,13 +1067,14 @@ __device__ __forceinline__ void bsum_f64(double (&v)[R], double (*sh)[R]) {
 
 // FGMRESflex::Solve prologue per pair (gmres.hpp:228-233)
 __global__ void k_bbegin(int P, const double *__restrict__ e0, double eps, BPair *pairs, long long *e,
-                         unsigned long long *acc, int m) {
+                         unsigned long long *acc, int m, int cycle_bits) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= P) return;
     BPair &q = pairs[p];
     q.jn = 0;
     q.conv = 0;
     q.bad = 0;
+    q.cycle_target = cycle_bits <= 0 ? -1 : q.bit > cycle_bits ? 1LL << (q.bit - cycle_bits) : 1;
     for (int k = 0; k <= m + 1; k++) acc[(size_t)p * (m + 2) + k] = 0;
     if (!q.active) return;
     const double fact = (double)(1LL << q.bit);
@@ -1295,6 +1297,10 @@ __global__ void k_bgivens(int P, int j, int m, BPair *pairs, long long *Hall, lo
             q.active = 0;
         } else if (aen <= q.criteria) {
             q.conv = 1;
+            q.active = 0;
+        } else if (aen <= q.cycle_target) {
+            // the F-bit basis has stopped gaining: end this pair's cycle; the
+            // refinement restarts it from the true residual
             q.active = 0;
         } else if (j + 1 < m) {
             atomicAdd(&info->n_active, 1);
@@ -2415,7 +2421,7 @@ struct BatchEngine::Impl {
             SAGB_CUDA(cudaMemsetAsync(pflag, 0, sizeof(unsigned) * P * 2, c.stream));
             SAGB_CUDA(cudaMemcpyAsync(pairs, hp.data(), sizeof(BPair) * P, cudaMemcpyHostToDevice, c.stream));
             SAGB_CUDA(cudaMemcpyAsync(e0, nrm, sizeof(double) * P, cudaMemcpyDeviceToDevice, c.stream));
-            k_bbegin<<<(P + 127) / 128, 128, 0, c.stream>>>(P, e0, kp.eps, pairs, e, acc, m);
+            k_bbegin<<<(P + 127) / 128, 128, 0, c.stream>>>(P, e0, kp.eps, pairs, e, acc, m, kp.cycle_bits);
             by_r([&](auto RR) {
                 constexpr int R = decltype(RR)::value;
                 k_bv0<R><<<ntiles, kBThreads, 0, c.stream>>>(tiles, rvec, pairs, V);

@@ -202,6 +202,7 @@ struct KrylovParams {
     int verbose = 0;
     int fallback = 1;  // int: on overflow, discard the cycle and redo it with bit - 1
     int explicit_check = 0;  // stop on the explicit FP64 residual instead of the inner estimate
+    int cycle_bits = 0;      // batched int: end a cycle once |e_{j+1}| <= 2^(F - cycle_bits) (0: full cycles)
 };
 
 class Solver;

@@ -40,7 +40,8 @@ class AmgParams(C.Structure):
 
 class SolverParams(C.Structure):
     _fields_ = [("m", C.c_int), ("eps", C.c_double), ("max_outer", C.c_int), ("frac_bits", C.c_int),
-                ("verbose", C.c_int), ("overflow_fallback", C.c_int), ("explicit_stop", C.c_int)]
+                ("verbose", C.c_int), ("overflow_fallback", C.c_int), ("explicit_stop", C.c_int),
+                ("cycle_bits", C.c_int)]
 
 
 # name -> (restype, argtypes); the list is the ABI, checked by the CPU tests
@@ -543,9 +544,10 @@ class Amg:
             self.h = None
 
 
-def solver_params(m=30, eps=1e-10, max_outer=None, frac_bits=29, verbose=0, overflow_fallback=1, explicit_stop=0):
+def solver_params(m=30, eps=1e-10, max_outer=None, frac_bits=29, verbose=0, overflow_fallback=1, explicit_stop=0,
+                  cycle_bits=0):
     return SolverParams(m, eps, 1000 // m if max_outer is None else max_outer, frac_bits, verbose, overflow_fallback,
-                        explicit_stop)
+                        explicit_stop, cycle_bits)
 
 
 class Solver:

@@ -305,3 +305,39 @@ def test_tail_barrier_timeout_is_detected(ctx):
     B.tail(1)
     np.testing.assert_array_equal(B.precondition(vin), ref)
     B.close()
+
+
+def test_early_restart_matches_oracle(ctx):
+    """sa_solver_params.cycle_bits: a pair's cycle ends once its estimate has
+    fallen 2^K below the cycle's start.  Per system the batched solve takes
+    the iterations of the oracle's Restarted(FGMRESflex) with the same rule
+    on the same hierarchy (within 2: the FP64 residual norm is a parallel sum
+    on the GPU) and far fewer than with full cycles."""
+    nrhs = 1
+    systems, bs = _systems(SYSTEMS[:4], nrhs)
+    B = sagb.Batch(ctx, systems, nrhs)
+    b = _interleave(B, bs)
+    nrm_b = np.array([np.linalg.norm(bs[s][:, 0]) for s in range(B.nsys)])
+    its = {}
+    for K in (0, 12):
+        x = np.zeros(B.rows)
+        it, cv, fb = B.solve(sagb.solver_params(m=30, explicit_stop=1, cycle_bits=K), [29] * B.nsys, b, nrm_b, x)
+        assert cv.all(), (K, it)
+        its[K] = it
+        for s, (r, c, v) in enumerate(systems):
+            keep = of.Keep()
+            h = sv.oracle_amg(keep, B.system_setup(s))
+            dA = of.csr_f(keep, r, c, v, np.float64)
+            bq = np.ascontiguousarray(bs[s][:, 0])
+            xo = np.zeros(len(bq))
+            res = C.c_double()
+            of.lib().or_set_cycle_bits(K)
+            try:
+                it_o = of.lib().or_ir_solve_i32x(C.byref(dA), C.byref(h.A0), C.byref(h), 30, 1e-10, 29,
+                                                 of.ptr(bq, of.f64p), float(nrm_b[s]), of.ptr(xo, of.f64p), 100, 1,
+                                                 C.byref(res))
+            finally:
+                of.lib().or_set_cycle_bits(0)
+            assert it_o > 0 and abs(int(it[s]) - it_o) <= 2, (K, s, it[s], it_o)
+    assert its[12].sum() < its[0].sum(), (its[0], its[12])
+    B.close()
