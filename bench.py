@@ -57,6 +57,7 @@ def parse():
     ap.add_argument("--no-multicolor", action="store_true", help="skip the multicolour-smoother row")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-engine rows")
     ap.add_argument("--no-fp-batched", action="store_true", help="skip the FP64 / FP32 batched rows")
+    ap.add_argument("--no-tune-caps", action="store_true", help="keep the default colour caps (8 / 2)")
     ap.add_argument("--cycle-bits", type=int, default=12,
                     help="batched integer engine: end a restart cycle once its estimate has fallen 2^K below its "
                          "start (the fixed-point basis stops gaining about 2^20 down); 0: full FGMRESflex cycles")
@@ -194,6 +195,12 @@ def learned_bits(ctx, setup_int, ratio):
     return f
 
 
+# colour caps per level tried by the headline's tuner (the last entry holds for
+# deeper levels): 8 colours properly colour 7- and 27-point fine grids; below,
+# fewer colours mean fewer dependent steps per sweep and a weaker smoother
+CAP_CANDIDATES = [[8, 2], [8, 1], [8, 3], [8, 4], [8, 2, 1], [8, 4, 2], [8, 1, 2]]
+
+
 def run_ours(a, dist):
     """Headline: the batched engine (multicolour colour-pass sweeps, autotuned
     lanes per row, graph-captured Arnoldi steps) with the learned F and the
@@ -213,14 +220,20 @@ def run_ours(a, dist):
     t_tune = time.time() - t0
     ratio = float(B.rule_ratios(b, [nrm_b])[0])
     rule = bitsel.rule_of(ratio)
-    s0 = B.system_setup(0)
-    learned = learned_bits(ctx, s0, ratio)
-    bits = learned if learned is not None else rule
     params = sagb.solver_params(m=a.m, explicit_stop=1, cycle_bits=a.cycle_bits)
     db = sagb.DeviceArray.from_host(ctx, b)
     dx = sagb.DeviceArray(ctx, N, np.float64)
     zeros = sagb.DeviceArray.from_host(ctx, np.zeros(N))
     nb = np.array([nrm_b])
+    caps_table = None
+    if not a.no_tune_caps:
+        # colour caps by measured time to solution (setup, outside the timed region)
+        t0 = time.time()
+        caps_table = B.tune_colour_caps(params, [rule], db, nb, dx, CAP_CANDIDATES)
+        t_tune += time.time() - t0
+    s0 = B.system_setup(0)
+    learned = learned_bits(ctx, s0, ratio)
+    bits = learned if learned is not None else rule
     state = {"fallbacks": 0}
 
     def one_solve():
@@ -256,7 +269,9 @@ def run_ours(a, dist):
     out = {"iters": its[-1][0], "converged": all(q[1] for q in its), "explicit_res": explicit_res(r, c, v, b, x),
            "frac_bits": bits, "rule_bits": rule, "learned_bits": learned, "final_bits": its[-1][2],
            "selector_fallbacks": state["fallbacks"], "setup_s": t_setup, "autotune_s": t_tune,
-           "launches": launches, "clocks": clk}
+           "launches": launches, "clocks": clk, "colour_caps": B.colour_caps()}
+    if caps_table is not None:
+        out["colour_cap_tuning"] = [{"caps": t[0], "ms": round(t[1], 3), "iters": t[2][0]} for t in caps_table]
     if a.profile:
         return sec, out, ctx, None
     # ---- the same engine with full FGMRESflex cycles (no early restart)
@@ -294,54 +309,78 @@ def run_ours(a, dist):
         arr.close()
     # ---- the FP64 and FP32-mixed siblings on the same batched design
     if not a.no_fp_batched:
-        out["fp64_batched"] = fp_batched_row(ctx, a, B, r, c, v, b, nrm_b, sagb.F64)
         out["fp32_batched"] = fp_batched_row(ctx, a, B, r, c, v, b, nrm_b, sagb.F32)
+        out["fp64_batched"] = fp_batched_row(ctx, a, B, r, c, v, b, nrm_b, sagb.F64,
+                                             None if a.no_tune_caps else FP_CAP_CANDIDATES)
     B.close()
     # ---- comparison rows on the same GPU
     out["plain"] = plain_row(ctx, a, r, c, v, b, nrm_b)
     if not a.no_multicolor:
         out["multicolor"] = multicolor_row(ctx, a, r, c, v, b, nrm_b)
     if not a.no_batched:
-        out["batched"] = batched_rows(ctx, a, r, c, v, b, nrm_b, dist, bits, rule)
+        out["batched"] = batched_rows(ctx, a, r, c, v, b, nrm_b, dist, bits, rule, out.get("colour_caps"))
     out["setup"] = setup_row(ctx, r, c, v)
     return sec, out, ctx, out["plain"].pop("state")
 
 
-def fp_batched_row(ctx, a, B, r, c, v, b, nrm_b, prec):
+FP_CAP_CANDIDATES = [[8, 2], [8, 1], [8, 4], [8, 2, 1]]
+
+
+def fp_batched_row(ctx, a, B, r, c, v, b, nrm_b, prec, cap_candidates=None):
     """FP64-AMG-FGMRES (or FP32-mixed) on the headline's batched design: the
-    same coarsening, colour caps, coarsest-level size, graph-captured Arnoldi
-    steps and autotuned launch shapes as the integer engine; b, x in HBM,
-    explicit-residual stop, CUDA events on the library's stream."""
+    same coarsening, coarsest-level size, graph-captured Arnoldi steps and
+    autotuned launch shapes as the integer engine, the colour caps either the
+    integer batch's or tuned for this solver by its own time to solution
+    (cap_candidates); b, x in HBM, explicit-residual stop, CUDA events on the
+    library's stream."""
     import sagb
     N = len(b)
+    params = sagb.solver_params(m=a.m, explicit_stop=1)
+    db = sagb.DeviceArray.from_host(ctx, b)
+    dx = sagb.DeviceArray(ctx, N, np.float64)
+    zeros = sagb.DeviceArray.from_host(ctx, np.zeros(N))
+    nb = np.array([nrm_b])
+    e0, e1 = sagb.Event(), sagb.Event()
+
+    def timed(F, reps):
+        def one():
+            sagb.check(sagb.lib().sa_memcpy(ctx.h, dx.ptr, zeros.ptr, 8 * N))
+            return F.solve(params, db, nb, dx)
+        one()
+        ctx.sync()
+        e0.record(ctx)
+        for _ in range(reps):
+            it, cv = one()
+        e1.record(ctx)
+        ctx.sync()
+        return e0.elapsed_ms(e1) / 1000.0 / reps, it, cv
+
+    table = None
+    if cap_candidates:
+        table = []
+        keep_caps = B.colour_caps()
+        for caps in cap_candidates:
+            B.set_colour_caps(caps)
+            F = sagb.BatchFp(ctx, B, prec)
+            F.autotune(2)
+            sec, it, cv = timed(F, 2)
+            table.append((caps, sec if cv[0] else float("inf"), int(it[0])))
+            F.close()
+        B.set_colour_caps(min(table, key=lambda t: t[1])[0])
     t0 = time.time()
     F = sagb.BatchFp(ctx, B, prec)
     t_setup = time.time() - t0
     t0 = time.time()
     F.autotune(2)
     t_tune = time.time() - t0
-    params = sagb.solver_params(m=a.m, explicit_stop=1)
-    db = sagb.DeviceArray.from_host(ctx, b)
-    dx = sagb.DeviceArray(ctx, N, np.float64)
-    zeros = sagb.DeviceArray.from_host(ctx, np.zeros(N))
-    nb = np.array([nrm_b])
-
-    def one():
-        sagb.check(sagb.lib().sa_memcpy(ctx.h, dx.ptr, zeros.ptr, 8 * N))
-        return F.solve(params, db, nb, dx)
-
-    one()
-    reps = 3
-    e0, e1 = sagb.Event(), sagb.Event()
-    ctx.sync()
-    e0.record(ctx)
-    for _ in range(reps):
-        it, cv = one()
-    e1.record(ctx)
-    ctx.sync()
-    row = {"value": e0.elapsed_ms(e1) / 1000.0 / reps, "iters": int(it[0]), "converged": bool(cv[0]),
+    sec, it, cv = timed(F, 3)
+    row = {"value": sec, "iters": int(it[0]), "converged": bool(cv[0]),
            "explicit_res": explicit_res(r, c, v, b, dx.download()), "vcycle_ms": F.time_vcycle(10),
-           "setup_s": t_setup, "autotune_s": t_tune}
+           "setup_s": t_setup, "autotune_s": t_tune, "colour_caps": B.colour_caps()}
+    if table is not None:
+        row["colour_cap_tuning"] = [{"caps": t[0], "ms": round(t[1] * 1e3, 3), "iters": t[2]} for t in table]
+        B.set_colour_caps(keep_caps)
+        B.autotune(2)
     for arr in (db, dx, zeros):
         arr.close()
     F.close()
@@ -468,7 +507,7 @@ def batch_rooflines(ctx, B, a):
     return {"per_op": per, "families": fam, "coarse_lu_ms": t_lu, "vcycle_ms": t_v}
 
 
-def batched_rows(ctx, a, r, c, v, b, nrm_b, dist, bits, rule):
+def batched_rows(ctx, a, r, c, v, b, nrm_b, dist, bits, rule, caps=None):
     """Four right-hand sides of the same 128^3 system solved together (the
     matrix entries are read once for all four)."""
     import sagb
@@ -476,6 +515,8 @@ def batched_rows(ctx, a, r, c, v, b, nrm_b, dist, bits, rule):
     nrhs = 4
     t0 = time.time()
     B = sagb.Batch(ctx, [(r, c, v)], nrhs)
+    if caps:
+        B.set_colour_caps(caps)
     t_setup = time.time() - t0
     B.autotune(2)
     cols = [b] + [build_system(a.n, seed=1 + dist.rank + 1000 * k)[3] for k in range(1, nrhs)]
@@ -706,6 +747,9 @@ def main_ours(a):
         line["ops"] = [(p["level"], p["op"], p["n"], p["colours"], round(p["ms"], 4),
                         round(p["bytes"] / (p["ms"] * 1e-3) / 1e9, 1)) for p in k["per_op"]]
     line["cycle_bits"] = a.cycle_bits
+    line["colour_caps"] = out.get("colour_caps")
+    if "colour_cap_tuning" in out:
+        line["colour_cap_tuning"] = out["colour_cap_tuning"]
     for key in ("plain", "multicolor", "batched", "setup", "full_cycles"):
         if key in out:
             line[key] = out[key]

@@ -327,6 +327,16 @@ int sa_batch_system_setup(sa_batch B, int sys, sa_setup *out);
 int sa_batch_precondition(sa_ctx ctx, sa_batch B, const int32_t *in, int32_t *out);
 /* time every candidate lanes-per-row value of each level operator and keep the fastest */
 int sa_batch_autotune(sa_ctx ctx, sa_batch B, int reps);
+/* rebuild every system's multicolour SOR split with other colour caps: caps[l]
+ * for level l (the last for all deeper levels; 0 = a proper colouring), the
+ * coarsening kept.  The greedy colouring (Library/helper/helper_graph.hpp:191-219)
+ * stops after the cap and the rows left join their least conflicting colour
+ * (their couplings inside it act Jacobi-like).  Launch shapes fall back to
+ * their defaults (autotune again); results of earlier solves are unaffected.
+ * No counterpart in the reference, which colours without a cap. */
+int sa_batch_set_colour_caps(sa_ctx ctx, sa_batch B, int ncaps, const int *caps, int threads);
+/* the cap in force per level: *ncaps = depth, caps[l] for l < min(cap, depth) */
+int sa_batch_colour_caps(sa_batch B, int cap, int *ncaps, int *caps);
 /* the chosen lanes per row of one operator (op: 0 A, 1 LD sweep, 2 U, 3 P, 4 R) */
 int sa_batch_group(sa_batch B, int level, int op, int *group);
 /* sets the lanes per row of one operator (1, 2, 4, 8, 16, 32; 0 = tile-staged

@@ -52,6 +52,7 @@ struct sa_matrix {
 struct sa_hierarchy {
     int precision = SA_INT;
     sa_amg_params p{};
+    std::vector<int> level_caps;     // multicolour caps per level (a batch's tuned caps), overriding p's
     std::shared_ptr<CsrD> A;         // the scaled fine matrix
     std::shared_ptr<RsChain> chain;  // coarsening shared by all precisions
     std::shared_ptr<IntHierarchy> hi;
@@ -538,6 +539,7 @@ static void build_setup(sa_hierarchy &s, const CsrD &A, Ctx *gpu = nullptr) {
     sm.multicolor = s.p.multicolor;
     sm.max_colours = s.p.max_colours;
     sm.coarse_colours = s.p.coarse_colours;
+    sm.level_caps = s.level_caps;
     if (s.precision == SA_INT) s.hi = std::make_shared<IntHierarchy>(build_int_hierarchy(A, chain, sm));
     else if (s.precision == SA_F64) s.hd = std::make_shared<FpHierarchy<double>>(build_f64_hierarchy(A, chain, sm));
     else s.hf = std::make_shared<FpHierarchy<float>>(build_f32_hierarchy(A, chain, sm));
@@ -592,6 +594,7 @@ extern "C" int sa_setup_derive(sa_setup s, int precision, sa_setup *out) {
     auto *d = new sa_hierarchy();
     d->precision = precision;
     d->p = s->p;
+    d->level_caps = s->level_caps;
     d->A = s->A;
     d->chain = s->chain;
     try {
@@ -1191,6 +1194,34 @@ extern "C" int sa_batch_create(sa_ctx ctx, int nsys, const int *n, const int32_t
     SA_GUARD_END
 }
 
+extern "C" int sa_batch_set_colour_caps(sa_ctx ctx, sa_batch B, int ncaps, const int *caps, int threads) {
+    if (!ctx || !B || ncaps < 0 || (ncaps > 0 && !caps)) return fail(SA_ERR_ARG, "invalid argument");
+    for (int k = 0; k < ncaps; k++)
+        if (caps[k] < 0) return fail(SA_ERR_ARG, "colour caps must be >= 0");
+    SA_GUARD_BEGIN
+    SmootherSpec sm = B->h->sm;
+    sm.level_caps.assign(caps, caps + ncaps);
+    if (threads < 1) threads = (int)std::max(1u, std::thread::hardware_concurrency());
+    auto h = std::make_shared<BatchHierarchy>(rebuild_batch_smoothers(*B->h, sm, threads));
+    const int nrhs = B->eng->nrhs();
+    SAGB_CUDA(cudaSetDevice(ctx->c.device));
+    B->eng.reset();  // the old engine's device arrays go before the new ones come
+    B->h = h;
+    B->eng = std::make_unique<BatchEngine>(ctx->c, B->h, nrhs);
+    SAGB_CUDA(cudaDeviceSynchronize());
+    return SA_OK;
+    SA_GUARD_END
+}
+
+extern "C" int sa_batch_colour_caps(sa_batch B, int cap, int *ncaps, int *caps) {
+    if (!B || !ncaps) return fail(SA_ERR_ARG, "null argument");
+    const SmootherSpec &sm = B->h->sm;
+    const int D = B->h->Dmax;
+    *ncaps = D;
+    for (int l = 0; l < D && l < cap && caps; l++) caps[l] = sm.cap(l);
+    return SA_OK;
+}
+
 extern "C" int sa_batch_destroy(sa_batch B) {
     delete B;
     return SA_OK;
@@ -1218,6 +1249,7 @@ extern "C" int sa_batch_system_setup(sa_batch B, int sys, sa_setup *out) {
     auto *s = new sa_hierarchy();
     s->precision = SA_INT;
     s->p = B->p;
+    s->level_caps = B->h->sm.level_caps;
     s->A = B->h->A_sys[sys];
     s->chain = B->h->chain[sys];
     s->hi = B->h->hi[sys];
@@ -1307,12 +1339,7 @@ extern "C" int sa_batch_rule_ratios(sa_ctx ctx, sa_batch B, const double *b, con
     std::vector<double> hb(N0 * R), hn((size_t)S * R);
     SAGB_CUDA(cudaMemcpy(hb.data(), b, sizeof(double) * hb.size(), cudaMemcpyDefault));
     SAGB_CUDA(cudaMemcpy(hn.data(), nrm_b, sizeof(double) * hn.size(), cudaMemcpyDefault));
-    SmootherSpec sm;
-    sm.omega = B->p.omega;
-    sm.iter = B->p.smooth_iter;
-    sm.multicolor = 1;
-    sm.max_colours = B->p.max_colours;
-    sm.coarse_colours = B->p.coarse_colours;
+    const SmootherSpec sm = B->h->sm;
     // FP64 hierarchies of all systems on host threads (copies of one matrix share one)
     std::vector<std::shared_ptr<FpHierarchy<double>>> hds(S);
     {

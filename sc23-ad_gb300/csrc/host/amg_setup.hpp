@@ -8,6 +8,7 @@
 // therefore performs the same IEEE operations in the same order as the
 // reference and must be compiled without FP contraction (-ffp-contract=off).
 #pragma once
+#include <algorithm>
 #include <cstdint>
 #include <vector>
 
@@ -101,7 +102,11 @@ struct SmootherSpec {
     int multicolor = 0;  // 1: SOR in colour order (the multicolour variant)
     int max_colours = 0; // multicolour: at most this many colours (0: as many as a proper colouring needs)
     int coarse_colours = 0;  // multicolour: the cap below the finest level (0: max_colours)
-    int cap(int level) const { return level > 0 && coarse_colours > 0 ? coarse_colours : max_colours; }
+    std::vector<int> level_caps;  // multicolour: a cap per level, the last for all deeper ones (overrides both)
+    int cap(int level) const {
+        if (!level_caps.empty()) return level_caps[std::min(level, (int)level_caps.size() - 1)];
+        return level > 0 && coarse_colours > 0 ? coarse_colours : max_colours;
+    }
 };
 
 // Greedy colouring, colour by colour, on the symmetrised pattern (the

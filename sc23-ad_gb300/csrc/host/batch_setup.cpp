@@ -29,6 +29,8 @@ static void start(BatchCsr &B, int m) {
 
 static int level_size(const IntHierarchy &h, int l) { return l == 0 ? h.A0.n : h.R[l - 1].n; }
 
+static void assemble_batch(BatchHierarchy &B);
+
 BatchHierarchy build_batch(const std::vector<CsrD> &systems, double theta, int max_levels, double omega,
                            int smooth_iter, int threads, const std::vector<int> &src_in, int max_colours,
                            int coarse_colours, int coarse_size, const std::function<RsChain(const CsrD &)> &big_chain, int big_rows) {
@@ -92,10 +94,65 @@ BatchHierarchy build_batch(const std::vector<CsrD> &systems, double theta, int m
             B.chain[s] = B.chain[src[s]];
             B.hi[s] = B.hi[src[s]];
         }
+    assemble_batch(B);
+    return B;
+}
+
+BatchHierarchy rebuild_batch_smoothers(const BatchHierarchy &old, const SmootherSpec &sm, int threads) {
+    BatchHierarchy B;
+    const int S = old.S;
+    B.S = S;
+    B.chain = old.chain;
+    B.A_sys = old.A_sys;
+    B.hi.resize(S);
+    B.depth.resize(S);
+    B.n_sys.resize(S);
+    B.sm = sm;
+    // systems that shared a hierarchy keep sharing one
+    std::vector<int> src(S);
+    for (int s = 0; s < S; s++) {
+        src[s] = s;
+        for (int t = 0; t < s; t++)
+            if (old.hi[t] == old.hi[s]) {
+                src[s] = t;
+                break;
+            }
+    }
+    std::atomic<int> next{0};
+    std::vector<std::string> errs(S);
+    const int T = std::max(1, std::min(threads, S));
+    auto work = [&]() {
+        std::unique_ptr<HostSerial> serial(T > 1 ? new HostSerial() : nullptr);
+        for (;;) {
+            const int s = next.fetch_add(1);
+            if (s >= S) return;
+            if (src[s] != s) continue;
+            try {
+                B.hi[s] = std::make_shared<IntHierarchy>(build_int_hierarchy(*B.A_sys[s], *B.chain[s], sm));
+            } catch (const SetupError &e) {
+                errs[s] = e.msg;
+            }
+        }
+    };
+    std::vector<std::thread> pool;
+    for (int t = 1; t < T; t++) pool.emplace_back(work);
+    work();
+    for (auto &t : pool) t.join();
+    for (int s = 0; s < S; s++)
+        if (!errs[s].empty()) throw SetupError{"system " + std::to_string(s) + ": " + errs[s]};
+    for (int s = 0; s < S; s++) B.hi[s] = B.hi[src[s]];
+    assemble_batch(B);
+    return B;
+}
+
+// level order, offsets and the block-diagonal operators of a batch whose
+// per-system hierarchies (hi, A_sys, chain) are built
+static void assemble_batch(BatchHierarchy &B) {
+    const int S = B.S;
     int Dmax = 0;
     for (int s = 0; s < S; s++) {
         B.depth[s] = B.hi[s]->depth;
-        B.n_sys[s] = systems[s].n;
+        B.n_sys[s] = B.A_sys[s]->n;
         Dmax = std::max(Dmax, B.depth[s]);
     }
     B.Dmax = Dmax;
@@ -207,7 +264,6 @@ BatchHierarchy build_batch(const std::vector<CsrD> &systems, double theta, int m
             B.Af.rptr.push_back((int)B.Af.cind.size());
         }
     }
-    return B;
 }
 
 // ------------------------------------------------ floating-point sibling

@@ -63,6 +63,10 @@ struct BatchHierarchy {
     SmootherSpec sm;                                // the smoother every system was built with
 };
 
+// The same batch with every system's smoother split rebuilt for other colour
+// caps (sm): the coarsening chains and scaled matrices are kept.
+BatchHierarchy rebuild_batch_smoothers(const BatchHierarchy &old, const SmootherSpec &sm, int threads);
+
 // The FP64 / FP32 sibling of a batch (dfAMG, INTAMG.hpp:13-134, per system):
 // the same systems, coarsening chains, level order and row offsets as the
 // integer batch it derives from, with the floating-point level operators

@@ -132,6 +132,8 @@ SIGNATURES = {
     "sa_batch_system_setup": (C.c_int, [VP, C.c_int, C.POINTER(VP)]),
     "sa_batch_precondition": (C.c_int, [VP, VP, VP, VP]),
     "sa_batch_autotune": (C.c_int, [VP, VP, C.c_int]),
+    "sa_batch_set_colour_caps": (C.c_int, [VP, VP, C.c_int, I32P, C.c_int]),
+    "sa_batch_colour_caps": (C.c_int, [VP, C.c_int, C.POINTER(C.c_int), I32P]),
     "sa_batch_group": (C.c_int, [VP, C.c_int, C.c_int, C.POINTER(C.c_int)]),
     "sa_batch_set_group": (C.c_int, [VP, C.c_int, C.c_int, C.c_int]),
     "sa_batch_sweep_form": (C.c_int, [VP, C.c_int, C.c_int, C.POINTER(C.c_int)]),
@@ -749,6 +751,56 @@ class Batch:
 
     def autotune(self, reps=3):
         check(lib().sa_batch_autotune(self.ctx.h, self.h, reps))
+
+    def set_colour_caps(self, caps, threads=0):
+        """Rebuild the smoother splits with colour caps per level (the last
+        for deeper levels; 0 = proper colouring); launch shapes reset."""
+        a = np.ascontiguousarray(caps, np.int32)
+        check(lib().sa_batch_set_colour_caps(self.ctx.h, self.h, len(a), _ptr(a, I32P), threads))
+        self.depth = self._depth()
+
+    def colour_caps(self):
+        n = C.c_int()
+        check(lib().sa_batch_colour_caps(self.h, 0, C.byref(n), None))
+        a = np.zeros(max(n.value, 1), np.int32)
+        check(lib().sa_batch_colour_caps(self.h, len(a), C.byref(n), _ptr(a, I32P)))
+        return [int(v) for v in a[:n.value]]
+
+    def _depth(self):
+        ns, nr, d, rows = C.c_int(), C.c_int(), C.c_int(), C.c_int64()
+        check(lib().sa_batch_info(self.h, C.byref(ns), C.byref(nr), C.byref(d), C.byref(rows)))
+        return d.value
+
+    def tune_colour_caps(self, params, bits, b, nrm_b, x, candidates, reps=2, tune_reps=2):
+        """Pick the colour caps by measured time to solution: for each
+        candidate cap list, rebuild the splits, autotune the launch shapes and
+        time `reps` solves of (b, nrm_b) into x (device arrays; x is zeroed
+        before each solve) with CUDA events; keep the fastest.  Returns the
+        table [(caps, ms per solve, iterations per pair)] and leaves the
+        batch on the winner, tuned."""
+        table = []
+        zeros = np.zeros(self.rows * self.nrhs)
+        for caps in candidates:
+            self.set_colour_caps(caps)
+            self.autotune(tune_reps)
+            x.upload(zeros)
+            self.solve(params, bits, b, nrm_b, x)  # warm-up (graphs captured)
+            e0, e1 = Event(), Event()
+            best = None
+            for _ in range(reps):
+                x.upload(zeros)
+                self.ctx.sync()
+                e0.record(self.ctx)
+                it, cv, _ = self.solve(params, bits, b, nrm_b, x)
+                e1.record(self.ctx)
+                self.ctx.sync()
+                ms = e0.elapsed_ms(e1)
+                best = ms if best is None else min(best, ms)
+            table.append((list(caps), best if cv.all() else float("inf"), [int(i) for i in it]))
+        win = min(table, key=lambda t: t[1])
+        self.set_colour_caps(win[0])
+        self.autotune(tune_reps)
+        return table
 
     def group(self, level, op):
         g = C.c_int()

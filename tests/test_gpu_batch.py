@@ -341,3 +341,41 @@ def test_early_restart_matches_oracle(ctx):
             assert it_o > 0 and abs(int(it[s]) - it_o) <= 2, (K, s, it[s], it_o)
     assert its[12].sum() < its[0].sum(), (its[0], its[12])
     B.close()
+
+
+def test_colour_caps_rebuild_and_tune(ctx):
+    """sa_batch_set_colour_caps rebuilds every system's split with caps per
+    level (the coarsening kept): the V-cycle is still the oracle's, in the new
+    colour order, bit for bit; colour counts respect the caps; the
+    time-to-solution tuner leaves the batch on its fastest candidate."""
+    systems, bs = _systems(SYSTEMS, 1)
+    B = sagb.Batch(ctx, systems, 1)
+    depth = B.depth
+    B.set_colour_caps([8, 4, 1])
+    caps = B.colour_caps()
+    assert B.depth == depth and caps[:3] == [8, 4, 1] and all(c == 1 for c in caps[2:])
+    for lv in range(B.depth):
+        assert B.level_info(lv, 1)[3] <= caps[lv], lv
+    vin = np.random.default_rng(21).integers(-(1 << 28), 1 << 28, size=B.rows).astype(np.int32)
+    out = B.precondition(vin)
+    keep = of.Keep()
+    for s in range(B.nsys):
+        h = sv.oracle_amg(keep, B.system_setup(s))
+        a, e = B.offsets[s], B.offsets[s + 1]
+        x = np.ascontiguousarray(vin[a:e])
+        ref = np.zeros_like(x)
+        of.lib().or_vcycle_i32(C.byref(h), of.ptr(x, of.i32p), of.ptr(ref, of.i32p))
+        np.testing.assert_array_equal(out[a:e], ref, err_msg=f"system {s}")
+    b = _interleave(B, bs)
+    nrm_b = np.array([np.linalg.norm(x[:, 0]) for x in bs])
+    db = sagb.DeviceArray.from_host(ctx, b)
+    dx = sagb.DeviceArray(ctx, B.rows, np.float64)
+    params = sagb.solver_params(m=20, explicit_stop=1, cycle_bits=12)
+    table = B.tune_colour_caps(params, [29] * B.nsys, db, nrm_b, dx, [[8, 2], [8, 1], [0, 2]], reps=1)
+    assert len(table) == 3 and all(t[1] < float("inf") for t in table), table
+    best = min(table, key=lambda t: t[1])[0]
+    assert B.colour_caps()[:len(best)] == best
+    it, cv, _ = B.solve(params, [29] * B.nsys, db, nrm_b, dx)
+    assert cv.all()
+    db.close(); dx.close()
+    B.close()
