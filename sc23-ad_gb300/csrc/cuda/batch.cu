@@ -131,18 +131,37 @@ __device__ __forceinline__ void row_accumulate(const int *__restrict__ cind, con
                 else acc[r] = wadd(acc[r], vv[q] * (long long)xv[q][r]);
             }
     }
-    for (; j < e1; j += G) {
-        const long long v = __ldg(val + j);
-        const int col = D16 ? row + (int)__ldg(cd + j) : __ldg(cind + j);
-        int xv[R];
-        if constexpr (CG) load_cg_r<R>(x, col, xv);
-        else if constexpr (!SUB) load_r<R>(x, col, xv);
-        else load_rw<R>(x, col, xv);
+    if (j < e1) {  // the last 1-3 entries of this lane: one predicated round, not one round trip each
+        int cc[3];
+        long long vv[3];
 #pragma unroll
-        for (int r = 0; r < R; r++) {
-            if constexpr (SUB) acc[r] = wsub(acc[r], v * (long long)xv[r]);
-            else acc[r] = wadd(acc[r], v * (long long)xv[r]);
+        for (int q = 0; q < 3; q++) {
+            const int jj = j + q * G;
+            const bool ok = jj < e1;
+            cc[q] = ok ? (D16 ? row + (int)__ldg(cd + jj) : __ldg(cind + jj)) : -1;
+            vv[q] = ok ? __ldg(val + jj) : 0;
         }
+        int xv[3][R];
+#pragma unroll
+        for (int q = 0; q < 3; q++) {
+            if (cc[q] < 0) {
+#pragma unroll
+                for (int r = 0; r < R; r++) xv[q][r] = 0;
+            } else if constexpr (CG) {
+                load_cg_r<R>(x, cc[q], xv[q]);
+            } else if constexpr (!SUB) {
+                load_r<R>(x, cc[q], xv[q]);
+            } else {
+                load_rw<R>(x, cc[q], xv[q]);
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < 3; q++)
+#pragma unroll
+            for (int r = 0; r < R; r++) {
+                if constexpr (SUB) acc[r] = wsub(acc[r], vv[q] * (long long)xv[q][r]);
+                else acc[r] = wadd(acc[r], vv[q] * (long long)xv[q][r]);
+            }
     }
 }
 
@@ -181,42 +200,52 @@ __device__ __forceinline__ void bspmv_finish(const DBCsr &A, int row, const long
     if (any) atomicOr(flags, ST_OVERFLOW);
 }
 
+// entries per lane fetched before the launch wait (level SpMVs); eight would
+// cover a 7-point row in one round trip but take 48 registers a thread, and
+// the lost occupancy cost more than the round trip saved (level-0 SpMV of
+// Poisson 128^3: 26.9 us with four, 32.1 us with eight)
+template <int R>
+constexpr int spmv_pre() { return 4; }
+
 template <int R, int G, int MODE, bool D16>
 __global__ void __launch_bounds__(kBThreads)
 k_bspmv(DBCsr A, const int *__restrict__ x, int *__restrict__ y, const int *__restrict__ z,
         const int *__restrict__ row_sys, unsigned *__restrict__ pflag, unsigned *__restrict__ flags) {
     pdl_trigger();
+    constexpr int kSpmvPre = spmv_pre<R>();
     const long long tid = (long long)blockIdx.x * kBThreads + threadIdx.x;
     const int row = (int)(tid / G), lane = (int)(tid % G);
     long long acc[R];
 #pragma unroll
     for (int r = 0; r < R; r++) acc[r] = 0;
     const int e0 = row < A.n ? __ldg(A.rptr + row) : 0, e1 = row < A.n ? __ldg(A.rptr + row + 1) : 0;
-    // the first four entries of each lane are static: fetched before the wait
-    int cc[4], vv[4];
+    // the first kSpmvPre entries of each lane are static: fetched before the
+    // wait, so a row of up to kSpmvPre * G entries costs one round trip for
+    // its entries and one for its vector values
+    int cc[kSpmvPre], vv[kSpmvPre];
 #pragma unroll
-    for (int q = 0; q < 4; q++) {
+    for (int q = 0; q < kSpmvPre; q++) {
         const int j = e0 + lane + q * G;
         cc[q] = j < e1 ? (D16 ? row + (int)__ldg(A.cd + j) : __ldg(A.cind + j)) : -1;
         vv[q] = j < e1 ? __ldg(A.val + j) : 0;
     }
     pdl_wait();
     {
-        int xv[4][R];
+        int xv[kSpmvPre][R];
 #pragma unroll
-        for (int q = 0; q < 4; q++) {
+        for (int q = 0; q < kSpmvPre; q++) {
             if (cc[q] >= 0) load_r<R>(x, cc[q], xv[q]);
             else
 #pragma unroll
                 for (int r = 0; r < R; r++) xv[q][r] = 0;
         }
 #pragma unroll
-        for (int q = 0; q < 4; q++)
+        for (int q = 0; q < kSpmvPre; q++)
 #pragma unroll
             for (int r = 0; r < R; r++) acc[r] = wadd(acc[r], (long long)vv[q] * (long long)xv[q][r]);
     }
-    if (e1 - e0 > 4 * G)
-        row_accumulate<R, G, false, false, D16>(A.cind, A.cd, A.val, e0 + 4 * G, e1, lane, row, x, acc);
+    if (e1 - e0 > kSpmvPre * G)
+        row_accumulate<R, G, false, false, D16>(A.cind, A.cd, A.val, e0 + kSpmvPre * G, e1, lane, row, x, acc);
 #pragma unroll
     for (int r = 0; r < R; r++)
 #pragma unroll
@@ -1404,11 +1433,23 @@ __global__ void k_bresid_f64(int n, const int *__restrict__ rptr, const int *__r
     double acc[R];
 #pragma unroll
     for (int r = 0; r < R; r++) acc[r] = 0.0;
-    for (int j = rptr[row]; j < rptr[row + 1]; j++) {
-        const double a = val[j];
-        const size_t c = (size_t)cind[j] * R;
+    const int e1 = rptr[row + 1];
+    // the row in index order, eight entries' loads issued together
+    for (int j0 = rptr[row]; j0 < e1; j0 += 8) {
+        double a[8], xv[8][R];
 #pragma unroll
-        for (int r = 0; r < R; r++) acc[r] = __dadd_rn(acc[r], __dmul_rn(a, x[c + r]));
+        for (int q = 0; q < 8; q++) {
+            const int j = j0 + q;
+            a[q] = j < e1 ? __ldg(val + j) : 0.0;
+            const size_t c = j < e1 ? (size_t)__ldg(cind + j) * R : 0;
+#pragma unroll
+            for (int r = 0; r < R; r++) xv[q][r] = j < e1 ? __ldg(x + c + r) : 0.0;
+        }
+#pragma unroll
+        for (int q = 0; q < 8; q++)
+            if (j0 + q < e1)
+#pragma unroll
+                for (int r = 0; r < R; r++) acc[r] = __dadd_rn(acc[r], __dmul_rn(a[q], xv[q][r]));
     }
 #pragma unroll
     for (int r = 0; r < R; r++) rv[(size_t)row * R + r] = __dsub_rn(b[(size_t)row * R + r], acc[r]);

@@ -131,12 +131,23 @@ __device__ __forceinline__ void row_acc(const int *__restrict__ cind, const T *_
 #pragma unroll
             for (int r = 0; r < R; r++) acc[r] += vv[q] * xv[q][r];
     }
-    for (; j < e1; j += G) {
-        T xv[R];
-        fld<T, R, MODE>(x, __ldg(cind + j), xv);
-        const T v = __ldg(val + j);
+    if (j < e1) {  // the last 1-3 entries of this lane in one predicated round
+        int cc[3];
+        T vv[3];
 #pragma unroll
-        for (int r = 0; r < R; r++) acc[r] += v * xv[r];
+        for (int q = 0; q < 3; q++) {
+            const int jj = j + q * G;
+            cc[q] = jj < e1 ? __ldg(cind + jj) : -1;
+            vv[q] = jj < e1 ? __ldg(val + jj) : T(0);
+        }
+#pragma unroll
+        for (int q = 0; q < 3; q++) {
+            if (cc[q] < 0) continue;
+            T xv[R];
+            fld<T, R, MODE>(x, cc[q], xv);
+#pragma unroll
+            for (int r = 0; r < R; r++) acc[r] += vv[q] * xv[r];
+        }
     }
 }
 
@@ -151,10 +162,11 @@ k_fspmv(FMat<T> A, const T *__restrict__ x, T *__restrict__ y, const T *__restri
     const int row = (int)(tid / G), lane = (int)(tid % G);
     const bool ok = row < A.n;
     const int e0 = ok ? __ldg(A.rptr + row) : 0, e1 = ok ? __ldg(A.rptr + row + 1) : 0;
-    int cc[4];
-    T vv[4];
+    constexpr int kPre = 4;  // entries per lane fetched before the wait (more cost occupancy)
+    int cc[kPre];
+    T vv[kPre];
 #pragma unroll
-    for (int q = 0; q < 4; q++) {  // static: fetched before the wait
+    for (int q = 0; q < kPre; q++) {  // static: fetched before the wait
         const int j = e0 + lane + q * G;
         cc[q] = j < e1 ? __ldg(A.cind + j) : -1;
         vv[q] = j < e1 ? __ldg(A.val + j) : T(0);
@@ -164,14 +176,14 @@ k_fspmv(FMat<T> A, const T *__restrict__ x, T *__restrict__ y, const T *__restri
 #pragma unroll
     for (int r = 0; r < R; r++) acc[r] = 0;
 #pragma unroll
-    for (int q = 0; q < 4; q++) {
+    for (int q = 0; q < kPre; q++) {
         if (cc[q] < 0) continue;
         T xv[R];
         fld<T, R, 0>(x, cc[q], xv);
 #pragma unroll
         for (int r = 0; r < R; r++) acc[r] += vv[q] * xv[r];
     }
-    if (e1 - e0 > 4 * G) row_acc<T, R, G, 0>(A.cind, A.val, e0 + lane + 4 * G, e1, x, acc);
+    if (e1 - e0 > kPre * G) row_acc<T, R, G, 0>(A.cind, A.val, e0 + lane + kPre * G, e1, x, acc);
     lane_reduce<T, R, G>(acc);
     if (lane == 0 && ok) {
         T out[R];

@@ -7,10 +7,13 @@
 
 namespace sagb {
 
-// append rows of a system block with row/column offsets and the block's shifts
-static void append_block(BatchCsr &B, const CsrI &M, int col_off, int bit, int dbit) {
+// append rows of a system block with row/column offsets and the block's shifts;
+// drop_zeros leaves out stored zero values (they add nothing to an integer row
+// sum: SOR's U holds (1 - 1/omega) d = 0 first in every row at omega = 1)
+static void append_block(BatchCsr &B, const CsrI &M, int col_off, int bit, int dbit, bool drop_zeros = false) {
     for (int i = 0; i < M.n; i++) {
         for (int j = M.rptr[i]; j < M.rptr[i + 1]; j++) {
+            if (drop_zeros && M.val[j] == 0) continue;
             B.cind.push_back(M.cind[j] + col_off);
             B.val.push_back(M.val[j]);
         }
@@ -198,7 +201,7 @@ static void assemble_batch(BatchHierarchy &B) {
             const CsrI &A = l == 0 ? h.A0 : h.CA[l - 1];
             append_block(L.A, A, off, A.bit, 0);
             append_block(L.LD, h.LD[l], off, h.LD[l].bit, h.LD[l].dbit);
-            append_block(L.U, h.U[l], off, h.U[l].bit, 0);
+            append_block(L.U, h.U[l], off, h.U[l].bit, 0, true);
             append_block(L.P, h.P[l], B.offset[l + 1][s], h.P[l].bit, 0);
             const std::vector<int> &col = h.colour[l];
             int nc = 0;
@@ -276,9 +279,10 @@ static void start_t(BatchCsrT<T> &B, int m) {
 }
 
 template <typename T>
-static void append_t(BatchCsrT<T> &B, const CsrT<T> &M, int col_off) {
+static void append_t(BatchCsrT<T> &B, const CsrT<T> &M, int col_off, bool drop_zeros = false) {
     for (int i = 0; i < M.n; i++) {
         for (int j = M.rptr[i]; j < M.rptr[i + 1]; j++) {
+            if (drop_zeros && M.val[j] == T(0)) continue;  // U's (1 - 1/omega) d at omega = 1
             B.cind.push_back(M.cind[j] + col_off);
             B.val.push_back(M.val[j]);
         }
@@ -360,7 +364,7 @@ BatchFp<T> build_batch_fp(const BatchHierarchy &B, int threads) {
             const int off = B.offset[l][s];
             append_t(L.A, l == 0 ? h.A0 : h.CA[l - 1], off);
             append_t(L.LD, h.LD[l], off);
-            append_t(L.U, h.U[l], off);
+            append_t(L.U, h.U[l], off, true);
             append_t(L.P, h.P[l], B.offset[l + 1][s]);
             int nc = 0;
             for (int c : h.colour[l]) nc = std::max(nc, c + 1);
