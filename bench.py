@@ -65,7 +65,9 @@ def parse():
     ap.add_argument("--tune-file", default=None,
                     help="vcycle workload: launch shapes to apply (written by a run without it, so that a run under "
                          "a profiler does not autotune under the profiler)")
-    ap.add_argument("--workload", choices=["poisson128", "batch256", "convdiff128", "precision", "vcycle"],
+    ap.add_argument("--caps", default="8,1", help="vcycle / solve workloads: colour caps per level")
+    ap.add_argument("--no-graphs", action="store_true", help="solve workload: launches without CUDA graphs")
+    ap.add_argument("--workload", choices=["poisson128", "batch256", "convdiff128", "precision", "vcycle", "solve"],
                     default="poisson128",
                     help="poisson128: the headline; batch256: 256 27-point systems x 4 right-hand sides; "
                          "convdiff128: learned vs rule bits on convection-diffusion 128^3, Pe 50")
@@ -1035,14 +1037,14 @@ def main_convdiff(a):
     dist.close()
 
 
-def main_vcycle(a):
-    """Profiling aid: the headline's batched V-cycle (autotuned) on the 128^3
-    system (--n), --steps V-cycles inside a profiler collection range (run
-    under a profiler started with collection off)."""
+def profiled_batch(a, ctx, r, c, v):
+    """The headline's batch with colour caps --caps and launch shapes from
+    --tune-file when it exists (else autotuned and written there), so that a
+    run under a profiler does not autotune under the profiler."""
     import sagb
-    ctx = sagb.Context(0)
-    r, c, v, b = build_system(a.n, seed=1)
     B = sagb.Batch(ctx, [(r, c, v)], 1)
+    if a.caps:
+        B.set_colour_caps([int(t) for t in a.caps.split(",")])
     if a.tune_file and os.path.exists(a.tune_file):
         with open(a.tune_file) as f:
             tune = json.load(f)
@@ -1059,6 +1061,17 @@ def main_vcycle(a):
                 json.dump({"forms": [B.sweep_form(l) for l in range(B.depth)],
                            "groups": [[B.group(l, op) for op in range(5)] for l in range(B.depth)],
                            "compressed": [[B.compressed(l, 0), B.compressed(l, 2)] for l in range(B.depth)]}, f)
+    return B
+
+
+def main_vcycle(a):
+    """Profiling aid: the headline's batched V-cycle (autotuned) on the 128^3
+    system (--n), --steps V-cycles inside a profiler collection range (run
+    under a profiler started with collection off)."""
+    import sagb
+    ctx = sagb.Context(0)
+    r, c, v, b = build_system(a.n, seed=1)
+    B = profiled_batch(a, ctx, r, c, v)
     x = sagb.DeviceArray.from_host(ctx, np.random.default_rng(3).integers(-(1 << 28), 1 << 28, size=B.rows)
                                    .astype(np.int32))
     y = sagb.DeviceArray(ctx, B.rows, np.int32)
@@ -1072,6 +1085,39 @@ def main_vcycle(a):
     ctx.sync()
     sagb.check(sagb.lib().sa_profiler_range(0))
     print(json.dumps({"workload": f"batched V-cycle, Poisson {a.n}^3", "vcycles": a.steps,
+                      "launches": ctx.launches() - l0}), flush=True)
+
+
+def main_solve_profile(a):
+    """Profiling aid: --steps whole headline solves (rule's F, early restart,
+    --caps colour caps, --tune-file shapes) inside a profiler collection range."""
+    import sagb
+    ctx = sagb.Context(0)
+    if a.no_graphs:  # every kernel a launch of its own (a profiler lists them one by one)
+        ctx.set_option(sagb.OPT_GRAPHS, 0)
+    r, c, v, b = build_system(a.n, seed=1)
+    B = profiled_batch(a, ctx, r, c, v)
+    N = len(b)
+    nb = np.array([np.linalg.norm(b)])
+    db = sagb.DeviceArray.from_host(ctx, b)
+    dx = sagb.DeviceArray(ctx, N, np.float64)
+    p = sagb.solver_params(m=a.m, explicit_stop=1, cycle_bits=a.cycle_bits)
+    zeros = np.zeros(N)
+    for _ in range(a.warmup):
+        dx.upload(zeros)
+        B.solve(p, [29], db, nb, dx)
+    ctx.sync()
+    l0 = ctx.launches()
+    its = []
+    for _ in range(a.steps):
+        dx.upload(zeros)
+        ctx.sync()
+        sagb.check(sagb.lib().sa_profiler_range(1))
+        it, cv, fb = B.solve(p, [29], db, nb, dx)
+        ctx.sync()
+        sagb.check(sagb.lib().sa_profiler_range(0))
+        its.append(int(it[0]))
+    print(json.dumps({"workload": f"batched solve, Poisson {a.n}^3", "solves": a.steps, "iters": its,
                       "launches": ctx.launches() - l0}), flush=True)
 
 
@@ -1151,5 +1197,7 @@ if __name__ == "__main__":
         main_precision(args)
     elif args.workload == "vcycle":
         main_vcycle(args)
+    elif args.workload == "solve":
+        main_solve_profile(args)
     else:
         main_ours(args)

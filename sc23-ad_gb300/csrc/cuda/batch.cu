@@ -1113,18 +1113,23 @@ __global__ void k_bbegin(int P, const double *__restrict__ e0, double eps, BPair
     e[(size_t)p * (m + 1)] = 1LL << q.bit;
 }
 
+// the elementwise Krylov kernels run one row per thread: block b covers rows
+// row0 + (b % kTileSub) * kBThreads + [0, kBThreads) of tile b / kTileSub
+constexpr int kTileSub = kTileRows / kBThreads;
+
 template <int R>
-__global__ void k_bv0(const BTile *__restrict__ tiles, const double *__restrict__ rv, const BPair *__restrict__ pairs,
-                      int *__restrict__ V0) {
-    const BTile t = tiles[blockIdx.x];
-    for (int i = t.row0 + threadIdx.x; i < t.row1; i += blockDim.x) {
+__global__ void __launch_bounds__(kBThreads)
+k_bv0(const BTile *__restrict__ tiles, const double *__restrict__ rv, const BPair *__restrict__ pairs,
+      int *__restrict__ V0) {
+    const BTile t = tiles[blockIdx.x / kTileSub];
+    const int i = t.row0 + (blockIdx.x % kTileSub) * kBThreads + threadIdx.x;
+    if (i >= t.row1) return;
 #pragma unroll
-        for (int r = 0; r < R; r++) {
-            const BPair &q = pairs[t.sys * R + r];
-            if (!q.active) continue;
-            const double fact = (double)(1LL << q.bit);
-            V0[(size_t)i * R + r] = d2i_x86(__dmul_rn(__dmul_rn(rv[(size_t)i * R + r], q.e_inv), fact));
-        }
+    for (int r = 0; r < R; r++) {
+        const BPair &q = pairs[t.sys * R + r];
+        if (!q.active) continue;
+        const double fact = (double)(1LL << q.bit);
+        V0[(size_t)i * R + r] = d2i_x86(__dmul_rn(__dmul_rn(__ldg(rv + (size_t)i * R + r), q.e_inv), fact));
     }
 }
 
@@ -1388,42 +1393,43 @@ __global__ void k_btrsv(int P, int m, const BPair *__restrict__ pairs, const lon
     }
 }
 
-// x += y_k Z_k 2^-bit, k = 0..jn-1 in order (Axpy_D, blas1.hpp:252-258)
+// x += y_k Z_k 2^-bit, k = 0..jn-1 in order (Axpy_D, blas1.hpp:252-258).  The
+// power-of-two scale is applied to y_k first (exact, so (y_k 2^-bit) Z equals
+// (y_k Z) 2^-bit) and each term is one fused multiply-add: GB300's FP64 rate
+// is low, and separate operations made this kernel FP64-bound
 template <int R>
-__global__ void k_bxupd(const BTile *__restrict__ tiles, int m, size_t vstride, const BPair *__restrict__ pairs,
-                        const double *__restrict__ yall, const int *__restrict__ Z, double *__restrict__ x) {
-    const BTile t = tiles[blockIdx.x];
+__global__ void __launch_bounds__(kBThreads)
+k_bxupd(const BTile *__restrict__ tiles, int m, size_t vstride, const BPair *__restrict__ pairs,
+        const double *__restrict__ yall, const int *__restrict__ Z, double *__restrict__ x) {
+    const BTile t = tiles[blockIdx.x / kTileSub];
     __shared__ double sy[R][64];
     __shared__ int sjn[R];
-    __shared__ double sfi[R];
     if (threadIdx.x < R) {
-        const int p = t.sys * R + threadIdx.x;
-        const BPair &q = pairs[p];
-        const bool ok = q.jn > 0 && !q.bad;
-        sjn[threadIdx.x] = ok ? q.jn : 0;
-        sfi[threadIdx.x] = 1.0 / (double)(1LL << q.bit);
+        const BPair &q = pairs[t.sys * R + threadIdx.x];
+        sjn[threadIdx.x] = q.jn > 0 && !q.bad ? q.jn : 0;
     }
     __syncthreads();
     for (int idx = threadIdx.x; idx < R * m; idx += blockDim.x) {
         const int r = idx / m, k = idx % m;
-        sy[r][k] = k < sjn[r] ? yall[(size_t)(t.sys * R + r) * m + k] : 0.0;
+        const BPair &q = pairs[t.sys * R + r];
+        sy[r][k] = k < sjn[r] ? __dmul_rn(yall[(size_t)(t.sys * R + r) * m + k], 1.0 / (double)(1LL << q.bit)) : 0.0;
     }
     __syncthreads();
-    for (int i = t.row0 + threadIdx.x; i < t.row1; i += blockDim.x) {
+    const int i = t.row0 + (blockIdx.x % kTileSub) * kBThreads + threadIdx.x;
+    if (i >= t.row1) return;
 #pragma unroll
-        for (int r = 0; r < R; r++) {
-            const int jn = sjn[r];
-            if (!jn) continue;
-            double xi = x[(size_t)i * R + r];
-            for (int k = 0; k < jn; k++)
-                xi = __dadd_rn(xi, __dmul_rn(__dmul_rn(sy[r][k], (double)Z[(size_t)k * vstride + (size_t)i * R + r]), sfi[r]));
-            x[(size_t)i * R + r] = xi;
-        }
+    for (int r = 0; r < R; r++) {
+        const int jn = sjn[r];
+        if (!jn) continue;
+        double xi = x[(size_t)i * R + r];
+        for (int k = 0; k < jn; k++) xi = fma(sy[r][k], (double)__ldg(Z + (size_t)k * vstride + (size_t)i * R + r), xi);
+        x[(size_t)i * R + r] = xi;
     }
 }
 
-// r = b - A x per row in the reference's order (row-sequential FP64 SpMV,
-// then Axpby(1, b, -1, r)), every right-hand side
+// r = b - A x per row (irsolver.hpp:32-33), every right-hand side: the row's
+// products summed in index order with fused multiply-adds (GB300's FP64 rate
+// is low; a separate multiply and add per entry made this kernel FP64-bound)
 template <int R>
 __global__ void k_bresid_f64(int n, const int *__restrict__ rptr, const int *__restrict__ cind,
                              const double *__restrict__ val, const double *__restrict__ x, const double *__restrict__ b,
@@ -1449,7 +1455,7 @@ __global__ void k_bresid_f64(int n, const int *__restrict__ rptr, const int *__r
         for (int q = 0; q < 8; q++)
             if (j0 + q < e1)
 #pragma unroll
-                for (int r = 0; r < R; r++) acc[r] = __dadd_rn(acc[r], __dmul_rn(a[q], xv[q][r]));
+                for (int r = 0; r < R; r++) acc[r] = fma(a[q], xv[q][r], acc[r]);
     }
 #pragma unroll
     for (int r = 0; r < R; r++) rv[(size_t)row * R + r] = __dsub_rn(b[(size_t)row * R + r], acc[r]);
@@ -1475,14 +1481,18 @@ __global__ void k_bnorm_part(const BTile *__restrict__ tiles, const double *__re
         for (int r = 0; r < R; r++) part[(size_t)blockIdx.x * R + r] = s[r];
 }
 
+// one warp per pair: lanes take the system's tiles in turn, then a fixed
+// shuffle tree (the same order every time)
 __global__ void k_bnorm_fin(int S, int R, const int *__restrict__ tile_ptr, const double *__restrict__ part,
                             double *__restrict__ out) {
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    const int p = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32, lane = threadIdx.x & 31;
     if (p >= S * R) return;
     const int s = p / R, r = p % R;
     double acc = 0;
-    for (int k = tile_ptr[s]; k < tile_ptr[s + 1]; k++) acc += part[(size_t)k * R + r];
-    out[p] = sqrt(acc);
+    for (int k = tile_ptr[s] + lane; k < tile_ptr[s + 1]; k += 32) acc += part[(size_t)k * R + r];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) out[p] = sqrt(acc);
 }
 
 // ============================================================== host side
@@ -2283,7 +2293,7 @@ struct BatchEngine::Impl {
             k_bnorm_part<R><<<ntiles, kBThreads, 0, c.stream>>>(tiles, v, npart);
         });
         const int P = S * Rn;
-        k_bnorm_fin<<<(P + 127) / 128, 128, 0, c.stream>>>(S, Rn, tile_ptr, npart, nrm);
+        k_bnorm_fin<<<(P + 7) / 8, 256, 0, c.stream>>>(S, Rn, tile_ptr, npart, nrm);
         c.launches += 2;
     }
 
@@ -2465,7 +2475,7 @@ struct BatchEngine::Impl {
             k_bbegin<<<(P + 127) / 128, 128, 0, c.stream>>>(P, e0, kp.eps, pairs, e, acc, m, kp.cycle_bits);
             by_r([&](auto RR) {
                 constexpr int R = decltype(RR)::value;
-                k_bv0<R><<<ntiles, kBThreads, 0, c.stream>>>(tiles, rvec, pairs, V);
+                k_bv0<R><<<ntiles * kTileSub, kBThreads, 0, c.stream>>>(tiles, rvec, pairs, V);
             });
             c.launches += 2;
             const bool in_graph = cycle_steps();
@@ -2473,7 +2483,7 @@ struct BatchEngine::Impl {
             k_btrsv<<<(P + 127) / 128, 128, 0, c.stream>>>(P, m, pairs, H, e, y);
             by_r([&](auto RR) {
                 constexpr int R = decltype(RR)::value;
-                k_bxupd<R><<<ntiles, kBThreads, 0, c.stream>>>(tiles, m, N0 * Rn, pairs, y, Z, x);
+                k_bxupd<R><<<ntiles * kTileSub, kBThreads, 0, c.stream>>>(tiles, m, N0 * Rn, pairs, y, Z, x);
             });
             c.launches += 2;
             SAGB_CUDA(cudaMemcpyAsync(hp.data(), pairs, sizeof(BPair) * P, cudaMemcpyDeviceToHost, c.stream));

@@ -471,21 +471,21 @@ __global__ void k_fbegin(int P, const double *__restrict__ nrm, double eps, FPai
     q.e_inv = 1.0 / (double)e0;
 }
 
+// the elementwise Krylov kernels run one row per thread: block b covers rows
+// row0 + (b % kFTileSub) * kFThreads + [0, kFThreads) of tile b / kFTileSub
+constexpr int kFTileSub = kFTileRows / kFThreads;
+
 template <typename T, int R>
-__global__ void k_fv0(const FTile *__restrict__ tiles, const double *__restrict__ rv, const FPair *__restrict__ pairs,
-                      T *__restrict__ V0) {
-    const FTile t = tiles[blockIdx.x];
-    double einv[R];
-    bool act[R];
+__global__ void __launch_bounds__(kFThreads)
+k_fv0(const FTile *__restrict__ tiles, const double *__restrict__ rv, const FPair *__restrict__ pairs,
+      T *__restrict__ V0) {
+    const FTile t = tiles[blockIdx.x / kFTileSub];
+    const int i = t.row0 + (blockIdx.x % kFTileSub) * kFThreads + threadIdx.x;
+    if (i >= t.row1) return;
 #pragma unroll
-    for (int r = 0; r < R; r++) {
-        act[r] = pairs[t.sys * R + r].active != 0;
-        einv[r] = pairs[t.sys * R + r].e_inv;
-    }
-    for (int i = t.row0 + threadIdx.x; i < t.row1; i += blockDim.x)
-#pragma unroll
-        for (int r = 0; r < R; r++)
-            if (act[r]) V0[(size_t)i * R + r] = (T)(rv[(size_t)i * R + r] * einv[r]);
+    for (int r = 0; r < R; r++)
+        if (pairs[t.sys * R + r].active)
+            V0[(size_t)i * R + r] = (T)(__ldg(rv + (size_t)i * R + r) * pairs[t.sys * R + r].e_inv);
 }
 
 // w = A z on one tile's rows, part[0][tile] = V0 . w
@@ -671,9 +671,10 @@ __global__ void k_ftrsv(int P, int m, const FPair *__restrict__ pairs, const T *
 // x += y_k Z_k, k = 0 .. jn-1 in order (Axpy<double>, or AxpyFD for float:
 // x += (double)(y_k * z), blas1.hpp:98-101)
 template <typename T, int R>
-__global__ void k_fxupd(const FTile *__restrict__ tiles, int m, size_t vstride, const FPair *__restrict__ pairs,
-                        const T *__restrict__ yall, const T *__restrict__ Z, double *__restrict__ x) {
-    const FTile t = tiles[blockIdx.x];
+__global__ void __launch_bounds__(kFThreads)
+k_fxupd(const FTile *__restrict__ tiles, int m, size_t vstride, const FPair *__restrict__ pairs,
+        const T *__restrict__ yall, const T *__restrict__ Z, double *__restrict__ x) {
+    const FTile t = tiles[blockIdx.x / kFTileSub];
     __shared__ T sy[R][64];
     __shared__ int sjn[R];
     if (threadIdx.x < R) {
@@ -686,15 +687,15 @@ __global__ void k_fxupd(const FTile *__restrict__ tiles, int m, size_t vstride, 
         sy[r][k] = k < sjn[r] ? yall[(size_t)(t.sys * R + r) * m + k] : T(0);
     }
     __syncthreads();
-    for (int i = t.row0 + threadIdx.x; i < t.row1; i += blockDim.x) {
+    const int i = t.row0 + (blockIdx.x % kFTileSub) * kFThreads + threadIdx.x;
+    if (i >= t.row1) return;
 #pragma unroll
-        for (int r = 0; r < R; r++) {
-            const int jn = sjn[r];
-            if (!jn) continue;
-            double xi = x[(size_t)i * R + r];
-            for (int k = 0; k < jn; k++) xi += (double)(sy[r][k] * Z[(size_t)k * vstride + (size_t)i * R + r]);
-            x[(size_t)i * R + r] = xi;
-        }
+    for (int r = 0; r < R; r++) {
+        const int jn = sjn[r];
+        if (!jn) continue;
+        double xi = x[(size_t)i * R + r];
+        for (int k = 0; k < jn; k++) xi += (double)(sy[r][k] * __ldg(Z + (size_t)k * vstride + (size_t)i * R + r));
+        x[(size_t)i * R + r] = xi;
     }
 }
 
@@ -708,14 +709,25 @@ __global__ void k_fresid(int n, const int *__restrict__ rptr, const int *__restr
     double acc[R];
 #pragma unroll
     for (int r = 0; r < R; r++) acc[r] = 0.0;
-    for (int j = rptr[row]; j < rptr[row + 1]; j++) {
-        const double a = val[j];
-        const size_t c = (size_t)cind[j] * R;
+    const int e1 = rptr[row + 1];
+    for (int j0 = rptr[row]; j0 < e1; j0 += 8) {  // eight entries' loads issued together, summed in order
+        double a[8], xv[8][R];
 #pragma unroll
-        for (int r = 0; r < R; r++) acc[r] = __dadd_rn(acc[r], __dmul_rn(a, x[c + r]));
+        for (int q = 0; q < 8; q++) {
+            const int j = j0 + q;
+            a[q] = j < e1 ? __ldg(val + j) : 0.0;
+            const size_t c = j < e1 ? (size_t)__ldg(cind + j) * R : 0;
+#pragma unroll
+            for (int r = 0; r < R; r++) xv[q][r] = j < e1 ? __ldg(x + c + r) : 0.0;
+        }
+#pragma unroll
+        for (int q = 0; q < 8; q++)
+            if (j0 + q < e1)
+#pragma unroll
+                for (int r = 0; r < R; r++) acc[r] = fma(a[q], xv[q][r], acc[r]);
     }
 #pragma unroll
-    for (int r = 0; r < R; r++) rv[(size_t)row * R + r] = __dsub_rn(b[(size_t)row * R + r], acc[r]);
+    for (int r = 0; r < R; r++) rv[(size_t)row * R + r] = b[(size_t)row * R + r] - acc[r];
 }
 
 // per-tile sums of squares, then per pair over its tiles (fixed order)
@@ -739,14 +751,17 @@ __global__ void __launch_bounds__(kFThreads) k_fnorm_part(const FTile *__restric
         for (int r = 0; r < R; r++) part[(size_t)blockIdx.x * R + r] = s[r];
 }
 
+// one warp per pair, lanes over the system's tiles, a fixed shuffle tree
 __global__ void k_fnorm_fin(int S, int R, const int *__restrict__ tile_ptr, const double *__restrict__ part,
                             double *__restrict__ out) {
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    const int p = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32, lane = threadIdx.x & 31;
     if (p >= S * R) return;
     const int s = p / R, r = p % R;
     double acc = 0;
-    for (int k = tile_ptr[s]; k < tile_ptr[s + 1]; k++) acc += part[(size_t)k * R + r];
-    out[p] = sqrt(acc);
+    for (int k = tile_ptr[s] + lane; k < tile_ptr[s + 1]; k += 32) acc += part[(size_t)k * R + r];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) out[p] = sqrt(acc);
 }
 
 // ============================================================== host side
@@ -1169,7 +1184,7 @@ class FpImpl : public BatchFpEngine::Base {
             k_fnorm_part<R><<<ntiles, kFThreads, 0, c.stream>>>(tiles, v, npart);
         });
         const int P = S * Rn;
-        k_fnorm_fin<<<(P + 127) / 128, 128, 0, c.stream>>>(S, Rn, tile_ptr, npart, nrm);
+        k_fnorm_fin<<<(P + 7) / 8, 256, 0, c.stream>>>(S, Rn, tile_ptr, npart, nrm);
         c.launches += 2;
     }
 
@@ -1314,7 +1329,7 @@ class FpImpl : public BatchFpEngine::Base {
             k_fbegin<T><<<(P + 127) / 128, 128, 0, c.stream>>>(P, nrm, kp.eps, pairs, e, m);
             by_r([&](auto RR) {
                 constexpr int R = decltype(RR)::value;
-                k_fv0<T, R><<<ntiles, kFThreads, 0, c.stream>>>(tiles, rvec, pairs, V);
+                k_fv0<T, R><<<ntiles * kFTileSub, kFThreads, 0, c.stream>>>(tiles, rvec, pairs, V);
             });
             c.launches += 2;
             const bool in_graph = cycle_steps();
@@ -1322,7 +1337,7 @@ class FpImpl : public BatchFpEngine::Base {
             k_ftrsv<T><<<(P + 127) / 128, 128, 0, c.stream>>>(P, m, pairs, H, e, y);
             by_r([&](auto RR) {
                 constexpr int R = decltype(RR)::value;
-                k_fxupd<T, R><<<ntiles, kFThreads, 0, c.stream>>>(tiles, m, N0 * Rn, pairs, y, Z, x);
+                k_fxupd<T, R><<<ntiles * kFTileSub, kFThreads, 0, c.stream>>>(tiles, m, N0 * Rn, pairs, y, Z, x);
             });
             c.launches += 2;
             SAGB_CUDA(cudaMemcpyAsync(hp.data(), pairs, sizeof(FPair) * P, cudaMemcpyDeviceToHost, c.stream));
