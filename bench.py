@@ -467,9 +467,13 @@ def plain_row(ctx, a, r, c, v, b, nrm_b):
 
 
 def batch_rooflines(ctx, B, a):
-    """Average time per call (CUDA events on the library stream around a CUDA
-    graph of repeated calls, as the solver's graphs run them) and algorithmic
-    bytes of every batched level operator, and the V-cycle they make up."""
+    """Average time per call and algorithmic bytes of every batched level
+    operator, and the V-cycle they make up.  Each call is timed cold: CUDA
+    events on the library stream around a CUDA graph of calls, each preceded
+    by a read of a buffer three times the L2, less the time of the reads
+    alone, so that every operator comes from HBM as in the solver's V-cycle
+    (1.3 GB streamed between two uses of one operator); `ms_warm` is the same
+    call repeated on L2-resident data."""
     import sagb
     R = B.nrhs
     rng = np.random.default_rng(3)
@@ -484,7 +488,8 @@ def batch_rooflines(ctx, B, a):
             n, m, nnz, ncol = B.level_info(l, op)
             if n == 0:
                 continue
-            t = B.time_op(l, op, xin, xout, reps)
+            t = B.time_op(l, op, xin, xout, reps, cold=True)
+            t_warm = B.time_op(l, op, xin, xout, reps)
             if op == 1:
                 # LD entries, row pointers, two shifts, the colour row list, in once, out written once
                 by = 8 * nnz + 4 * (n + 1) + 2 * n + 4 * n + 8 * R * n
@@ -496,7 +501,7 @@ def batch_rooflines(ctx, B, a):
                 by = (4 + colb) * nnz + 4 * (n + 1) + n + 4 * R * m + 4 * R * n
                 calls = 1  # A (residual), U (post-smoothing residual), P and R once per V-cycle
             per.append({"level": l, "op": name, "n": n, "nnz": nnz, "colours": ncol if op == 1 else None,
-                        "ms": t, "bytes": by, "per_vcycle": calls,
+                        "ms": t, "ms_warm": t_warm, "bytes": by, "per_vcycle": calls,
                         "d16": bool(op in (0, 2) and B.compressed(l, op))})
             key = "sweep" if op == 1 else "spmv"
             fam[key][0] += calls * t

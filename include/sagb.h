@@ -377,6 +377,11 @@ int sa_batch_coarse_solve(sa_ctx ctx, sa_batch B);
  * stream): op 0..4 as sa_batch_level_op, 5 the coarsest LU (in/out unused), 6
  * the whole V-cycle (level unused); the autotuner times its candidates so */
 int sa_batch_time_op(sa_ctx ctx, sa_batch B, int level, int op, const int32_t *in, int32_t *out, int reps, float *ms);
+/* the same with the L2 flushed (a buffer three times its size read) before
+ * every call and the flush's own time subtracted: the call reads its operator
+ * from HBM, as it does inside a V-cycle, which streams ~1 GB between two uses */
+int sa_batch_time_op_cold(sa_ctx ctx, sa_batch B, int level, int op, const int32_t *in, int32_t *out, int reps,
+                          float *ms);
 /* rows, columns, entries and colour count of one batch level operator */
 int sa_batch_level_info(sa_batch B, int level, int op, int *n, int *m, int64_t *nnz, int *ncolours);
 /* Restarted(FGMRESflex) per pair; bits: F_G per system; nrm_b per pair;

@@ -1454,6 +1454,17 @@ extern "C" int sa_batch_time_op(sa_ctx ctx, sa_batch B, int level, int op, const
     SA_GUARD_END
 }
 
+extern "C" int sa_batch_time_op_cold(sa_ctx ctx, sa_batch B, int level, int op, const int32_t *in, int32_t *out,
+                                     int reps, float *ms) {
+    if (!ctx || !B || !ms || reps < 1 || op < 0 || op > 6 || (op <= 4 && (level < 0 || level >= B->h->Dmax)) ||
+        (op != 5 && (!in || !out)))
+        return fail(SA_ERR_ARG, "invalid argument");
+    SA_GUARD_BEGIN
+    *ms = B->eng->time_op(level, op, in, out, reps, true);
+    return SA_OK;
+    SA_GUARD_END
+}
+
 extern "C" int sa_batch_coarse_solve(sa_ctx ctx, sa_batch B) {
     if (!ctx || !B) return fail(SA_ERR_ARG, "null argument");
     SA_GUARD_BEGIN

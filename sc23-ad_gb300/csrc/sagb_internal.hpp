@@ -295,7 +295,8 @@ class BatchEngine {
     void coarse_solve();  // the batched LU on the engine's own level vectors
     // milliseconds per call as the solver runs it (inside a CUDA graph when
     // graphs are on): op 0..4 as level_op, 5 the coarsest LU, 6 the V-cycle
-    float time_op(int level, int op, const int *in, int *out, int reps);
+    // cold: the L2 flushed before every call (the flush's own time subtracted)
+    float time_op(int level, int op, const int *in, int *out, int reps, bool cold = false);
     void level_info(int level, int op, int *n, int *m, int64_t *nnz, int *ncolours) const;
 
   private:

@@ -141,6 +141,7 @@ SIGNATURES = {
     "sa_batch_tail": (C.c_int, [VP, C.c_int, C.POINTER(C.c_int)]),
     "sa_batch_tail_selftest": (C.c_int, [VP, VP, C.c_int, C.c_double, C.POINTER(C.c_uint)]),
     "sa_batch_time_op": (C.c_int, [VP, VP, C.c_int, C.c_int, VP, VP, C.c_int, C.POINTER(C.c_float)]),
+    "sa_batch_time_op_cold": (C.c_int, [VP, VP, C.c_int, C.c_int, VP, VP, C.c_int, C.POINTER(C.c_float)]),
     "sa_batch_rule_ratios": (C.c_int, [VP, VP, VP, VP, F64P]),
     "sa_batch_solve": (C.c_int, [VP, VP, C.POINTER(SolverParams), I32P, VP, VP, VP, I32P, I32P, I32P]),
     "sa_profiler_range": (C.c_int, [C.c_int]),
@@ -740,13 +741,15 @@ class Batch:
 
     OP_LU, OP_VCYCLE = 5, 6
 
-    def time_op(self, level, op, x=None, out=None, reps=10):
+    def time_op(self, level, op, x=None, out=None, reps=10, cold=False):
         """Milliseconds per call of one level operator (0 A, 1 LD sweep, 2 U,
         3 P, 4 R), the coarsest LU (5) or the V-cycle (6), timed as the solver
-        runs it; x and out are DeviceArrays."""
+        runs it; x and out are DeviceArrays.  cold: the L2 flushed before every
+        call (the operator read from HBM)."""
         ms = C.c_float()
-        check(lib().sa_batch_time_op(self.ctx.h, self.h, level, op, None if x is None else x.ptr,
-                                     None if out is None else out.ptr, reps, C.byref(ms)))
+        fn = lib().sa_batch_time_op_cold if cold else lib().sa_batch_time_op
+        check(fn(self.ctx.h, self.h, level, op, None if x is None else x.ptr, None if out is None else out.ptr, reps,
+                 C.byref(ms)))
         return ms.value
 
     def autotune(self, reps=3):

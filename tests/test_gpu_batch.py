@@ -284,6 +284,8 @@ def test_launch_options_do_not_change_results(ctx):
         assert B.time_op(0, op, x, y, 3) > 0
     assert B.time_op(0, B.OP_LU, reps=3) > 0
     assert B.time_op(0, B.OP_VCYCLE, x, y, 3) > 0
+    # cold timing (the L2 flushed before every call, the flush's time subtracted)
+    assert B.time_op(0, 0, x, y, 3, cold=True) > 0
     x.close(); y.close()
     B.close()
 
