@@ -58,6 +58,8 @@ def parse():
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-engine rows")
     ap.add_argument("--no-fp-batched", action="store_true", help="skip the FP64 / FP32 batched rows")
     ap.add_argument("--no-tune-caps", action="store_true", help="keep the default colour caps (8 / 2)")
+    ap.add_argument("--no-learned-gain", action="store_true",
+                    help="skip the learned-vs-rule rows (convection-diffusion 128^3, anisotropic 1024^2)")
     ap.add_argument("--cycle-bits", type=int, default=12,
                     help="batched integer engine: end a restart cycle once its estimate has fallen 2^K below its "
                          "start (the fixed-point basis stops gaining about 2^20 down); 0: full FGMRESflex cycles")
@@ -322,6 +324,8 @@ def run_ours(a, dist):
     if not a.no_batched:
         out["batched"] = batched_rows(ctx, a, r, c, v, b, nrm_b, dist, bits, rule, out.get("colour_caps"))
     out["setup"] = setup_row(ctx, r, c, v)
+    if not a.no_learned_gain:
+        out["learned_gain"] = learned_gain_rows(ctx, a)
     return sec, out, ctx, out["plain"].pop("state")
 
 
@@ -387,6 +391,56 @@ def fp_batched_row(ctx, a, B, r, c, v, b, nrm_b, prec, cap_candidates=None):
         arr.close()
     F.close()
     return row
+
+
+def learned_gain_rows(ctx, a):
+    """The learned F against the method without the network (the rule's F
+    with the overflow fallback) on the selector's evaluation system
+    (upwinded convection-diffusion 128^3, Peclet 50) and on the anisotropic
+    1024^2 system of the precision workload (eps 1e-3), both through the
+    batched engine with its defaults: time per solve (best of three, CUDA
+    events, discarded cycles included) and iterations."""
+    import bitsel
+    import sagb
+    out = {}
+    sel = bitsel.Selector(ctx)
+    for name, spec in (("convdiff128_pe50", (sagb.GEN_CONVDIFF3D, 128, 50.0, 1, 0)),
+                       ("aniso1024_eps1e-3", (sagb.GEN_ANISO2D, 1024, 1e-3, 1, 0))):
+        r, c, v, b = bitsel.make_system(spec)
+        B = sagb.Batch(ctx, [(r, c, v)], 1)
+        B.autotune(1)
+        nrm = float(np.linalg.norm(b))
+        q = float(B.rule_ratios(b, [nrm])[0])
+        rule = bitsel.rule_of(q)
+        f = sel.choose(sagb.setup_features(B.system_setup(0), q), rule)
+        db = sagb.DeviceArray.from_host(ctx, b)
+        dx = sagb.DeviceArray(ctx, len(b), np.float64)
+        nb = np.array([nrm])
+        p = sagb.solver_params(m=a.m, explicit_stop=1, overflow_fallback=1, cycle_bits=a.cycle_bits)
+        row = {"rows": len(b), "rule_bits": rule, "learned_bits": f}
+        for key, F in (("rule", rule), ("learned", f)):
+            dx.upload(np.zeros(len(b)))
+            B.solve(p, [F], db, nb, dx)
+            best = None
+            for _ in range(3):
+                dx.upload(np.zeros(len(b)))
+                e0, e1 = sagb.Event(), sagb.Event()
+                ctx.sync()
+                e0.record(ctx)
+                it, cv, fb = B.solve(p, [F], db, nb, dx)
+                e1.record(ctx)
+                ctx.sync()
+                ms = e0.elapsed_ms(e1)
+                best = ms if best is None else min(best, ms)
+            row[key] = {"ms": round(best, 3), "iters": int(it[0]), "converged": bool(cv[0]),
+                        "final_bits": int(fb[0]), "explicit_res": explicit_res(r, c, v, b, dx.download())}
+        row["speedup"] = row["rule"]["ms"] / row["learned"]["ms"]
+        out[name] = row
+        db.close()
+        dx.close()
+        B.close()
+    sel.net.close()
+    return out
 
 
 def setup_row(ctx, r, c, v):
@@ -757,7 +811,7 @@ def main_ours(a):
     line["colour_caps"] = out.get("colour_caps")
     if "colour_cap_tuning" in out:
         line["colour_cap_tuning"] = out["colour_cap_tuning"]
-    for key in ("plain", "multicolor", "batched", "setup", "full_cycles"):
+    for key in ("plain", "multicolor", "batched", "setup", "full_cycles", "learned_gain"):
         if key in out:
             line[key] = out[key]
     for key in ("fp64_batched", "fp32_batched"):
@@ -776,8 +830,26 @@ def main_ours(a):
                                 "sample": "one full plain int solve of the same 128^3 system (same hierarchy and "
                                           f"rule bit), oracle C restatement, {threads} threads; iters={it} "
                                           f"res={res:.2e}"}
-    print(json.dumps(line), flush=True)
+    print(json.dumps(tail_last(line)), flush=True)
     dist.close()
+
+
+# the comparisons a reader of the line looks for first, in this order at its
+# end (a log that keeps only the end of a long line still shows them)
+TAIL_KEYS = ("vcycle_ms", "families_ms_per_vcycle", "spmv_A0", "full_cycles", "batched", "fp32_batched",
+             "fp64_batched", "learned_gain", "speedup_vs_plain", "speedup_vs_fp64_plain_gpu", "speedup_vs_fp64_gpu",
+             "roofline", "cpu_baseline", "e2e")
+
+
+def tail_last(line):
+    """The same dict with the bulky per-level diagnostics first and TAIL_KEYS last."""
+    out = {k: v for k, v in line.items() if k not in TAIL_KEYS}
+    for k in ("fp64_batched", "fp32_batched"):
+        if k in line and "colour_cap_tuning" in line[k]:
+            line[k] = dict(line[k])
+            out[k + "_colour_cap_tuning"] = line[k].pop("colour_cap_tuning")
+    out.update((k, line[k]) for k in TAIL_KEYS if k in line)
+    return out
 
 
 # ------------------------------------------------------------- reference arm

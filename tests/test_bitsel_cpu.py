@@ -93,8 +93,12 @@ def test_features_of_a_setup():
 
 def test_trained_selector_gains_on_heldout_sweeps():
     """The committed network, evaluated by the oracle's forward pass on the
-    held-out 20 % of the GPU sweep dataset, needs fewer integer iterations than
-    the reference's rule (a failed F costs the sweep's cap plus the rule)."""
+    held-out 20 % of the GPU sweep dataset, against the reference's rule with
+    the overflow fallback (a failing F redone with one bit less: the first F at
+    or below the rule's that converges, its failed attempts not charged, which
+    favours the rule).  The selector must need fewer iterations overall, a
+    fifth fewer on the anisotropic systems (where the rule's F = 29 converges
+    slowly), pick no failing F, and never cost much more than the rule."""
     import json
     import os
     d = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "sc23-ad_gb300", "data")
@@ -103,23 +107,33 @@ def test_trained_selector_gains_on_heldout_sweeps():
     X, meta = ds["X"].astype(np.float64), json.loads(str(ds["meta"]))
     nin, hid, nout, f_lo = int(z["n_in"]), int(z["hidden"]), int(z["n_out"]), int(z["f_lo"])
     ntr = int(round(0.8 * len(X)))
-    Y, _ = mo.forward(z["params"].astype(np.float64), X[ntr:], nin, hid, nout, z["mu"].astype(np.float64),
+    # the selector clamps features to the training range before the forward pass
+    np.testing.assert_array_equal(z["x_lo"], X[:ntr].min(0))
+    np.testing.assert_array_equal(z["x_hi"], X[:ntr].max(0))
+    Xh = np.clip(X[ntr:], z["x_lo"].astype(np.float64), z["x_hi"].astype(np.float64))
+    Y, _ = mo.forward(z["params"].astype(np.float64), Xh, nin, hid, nout, z["mu"].astype(np.float64),
                       z["sd"].astype(np.float64))
-    sel_it = rule_it = 0
-    fails_sel = fails_rule = 0
+    sel_it = rule_it = sel_an = rule_an = 0
+    fails_sel = 0
     for k, y in enumerate(Y):
-        sw = {q["bit"]: q for q in meta[ntr + k]["sweep"]}
+        m = meta[ntr + k]
+        sw = {q["bit"]: q for q in m["sweep"]}
+        rule = m["rule"]
         f = f_lo + int(np.argmin(y))
-        if y[meta[ntr + k]["rule"] - f_lo] - y[f - f_lo] < bitsel.MARGIN:  # the selector's margin
-            f = meta[ntr + k]["rule"]
-        rule = sw[meta[ntr + k]["rule"]]
-        r_it = rule["iters"] if rule["converged"] else 120
-        fails_rule += not rule["converged"]
+        if y[rule - f_lo] - y[f - f_lo] < bitsel.MARGIN:  # the selector's margin
+            f = rule
+        r_it = next((sw[g]["iters"] for g in range(rule, f_lo - 1, -1) if sw[g]["converged"]), 120)
         if sw[f]["converged"]:
-            sel_it += sw[f]["iters"]
+            s_it = sw[f]["iters"]
         else:
             fails_sel += 1
-            sel_it += 120 + r_it
+            s_it = 120 + r_it
+        assert s_it <= 1.5 * r_it + 4, (m["spec"], f, s_it, rule, r_it)
+        sel_it += s_it
         rule_it += r_it
-    assert fails_sel < fails_rule
-    assert sel_it < 0.95 * rule_it, (sel_it, rule_it)
+        if m["spec"][0] == sagb.GEN_ANISO2D:
+            sel_an += s_it
+            rule_an += r_it
+    assert fails_sel == 0
+    assert sel_it < rule_it, (sel_it, rule_it)
+    assert sel_an < 0.8 * rule_an, (sel_an, rule_an)
