@@ -69,7 +69,8 @@ def parse():
                          "a profiler does not autotune under the profiler)")
     ap.add_argument("--caps", default="8,1", help="vcycle / solve workloads: colour caps per level")
     ap.add_argument("--no-graphs", action="store_true", help="solve workload: launches without CUDA graphs")
-    ap.add_argument("--workload", choices=["poisson128", "batch256", "convdiff128", "precision", "vcycle", "solve"],
+    ap.add_argument("--workload", choices=["poisson128", "batch256", "convdiff128", "precision", "vcycle", "solve",
+                                           "plain_vcycle"],
                     default="poisson128",
                     help="poisson128: the headline; batch256: 256 27-point systems x 4 right-hand sides; "
                          "convdiff128: learned vs rule bits on convection-diffusion 128^3, Pe 50")
@@ -1165,6 +1166,31 @@ def main_vcycle(a):
                       "launches": ctx.launches() - l0}), flush=True)
 
 
+def main_plain_vcycle(a):
+    """Profiling aid: the plain drop-in's V-cycle (reference parameters,
+    natural-order SOR sweeps) on the 128^3 system (--n), --steps V-cycles
+    inside a profiler collection range."""
+    import sagb
+    ctx = sagb.Context(0)
+    r, c, v, b = build_system(a.n, seed=1)
+    M = sagb.Amg(ctx, sagb.INT, setup=sagb.Setup(sagb.INT, r, c, v))
+    N = len(b)
+    x = sagb.DeviceArray.from_host(ctx, np.random.default_rng(3).integers(-(1 << 28), 1 << 28, size=N)
+                                   .astype(np.int32))
+    y = sagb.DeviceArray(ctx, N, np.int32)
+    for _ in range(a.warmup):
+        M.precondition(x, y)
+    ctx.sync()
+    l0 = ctx.launches()
+    sagb.check(sagb.lib().sa_profiler_range(1))
+    for _ in range(a.steps):
+        M.precondition(x, y)
+    ctx.sync()
+    sagb.check(sagb.lib().sa_profiler_range(0))
+    print(json.dumps({"workload": f"plain V-cycle, Poisson {a.n}^3", "vcycles": a.steps,
+                      "launches": ctx.launches() - l0}), flush=True)
+
+
 def main_solve_profile(a):
     """Profiling aid: --steps whole headline solves (rule's F, early restart,
     --caps colour caps, --tune-file shapes) inside a profiler collection range."""
@@ -1276,5 +1302,7 @@ if __name__ == "__main__":
         main_vcycle(args)
     elif args.workload == "solve":
         main_solve_profile(args)
+    elif args.workload == "plain_vcycle":
+        main_plain_vcycle(args)
     else:
         main_ours(args)

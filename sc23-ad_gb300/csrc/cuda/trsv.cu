@@ -14,8 +14,9 @@
 //    result vector lives in shared memory, seeded with `in` (a row reads its own
 //    input once and then overwrites it).  Each level's row data is one 16-byte
 //    aligned block that a bulk copy (cp.async.bulk + mbarrier) brings into a
-//    ring of shared-memory stages several levels ahead, so a level costs shared
-//    memory traffic and one block barrier.
+//    byte ring in shared memory (all of it not taken by the vector) up to
+//    kSlots levels ahead, so a level costs shared memory traffic and one block
+//    barrier.
 //  * k_tri (fine levels): one CTA per SM claims chunks of level-ordered rows
 //    by ticket; a row waits only for the rows it reads.  Integer and FP32
 //    results are published as one 64-bit word {epoch, value}, so a dependency
@@ -38,7 +39,7 @@ namespace sagb {
 constexpr int kTriThreads = 256;   // multi-CTA kernel
 constexpr int kCtaThreads = 1024;  // single-CTA kernel
 constexpr int kBatch = 4;          // dependencies read together per lane (multi-CTA)
-constexpr int kStages = 4;         // bulk-copy ring depth (single CTA)
+constexpr int kSlots = 8;          // levels in flight in the single CTA's bulk-copy ring
 constexpr size_t kSmemMax = 227 * 1024;
 constexpr size_t kCtaVecMax = 150 * 1024;  // largest shared result vector
 
@@ -253,7 +254,7 @@ __device__ __forceinline__ void cta_level(const unsigned char *blk, vt_t<VT> *s_
                                           int sub, int g, bool &ovf) {
     using V = vt_t<VT>;
     constexpr int RPW = 32 / G;
-    constexpr int NW = kCtaThreads / 32;
+    constexpr int NW = kCtaThreads / 32 - 1;  // the last warp issues the bulk copies
     const int *hdr = (const int *)blk;
     const int R = hdr[0];
     const V *val = (const V *)(blk + hdr[2]);
@@ -270,56 +271,121 @@ __device__ __forceinline__ void cta_level(const unsigned char *blk, vt_t<VT> *s_
             row = perm[r];
             const int jb = rp[r], je = rp[r + 1];
             if (g == 0) t = acc_init<VT>(s_out[row], bit);
-            for (int j = jb + g; j < je; j += G) t = acc_sub<VT, EXACT>(t, val[j], s_out[pci[j]]);
+            // four entries of the lane at a time: their loads are issued
+            // together, the products are taken in the lane's order
+            int j = jb + g;
+            for (; j + 3 * G < je; j += 4 * G) {
+                const int c0 = pci[j], c1 = pci[j + G], c2 = pci[j + 2 * G], c3 = pci[j + 3 * G];
+                const V v0 = val[j], v1 = val[j + G], v2 = val[j + 2 * G], v3 = val[j + 3 * G];
+                const V o0 = s_out[c0], o1 = s_out[c1], o2 = s_out[c2], o3 = s_out[c3];
+                t = acc_sub<VT, EXACT>(t, v0, o0);
+                t = acc_sub<VT, EXACT>(t, v1, o1);
+                t = acc_sub<VT, EXACT>(t, v2, o2);
+                t = acc_sub<VT, EXACT>(t, v3, o3);
+            }
+            for (; j < je; j += G) t = acc_sub<VT, EXACT>(t, val[j], s_out[pci[j]]);
         }
         t = acc_reduce<VT>(t, G);
         if (valid && g == 0) s_out[row] = acc_finish<VT>(t, dv[r], bit, dbit, ovf);
     }
 }
 
+// Shared memory of the single-CTA kernel: the result vector, a byte ring for
+// the level blocks, kSlots mbarriers, the ring position of each level in
+// flight, the block offsets and the rows of each level.  The first lane of
+// the last warp (the producer; that warp computes no rows, so issuing copies
+// never delays a level) places every block contiguously in the ring, in level
+// order (at the write position, or at the ring's start when the end has no
+// room), as soon as the ring has room and fewer than kSlots levels are in
+// flight; a block larger than the whole ring is read from global memory
+// instead.  Level d is always placed by the time the CTA reaches it: the
+// producer places it right after the barrier of level d-1 at the latest, when
+// every earlier level has been consumed and the ring is empty.
+//
+// (A variant without the barrier per level, each row waiting on done bits of
+// the rows it reads, ran about twice as slow on the coarse levels of Poisson
+// 128^3: the waiting rows' shared-memory polling slowed the rows being
+// computed more than the barrier costs.)
 template <int VT, int G, bool EXACT>
 __global__ void __launch_bounds__(kCtaThreads, 1)
 k_tri_cta(const unsigned char *__restrict__ blocks, const unsigned *__restrict__ blk_off, int nlev, int n,
-          int bit, int dbit, int stage_bytes, const void *in_, void *out_, unsigned *flags) {
+          int bit, int dbit, int ring_bytes, const void *in_, void *out_, unsigned *flags) {
     using V = vt_t<VT>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     V *s_out = (V *)smem_raw;
     const size_t vec_bytes = ((size_t)n * sizeof(V) + 15) & ~(size_t)15;
-    unsigned char *stage = smem_raw + vec_bytes;
-    unsigned long long *bar = (unsigned long long *)(stage + (size_t)kStages * stage_bytes);
-    unsigned *s_off = (unsigned *)(bar + kStages);  // block offsets in 16-byte units
+    unsigned char *ring = smem_raw + vec_bytes;
+    unsigned long long *bar = (unsigned long long *)(ring + ring_bytes);
+    unsigned *s_pos = (unsigned *)(bar + kSlots);  // ring offset of each level in flight
+    unsigned *s_off = s_pos + kSlots;              // block offsets in 16-byte units
+    const unsigned *s_rows = s_off + nlev + 1;     // rows of each level
     const V *in = (const V *)in_;
     V *out = (V *)out_;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int g = lane % G, sub = lane / G;
+    constexpr int kProducerWarp = kCtaThreads / 32 - 1;
+    const bool compute = warp != kProducerWarp;
+    const bool producer = warp == kProducerWarp && lane == 0;
     bool ovf = false;
 
-    if (threadIdx.x == 0) {
-        for (int s = 0; s < kStages; s++) mbar_init(bar + s, 1);
+    if (producer) {
+        for (int s = 0; s < kSlots; s++) mbar_init(bar + s, 1);
         fence_mbar_init();
     }
     for (int i = threadIdx.x; i < n; i += kCtaThreads) s_out[i] = in[i];
-    for (int i = threadIdx.x; i <= nlev; i += kCtaThreads) s_off[i] = __ldg(blk_off + i);
+    for (int i = threadIdx.x; i <= 2 * nlev; i += kCtaThreads) s_off[i] = __ldg(blk_off + i);
     __syncthreads();
-    auto fits = [&](int d) { return (int)(s_off[d + 1] - s_off[d]) * 16 <= stage_bytes; };
-    auto issue = [&](int d) {  // thread 0: bring level d's block into its stage
-        if (!fits(d)) return;
-        const int s = d % kStages;
-        fence_proxy_async_smem();
-        const unsigned bytes = (s_off[d + 1] - s_off[d]) * 16u;
-        mbar_expect_tx(bar + s, bytes);
-        bulk_g2s(stage + (size_t)s * stage_bytes, blocks + (size_t)s_off[d] * 16, bytes, bar + s);
+    auto bytes_of = [&](int d) { return (s_off[d + 1] - s_off[d]) * 16u; };
+    auto staged = [&](int d) { return bytes_of(d) <= (unsigned)ring_bytes; };
+    // the producer's ring state: levels [consumed, issued) are in flight; the
+    // nst staged ones among them occupy [lo, head), wrapped once when head <= lo
+    int issued = 0, nst = 0;
+    unsigned lo = 0, head = 0;
+    auto issue_more = [&](int consumed) {  // producer only
+        while (issued < nlev && issued - consumed < kSlots) {
+            const int d = issued;
+            if (staged(d)) {
+                const unsigned b = bytes_of(d);
+                unsigned pos;
+                if (nst == 0) {
+                    pos = 0;
+                    lo = 0;
+                } else if (head > lo) {  // [lo, head): room at the end, else at the start
+                    if (b <= (unsigned)ring_bytes - head) pos = head;
+                    else if (b <= lo) pos = 0;
+                    else break;
+                } else {  // [lo, ring) and [0, head): room between head and lo
+                    if (b <= lo - head) pos = head;
+                    else break;
+                }
+                head = pos + b;
+                nst++;
+                const int s = d % kSlots;
+                // the region's previous readers passed the level barrier
+                // before this copy is issued (no proxy fence is needed for a
+                // bulk copy into memory that generic loads only read)
+                s_pos[s] = pos;  // published to the waiting threads by the arrive below
+                mbar_expect_tx(bar + s, b);
+                bulk_g2s(ring + pos, blocks + (size_t)s_off[d] * 16, b, bar + s);
+            }
+            issued++;
+        }
     };
-    if (threadIdx.x == 0)
-        for (int d = 0; d < nlev && d < kStages; d++) issue(d);
-    unsigned phase = 0;  // bit s: parity of stage s's next completion
+    if (producer) issue_more(0);
+    unsigned phase = 0;  // bit s: parity of slot s's next completion
     int stuck = -1;      // level whose copy did not arrive in time
     for (int d = 0; d < nlev; d++) {
-        const bool staged = fits(d);
-        const int s = d % kStages;
+        const bool st = staged(d);
+        const int s = d % kSlots;
         const unsigned char *blk = blocks + (size_t)s_off[d] * 16;
         bool timed_out = false;
-        if (staged) {
+        // a warp with no row in this level neither waits for its block nor
+        // reads it (it only keeps the slot parities)
+        constexpr int kRowsPerWarp = 32 / G;
+        const bool mine = compute && warp * kRowsPerWarp < (int)s_rows[d];
+        if (st && !mine) {
+            phase ^= 1u << s;
+        } else if (st) {
             // bounded wait for the bulk copy of this level
             const unsigned par = (phase >> s) & 1u;
             if (!mbar_try_wait(bar + s, par)) {
@@ -332,25 +398,34 @@ k_tri_cta(const unsigned char *__restrict__ blocks, const unsigned *__restrict__
                 }
             }
             phase ^= 1u << s;
-            blk = stage + (size_t)s * stage_bytes;
+            blk = ring + s_pos[s];
         }
-        if (!timed_out) cta_level<VT, G, EXACT>(blk, s_out, bit, dbit, warp, sub, g, ovf);
-        // one barrier per level: results visible, stage free for reuse
+        if (mine && !timed_out) cta_level<VT, G, EXACT>(blk, s_out, bit, dbit, warp, sub, g, ovf);
+        // one barrier per level: results visible, the level's ring space free
         if (__syncthreads_or(timed_out)) {
             stuck = d;
             break;
         }
-        if (threadIdx.x == 0 && d + kStages < nlev) issue(d + kStages);
+        if (producer) {
+            if (st && --nst > 0) {
+                for (int e = d + 1; e < issued; e++)
+                    if (staged(e)) {
+                        lo = s_pos[e % kSlots];
+                        break;
+                    }
+            }
+            issue_more(d + 1);
+        }
     }
     if (stuck >= 0) {
         // report, then wait (bounded) for the copies this CTA still has in
         // flight before its shared memory goes away
-        if (threadIdx.x == 0) {
+        if (producer) {
             atomicOr(flags, ST_TIMEOUT);
             const unsigned long long t0 = globaltimer_ns();
-            for (int dd = stuck; dd < nlev && dd < stuck + kStages; dd++) {
-                if (!fits(dd)) continue;
-                const int s = dd % kStages;
+            for (int dd = stuck; dd < issued; dd++) {
+                if (!staged(dd)) continue;
+                const int s = dd % kSlots;
                 // the stuck level's wait already flipped its parity bit
                 const unsigned par = ((phase >> s) & 1u) ^ (dd == stuck ? 1u : 0u);
                 while (!mbar_try_wait(bar + s, par) && globaltimer_ns() - t0 < kSpinLimitNs) {
@@ -478,15 +553,17 @@ DevTri upload_tri(const Ctx &c, int n, const int *rptr, const int *cind, const v
     else put_vals(float());
     if (d.one_cta) {
         d.blocks = blob.empty() ? (unsigned char *)dmalloc(16) : dupload(blob);
-        std::vector<unsigned> off16(off.size());
+        // block offsets in 16-byte units (nlev + 1), then the rows of each level (nlev)
+        std::vector<unsigned> off16(off.size() + s.nlev);
         for (size_t i = 0; i < off.size(); i++) off16[i] = (unsigned)(off[i] / 16);
+        for (int l = 0; l < s.nlev; l++) off16[off.size() + l] = (unsigned)(s.lvl_ptr[l + 1] - s.lvl_ptr[l]);
         d.blk_off = dupload(off16);
-        const size_t offs_bytes = up(4 * ((size_t)s.nlev + 1), 16);
-        if (vec_bytes + offs_bytes + 8 * kStages + (size_t)kStages * 1024 > kSmemMax)
+        const size_t offs_bytes = up(4 * (2 * (size_t)s.nlev + 1), 16);
+        const size_t slot_bytes = 8 * kSlots + 4 * kSlots;  // mbarriers and ring positions
+        if (vec_bytes + offs_bytes + slot_bytes + 4096 > kSmemMax)
             throw CudaError{"sweep schedule too large for the single-CTA kernel"};
-        const size_t avail = kSmemMax - vec_bytes - offs_bytes - 8 * kStages;
-        d.stage_bytes = (int)std::min<size_t>(avail / kStages / 16 * 16, 64 * 1024);
-        d.cta_smem = vec_bytes + (size_t)kStages * d.stage_bytes + 8 * kStages + offs_bytes;
+        d.stage_bytes = (int)((kSmemMax - vec_bytes - offs_bytes - slot_bytes) / 16 * 16);
+        d.cta_smem = vec_bytes + (size_t)d.stage_bytes + slot_bytes + offs_bytes;
     } else {
         d.perm = dupload(s.perm);
         d.prp = dupload(s.prp);

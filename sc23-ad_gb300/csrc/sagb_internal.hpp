@@ -123,8 +123,9 @@ struct DevTri {
     // data in one 16-byte aligned block fetched ahead by bulk copies
     bool one_cta = false;
     unsigned char *blocks = nullptr;
-    unsigned *blk_off = nullptr;       // offset of each level's block in 16-byte units (nlev + 1)
-    int stage_bytes = 0;               // largest block that goes through the staging ring
+    unsigned *blk_off = nullptr;       // offset of each level's block in 16-byte units (nlev + 1), then
+                                       // the rows of each level (nlev)
+    int stage_bytes = 0;               // bytes of the single-CTA kernel's bulk-copy ring
     size_t cta_smem = 0;
     void release();
 };
