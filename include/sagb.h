@@ -353,6 +353,13 @@ int sa_batch_sweep_form(sa_batch B, int level, int set, int *form);
  * set 1 / 0 chooses it (SA_ERR_ARG / an error if the operator has none), -1
  * reads it; results do not depend on it (the autotuner chooses per operator) */
 int sa_batch_compressed(sa_batch B, int level, int op, int set, int *on);
+/* sweeps of the levels below the finest whose multicolour split kept one
+ * colour (LD is the diagonal: ldtri.hpp:172-183 without off-diagonal terms),
+ * fused into the SpMVs around them: the pre-smoothing sweep into the
+ * restriction that produces the level's e, the post-smoothing one into its U
+ * residual; set 1 / 0 turns it on / off (default on), -1 reads; *levels = the
+ * levels fused; results do not depend on it */
+int sa_batch_fused_sweeps(sa_batch B, int set, int *levels);
 /* the V-cycle's persistent coarse tail: set = t >= 1 runs levels t .. depth-1
  * and the coarsest LU solves in one cooperative launch (a grid barrier between
  * steps), 0 turns it off, -1 reads; *from = the tail's first level (0: none).

@@ -166,11 +166,37 @@ __device__ __forceinline__ void row_accumulate(const int *__restrict__ cind, con
 }
 
 // ------------------------------------------------------------------ SpMV
+// The one-colour smoother step fused into a level SpMV's epilogue.  Where the
+// multicolour split of a level kept a single colour, its LD is the diagonal
+// alone and a sweep is out_i = (int)(((in_i << b) >> b) * dinv_i >> db)
+// (ldtri.hpp:172-183 with no off-diagonal term): a function of the row's own
+// input, so it is applied where that input is produced.
+//   JAC_PRE:  y = R r (the next level's e) and also x2 = step(y) on that
+//             level's smoothing rows (its pre-smoothing sweep from zero)
+//   JAC_POST: y = step(z - U x) (the post-smoothing sweep; y is not x: the
+//             product reads x of other rows)
+enum { JAC_NONE = 0, JAC_PRE = 1, JAC_POST = 2 };
+struct BJac {
+    const int *dinv;                 // the one-colour LD's values (its inverted diagonal), one per row
+    const signed char *bit, *dbit;   // its row shifts
+    int n;                           // JAC_PRE: rows of y that smooth (a prefix)
+    int *x2;                         // JAC_PRE: the step's output
+};
+
+// the sweep step of one row and right-hand side, with the colour kernel's overflow report
+__device__ __forceinline__ int jac_step(int v, long long dinv, int bit, int dbit, bool &ovf) {
+    const long long t = wshl((long long)v, bit);
+    const long long s = wmul(t >> bit, dinv) >> dbit;
+    ovf |= !fits32(s);
+    return lo32(s);
+}
+
 // y = A x (SET), y = z - A x (RESID) or y = A x + y (ADD), per row shift;
 // the same integer results as k_spmv_i32 for every right-hand side.
-template <int R, int MODE, bool CG = false>
+template <int R, int MODE, bool CG = false, int JAC = JAC_NONE>
 __device__ __forceinline__ void bspmv_finish(const DBCsr &A, int row, const long long (&acc)[R], int *y,
-                                             const int *z, const int *row_sys, unsigned *pflag, unsigned *flags) {
+                                             const int *z, const int *row_sys, unsigned *pflag, unsigned *flags,
+                                             const BJac &J = BJac{}) {
     const int bit = A.bit[row];
     int out[R], zz[R], yy[R];
     if (MODE == SPMV_RESID) {
@@ -191,12 +217,31 @@ __device__ __forceinline__ void bspmv_finish(const DBCsr &A, int row, const long
         if (MODE == SPMV_ADD) v = v + (long long)yy[r];
         ovf |= !fits32(v);
         out[r] = lo32(v);
+        if constexpr (JAC == JAC_POST)
+            out[r] = jac_step(out[r], __ldg(J.dinv + row), J.bit[row], J.dbit[row], ovf);
         if (ovf) {
             atomicOr(pflag + (size_t)row_sys[row] * R + r, ST_OVERFLOW);
             any = true;
         }
     }
     store_r<R>(y, row, out);
+    if constexpr (JAC == JAC_PRE) {
+        if (row < J.n) {
+            const long long dinv = __ldg(J.dinv + row);
+            const int b = J.bit[row], db = J.dbit[row];
+            int x2[R];
+#pragma unroll
+            for (int r = 0; r < R; r++) {
+                bool ovf = false;
+                x2[r] = jac_step(out[r], dinv, b, db, ovf);
+                if (ovf) {
+                    atomicOr(pflag + (size_t)row_sys[row] * R + r, ST_OVERFLOW);
+                    any = true;
+                }
+            }
+            store_r<R>(J.x2, row, x2);
+        }
+    }
     if (any) atomicOr(flags, ST_OVERFLOW);
 }
 
@@ -207,10 +252,10 @@ __device__ __forceinline__ void bspmv_finish(const DBCsr &A, int row, const long
 template <int R>
 constexpr int spmv_pre() { return 4; }
 
-template <int R, int G, int MODE, bool D16>
+template <int R, int G, int MODE, bool D16, int JAC = JAC_NONE>
 __global__ void __launch_bounds__(kBThreads)
 k_bspmv(DBCsr A, const int *__restrict__ x, int *__restrict__ y, const int *__restrict__ z,
-        const int *__restrict__ row_sys, unsigned *__restrict__ pflag, unsigned *__restrict__ flags) {
+        const int *__restrict__ row_sys, unsigned *__restrict__ pflag, unsigned *__restrict__ flags, BJac J) {
     pdl_trigger();
     constexpr int kSpmvPre = spmv_pre<R>();
     const long long tid = (long long)blockIdx.x * kBThreads + threadIdx.x;
@@ -250,14 +295,15 @@ k_bspmv(DBCsr A, const int *__restrict__ x, int *__restrict__ y, const int *__re
     for (int r = 0; r < R; r++)
 #pragma unroll
         for (int o = G / 2; o > 0; o >>= 1) acc[r] = wadd(acc[r], shfl_xor(acc[r], o));
-    if (lane == 0 && row < A.n) bspmv_finish<R, MODE>(A, row, acc, y, z, row_sys, pflag, flags);
+    if (lane == 0 && row < A.n) bspmv_finish<R, MODE, false, JAC>(A, row, acc, y, z, row_sys, pflag, flags, J);
 }
 
 // the same rows through the tile-staged stream (short rows, group 0)
-template <int R, int MODE>
+template <int R, int MODE, int JAC = JAC_NONE>
 __global__ void __launch_bounds__(kStreamThreads)
 k_bspmv_stream(DBCsr A, const int *__restrict__ x, int *__restrict__ y, const int *__restrict__ z,
-               const int *__restrict__ row_sys, unsigned *__restrict__ pflag, unsigned *__restrict__ flags) {
+               const int *__restrict__ row_sys, unsigned *__restrict__ pflag, unsigned *__restrict__ flags,
+               BJac J) {
     pdl_trigger();
     long long acc[R];
 #pragma unroll
@@ -265,7 +311,7 @@ k_bspmv_stream(DBCsr A, const int *__restrict__ x, int *__restrict__ y, const in
     const int r0 = blockIdx.x * kStreamThreads;
     stream_rows<R, true>(r0, min(A.n, r0 + kStreamThreads), A.rptr, A.cind, A.val, x, acc);  // waits inside
     const int row = r0 + threadIdx.x;
-    if (row < A.n) bspmv_finish<R, MODE>(A, row, acc, y, z, row_sys, pflag, flags);
+    if (row < A.n) bspmv_finish<R, MODE, false, JAC>(A, row, acc, y, z, row_sys, pflag, flags, J);
 }
 
 // --------------------------------------------------------- colour sweep
@@ -1549,6 +1595,7 @@ struct DevBMat {
 
 struct DevBLevel {
     int n_all = 0, n_smooth = 0;
+    bool one_colour = false;  // LD is the diagonal alone (one colour): the sweep can be fused
     DevBMat A, LD, U, P, R;
     int *colour_rows = nullptr;
     std::vector<int> colour_ptr;
@@ -1572,6 +1619,7 @@ struct BatchEngine::Impl {
     std::shared_ptr<BatchHierarchy> h;
     std::vector<DevBLevel> lv;
     std::vector<int> n_level;
+    bool fuse_jac = true;  // one-colour levels' sweeps fused into the neighbouring SpMVs
     std::vector<int *> ee, xx, rr, tmp;  // per level (ee/xx index l = 0 unused)
     std::vector<int *> row_sys;          // per level 0 .. Dmax
     BLuDesc *d_lu = nullptr;
@@ -1645,6 +1693,11 @@ struct BatchEngine::Impl {
             d.LD.group = pick_group(L.LD.n ? (double)(L.LD.nnz() - L.LD.n) / L.LD.n : 1.0);
             d.colour_rows = L.colour_rows.empty() ? nullptr : dupload(L.colour_rows);
             d.colour_ptr = L.colour_ptr;
+            // one colour: every LD row holds its diagonal alone, so row i's
+            // entry is entry i (what the fused sweep step reads)
+            d.one_colour = L.LD.n > 0 && L.LD.nnz() == L.LD.n;
+            for (int i = 0; d.one_colour && i < L.LD.n; i++)
+                d.one_colour = L.LD.rptr[i] == i && L.LD.cind[i] == i;
         }
         for (int l = 0; l < Dmax; l++) build_cluster_groups(l);
         for (int l = 0; l < Dmax; l++) build_colour_pack(l);
@@ -2065,15 +2118,20 @@ struct BatchEngine::Impl {
         c.launches++;
     }
 
-    void bspmv(const DevBMat &M, const int *x, int *y, int mode, const int *z, const int *row_sys) {
+    // jac: JAC_NONE, or JAC_PRE with mode SET / JAC_POST with mode RESID (the
+    // one-colour smoother step in the epilogue, J its level's diagonal)
+    void bspmv(const DevBMat &M, const int *x, int *y, int mode, const int *z, const int *row_sys,
+               int jac = JAC_NONE, const BJac &J = BJac{}) {
         if (M.d.n == 0) return;
         if (M.group == 0) {
             const int blocks = (M.d.n + kStreamThreads - 1) / kStreamThreads;
             by_r([&](auto RR) {
                 constexpr int R = decltype(RR)::value;
-                auto k = mode == SPMV_SET ? k_bspmv_stream<R, SPMV_SET>
+                auto k = jac == JAC_PRE ? k_bspmv_stream<R, SPMV_SET, JAC_PRE>
+                         : jac == JAC_POST ? k_bspmv_stream<R, SPMV_RESID, JAC_POST>
+                         : mode == SPMV_SET ? k_bspmv_stream<R, SPMV_SET>
                          : mode == SPMV_RESID ? k_bspmv_stream<R, SPMV_RESID> : k_bspmv_stream<R, SPMV_ADD>;
-                launch(k, blocks, kStreamThreads, 0, 1, M.d, x, y, z, row_sys, cur_pflag, c.d_flags);
+                launch(k, blocks, kStreamThreads, 0, 1, M.d, x, y, z, row_sys, cur_pflag, c.d_flags, J);
             });
             return;
         }
@@ -2084,14 +2142,23 @@ struct BatchEngine::Impl {
             constexpr int R = decltype(RR)::value;
             by_g(M.group, [&](auto GG) {
                 constexpr int G = decltype(GG)::value;
-                auto k = d16 ? (mode == SPMV_SET ? k_bspmv<R, G, SPMV_SET, true>
-                                : mode == SPMV_RESID ? k_bspmv<R, G, SPMV_RESID, true> : k_bspmv<R, G, SPMV_ADD, true>)
-                             : (mode == SPMV_SET ? k_bspmv<R, G, SPMV_SET, false>
-                                : mode == SPMV_RESID ? k_bspmv<R, G, SPMV_RESID, false>
-                                                     : k_bspmv<R, G, SPMV_ADD, false>);
-                launch(k, blocks, kBThreads, 0, 1, M.d, x, y, z, row_sys, cur_pflag, c.d_flags);
+                auto pick = [&](auto D) {
+                    constexpr bool D16 = decltype(D)::value;
+                    return jac == JAC_PRE ? k_bspmv<R, G, SPMV_SET, D16, JAC_PRE>
+                           : jac == JAC_POST ? k_bspmv<R, G, SPMV_RESID, D16, JAC_POST>
+                           : mode == SPMV_SET ? k_bspmv<R, G, SPMV_SET, D16>
+                           : mode == SPMV_RESID ? k_bspmv<R, G, SPMV_RESID, D16> : k_bspmv<R, G, SPMV_ADD, D16>;
+                };
+                auto k = d16 ? pick(std::true_type()) : pick(std::false_type());
+                launch(k, blocks, kBThreads, 0, 1, M.d, x, y, z, row_sys, cur_pflag, c.d_flags, J);
             });
         });
+    }
+
+    // the one-colour step of level l (LD is its diagonal: row i's entry is i)
+    BJac jac_of(int l, int *x2 = nullptr) const {
+        const DevBMat &LD = lv[l].LD;
+        return BJac{LD.d.val, LD.d.bit, LD.d.dbit, LD.d.n, x2};
     }
 
     void sweep(int l, const int *in, int *out) {
@@ -2292,22 +2359,36 @@ struct BatchEngine::Impl {
         cur_pflag = pflag;
     }
 
+    // a level whose sweeps are fused into its neighbours' SpMVs (one colour,
+    // one smoothing step, outside the persistent tail): its pre-smoothing
+    // sweep in the restriction that produces its e, its post-smoothing sweep
+    // in its U residual, whose result (in tmp) the interpolation above reads
+    bool fused_pre(int l, int t) const { return fuse_jac && smooth_iter == 1 && l >= 1 && l < t && lv[l].one_colour; }
+    bool fused_post(int l, int t) const { return fused_pre(l, t) && lv[l].n_all == lv[l].n_smooth; }
+
     void vcycle_body(const int *in, int *out) {
         const int t = tail_from > 0 && d_steps ? tail_from : Dmax;
         for (int l = 0; l < t; l++) {
             const int *e_l = l == 0 ? in : ee[l];
             int *x_l = l == 0 ? out : xx[l];
-            smooth(l, e_l, x_l, false);
+            if (!fused_pre(l, t)) smooth(l, e_l, x_l, false);
             bspmv(lv[l].A, x_l, rr[l], SPMV_RESID, e_l, lv[l].row_sys);
-            bspmv(lv[l].R, rr[l], ee[l + 1], SPMV_SET, nullptr, lv[l].row_sys_next);
+            if (fused_pre(l + 1, t))
+                bspmv(lv[l].R, rr[l], ee[l + 1], SPMV_SET, nullptr, lv[l].row_sys_next, JAC_PRE,
+                      jac_of(l + 1, xx[l + 1]));
+            else
+                bspmv(lv[l].R, rr[l], ee[l + 1], SPMV_SET, nullptr, lv[l].row_sys_next);
         }
         if (t < Dmax) launch_tail();
         else lu(cur_pflag);
         for (int l = t - 1; l >= 0; l--) {
             const int *e_l = l == 0 ? in : ee[l];
             int *x_l = l == 0 ? out : xx[l];
-            bspmv(lv[l].P, xx[l + 1], x_l, SPMV_ADD, nullptr, lv[l].row_sys);
-            smooth(l, e_l, x_l, true);
+            bspmv(lv[l].P, fused_post(l + 1, t) ? tmp[l + 1] : xx[l + 1], x_l, SPMV_ADD, nullptr, lv[l].row_sys);
+            if (fused_post(l, t))
+                bspmv(lv[l].U, x_l, tmp[l], SPMV_RESID, e_l, lv[l].row_sys, JAC_POST, jac_of(l));
+            else
+                smooth(l, e_l, x_l, true);
         }
     }
 
@@ -2616,6 +2697,17 @@ int BatchEngine::sweep_form(int level, int set) {
         impl_->clear_graphs();
     }
     return L.use_cluster;
+}
+int BatchEngine::fused_sweeps(int set) {
+    Impl &I = *impl_;
+    if (set >= 0) {
+        I.fuse_jac = set > 0;
+        I.clear_graphs();
+    }
+    const int t = I.tail_from > 0 && I.d_steps ? I.tail_from : I.Dmax;
+    int n = 0;
+    for (int l = 0; l < I.Dmax; l++) n += I.fused_pre(l, t);
+    return n;
 }
 int BatchEngine::compressed(int level, int op, int set) {
     if (level < 0 || level >= impl_->Dmax || (op != 0 && op != 2)) throw CudaError{"no such operator"};

@@ -282,6 +282,9 @@ class BatchEngine {
     // 16-bit column offsets for A (op 0) or U (op 2) of one level: set 1 / 0
     // chooses them (1 needs offsets that fit), -1 only reads
     int compressed(int level, int op, int set);
+    // sweeps of one-colour levels fused into the neighbouring SpMVs: set 1 / 0
+    // turns it on / off, -1 reads; returns the levels whose sweeps are fused
+    int fused_sweeps(int set);
     // the V-cycle's persistent coarse tail: set t >= 1 runs levels t .. Dmax-1
     // and the coarsest LU in one cooperative launch, 0 turns it off, -1 reads;
     // returns the first level of the tail (0: none); grid > 0: that many CTAs

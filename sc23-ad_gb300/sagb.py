@@ -138,6 +138,7 @@ SIGNATURES = {
     "sa_batch_set_group": (C.c_int, [VP, C.c_int, C.c_int, C.c_int]),
     "sa_batch_sweep_form": (C.c_int, [VP, C.c_int, C.c_int, C.POINTER(C.c_int)]),
     "sa_batch_compressed": (C.c_int, [VP, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int)]),
+    "sa_batch_fused_sweeps": (C.c_int, [VP, C.c_int, C.POINTER(C.c_int)]),
     "sa_batch_tail": (C.c_int, [VP, C.c_int, C.POINTER(C.c_int)]),
     "sa_batch_tail_selftest": (C.c_int, [VP, VP, C.c_int, C.c_double, C.POINTER(C.c_uint)]),
     "sa_batch_time_op": (C.c_int, [VP, VP, C.c_int, C.c_int, VP, VP, C.c_int, C.POINTER(C.c_float)]),
@@ -820,6 +821,13 @@ class Batch:
         0 chooses them."""
         f = C.c_int()
         check(lib().sa_batch_compressed(self.h, level, op, set, C.byref(f)))
+        return f.value
+
+    def fused_sweeps(self, set=-1):
+        """Sweeps of one-colour levels fused into the neighbouring SpMVs: set 1
+        / 0 turns it on / off; returns the levels fused."""
+        f = C.c_int()
+        check(lib().sa_batch_fused_sweeps(self.h, set, C.byref(f)))
         return f.value
 
     def tail(self, set=-1):

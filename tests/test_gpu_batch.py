@@ -345,6 +345,52 @@ def test_early_restart_matches_oracle(ctx):
     B.close()
 
 
+@pytest.mark.parametrize("nrhs", [1, 4])
+def test_fused_one_colour_sweeps(ctx, nrhs):
+    """With one colour below the finest level (caps [8, 1]) those levels'
+    sweeps are fused into the SpMVs around them (sa_batch_fused_sweeps): the
+    pre-smoothing sweep into the restriction that produces the level's e, the
+    post-smoothing sweep into its U residual.  The V-cycle is still the
+    oracle's bit for bit per system and right-hand side, the same with fusion
+    on and off, and a solve gives the same iterations and x.  The systems end
+    at different depths, so some levels also hold other systems' coarsest rows
+    (there the post-smoothing sweep stays a launch of its own)."""
+    systems, bs = _systems(SYSTEMS, nrhs)
+    B = sagb.Batch(ctx, systems, nrhs)
+    B.set_colour_caps([8, 1])
+    nf = B.fused_sweeps()
+    assert 0 < nf <= B.depth - 1, (nf, B.depth)
+    rng = np.random.default_rng(40 + nrhs)
+    vin = rng.integers(-(1 << 28), 1 << 28, size=B.rows * nrhs).astype(np.int32)
+    out_on = B.precondition(vin)
+    assert B.fused_sweeps(0) == 0
+    np.testing.assert_array_equal(B.precondition(vin), out_on)
+    assert B.fused_sweeps(1) == nf
+    out2, vin2 = out_on.reshape(B.rows, nrhs), vin.reshape(B.rows, nrhs)
+    keep = of.Keep()
+    for s in range(B.nsys):
+        h = sv.oracle_amg(keep, B.system_setup(s))
+        a, e = B.offsets[s], B.offsets[s + 1]
+        for r in range(nrhs):
+            x = np.ascontiguousarray(vin2[a:e, r])
+            ref = np.zeros_like(x)
+            of.lib().or_vcycle_i32(C.byref(h), of.ptr(x, of.i32p), of.ptr(ref, of.i32p))
+            np.testing.assert_array_equal(out2[a:e, r], ref, err_msg=f"system {s} rhs {r}")
+    b = _interleave(B, bs)
+    nrm_b = np.array([np.linalg.norm(x[:, r]) for x in bs for r in range(nrhs)])
+    params = sagb.solver_params(m=20, explicit_stop=1, cycle_bits=12)
+    res = []
+    for on in (1, 0):
+        B.fused_sweeps(on)
+        x = np.zeros(B.rows * nrhs)
+        it, cv, _ = B.solve(params, [29] * B.nsys, b, nrm_b, x)
+        assert cv.all(), it
+        res.append((it.copy(), x))
+    np.testing.assert_array_equal(res[0][0], res[1][0])
+    np.testing.assert_array_equal(res[0][1], res[1][1])
+    B.close()
+
+
 def test_colour_caps_rebuild_and_tune(ctx):
     """sa_batch_set_colour_caps rebuilds every system's split with caps per
     level (the coarsening kept): the V-cycle is still the oracle's, in the new
