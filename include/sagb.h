@@ -419,6 +419,8 @@ int sa_batch_fp_precondition(sa_ctx ctx, sa_batch_fp F, const void *in, void *ou
 int sa_batch_fp_autotune(sa_ctx ctx, sa_batch_fp F, int reps);
 /* milliseconds per V-cycle as the solver runs it */
 int sa_batch_fp_time_vcycle(sa_ctx ctx, sa_batch_fp F, int reps, float *ms);
+/* as sa_batch_fused_sweeps for the floating-point engine (default on) */
+int sa_batch_fp_fused_sweeps(sa_batch_fp F, int set, int *levels);
 /* Restarted(FGMRES<T>) per pair; nrm_b per pair; iters / converged per pair (optional) */
 int sa_batch_fp_solve(sa_ctx ctx, sa_batch_fp F, const sa_solver_params *p, const double *b, const double *nrm_b,
                       double *x, int *iters, int *converged);

@@ -1306,6 +1306,14 @@ extern "C" int sa_batch_fused_sweeps(sa_batch B, int set, int *levels) {
     SA_GUARD_END
 }
 
+extern "C" int sa_batch_fp_fused_sweeps(sa_batch_fp F, int set, int *levels) {
+    if (!F || !levels || set < -1 || set > 1) return fail(SA_ERR_ARG, "invalid argument");
+    SA_GUARD_BEGIN
+    *levels = F->eng->fused_sweeps(set);
+    return SA_OK;
+    SA_GUARD_END
+}
+
 extern "C" int sa_batch_tail(sa_batch B, int set, int *from) {
     if (!B || !from || set < -1 || set >= B->h->Dmax) return fail(SA_ERR_ARG, "invalid argument");
     SA_GUARD_BEGIN

@@ -152,11 +152,24 @@ __device__ __forceinline__ void row_acc(const int *__restrict__ cind, const T *_
 }
 
 // ------------------------------------------------------------------ SpMV
+// The one-colour smoother step fused into a level SpMV's epilogue (as in the
+// integer engine): where a level's split kept one colour, LD is its diagonal
+// and a sweep is out_i = (in_i - 0) * dinv_i (ldtri::CSR<T>, ldtri.hpp:49-58,
+// with no off-diagonal term).  jac 1: y = R r and x2 = step(y) on the next
+// level's smoothing rows; jac 2: y = step(z - U x).
+template <typename T>
+struct FJac {
+    const T *dinv;  // the one-colour LD's values (its inverted diagonal), one per row
+    int n;          // jac 1: rows of y that smooth (a prefix)
+    T *x2;          // jac 1: the step's output
+};
+
 // y = A x (SPMV_SET), y = z - A x (SPMV_RESID) or y = y + A x (SPMV_ADD):
 // CSR<T>::SpMV (spmat.hpp:43-52) with Sub / Add (blas1.hpp:62-72)
 template <typename T, int R, int G>
 __global__ void __launch_bounds__(kFThreads)
-k_fspmv(FMat<T> A, const T *__restrict__ x, T *__restrict__ y, const T *__restrict__ z, int mode) {
+k_fspmv(FMat<T> A, const T *__restrict__ x, T *__restrict__ y, const T *__restrict__ z, int mode, int jac,
+        FJac<T> J) {
     pdl_trigger();
     const long long tid = (long long)blockIdx.x * kFThreads + threadIdx.x;
     const int row = (int)(tid / G), lane = (int)(tid % G);
@@ -201,7 +214,19 @@ k_fspmv(FMat<T> A, const T *__restrict__ x, T *__restrict__ y, const T *__restri
 #pragma unroll
             for (int r = 0; r < R; r++) out[r] = acc[r];
         }
+        if (jac == 2) {
+            const T dinv = __ldg(J.dinv + row);
+#pragma unroll
+            for (int r = 0; r < R; r++) out[r] = (out[r] - T(0)) * dinv;
+        }
         fst<T, R>(y, row, out);
+        if (jac == 1 && row < J.n) {
+            const T dinv = __ldg(J.dinv + row);
+            T x2[R];
+#pragma unroll
+            for (int r = 0; r < R; r++) x2[r] = (out[r] - T(0)) * dinv;
+            fst<T, R>(J.x2, row, x2);
+        }
     }
 }
 
@@ -791,6 +816,7 @@ struct DevFMat {
 template <typename T>
 struct DevFLevel {
     int n_all = 0, n_smooth = 0;
+    bool one_colour = false;  // LD is the diagonal alone (one colour): the sweep can be fused
     DevFMat<T> A, LD, U, P, R;
     int *colour_rows = nullptr;
     std::vector<int> colour_ptr;
@@ -814,6 +840,7 @@ class BatchFpEngine::Base {
     virtual void solve(const KrylovParams &kp, const double *b, const double *nrm_b, double *x, BatchStats &st) = 0;
     virtual void autotune(int reps) = 0;
     virtual float time_vcycle(int reps) = 0;
+    virtual int fused_sweeps(int set) = 0;
     virtual int depth() const = 0;
     virtual size_t rows() const = 0;
 };
@@ -830,6 +857,7 @@ class FpImpl : public BatchFpEngine::Base {
     std::vector<int> n_level;
     std::vector<DevFLevel<T>> lv;
     std::vector<T *> ee, xx, rr, tmp;
+    bool fuse_jac = true;
     FLuDesc<T> *d_lu = nullptr;
     int nlu = 0;
     size_t lu_smem = 0;
@@ -877,6 +905,9 @@ class FpImpl : public BatchFpEngine::Base {
             d.LD.group = pick_group(L.LD.n ? (double)(L.LD.nnz() - L.LD.n) / L.LD.n : 1.0);
             d.colour_rows = dupload(L.colour_rows);
             d.colour_ptr = L.colour_ptr;
+            d.one_colour = L.LD.n > 0 && L.LD.nnz() == L.LD.n;
+            for (int i = 0; d.one_colour && i < L.LD.n; i++)
+                d.one_colour = L.LD.rptr[i] == i && L.LD.cind[i] == i;
             pack(L, d);
         }
         auto vec = [&](int rows) { return (T *)dmalloc(sizeof(T) * (size_t)std::max(rows, 1) * Rn); };
@@ -1043,14 +1074,15 @@ class FpImpl : public BatchFpEngine::Base {
         c.launches++;
     }
 
-    void spmv(const DevFMat<T> &M, const T *x, T *y, int mode, const T *z) {
+    void spmv(const DevFMat<T> &M, const T *x, T *y, int mode, const T *z, int jac = 0, FJac<T> J = FJac<T>{}) {
         if (M.d.n == 0) return;
         by_r([&](auto RR) {
             constexpr int R = decltype(RR)::value;
             by_g(M.group, [&](auto GG) {
                 constexpr int G = decltype(GG)::value;
                 const long long thr = (long long)M.d.n * G;
-                launch(k_fspmv<T, R, G>, (int)((thr + kFThreads - 1) / kFThreads), kFThreads, 0, M.d, x, y, z, mode);
+                launch(k_fspmv<T, R, G>, (int)((thr + kFThreads - 1) / kFThreads), kFThreads, 0, M.d, x, y, z, mode,
+                       jac, J);
             });
         });
     }
@@ -1100,21 +1132,39 @@ class FpImpl : public BatchFpEngine::Base {
         });
     }
 
+    // one-colour levels below the finest with their sweeps fused into the
+    // neighbouring SpMVs (pre: the restriction producing e; post: the U
+    // residual, result in tmp, which the interpolation above reads)
+    bool fused_pre(int l) const { return fuse_jac && smooth_iter == 1 && l >= 1 && l < Dmax && lv[l].one_colour; }
+    bool fused_post(int l) const { return fused_pre(l) && lv[l].n_all == lv[l].n_smooth; }
+    FJac<T> jac_of(int l, T *x2 = nullptr) const { return FJac<T>{lv[l].LD.d.val, lv[l].LD.d.n, x2}; }
+    int fused_sweeps(int set) override {
+        if (set >= 0) {
+            fuse_jac = set > 0;
+            clear_graphs();
+        }
+        int n = 0;
+        for (int l = 0; l < Dmax; l++) n += fused_pre(l);
+        return n;
+    }
+
     // dfAMG::Precondition (INTAMG.hpp:86-134) for the whole batch
     void vcycle(const T *in, T *out) {
         for (int l = 0; l < Dmax; l++) {
             const T *e_l = l == 0 ? in : ee[l];
             T *x_l = l == 0 ? out : xx[l];
-            smooth(l, e_l, x_l, false);
+            if (!fused_pre(l)) smooth(l, e_l, x_l, false);
             spmv(lv[l].A, x_l, rr[l], SPMV_RESID, e_l);
-            spmv(lv[l].R, rr[l], ee[l + 1], SPMV_SET, nullptr);
+            if (fused_pre(l + 1)) spmv(lv[l].R, rr[l], ee[l + 1], SPMV_SET, nullptr, 1, jac_of(l + 1, xx[l + 1]));
+            else spmv(lv[l].R, rr[l], ee[l + 1], SPMV_SET, nullptr);
         }
         lu();
         for (int l = Dmax - 1; l >= 0; l--) {
             const T *e_l = l == 0 ? in : ee[l];
             T *x_l = l == 0 ? out : xx[l];
-            spmv(lv[l].P, xx[l + 1], x_l, SPMV_ADD, nullptr);
-            smooth(l, e_l, x_l, true);
+            spmv(lv[l].P, fused_post(l + 1) ? tmp[l + 1] : xx[l + 1], x_l, SPMV_ADD, nullptr);
+            if (fused_post(l)) spmv(lv[l].U, x_l, tmp[l], SPMV_RESID, e_l, 2, jac_of(l));
+            else smooth(l, e_l, x_l, true);
         }
     }
 
@@ -1496,6 +1546,7 @@ void BatchFpEngine::solve(const KrylovParams &kp, const double *b, const double 
 }
 void BatchFpEngine::autotune(int reps) { impl_->autotune(reps); }
 float BatchFpEngine::time_vcycle(int reps) { return impl_->time_vcycle(reps); }
+int BatchFpEngine::fused_sweeps(int set) { return impl_->fused_sweeps(set); }
 int BatchFpEngine::depth() const { return impl_->depth(); }
 size_t BatchFpEngine::rows() const { return impl_->rows(); }
 

@@ -248,6 +248,9 @@ class BatchFpEngine {
     void solve(const KrylovParams &kp, const double *b, const double *nrm_b, double *x, BatchStats &st);
     void autotune(int reps);
     float time_vcycle(int reps);
+    // sweeps of one-colour levels fused into the neighbouring SpMVs: set 1 /
+    // 0 / -1 (read); returns the levels fused
+    int fused_sweeps(int set);
     int last_cycle_graphs() const { return last_cycle_graphs_; }
     class Base;
 

@@ -151,6 +151,7 @@ SIGNATURES = {
     "sa_batch_fp_precondition": (C.c_int, [VP, VP, VP, VP]),
     "sa_batch_fp_autotune": (C.c_int, [VP, VP, C.c_int]),
     "sa_batch_fp_time_vcycle": (C.c_int, [VP, VP, C.c_int, C.POINTER(C.c_float)]),
+    "sa_batch_fp_fused_sweeps": (C.c_int, [VP, C.c_int, C.POINTER(C.c_int)]),
     "sa_batch_fp_solve": (C.c_int, [VP, VP, C.POINTER(SolverParams), VP, VP, VP, I32P, I32P]),
     "sa_batch_cycle_graphs": (C.c_int, [VP, VP, C.POINTER(C.c_int)]),
     "sa_batch_level_op": (C.c_int, [VP, VP, C.c_int, C.c_int, VP, VP]),
@@ -909,6 +910,13 @@ class BatchFp:
         ms = C.c_float()
         check(lib().sa_batch_fp_time_vcycle(self.ctx.h, self.h, reps, C.byref(ms)))
         return ms.value
+
+    def fused_sweeps(self, set=-1):
+        """Sweeps of one-colour levels fused into the neighbouring SpMVs: set 1
+        / 0 turns it on / off; returns the levels fused."""
+        f = C.c_int()
+        check(lib().sa_batch_fp_fused_sweeps(self.h, set, C.byref(f)))
+        return f.value
 
     def cycle_graphs(self):
         """Restart cycles of the last solve that ran as one graph each."""

@@ -107,6 +107,29 @@ def test_batched_fp64_vcycle_poisson128(ctx):
 
 
 @pytest.mark.parametrize("prec", [sagb.F64, sagb.F32])
+def test_batched_fp_fused_one_colour_sweeps(ctx, prec):
+    """With one colour below the finest level (caps [8, 1]) the FP engine fuses
+    those levels' sweeps into the neighbouring SpMVs (sa_batch_fp_fused_sweeps):
+    the V-cycle stays within the oracle's tolerance and is bit-identical to the
+    unfused one (the step (in - 0) * dinv is the same IEEE operation in the
+    SpMV's epilogue as in the colour kernel)."""
+    nrhs = 2
+    systems, _ = _systems(SYSTEMS)
+    B = sagb.Batch(ctx, systems, nrhs)
+    B.set_colour_caps([8, 1])
+    F = sagb.BatchFp(ctx, B, prec)
+    nf = F.fused_sweeps()
+    assert nf > 0
+    tol = FP64_TOL if prec == sagb.F64 else FP32_TOL
+    vin, out_on = _check_vcycle(B, F, prec, nrhs, 31, tol)
+    assert F.fused_sweeps(0) == 0
+    np.testing.assert_array_equal(F.precondition(vin), out_on.ravel())
+    assert F.fused_sweeps(1) == nf
+    F.close()
+    B.close()
+
+
+@pytest.mark.parametrize("prec", [sagb.F64, sagb.F32])
 def test_batched_fp_solve(ctx, prec):
     """Restarted(FGMRES<T>) per pair against the oracle's solve on each
     system's own hierarchy, both stopping on the inner solver's estimate as
