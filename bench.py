@@ -991,6 +991,19 @@ def main_batch(a):
     ratios = B.rule_ratios(bvec, nrm_b)
     t_rule = time.time() - t0
     rule = [min(bitsel.rule_of(q) for q in ratios[s * nrhs:(s + 1) * nrhs]) for s in range(B.nsys)]
+    params = sagb.solver_params(m=20, explicit_stop=1, cycle_bits=a.cycle_bits)
+    db = sagb.DeviceArray.from_host(ctx, bvec)
+    dx = sagb.DeviceArray(ctx, B.rows * nrhs, np.float64)
+    caps_table = None
+    if not a.no_tune_caps:
+        # the coarse colour cap by measured time to solution with the rule's
+        # bits (outside the timed region); the ratios, the rule and the
+        # selector's features then describe the kept smoother
+        t0 = time.time()
+        caps_table = B.tune_colour_caps(params, rule, db, nrm_b, dx, [[8, 2], [8, 1]], reps=1)
+        t_tune += time.time() - t0
+        ratios = B.rule_ratios(bvec, nrm_b)
+        rule = [min(bitsel.rule_of(q) for q in ratios[s * nrhs:(s + 1) * nrhs]) for s in range(B.nsys)]
     bits = list(rule)
     learned = None
     if os.path.exists(bitsel.WEIGHTS):
@@ -999,9 +1012,6 @@ def main_batch(a):
                    for s in range(B.nsys)]
         sel.net.close()
         bits = learned
-    params = sagb.solver_params(m=20, explicit_stop=1, cycle_bits=a.cycle_bits)
-    db = sagb.DeviceArray.from_host(ctx, bvec)
-    dx = sagb.DeviceArray(ctx, B.rows * nrhs, np.float64)
     zeros = sagb.DeviceArray.from_host(ctx, np.zeros(B.rows * nrhs))
 
     def one(bb):
@@ -1061,6 +1071,9 @@ def main_batch(a):
             "pairs_converged": int(cv.sum()), "pairs": int(len(cv)), "iters_total": int(it.sum()),
             "iters_max": int(it.max()), "worst_explicit_res": worst,
             "bits": "learned" if learned is not None else "rule", "rule_row": rule_row,
+            "colour_caps": B.colour_caps()[:3], "cycle_bits": a.cycle_bits,
+            "colour_cap_tuning": None if caps_table is None else
+            [{"caps": t[0], "ms": round(t[1], 3), "iters_max": int(np.max(t[2]))} for t in caps_table],
             "gen_s": t_gen, "setup_s": t_setup, "autotune_s": t_tune, "rule_s": t_rule,
             "gpu_launches": launches, "clocks": clk, "vcycle_ms": k["vcycle_ms"], "coarse_lu_ms": k["coarse_lu_ms"],
             "roofline": {"kernel": name, "bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
