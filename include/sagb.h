@@ -353,6 +353,14 @@ int sa_batch_sweep_form(sa_batch B, int level, int set, int *form);
  * set 1 / 0 chooses it (SA_ERR_ARG / an error if the operator has none), -1
  * reads it; results do not depend on it (the autotuner chooses per operator) */
 int sa_batch_compressed(sa_batch B, int level, int op, int set, int *on);
+/* ELL copy of a level's A (op 0) or U (op 2), kept when its rows have at most
+ * 8 entries and at most a quarter of the slots would be empty (the finest
+ * level of a stencil matrix): slot-major, 16-bit column offsets, so a row's
+ * entries need no row pointers (the reference prototypes the same idea as
+ * SELL, spmat.hpp:208-281); set 1 / 0 chooses it (for the level-0 A also in
+ * the Arnoldi SpMV), -1 reads; results do not depend on it (the autotuner
+ * chooses) */
+int sa_batch_ell(sa_batch B, int level, int op, int set, int *on);
 /* sweeps of the levels below the finest whose multicolour split kept one
  * colour (LD is the diagonal: ldtri.hpp:172-183 without off-diagonal terms),
  * fused into the SpMVs around them: the pre-smoothing sweep into the

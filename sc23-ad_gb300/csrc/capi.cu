@@ -1298,6 +1298,15 @@ extern "C" int sa_batch_compressed(sa_batch B, int level, int op, int set, int *
     SA_GUARD_END
 }
 
+extern "C" int sa_batch_ell(sa_batch B, int level, int op, int set, int *on) {
+    if (!B || !on || level < 0 || level >= B->h->Dmax || (op != 0 && op != 2) || set < -1 || set > 1)
+        return fail(SA_ERR_ARG, "invalid argument");
+    SA_GUARD_BEGIN
+    *on = B->eng->ell(level, op, set);
+    return SA_OK;
+    SA_GUARD_END
+}
+
 extern "C" int sa_batch_fused_sweeps(sa_batch B, int set, int *levels) {
     if (!B || !levels || set < -1 || set > 1) return fail(SA_ERR_ARG, "invalid argument");
     SA_GUARD_BEGIN

@@ -314,6 +314,55 @@ k_bspmv_stream(DBCsr A, const int *__restrict__ x, int *__restrict__ y, const in
     if (row < A.n) bspmv_finish<R, MODE, false, JAC>(A, row, acc, y, z, row_sys, pflag, flags, J);
 }
 
+// ------------------------------------------------------------ ELL SpMV
+// Square level operators with short, even rows (the finest level of a stencil
+// matrix) also keep their entries as ELL: w slots a row, slot-major (slot k
+// of row i at k * n + i, coalesced across rows), 16-bit column offsets
+// (column = row + offset), empty slots holding offset 0 and value 0.  A row's
+// entries then need no row pointers: their loads depend on the row index
+// alone and are all issued before the programmatic-launch wait, so after it a
+// row costs one round trip for its vector values.  The sums are the CSR
+// sums (integer, order-free; an empty slot adds 0).
+constexpr int kEllMax = 8;
+
+struct DEll {
+    int n, w;
+    const short *cd;  // w * n column offsets
+    const int *val;   // w * n values
+};
+
+template <int R, int MODE, int JAC = JAC_NONE>
+__global__ void __launch_bounds__(kBThreads)
+k_bspmv_ell(DBCsr A, DEll E, const int *__restrict__ x, int *__restrict__ y, const int *__restrict__ z,
+            const int *__restrict__ row_sys, unsigned *__restrict__ pflag, unsigned *__restrict__ flags, BJac J) {
+    pdl_trigger();
+    const int row = blockIdx.x * kBThreads + threadIdx.x;
+    int cc[kEllMax], vv[kEllMax];
+#pragma unroll
+    for (int k = 0; k < kEllMax; k++) {
+        const bool ok = row < E.n && k < E.w;
+        vv[k] = ok ? __ldg(E.val + (size_t)k * E.n + row) : 0;
+        cc[k] = ok ? row + (int)__ldg(E.cd + (size_t)k * E.n + row) : 0;
+    }
+    pdl_wait();
+    long long acc[R];
+#pragma unroll
+    for (int r = 0; r < R; r++) acc[r] = 0;
+    int xv[kEllMax][R];
+#pragma unroll
+    for (int k = 0; k < kEllMax; k++) {
+        if (vv[k] != 0) load_r<R>(x, cc[k], xv[k]);
+        else
+#pragma unroll
+            for (int r = 0; r < R; r++) xv[k][r] = 0;
+    }
+#pragma unroll
+    for (int k = 0; k < kEllMax; k++)
+#pragma unroll
+        for (int r = 0; r < R; r++) acc[r] = wadd(acc[r], (long long)vv[k] * (long long)xv[k][r]);
+    if (row < A.n) bspmv_finish<R, MODE, false, JAC>(A, row, acc, y, z, row_sys, pflag, flags, J);
+}
+
 // --------------------------------------------------------- colour sweep
 // One colour of the multicolour Gauss-Seidel sweep (ldtri::CSRflex row rule,
 // ldtri.hpp:172-183): t = in << b; t -= sum l_ij out_j; out = (int)((t >> b) * dinv >> db).
@@ -1274,6 +1323,68 @@ k_bspmv_dot_stream(const BTile *__restrict__ tiles, DBCsr A, const int *__restri
     }
 }
 
+// w = A z and acc[p][0] += V0 . w over the ELL copy of the level-0 A: one row
+// per thread (block b: rows row0 + (b % kTileSub) * kBThreads + [0, kBThreads)
+// of tile b / kTileSub), the entries fetched before the launch wait
+template <int R>
+__global__ void __launch_bounds__(kBThreads)
+k_bspmv_dot_ell(const BTile *__restrict__ tiles, DBCsr A, DEll E, const int *__restrict__ z, int *__restrict__ w,
+                const int *__restrict__ v0, unsigned long long *acc, int m, unsigned *__restrict__ pflag,
+                unsigned *__restrict__ flags) {
+    pdl_trigger();
+    __shared__ long long sh[kBThreads / 32][R];
+    const BTile t = tiles[blockIdx.x / kTileSub];
+    const int row = t.row0 + (blockIdx.x % kTileSub) * kBThreads + threadIdx.x;
+    const bool ok = row < t.row1;
+    int cc[kEllMax], vv[kEllMax];
+#pragma unroll
+    for (int k = 0; k < kEllMax; k++) {
+        const bool in = ok && k < E.w;
+        vv[k] = in ? __ldg(E.val + (size_t)k * E.n + row) : 0;
+        cc[k] = in ? row + (int)__ldg(E.cd + (size_t)k * E.n + row) : 0;
+    }
+    pdl_wait();
+    long long a[R], dot[R];
+#pragma unroll
+    for (int r = 0; r < R; r++) a[r] = dot[r] = 0;
+    int xv[kEllMax][R];
+#pragma unroll
+    for (int k = 0; k < kEllMax; k++) {
+        if (vv[k] != 0) load_r<R>(z, cc[k], xv[k]);
+        else
+#pragma unroll
+            for (int r = 0; r < R; r++) xv[k][r] = 0;
+    }
+#pragma unroll
+    for (int k = 0; k < kEllMax; k++)
+#pragma unroll
+        for (int r = 0; r < R; r++) a[r] = wadd(a[r], (long long)vv[k] * (long long)xv[k][r]);
+    unsigned ovf = 0;
+    if (ok) {
+        const int bit = A.bit[row];
+        int y[R], vq[R];
+        load_r<R>(v0, row, vq);
+#pragma unroll
+        for (int r = 0; r < R; r++) {
+            const long long s = a[r] >> bit;
+            if (!fits32(s)) ovf |= 1u << r;
+            y[r] = lo32(s);
+            dot[r] = wadd(dot[r], (long long)vq[r] * y[r]);
+        }
+        store_r<R>(w, row, y);
+    }
+    bsum_i64<R>(dot, sh);
+    if (threadIdx.x == 0)
+#pragma unroll
+        for (int r = 0; r < R; r++) atomicAdd(acc + (size_t)(t.sys * R + r) * (m + 2), (unsigned long long)dot[r]);
+    if (ovf) {
+#pragma unroll
+        for (int r = 0; r < R; r++)
+            if (ovf & (1u << r)) atomicOr(pflag + (size_t)t.sys * R + r, ST_OVERFLOW);
+        atomicOr(flags, ST_OVERFLOW);
+    }
+}
+
 // MGS pass k of step j for every active pair: h = acc[k] >> bit, H[j][k] = h,
 // w += (int)((-h) V_k >> bit), then acc[k+1] += V_{k+1} . w (or w . w).
 template <int R, bool LAST>
@@ -1570,6 +1681,13 @@ struct DevBMat {
     signed char *bi = nullptr, *db = nullptr;
     short *cdv = nullptr;  // 16-bit column offsets (square operators whose offsets all fit)
     bool d16 = false;      // the lane kernels read cdv instead of ci (6 bytes an entry instead of 8)
+    // ELL copy (square operators with at most kEllMax entries a row and at
+    // most a quarter of the slots empty, 16-bit offsets): the kernels read it
+    // instead of the CSR when ell is set
+    DEll e{};
+    short *ell_cd = nullptr;
+    int *ell_va = nullptr;
+    bool ell = false;
     void up(const BatchCsr &M, bool square = false) {
         d = dview(M, rp, ci, va, bi, db);
         const double avg = M.n ? (double)M.nnz() / M.n : 1.0;
@@ -1584,12 +1702,27 @@ struct DevBMat {
             }
         cdv = dupload(cd);
         d.cd = cdv;
+        int w = 0;
+        for (int i = 0; i < M.n; i++) w = std::max(w, M.rptr[i + 1] - M.rptr[i]);
+        if (w == 0 || w > kEllMax || (double)M.nnz() < 0.75 * (double)M.n * w) return;
+        std::vector<short> ecd((size_t)w * M.n, 0);
+        std::vector<int> eva((size_t)w * M.n, 0);
+        for (int i = 0; i < M.n; i++)
+            for (int j = M.rptr[i], k = 0; j < M.rptr[i + 1]; j++, k++) {
+                ecd[(size_t)k * M.n + i] = cd[j];
+                eva[(size_t)k * M.n + i] = M.val[j];
+            }
+        ell_cd = dupload(ecd);
+        ell_va = dupload(eva);
+        e = DEll{M.n, w, ell_cd, ell_va};
     }
     void release() {
-        dfree(rp); dfree(ci); dfree(va); dfree(bi); dfree(db); dfree(cdv);
+        dfree(rp); dfree(ci); dfree(va); dfree(bi); dfree(db); dfree(cdv); dfree(ell_cd); dfree(ell_va);
         rp = ci = va = nullptr;
         bi = db = nullptr;
         cdv = nullptr;
+        ell_cd = nullptr;
+        ell_va = nullptr;
     }
 };
 
@@ -1652,6 +1785,7 @@ struct BatchEngine::Impl {
     // V-cycle's A: its tiles and reductions favour other lanes per row)
     int dot_group = -1;  // -1: the level-0 A's lanes per row
     bool dot_d16 = false;
+    bool dot_ell = false;  // the Arnoldi SpMV + dot over the level-0 A's ELL copy
     // persistent coarse tail (k_btail): levels tail_from .. Dmax-1 and the LU in
     // one cooperative launch (0: off)
     int tail_from = 0;
@@ -2123,6 +2257,18 @@ struct BatchEngine::Impl {
     void bspmv(const DevBMat &M, const int *x, int *y, int mode, const int *z, const int *row_sys,
                int jac = JAC_NONE, const BJac &J = BJac{}) {
         if (M.d.n == 0) return;
+        if (M.ell && M.ell_va) {
+            const int blocks = (M.d.n + kBThreads - 1) / kBThreads;
+            by_r([&](auto RR) {
+                constexpr int R = decltype(RR)::value;
+                auto k = jac == JAC_PRE ? k_bspmv_ell<R, SPMV_SET, JAC_PRE>
+                         : jac == JAC_POST ? k_bspmv_ell<R, SPMV_RESID, JAC_POST>
+                         : mode == SPMV_SET ? k_bspmv_ell<R, SPMV_SET>
+                         : mode == SPMV_RESID ? k_bspmv_ell<R, SPMV_RESID> : k_bspmv_ell<R, SPMV_ADD>;
+                launch(k, blocks, kBThreads, 0, 1, M.d, M.e, x, y, z, row_sys, cur_pflag, c.d_flags, J);
+            });
+            return;
+        }
         if (M.group == 0) {
             const int blocks = (M.d.n + kStreamThreads - 1) / kStreamThreads;
             by_r([&](auto RR) {
@@ -2428,7 +2574,10 @@ struct BatchEngine::Impl {
         const bool d16 = dot_d16 && A0.cdv && g > 0;
         by_r([&](auto RR) {
             constexpr int R = decltype(RR)::value;
-            if (g == 0) {
+            if (dot_ell && A0.ell_va) {
+                launch(k_bspmv_dot_ell<R>, ntiles * kTileSub, kBThreads, 0, 1, (const BTile *)tiles, A0.d, A0.e, z, w,
+                       v0, accp, mm, pflag, c.d_flags);
+            } else if (g == 0) {
                 launch(k_bspmv_dot_stream<R>, nstiles, kStreamThreads, 0, 1, (const BTile *)stiles, A0.d, z, w, v0,
                        accp, mm, pflag, c.d_flags);
             } else {
@@ -2698,6 +2847,17 @@ int BatchEngine::sweep_form(int level, int set) {
     }
     return L.use_cluster;
 }
+int BatchEngine::ell(int level, int op, int set) {
+    if (level < 0 || level >= impl_->Dmax || (op != 0 && op != 2)) throw CudaError{"no such operator"};
+    DevBMat &M = op == 0 ? impl_->lv[level].A : impl_->lv[level].U;
+    if (set >= 0) {
+        if (set > 0 && !M.ell_va) throw CudaError{"this operator has no ELL copy"};
+        M.ell = set > 0;
+        if (level == 0 && op == 0) impl_->dot_ell = M.ell;
+        impl_->clear_graphs();
+    }
+    return M.ell && M.ell_va ? 1 : 0;
+}
 int BatchEngine::fused_sweeps(int set) {
     Impl &I = *impl_;
     if (set >= 0) {
@@ -2867,6 +3027,7 @@ void BatchEngine::autotune(int reps) {
             float best = 1e30f;
             int bestg = M->group;
             bool bestd = false;
+            M->ell = false;
             for (int dd = 0; dd < (M->cdv ? 2 : 1); dd++)
                 for (int g : cand) {
                     if (dd && g == 0) continue;  // the compressed columns are read by the lane kernels
@@ -2881,6 +3042,11 @@ void BatchEngine::autotune(int reps) {
                 }
             M->group = bestg;
             M->d16 = bestd;
+            if (M->ell_va) {  // the ELL copy, where the operator has one
+                M->ell = true;
+                const float ms = timeit([&] { I.bspmv(*M, xa, xb, SPMV_SET, nullptr, L.row_sys); });
+                M->ell = ms < best;
+            }
         }
     }
     {
@@ -2937,6 +3103,12 @@ void BatchEngine::autotune(int reps) {
             }
         I.dot_group = bestg;
         I.dot_d16 = bestd;
+        I.dot_ell = false;
+        if (I.lv[0].A.ell_va) {
+            I.dot_ell = true;
+            const float ms = timeit([&] { I.spmv_dot(xa, xb, xa, acct, 1); });
+            I.dot_ell = ms < best;
+        }
         dfree(acct);
     }
     SAGB_CUDA(cudaMemsetAsync(I.pflag, 0, sizeof(unsigned) * (size_t)I.S * I.Rn * 2, c.stream));

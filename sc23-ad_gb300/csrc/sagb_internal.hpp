@@ -285,6 +285,9 @@ class BatchEngine {
     // 16-bit column offsets for A (op 0) or U (op 2) of one level: set 1 / 0
     // chooses them (1 needs offsets that fit), -1 only reads
     int compressed(int level, int op, int set);
+    // the ELL copy of a level's A (op 0) or U (op 2), where it has one: set 1 /
+    // 0 chooses it (for the level-0 A also in the Arnoldi SpMV), -1 reads
+    int ell(int level, int op, int set);
     // sweeps of one-colour levels fused into the neighbouring SpMVs: set 1 / 0
     // turns it on / off, -1 reads; returns the levels whose sweeps are fused
     int fused_sweeps(int set);

@@ -139,6 +139,7 @@ SIGNATURES = {
     "sa_batch_sweep_form": (C.c_int, [VP, C.c_int, C.c_int, C.POINTER(C.c_int)]),
     "sa_batch_compressed": (C.c_int, [VP, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int)]),
     "sa_batch_fused_sweeps": (C.c_int, [VP, C.c_int, C.POINTER(C.c_int)]),
+    "sa_batch_ell": (C.c_int, [VP, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int)]),
     "sa_batch_tail": (C.c_int, [VP, C.c_int, C.POINTER(C.c_int)]),
     "sa_batch_tail_selftest": (C.c_int, [VP, VP, C.c_int, C.c_double, C.POINTER(C.c_uint)]),
     "sa_batch_time_op": (C.c_int, [VP, VP, C.c_int, C.c_int, VP, VP, C.c_int, C.POINTER(C.c_float)]),
@@ -829,6 +830,13 @@ class Batch:
         / 0 turns it on / off; returns the levels fused."""
         f = C.c_int()
         check(lib().sa_batch_fused_sweeps(self.h, set, C.byref(f)))
+        return f.value
+
+    def ell(self, level, op, set=-1):
+        """The ELL copy of the level's A (op 0) or U (op 2); set 1 / 0 chooses
+        it (level-0 A: also in the Arnoldi SpMV)."""
+        f = C.c_int()
+        check(lib().sa_batch_ell(self.h, level, op, set, C.byref(f)))
         return f.value
 
     def tail(self, set=-1):

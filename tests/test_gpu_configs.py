@@ -105,6 +105,14 @@ def _batch_forms_match(B, vin, ref, nrhs):
                     pass
         assert n_on > 0 or on == 0
         np.testing.assert_array_equal(out(), ref, err_msg=f"16-bit column offsets {on}")
+    for on in (1, 0):
+        for lv in range(B.depth):
+            for op in (0, 2):
+                try:
+                    B.ell(lv, op, on)
+                except sagb.SagbError:
+                    pass
+        np.testing.assert_array_equal(out(), ref, err_msg=f"ELL copies {on}")
     for t in (B.depth - 1, max(1, B.depth - 4)):
         assert B.tail(t) == t
         np.testing.assert_array_equal(out(), ref, err_msg=f"persistent tail from level {t}")
@@ -125,6 +133,7 @@ def test_batched_vcycle_poisson128(ctx):
     B.autotune(2)
     for x, ref in zip(ins, refs):
         np.testing.assert_array_equal(B.precondition(x), ref, err_msg="after autotuning")
+    assert B.ell(0, 0, 1) == 1  # the 7-point finest level has an ELL copy
     _batch_forms_match(B, ins[1], refs[1][:, None], 1)
     B.close()
 
