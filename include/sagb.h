@@ -94,7 +94,10 @@ typedef struct {
     double omega;        /* SORParam::omega (1.0)                                                     */
     int smooth_iter;     /* SORParam::iter (1)                                                        */
     int multicolor;      /* 1: SOR in greedy-colour order (ldtri::MCCSR, matrix/trispmat.hpp:597-640,
-                            colouring helper/helper_graph.hpp:191-219); 0: natural order (default) */
+                            colouring helper/helper_graph.hpp:191-219); 2: JacobiSORflex
+                            (smoother/stationary.hpp:564-676: chunks of 1200 consecutive rows, GS
+                            across chunks, Jacobi inside one; single-system setups only); 0: natural
+                            order (default) */
     int max_colours;     /* multicolour: cap on the colours per level, rows beyond it join their least
                             conflicting colour (Jacobi-like inside it); 0: no cap (default) */
     int coarse_size;     /* coarsen while the coarsest level has more rows than this; 0: the

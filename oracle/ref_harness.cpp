@@ -124,7 +124,10 @@ static double *read_vec(const char *path, int n) {
 #define AMG_THETA 0.8
 
 // ------------------------------------------------------------ integer hierarchy
-template <class SMO, bool BJ, class AMG>
+// LDK: the smoother's LD class: 0 ldtri::CSRflex, 1 ldtri::BJCSRflex (block
+// sizes dumped as _bjsize), 2 ldtri::MCCSRflex (colour sizes as _csize; the
+// same field layout as BJCSRflex)
+template <class SMO, int LDK, class AMG>
 static void dump_int_hierarchy(AMG *iM, CSR<Fixed<30>> *iA) {
     auto *a0 = reinterpret_cast<MFixed *>(iA);
     dump_csr_int("A0", a0, 30, 0);
@@ -136,10 +139,10 @@ static void dump_int_hierarchy(AMG *iM, CSR<Fixed<30>> *iA) {
         if (l < depth) {
             SMO *s = iM->smoother[l];
             std::string p = "S" + std::to_string(l);
-            if constexpr (BJ) {
+            if constexpr (LDK == 1 || LDK == 2) {
                 auto *ld = reinterpret_cast<MBJ *>(s->LD);
                 dump_csr_int(p + "_LD", ld, ld->bit, ld->dbit);
-                dump(p + "_bjsize", ld->bj_size, ld->bj_num + 1);
+                dump(p + (LDK == 1 ? "_bjsize" : "_csize"), ld->bj_size, ld->bj_num + 1);
             } else {
                 auto *ld = reinterpret_cast<MLD *>(s->LD);
                 dump_csr_int(p + "_LD", ld, ld->bit, ld->dbit);
@@ -338,7 +341,7 @@ static void blas_tests() {
 // --------------------------------------------------------------------- main
 // usage:
 //   ref_harness blas <outdir>
-//   ref_harness solve <A.mtx> <b.f64> <outdir> <smoother 0|1> <m> <what> <dump_cycle 0|1>
+//   ref_harness solve <A.mtx> <b.f64> <outdir> <smoother 0 SOR|1 BlockSOR-40|2 JacobiSOR> <m> <what> <dump_cycle 0|1>
 // where <what> is a comma list of: fp64 (FP64 solve), fp32 (FP32 solve),
 // inth (int hierarchy + kernel tests), ints (int solve), dh / fh (dump the
 // FP64 / FP32 hierarchies).
@@ -395,11 +398,12 @@ int main(int argc, char **argv) {
     using FBJ = BlockSOR<ldtri::BJCSR<float>, CSR<float>>;
     using ISOR = SOR<ldtri::CSRflex, CSRflex>;
     using IBJ = BlockSORflex<ldtri::BJCSRflex, CSRflex>;
+    using IJS = JacobiSORflex<ldtri::MCCSRflex, CSRflex>;
 
     Timer timer;
     // ---- FP64 preconditioner (also used by the bit rule, Work/main.cpp:153-161)
     Preconditioner<double> *M;
-    if (smoother == 0) {
+    if (smoother != 1) {  // SOR (also for the integer JacobiSOR case: the rule's V-cycle)
         auto *mm = new dfAMG<CSR<double>, DSOR, double>(Abase, dA, new AMGParam(20, AMG_THETA, 1, sor_param));
         if (has("dh")) dump_fp_hierarchy<double>("d_", mm);
         fp_kernel_tests<double>("d_", mm, N);
@@ -455,7 +459,7 @@ int main(int argc, char **argv) {
         auto iA = new CSR<Fixed<30>>(Abase);
         if (smoother == 0) {
             auto *iM = new intAMGflex<CSRflex, CSRflex, ISOR>(Abase, iA, new AMGParam(20, AMG_THETA, 1, sor_param));
-            dump_int_hierarchy<ISOR, false>(iM, iA);
+            dump_int_hierarchy<ISOR, 0>(iM, iA);
             int_kernel_tests<ISOR>(iM, iA, N, bit);
             auto inner = new FGMRESflex(iA, m, epsilon, iM, bit);
             if (dump_cycle) {
@@ -484,9 +488,24 @@ int main(int argc, char **argv) {
                 dump_scalar_i("int_iter", cv.iter);
                 explicit_res("int");
             }
+        } else if (smoother == 2) {
+            auto *iM = new intAMGflex<CSRflex, CSRflex, IJS>(Abase, iA, new AMGParam(20, AMG_THETA, 1, sor_param));
+            dump_int_hierarchy<IJS, 2>(iM, iA);
+            int_kernel_tests<IJS>(iM, iA, N, bit);
+            auto inner = new FGMRESflex(iA, m, epsilon, iM, bit);
+            if (has("ints")) {
+                auto solver = new Restarted(dA, inner, outer, epsilon);
+                utils::Set<double>(0, x, N);
+                timer.Restart();
+                auto cv = solver->Solve(b, nrm_b, x);
+                timer.Elapsed();
+                printf("[Iter] : %d\n", cv.iter);
+                dump_scalar_i("int_iter", cv.iter);
+                explicit_res("int");
+            }
         } else {
             auto *iM = new intAMGflex<CSRflex, CSRflex, IBJ>(Abase, iA, new AMGParam(20, AMG_THETA, 1, hybrid_param));
-            dump_int_hierarchy<IBJ, true>(iM, iA);
+            dump_int_hierarchy<IBJ, 1>(iM, iA);
             int_kernel_tests<IBJ>(iM, iA, N, bit);
             auto inner = new FGMRESflex(iA, m, epsilon, iM, bit);
             if (has("ints")) {

@@ -555,7 +555,7 @@ static int setup_create(Ctx *gpu, int precision, const sa_amg_params *p, int n, 
     if (p) s->p = *p;
     else sa_amg_params_default(&s->p);
     if (s->p.smooth_iter < 1 || s->p.max_levels < 1 || s->p.smoother_blocks < 0 ||
-        s->p.multicolor < 0 || s->p.multicolor > 1 || (s->p.multicolor && s->p.smoother_blocks) ||
+        s->p.multicolor < 0 || s->p.multicolor > 2 || (s->p.multicolor && s->p.smoother_blocks) ||
         s->p.max_colours < 0 || s->p.coarse_size < 0 || s->p.coarse_colours < 0) {
         delete s;
         return fail(SA_ERR_ARG, "invalid AMG parameters");

@@ -873,6 +873,37 @@ void mc_sor_split(const CsrD &A, double omega, const std::vector<int> &col, CsrD
     }
 }
 
+void jacobi_sor_split(const CsrD &A, double omega, CsrD &LD, CsrD &U, std::vector<int> &colour) {
+    const int N = A.n;
+    LD.n = LD.m = U.n = U.m = N;
+    LD.rptr.assign(N + 1, 0);
+    U.rptr.assign(N + 1, 0);
+    LD.cind.clear(); LD.val.clear(); U.cind.clear(); U.val.clear();
+    colour.resize(N);
+    for (int i = 0; i < N; i++) {
+        colour[i] = i / kJacobiSorChunk;
+        const int left = colour[i] * kJacobiSorChunk;  // the first row of row i's chunk
+        for (int j = A.rptr[i]; j < A.rptr[i + 1]; j++) {
+            const int c = A.cind[j];
+            const double v = A.val[j];
+            if (c == i) {
+                LD.cind.push_back(c);
+                LD.val.push_back(1.0 / omega * v);
+                U.cind.push_back(c);
+                U.val.push_back((1 - 1.0 / omega) * v);
+            } else if (c < left) {
+                LD.cind.push_back(c);
+                LD.val.push_back(v);
+            } else {
+                U.cind.push_back(c);
+                U.val.push_back(v);
+            }
+        }
+        LD.rptr[i + 1] = (int)LD.cind.size();
+        U.rptr[i + 1] = (int)U.cind.size();
+    }
+}
+
 // LD with its diagonal (the last entry of each row) inverted: extractLDinv for a
 // split whose couplings may lie on either side of the diagonal (colour order).
 static CsrD invert_last(const CsrD &LD) {
@@ -886,7 +917,9 @@ static void smoother_split(const CsrD &A, const SmootherSpec &sm, int level, Csr
                            std::vector<int> &bj, std::vector<int> &colour) {
     colour.clear();
     bj.clear();
-    if (sm.multicolor) {
+    if (sm.multicolor == 2) {
+        jacobi_sor_split(A, sm.omega, LD, U, colour);
+    } else if (sm.multicolor) {
         int nc = 0;
         colour = greedy_colouring(A, &nc, sm.cap(level));
         mc_sor_split(A, sm.omega, colour, LD, U);

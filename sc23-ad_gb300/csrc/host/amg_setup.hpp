@@ -99,7 +99,7 @@ struct SmootherSpec {
     int block = 0;       // 0: SOR, else BlockSOR with this many blocks
     double omega = 1.0;
     int iter = 1;
-    int multicolor = 0;  // 1: SOR in colour order (the multicolour variant)
+    int multicolor = 0;  // 1: SOR in colour order (the multicolour variant); 2: JacobiSORflex
     int max_colours = 0; // multicolour: at most this many colours (0: as many as a proper colouring needs)
     int coarse_colours = 0;  // multicolour: the cap below the finest level (0: max_colours)
     std::vector<int> level_caps;  // multicolour: a cap per level, the last for all deeper ones (overrides both)
@@ -120,6 +120,14 @@ std::vector<int> greedy_colouring(const CsrD &A, int *ncolors, int max_colours =
 // (diagonal last), U = (1 - 1/omega) diag first + couplings to later colours.
 // GS with this split is ldtri::MCCSRflex (ldtri.hpp:635-700) without renumbering.
 void mc_sor_split(const CsrD &A, double omega, const std::vector<int> &colour, CsrD &LD, CsrD &U);
+// JacobiSORflex (smoother/stationary.hpp:564-676): consecutive chunks of
+// kJacobiSorChunk rows; LD holds a row's couplings to earlier chunks and
+// diag/omega, U the (1 - 1/omega) diagonal and every coupling inside the
+// chunk or to later ones, each in the row's own entry order (the reference's
+// arrays entry for entry).  The chunks are the colours of the sweep
+// (ldtri::MCCSRflex order): a chunk's rows read only earlier chunks.
+constexpr int kJacobiSorChunk = 1200;
+void jacobi_sor_split(const CsrD &A, double omega, CsrD &LD, CsrD &U, std::vector<int> &colour);
 
 struct IntHierarchy {
     int depth = 0;

@@ -26,7 +26,7 @@ import gen_matrices as gm  # noqa: E402
 
 HARNESS = os.path.join(ROOT, "oracle", "_ref", "ref_harness")
 
-# name: (generator, smoother 0=SOR 1=BlockSOR-40, m, what, dump_cycle)
+# name: (generator, smoother 0=SOR 1=BlockSOR-40 2=JacobiSOR, m, what, dump_cycle)
 CASES = {
     "p2d64": (lambda: gm.poisson2d(64), 0, 30, "fp64,fp32,inth,ints,dh", 1),
     "p3d16": (lambda: gm.poisson3d(16), 0, 30, "fp64,fp32,inth,ints,dh,fh", 1),
@@ -38,6 +38,9 @@ CASES = {
     "an2d64": (lambda: gm.aniso2d(64, 1e-3), 0, 30, "fp64,fp32,inth", 0),
     "s27n14": (lambda: gm.stencil27(14, 11), 0, 20, "fp64,fp32,inth,ints", 0),
     "p3d16bj": (lambda: gm.poisson3d(16), 1, 30, "fp64,inth,ints", 0),
+    # JacobiSORflex: 1200-row chunks (4 on the finest level of both systems)
+    "p3d16js": (lambda: gm.poisson3d(16), 2, 30, "fp64,inth,ints", 0),
+    "p2d64js": (lambda: gm.poisson2d(64), 2, 30, "fp64,inth,ints", 0),
 }
 RHS_SEED = 12345
 

@@ -17,7 +17,7 @@ import setup_views as sv
 
 pytestmark = pytest.mark.gpu
 
-INT_CASES = ["p2d64", "p3d16", "cd3d16", "vc3d16", "an2d64", "s27n14", "p3d16bj"]
+INT_CASES = ["p2d64", "p3d16", "cd3d16", "vc3d16", "an2d64", "s27n14", "p3d16bj", "p3d16js", "p2d64js"]
 FP_TOL = 1e-12
 
 
@@ -29,7 +29,8 @@ def ctx():
 
 
 def _params(case):
-    return sagb.amg_params(smoother_blocks=40 if case.endswith("bj") else 0)
+    """SOR (the default), BlockSOR-40 ("bj") or JacobiSORflex ("js")."""
+    return sagb.amg_params(smoother_blocks=40 if case.endswith("bj") else 0, multicolor=2 if case.endswith("js") else 0)
 
 
 def _amg(ctx, g, case, prec=sagb.INT):
@@ -121,7 +122,7 @@ def test_int_fgmres_cycle_bit_exact(ctx, case):
     S.close()
 
 
-@pytest.mark.parametrize("case", ["p2d64", "p3d16", "cd3d16", "vc3d16", "s27n14", "p3d16bj"])
+@pytest.mark.parametrize("case", ["p2d64", "p3d16", "cd3d16", "vc3d16", "s27n14", "p3d16bj", "p3d16js", "p2d64js"])
 def test_int_full_solve(ctx, case):
     g = of.load_golden(case)
     S, keep = _solver(ctx, g, case, sagb.INT)

@@ -85,7 +85,9 @@ def test_bad_params_rejected():
     with pytest.raises(sagb.SagbError):
         sagb.Setup(sagb.F64, r, c, v, sagb.amg_params(multicolor=1, smoother_blocks=4))
     with pytest.raises(sagb.SagbError):
-        sagb.Setup(sagb.F64, r, c, v, sagb.amg_params(multicolor=2))
+        sagb.Setup(sagb.F64, r, c, v, sagb.amg_params(multicolor=3))  # 2 is JacobiSORflex
+    with pytest.raises(sagb.SagbError):
+        sagb.Setup(sagb.F64, r, c, v, sagb.amg_params(multicolor=2, smoother_blocks=4))
     s = sagb.Setup(sagb.F64, r, c, v)
     with pytest.raises(sagb.SagbError):
         s.view(sagb.OP_COLOR, 0)   # natural-order setup has no colours

@@ -9,7 +9,9 @@ import pytest
 
 import oracle_ffi as of
 
-CASES_INT = ["p2d64", "p3d16", "cd3d16", "vc3d16", "an2d64", "s27n14", "p3d16bj"]
+# "js": JacobiSORflex, whose LD holds only couplings to earlier chunks, so the
+# natural-order sweep of the oracle is its chunk-ordered sweep
+CASES_INT = ["p2d64", "p3d16", "cd3d16", "vc3d16", "an2d64", "s27n14", "p3d16bj", "p3d16js", "p2d64js"]
 
 
 @pytest.fixture(scope="module")
@@ -128,7 +130,7 @@ def test_int_fgmres_cycle(L, case):
     np.testing.assert_array_equal(x, g["cyc_x"])
 
 
-@pytest.mark.parametrize("case", ["p2d64", "p3d16", "cd3d16", "vc3d16", "s27n14", "p3d16bj"])
+@pytest.mark.parametrize("case", ["p2d64", "p3d16", "cd3d16", "vc3d16", "s27n14", "p3d16bj", "p3d16js", "p2d64js"])
 def test_int_full_solve(L, case):
     g = of.load_golden(case)
     keep = of.Keep()

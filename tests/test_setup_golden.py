@@ -10,11 +10,12 @@ import pytest
 import oracle_ffi as of
 import sagb
 
-CASES = ["p2d64", "p3d16", "cd3d16", "vc3d16", "an2d64", "s27n14", "p3d16bj"]
+CASES = ["p2d64", "p3d16", "cd3d16", "vc3d16", "an2d64", "s27n14", "p3d16bj", "p3d16js", "p2d64js"]
 
 
 def _params(case):
-    return sagb.amg_params(smoother_blocks=40 if case.endswith("bj") else 0)
+    """SOR (the default), BlockSOR-40 ("bj") or JacobiSORflex ("js")."""
+    return sagb.amg_params(smoother_blocks=40 if case.endswith("bj") else 0, multicolor=2 if case.endswith("js") else 0)
 
 
 def _cmp(got, g, pfx, with_bits=True):
@@ -57,6 +58,10 @@ def test_int_hierarchy(case):
         _cmp(s.view(sagb.OP_U, i), g, f"S{i}_U", with_bits=False)
         if case.endswith("bj"):
             np.testing.assert_array_equal(s.view(sagb.OP_BJ, i), g[f"S{i}_bjsize"])
+        if case.endswith("js"):
+            # the sweep's colours are the reference's chunks (MCCSRflex c_size)
+            cs = g[f"S{i}_csize"]
+            np.testing.assert_array_equal(s.view(sagb.OP_COLOR, i), np.repeat(np.arange(len(cs) - 1), np.diff(cs)))
     _cmp(s.view(sagb.OP_LUL), g, "LU_L", with_bits=False)
     _cmp(s.view(sagb.OP_LUU), g, "LU_U")
 
