@@ -116,21 +116,48 @@ class Staged {
         if (is_device_ptr(p)) {
             dev_ = user_;
         } else {
-            own_ = dmalloc(bytes);
-            dev_ = own_;
-            if (in) SAGB_CUDA(cudaMemcpyAsync(dev_, p, bytes, cudaMemcpyHostToDevice, c.stream));
+            const int slot = c.stage_used;
+            void *buf = nullptr;
+            if (slot < 2) {  // the context's kept buffer for this argument
+                if (c.stage_cap[slot] < bytes) {
+                    cudaStreamSynchronize(c.stream);
+                    dfree(c.stage[slot]);
+                    c.stage[slot] = nullptr;
+                    c.stage_cap[slot] = 0;
+                    c.stage[slot] = dmalloc(bytes);
+                    c.stage_cap[slot] = bytes;
+                }
+                buf = c.stage[slot];
+            } else {
+                buf = dmalloc(bytes);
+                own_ = buf;
+            }
+            if (in) {
+                const cudaError_t e = cudaMemcpyAsync(buf, p, bytes, cudaMemcpyHostToDevice, c.stream);
+                if (e != cudaSuccess) {
+                    dfree(own_);
+                    own_ = nullptr;
+                    SAGB_CUDA(e);
+                }
+            }
+            dev_ = buf;
+            if (slot < 2) {  // in use until this object goes
+                slot_ = slot;
+                c.stage_used++;
+            }
         }
     }
     ~Staged() {
-        if (own_) {
+        if (dev_ && dev_ != user_) {
             cudaStreamSynchronize(c_.stream);
-            dfree(own_);
+            if (slot_ >= 0) c_.stage_used--;
+            else dfree(own_);
         }
     }
     // Host outputs are copied back and the stream is synchronised; with device
     // buffers only, the call stays asynchronous on the context's stream.
     void finish() {
-        if (!own_) return;
+        if (!dev_ || dev_ == user_) return;
         if (out_) SAGB_CUDA(cudaMemcpyAsync(user_, dev_, bytes_, cudaMemcpyDeviceToHost, c_.stream));
         SAGB_CUDA(cudaStreamSynchronize(c_.stream));
     }
@@ -141,6 +168,7 @@ class Staged {
     void *user_, *dev_ = nullptr, *own_ = nullptr;
     size_t bytes_;
     bool out_;
+    int slot_ = -1;  // the context's kept buffer in use, or -1 (an allocation of this call)
 };
 
 // ---------------------------------------------------------------- library
@@ -173,6 +201,8 @@ extern "C" int sa_ctx_create(int device, sa_ctx *out) {
 extern "C" int sa_ctx_destroy(sa_ctx ctx) {
     if (!ctx) return SA_OK;
     cudaStreamSynchronize(ctx->c.stream);
+    dfree(ctx->c.stage[0]);
+    dfree(ctx->c.stage[1]);
     dfree(ctx->c.d_flags_main);
     cudaFreeHost(ctx->c.h_flags);
     cudaStreamDestroy(ctx->c.stream);

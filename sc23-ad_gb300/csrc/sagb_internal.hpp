@@ -40,6 +40,12 @@ struct Ctx {
     int gpu_setup_rows = 1 << 20;    // batches: systems from this size on build their Ruge-Stueben chain
                                      // on the GPU (0: none); smaller ones share the host threads
     long long launches = 0;          // kernels launched by this context (for reporting)
+    // device copies of a call's host arguments, kept between calls (grow-only;
+    // calls on a context do not overlap): allocating and freeing them per call
+    // cost more than the copies
+    void *stage[2] = {nullptr, nullptr};
+    size_t stage_cap[2] = {0, 0};
+    int stage_used = 0;
     std::string err;
 };
 
