@@ -103,47 +103,47 @@ __device__ __forceinline__ void store_r(int *x, int row, const int (&v)[R]) {
 //                plain loads)
 //   CG:          x through L2 (written earlier in the same launch)
 //   D16:         columns from the 16-bit offsets cd (column = row + cd[j])
-template <int R, int G, bool SUB, bool CG, bool D16 = false>
+template <int R, int G, bool SUB, bool CG, bool D16 = false, int U = 4>
 __device__ __forceinline__ void row_accumulate(const int *__restrict__ cind, const short *__restrict__ cd,
                                                const int *__restrict__ val, int e0, int e1, int lane, int row,
                                                const int *x, long long (&acc)[R]) {
     int j = e0 + lane;
-    for (; j + 3 * G < e1; j += 4 * G) {
-        int cc[4];
-        long long vv[4];
+    for (; j + (U - 1) * G < e1; j += U * G) {
+        int cc[U];
+        long long vv[U];
 #pragma unroll
-        for (int q = 0; q < 4; q++) {
+        for (int q = 0; q < U; q++) {
             cc[q] = D16 ? row + (int)__ldg(cd + j + q * G) : __ldg(cind + j + q * G);
             vv[q] = __ldg(val + j + q * G);
         }
-        int xv[4][R];
+        int xv[U][R];
 #pragma unroll
-        for (int q = 0; q < 4; q++) {
+        for (int q = 0; q < U; q++) {
             if constexpr (CG) load_cg_r<R>(x, cc[q], xv[q]);
             else if constexpr (!SUB) load_r<R>(x, cc[q], xv[q]);
             else load_rw<R>(x, cc[q], xv[q]);
         }
 #pragma unroll
-        for (int q = 0; q < 4; q++)
+        for (int q = 0; q < U; q++)
 #pragma unroll
             for (int r = 0; r < R; r++) {
                 if constexpr (SUB) acc[r] = wsub(acc[r], vv[q] * (long long)xv[q][r]);
                 else acc[r] = wadd(acc[r], vv[q] * (long long)xv[q][r]);
             }
     }
-    if (j < e1) {  // the last 1-3 entries of this lane: one predicated round, not one round trip each
-        int cc[3];
-        long long vv[3];
+    if (j < e1) {  // the last 1 .. U-1 entries of this lane: one predicated round, not one round trip each
+        int cc[U - 1];
+        long long vv[U - 1];
 #pragma unroll
-        for (int q = 0; q < 3; q++) {
+        for (int q = 0; q < U - 1; q++) {
             const int jj = j + q * G;
             const bool ok = jj < e1;
             cc[q] = ok ? (D16 ? row + (int)__ldg(cd + jj) : __ldg(cind + jj)) : -1;
             vv[q] = ok ? __ldg(val + jj) : 0;
         }
-        int xv[3][R];
+        int xv[U - 1][R];
 #pragma unroll
-        for (int q = 0; q < 3; q++) {
+        for (int q = 0; q < U - 1; q++) {
             if (cc[q] < 0) {
 #pragma unroll
                 for (int r = 0; r < R; r++) xv[q][r] = 0;
@@ -156,7 +156,7 @@ __device__ __forceinline__ void row_accumulate(const int *__restrict__ cind, con
             }
         }
 #pragma unroll
-        for (int q = 0; q < 3; q++)
+        for (int q = 0; q < U - 1; q++)
 #pragma unroll
             for (int r = 0; r < R; r++) {
                 if constexpr (SUB) acc[r] = wsub(acc[r], vv[q] * (long long)xv[q][r]);
@@ -289,8 +289,11 @@ k_bspmv(DBCsr A, const int *__restrict__ x, int *__restrict__ y, const int *__re
 #pragma unroll
             for (int r = 0; r < R; r++) acc[r] = wadd(acc[r], (long long)vv[q] * (long long)xv[q][r]);
     }
+    // rows long enough for G >= 8 lanes: eight entries a lane in flight (a
+    // warp then has 256 of a row's entries in flight at once)
+    constexpr int kU = G >= 8 && R == 1 ? 8 : 4;
     if (e1 - e0 > kSpmvPre * G)
-        row_accumulate<R, G, false, false, D16>(A.cind, A.cd, A.val, e0 + kSpmvPre * G, e1, lane, row, x, acc);
+        row_accumulate<R, G, false, false, D16, kU>(A.cind, A.cd, A.val, e0 + kSpmvPre * G, e1, lane, row, x, acc);
 #pragma unroll
     for (int r = 0; r < R; r++)
 #pragma unroll
