@@ -843,7 +843,9 @@ TAIL_KEYS = ("vcycle_ms", "families_ms_per_vcycle", "spmv_A0", "full_cycles", "b
 
 
 def tail_last(line):
-    """The same dict with the bulky per-level diagnostics first and TAIL_KEYS last."""
+    """A copy of the line with the bulky per-level diagnostics first and
+    TAIL_KEYS last (the siblings' colour-cap tables moved to keys of their own)."""
+    line = dict(line)
     out = {k: v for k, v in line.items() if k not in TAIL_KEYS}
     for k in ("fp64_batched", "fp32_batched"):
         if k in line and "colour_cap_tuning" in line[k]:

@@ -39,3 +39,25 @@ def test_reference_arm_does_not_load_the_library():
     out = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=600, cwd=ROOT)
     assert out.returncode == 0, out.stderr
     assert "MAPS True False" in out.stdout, out.stdout[-500:]
+
+
+def test_headline_line_keeps_its_comparisons_last():
+    """The headline line puts its bulky per-level diagnostics first and the
+    comparisons (V-cycle, level-0 SpMV, siblings, learned gain, speed-ups,
+    roofline, CPU baseline, e2e) last, in a fixed order, so a log that keeps
+    only the end of a long line still shows them; every key survives."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("bench_mod", os.path.join(ROOT, "bench.py"))
+    bench = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(bench)
+    line = {"metric": "m", "value": 1.0, "roofline": {"frac": 0.4}, "ops": [[0, "A"]] * 200,
+            "fp64_batched": {"value": 2.0, "colour_cap_tuning": [{"caps": [8, 1]}]}, "e2e": {"value": 1.1},
+            "plain": {"sweep_levels": [[0, 1, 2, 3]] * 50}, "cpu_baseline": {"value": 9.0}, "vcycle_ms": 0.5}
+    out = bench.tail_last(line)
+    keys = list(out)
+    tail = [k for k in bench.TAIL_KEYS if k in line]
+    assert keys[-len(tail):] == tail
+    assert set(keys) == set(line) | {"fp64_batched_colour_cap_tuning"}
+    assert "colour_cap_tuning" not in out["fp64_batched"] and "colour_cap_tuning" in line["fp64_batched"]
+    s = json.dumps(out)
+    assert '"e2e"' in s[-200:] and '"cpu_baseline"' in s[-200:]
