@@ -182,6 +182,7 @@ class CSRflex {};
 namespace ldtri {
 class CSRflex {};
 class BJCSRflex {};
+class MCCSRflex {};
 template <typename T>
 class CSR {};
 template <typename T>
@@ -193,6 +194,15 @@ template <typename LD, typename U>
 class BlockSOR {};
 template <typename LD, typename U>
 class BlockSORflex {};
+template <typename LD, typename U>
+class JacobiSORflex {};  // smoother/stationary.hpp:564-676 (with SORParam)
+
+namespace detail {
+template <typename S>
+struct is_jacobi_sor : std::false_type {};
+template <typename LD, typename U>
+struct is_jacobi_sor<JacobiSORflex<LD, U>> : std::true_type {};
+}  // namespace detail
 
 // ---------------------------------------------------------- parameters.hpp
 struct SmootherParam {
@@ -276,7 +286,8 @@ template <typename C, typename I, typename Smoother>
 class intAMGflex : public Preconditioner<int> {
   public:
     intAMGflex(CSRMat *A, SpMat<int> *, PreconditionerParam *p) {
-        const sa_amg_params q = detail::amg_params(p);
+        sa_amg_params q = detail::amg_params(p);
+        if (detail::is_jacobi_sor<Smoother>::value) q.multicolor = 2;  // JacobiSORflex: 1200-row chunks
         detail::check(sa_amg_create(detail::context(), SA_INT, &q, A->N, A->rptr, A->cind, A->val, &this->h),
                       "intAMGflex");
     }

@@ -2,7 +2,7 @@
 // Market file, scales it, builds the FP64, FP32 or integer AMG preconditioner,
 // picks F by the reference's rule and solves with Restarted(FGMRES<double>),
 // Restarted(FGMRES<float>) or Restarted(FGMRESflex), as Work/main.cpp does.
-// Arguments: <matrix.mtx> <0: FP64, 1: FP32-mixed, 2: int> <m> [b.f64], where
+// Arguments: <matrix.mtx> <0: FP64, 1: FP32-mixed, 2: int, 3: int with JacobiSORflex> <m> [b.f64], where
 // the optional file holds the unscaled right-hand side as raw FP64 values.
 // Prints "[Iter] : n" and "# [Res] : r" like the reference's driver.
 #include <cmath>
@@ -63,7 +63,9 @@ int main(int argc, char **argv) {
     } else {
         auto *iA = new CSR<Fixed<30>>(A);
         auto *M = new dfAMG<CSR<double>, SOR<ldtri::CSR<double>, CSR<double>>, double>(A, dA, param);
-        auto *iM = new intAMGflex<CSRflex, CSRflex, SOR<ldtri::CSRflex, CSRflex>>(A, iA, param);
+        Preconditioner<int> *iM;
+        if (kind == 3) iM = new intAMGflex<CSRflex, CSRflex, JacobiSORflex<ldtri::MCCSRflex, CSRflex>>(A, iA, param);
+        else iM = new intAMGflex<CSRflex, CSRflex, SOR<ldtri::CSRflex, CSRflex>>(A, iA, param);
         double *c = utils::SafeMalloc<double>(N);
         M->Precondition(b, c);
         double cmax = 0;

@@ -58,7 +58,7 @@ def _write_mm(path, r, c, v):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("kind", [0, 2])
+@pytest.mark.parametrize("kind", [0, 2, 3])
 def test_facade_driver_solves(tmp_path, kind):
     A = sagb.HostCsr.generate(sagb.GEN_POISSON3D, 20)
     r, c, v = A.arrays()
