@@ -12,7 +12,7 @@ import pytest
 
 import oracle_ffi as of
 
-CASES = ["p2d64", "p3d16", "cd3d16", "vc3d16", "an2d64", "s27n14", "p3d16bj"]
+CASES = ["p2d64", "p3d16", "cd3d16", "vc3d16", "an2d64", "s27n14", "p3d16bj", "p3d16js", "p2d64js"]
 
 
 def _same_i32(g, pfx, c):
@@ -47,12 +47,13 @@ def test_oracle_setup_equals_reference_hierarchy(case):
             _same_i32(g, f"L{i}_CA", h.CA[i])
         _same_i32(g, f"L{i}_P", h.P[i])
         _same_i32(g, f"L{i}_R", h.R[i])
-        if not case.endswith("bj"):  # the oracle setup builds the SOR split (BlockSOR is the product's)
+        # the oracle setup builds the SOR split (the BlockSOR and JacobiSOR splits are the product's)
+        if not case.endswith(("bj", "js")):
             _same_i32(g, f"S{i}_LD", h.LD[i])
             _same_i32(g, f"S{i}_U", h.U[i])
     _same_i32(g, "LU_L", h.LUL)
     _same_i32(g, "LU_U", h.LUU)
-    if "d_depth" in g and not case.endswith("bj"):
+    if "d_depth" in g and not case.endswith(("bj", "js")):
         d = s.h_f64
         for i in range(D):
             if i < D - 1:
